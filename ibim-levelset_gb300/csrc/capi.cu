@@ -1,0 +1,737 @@
+// The C ABI (include/ibim.h): status codes, handles, and the whole-path entry points.
+// Every entry point catches library errors and returns a status; ibim_last_error() gives text.
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+
+#include "solve.cuh"
+
+namespace ibim {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+template <class F>
+static int guard(F &&f) {
+    try {
+        f();
+        return IBIM_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return IBIM_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return IBIM_ERR_INVALID_ARGUMENT;
+    }
+}
+
+static void bind(Ctx *c) { IBIM_CUDA(cudaSetDevice(c->device)); }
+
+// Single-kernel FMMs through the fused block: (input density slot, output field, sign) per
+// reference kernel (electric.cpp:67-291); H is symmetric, so K3ab reads slot b, field G_a.
+struct KernelMap {
+    int slot, field;
+    double sign;
+};
+static const KernelMap kKernelMap[16] = {
+    {0, 0, 1.},  {1, 0, 1.},  {2, 0, 1.},                          // K1x K1y K1z -> F
+    {3, 0, -1.},                                                    // K2: F = -K2 psi
+    {0, 1, 1.},  {1, 2, 1.},  {2, 3, 1.},                          // K3xx K3yy K3zz
+    {0, 2, 1.},  {1, 3, 1.},  {2, 1, 1.},                          // K3xy K3yz K3zx
+    {0, 2, 1.},  {1, 3, 1.},  {2, 1, 1.},                          // K3yx K3zy K3xz (same pairs)
+    {3, 1, -1.}, {3, 2, -1.}, {3, 3, -1.},                         // K4x K4y K4z: G = -K4 psi
+};
+
+static void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4) {
+    std::vector<double> h(4 * (size_t)std::max(1, natoms));
+    for (int a = 0; a < natoms; ++a) {
+        h[4 * a] = centers[3 * a];
+        h[4 * a + 1] = centers[3 * a + 1];
+        h[4 * a + 2] = centers[3 * a + 2];
+        h[4 * a + 3] = charges[a];
+    }
+    a4.alloc(h.size(), c->stream);
+    a4.upload(h.data(), h.size());
+    IBIM_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+static void check_config(const ibim_config &cfg) {
+    IBIM_REQUIRE(cfg.h > 0, "h must be positive");
+    IBIM_REQUIRE(cfg.n[0] > 0 && cfg.n[1] > 0 && cfg.n[2] > 0, "grid size must be positive");
+    IBIM_REQUIRE(cfg.thickness > 0, "lvlset_thickness must be positive");
+    IBIM_REQUIRE(cfg.np >= 2 && cfg.np <= 8, "fmm_np must be in [2, 8]");
+    IBIM_REQUIRE(cfg.maxpoint > 0, "fmm_maxpoint must be positive");
+    IBIM_REQUIRE(cfg.restart > 0 && cfg.maxiter > 0, "gmres_restart and gmres_maxiter must be positive");
+    IBIM_REQUIRE(cfg.kp.dE > 0 && cfg.kp.dI > 0, "solvent_dE and solvent_dI must be positive");
+    IBIM_REQUIRE(cfg.kp.kappa >= 0 && cfg.kp.tau >= 0, "solvent_kappa and tau must be non-negative");
+    IBIM_REQUIRE(cfg.precision == IBIM_PRECISION_FP64 || cfg.precision == IBIM_PRECISION_MIXED, "unknown precision");
+}
+
+// main.cpp:45-60 with s = 1
+static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *radii_dev, int natoms,
+                               const ibim_config &cfg, int steps[2]) {
+    Grid *g = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, cfg.init);
+    Grid *phi0 = nullptr;
+    try {
+        levelset_expand(*g, centers_dev, radii_dev, natoms, cfg.probe, cfg.band);
+        levelset_evolve(*g, cfg.probe, 1.0, 0.2);
+        grid_scale(*g, -1.0);
+        phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0.);
+        grid_copy(*phi0, *g);
+        steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
+        grid_copy(*phi0, *g);
+        steps[1] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
+    } catch (...) {
+        delete phi0;
+        delete g;
+        throw;
+    }
+    delete phi0;
+    return g;
+}
+
+static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
+                       const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
+                       const double *atoms4_dev) {
+    check_config(cfg);
+    IBIM_REQUIRE(natoms > 0, "need at least one atom");
+    std::memset(&res, 0, sizeof(res));
+    cudaStream_t s = c->stream;
+    Timer t0(s);
+    Grid *g = levelset_pipeline(c, centers_dev, radii_dev, natoms, cfg, res.reinit_steps);
+    res.t_levelset_ms = t0.ms();
+    Timer t1(s);
+    Tube *tube = nullptr;
+    try {
+        tube = surface_extract(*g, cfg.thickness, &res.inclusion);
+    } catch (...) {
+        delete g;
+        throw;
+    }
+    delete g;
+    res.n_points = tube->n;
+    res.t_surface_ms = t1.ms();
+    IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
+    Plan *P = nullptr;
+    try {
+        auto w0 = std::chrono::steady_clock::now();
+        P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
+        fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
+        if (cfg.precision != IBIM_PRECISION_FP64) fmm_prepare_operators(*P, cfg.kp, cfg.precision);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        res.t_plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+        // area = sum of quadrature weights (electric.cpp:60)
+        std::vector<double> w(tube->n);
+        P->sw.download(w.data(), tube->n);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        double area = 0.;
+        for (long i = 0; i < tube->n; ++i) area += w[i];
+        res.area = area;
+        DevBuf<double> a4;
+        const double *atoms4 = atoms4_dev;
+        if (!atoms4) {
+            atoms_to_device(c, centers_host, charges_host, natoms, a4);
+            atoms4 = a4.ptr;
+        }
+        electric_solve(*P, cfg.kp, atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol, cfg.precision,
+                       nullptr, nullptr, res);
+    } catch (...) {
+        delete P;
+        delete tube;
+        throw;
+    }
+    delete P;
+    delete tube;
+}
+
+// Serialise a tree in the reference's node numbering (see ibim_plan_lists).
+static void encode_lists(const TreeHost &T, int *buf, long cap, long *needed) {
+    const int nn = T.nnodes;
+    std::vector<int> lev_of_ref(nn);
+    for (int i = 0; i < nn; ++i) lev_of_ref[T.ref_id[i]] = i;
+    std::vector<int> out;
+    out.push_back(nn);
+    for (int r = 0; r < nn; ++r) {
+        const int i = lev_of_ref[r];
+        int level = 0;
+        while (T.level_begin[level + 1] <= i) ++level;
+        out.push_back(level);
+        out.push_back(T.parent[i] < 0 ? -1 : T.ref_id[T.parent[i]]);
+        out.push_back(T.leaf[i]);
+        out.push_back(T.empty[i]);
+        out.push_back(T.src_end[i] - T.src_begin[i]);
+        const std::vector<int> *L[4] = {&T.U[i], &T.V[i], &T.W[i], &T.X[i]};
+        for (auto *l : L) {
+            std::vector<int> v;
+            for (int x : *l) v.push_back(T.ref_id[x]);
+            std::sort(v.begin(), v.end());
+            out.push_back((int)v.size());
+            out.insert(out.end(), v.begin(), v.end());
+        }
+    }
+    if (needed) *needed = (long)out.size();
+    if (buf && cap >= (long)out.size()) std::copy(out.begin(), out.end(), buf);
+    else if (buf) throw Error(IBIM_ERR_INVALID_ARGUMENT, "list buffer too small");
+}
+
+}  // namespace ibim
+
+using namespace ibim;
+
+extern "C" {
+
+const char *ibim_last_error(void) { return g_last_error.c_str(); }
+
+const char *ibim_status_string(int st) {
+    switch (st) {
+        case IBIM_OK: return "ok";
+        case IBIM_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case IBIM_ERR_CUDA: return "CUDA error";
+        case IBIM_ERR_OUT_OF_MEMORY: return "out of memory";
+        case IBIM_ERR_UNSUPPORTED_KERNEL: return "unsupported kernel";
+        case IBIM_ERR_LIMIT: return "iteration limit reached";
+        case IBIM_ERR_IO: return "I/O error";
+        default: return "unknown status";
+    }
+}
+
+void ibim_config_default(ibim_config *cfg) {
+    // data/input.cfg and main.cpp constants; geometry left to the caller
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->band = 8;
+    cfg->probe = 1.4;
+    cfg->reinit_t = 60;
+    cfg->thickness = 2;
+    cfg->thres = 1e-4;
+    cfg->np = 4;
+    cfg->maxpoint = 160;
+    cfg->maxlevel = 10;
+    cfg->kp.kappa = 0.1257;
+    cfg->kp.dE = 80.0;
+    cfg->kp.dI = 1.0;
+    cfg->kp.tau = 1.0;
+    cfg->restart = 40;
+    cfg->maxiter = 100;
+    cfg->tol = 1e-5;
+    cfg->precision = IBIM_PRECISION_FP64;
+}
+
+int ibim_ctx_create(int device, ibim_ctx *out) {
+    return guard([&] {
+        IBIM_REQUIRE(out != nullptr, "null output handle");
+        int ndev = 0;
+        IBIM_CUDA(cudaGetDeviceCount(&ndev));
+        IBIM_REQUIRE(device >= 0 && device < ndev, "no such CUDA device");
+        auto *h = new ibim_ctx_s();
+        h->c.device = device;
+        try {
+            IBIM_CUDA(cudaSetDevice(device));
+            IBIM_CUDA(cudaDeviceGetAttribute(&h->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+            IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int ibim_ctx_destroy(ibim_ctx ctx) {
+    return guard([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->c.device);
+        cudaStreamSynchronize(ctx->c.stream);
+        cudaStreamDestroy(ctx->c.stream);
+        delete ctx;
+    });
+}
+
+int ibim_grid_create(ibim_ctx ctx, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value,
+                     ibim_grid *out) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && out, "null handle");
+        bind(&ctx->c);
+        Grid *g = grid_create(&ctx->c, nx, ny, nz, sx, sy, sz, dx, value);
+        *out = new ibim_grid_s{g};
+    });
+}
+
+int ibim_grid_destroy(ibim_grid g) {
+    return guard([&] {
+        if (!g) return;
+        bind(g->g->ctx);
+        delete g->g;
+        delete g;
+    });
+}
+
+int ibim_grid_upload(ibim_grid g, const double *host) {
+    return guard([&] {
+        IBIM_REQUIRE(g && host, "null argument");
+        bind(g->g->ctx);
+        g->g->data.upload(host, g->g->cells());
+        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+    });
+}
+
+int ibim_grid_download(ibim_grid g, double *host) {
+    return guard([&] {
+        IBIM_REQUIRE(g && host, "null argument");
+        bind(g->g->ctx);
+        g->g->data.download(host, g->g->cells());
+        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+    });
+}
+
+int ibim_grid_scale(ibim_grid g, double s) {
+    return guard([&] {
+        IBIM_REQUIRE(g, "null handle");
+        bind(g->g->ctx);
+        grid_scale(*g->g, s);
+    });
+}
+
+int ibim_grid_copy(ibim_grid dst, ibim_grid src) {
+    return guard([&] {
+        IBIM_REQUIRE(dst && src, "null handle");
+        bind(dst->g->ctx);
+        grid_copy(*dst->g, *src->g);
+    });
+}
+
+int ibim_levelset_expand(ibim_grid g, const double *centers, const double *radii, int natoms, double probe, int band) {
+    return guard([&] {
+        IBIM_REQUIRE(g && (natoms == 0 || (centers && radii)), "null argument");
+        IBIM_REQUIRE(natoms >= 0, "natoms must be non-negative");
+        Ctx *c = g->g->ctx;
+        bind(c);
+        DevBuf<double> dc, dr;
+        dc.alloc(3 * (size_t)natoms, c->stream);
+        dr.alloc(natoms, c->stream);
+        dc.upload(centers, 3 * (size_t)natoms);
+        dr.upload(radii, natoms);
+        levelset_expand(*g->g, dc.ptr, dr.ptr, natoms, probe, band);
+        IBIM_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int ibim_levelset_evolve(ibim_grid g, double final_t, double vel, double cfl) {
+    return guard([&] {
+        IBIM_REQUIRE(g, "null handle");
+        bind(g->g->ctx);
+        levelset_evolve(*g->g, final_t, vel, cfl);
+        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+    });
+}
+
+int ibim_levelset_reinitialize(ibim_grid g, ibim_grid phi0, double final_t, double vel, double cfl, int thickness,
+                               double thres, int *steps) {
+    return guard([&] {
+        IBIM_REQUIRE(g && phi0, "null handle");
+        bind(g->g->ctx);
+        const int st = levelset_reinitialize(*g->g, *phi0->g, final_t, vel, cfl, thickness, thres);
+        if (steps) *steps = st;
+    });
+}
+
+int ibim_levelset_count_gradient(ibim_grid g, double thickness, double thres, long *bad, long *total,
+                                 double *accum_error) {
+    return guard([&] {
+        IBIM_REQUIRE(g, "null handle");
+        bind(g->g->ctx);
+        levelset_count_gradient(*g->g, thickness, thres, bad, total, accum_error);
+    });
+}
+
+int ibim_levelset_build(ibim_ctx ctx, const double *centers, const double *radii, int natoms, const ibim_config *cfg,
+                        ibim_grid *out, int steps[2]) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && centers && radii && cfg && out, "null argument");
+        IBIM_REQUIRE(natoms > 0, "need at least one atom");
+        Ctx *c = &ctx->c;
+        bind(c);
+        DevBuf<double> dc, dr;
+        dc.alloc(3 * (size_t)natoms, c->stream);
+        dr.alloc(natoms, c->stream);
+        dc.upload(centers, 3 * (size_t)natoms);
+        dr.upload(radii, natoms);
+        int st[2] = {0, 0};
+        Grid *g = levelset_pipeline(c, dc.ptr, dr.ptr, natoms, *cfg, st);
+        IBIM_CUDA(cudaStreamSynchronize(c->stream));
+        if (steps) { steps[0] = st[0]; steps[1] = st[1]; }
+        *out = new ibim_grid_s{g};
+    });
+}
+
+int ibim_surface_extract(ibim_grid g, int thickness, ibim_tube *out, long *n_points, long *inclusion) {
+    return guard([&] {
+        IBIM_REQUIRE(g && out, "null argument");
+        bind(g->g->ctx);
+        long inc = 0;
+        Tube *t = surface_extract(*g->g, thickness, &inc);
+        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+        if (n_points) *n_points = t->n;
+        if (inclusion) *inclusion = inc;
+        *out = new ibim_tube_s{t};
+    });
+}
+
+int ibim_tube_create(ibim_ctx ctx, const double *points, const double *normals, const double *weights, long n, double h,
+                     ibim_tube *out) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && points && normals && weights && out, "null argument");
+        IBIM_REQUIRE(n > 0 && h > 0, "tube needs n > 0 and h > 0");
+        Ctx *c = &ctx->c;
+        bind(c);
+        Tube *t = new Tube();
+        t->ctx = c;
+        t->n = n;
+        t->h = h;
+        try {
+            std::vector<double> tmp(n);
+            DevBuf<double> *xyz[3] = {&t->x, &t->y, &t->z};
+            DevBuf<double> *nrm[3] = {&t->nx, &t->ny, &t->nz};
+            for (int a = 0; a < 3; ++a) {
+                for (long i = 0; i < n; ++i) tmp[i] = points[3 * i + a];
+                xyz[a]->alloc(n, c->stream);
+                xyz[a]->upload(tmp.data(), n);
+                IBIM_CUDA(cudaStreamSynchronize(c->stream));
+                for (long i = 0; i < n; ++i) tmp[i] = normals[3 * i + a];
+                nrm[a]->alloc(n, c->stream);
+                nrm[a]->upload(tmp.data(), n);
+                IBIM_CUDA(cudaStreamSynchronize(c->stream));
+            }
+            t->w.alloc(n, c->stream);
+            t->w.upload(weights, n);
+            IBIM_CUDA(cudaStreamSynchronize(c->stream));
+        } catch (...) {
+            delete t;
+            throw;
+        }
+        *out = new ibim_tube_s{t};
+    });
+}
+
+int ibim_tube_destroy(ibim_tube t) {
+    return guard([&] {
+        if (!t) return;
+        bind(t->t->ctx);
+        delete t->t;
+        delete t;
+    });
+}
+
+long ibim_tube_size(ibim_tube t) { return t ? t->t->n : -1; }
+
+int ibim_tube_download(ibim_tube t, double *points, double *normals, double *weights) {
+    return guard([&] {
+        IBIM_REQUIRE(t, "null handle");
+        Tube *T = t->t;
+        bind(T->ctx);
+        const long n = T->n;
+        std::vector<double> a(n), b(n), c(n);
+        auto three = [&](DevBuf<double> &X, DevBuf<double> &Y, DevBuf<double> &Z, double *dst) {
+            X.download(a.data(), n);
+            Y.download(b.data(), n);
+            Z.download(c.data(), n);
+            IBIM_CUDA(cudaStreamSynchronize(T->ctx->stream));
+            for (long i = 0; i < n; ++i) {
+                dst[3 * i] = a[i];
+                dst[3 * i + 1] = b[i];
+                dst[3 * i + 2] = c[i];
+            }
+        };
+        if (points) three(T->x, T->y, T->z, points);
+        if (normals) three(T->nx, T->ny, T->nz, normals);
+        if (weights) {
+            T->w.download(weights, n);
+            IBIM_CUDA(cudaStreamSynchronize(T->ctx->stream));
+        }
+    });
+}
+
+int ibim_fmm_plan(ibim_tube src, const double *targets, long nt, int order, int maxpoint, int maxlevel, int precision,
+                  ibim_plan *out) {
+    return guard([&] {
+        IBIM_REQUIRE(src && out, "null argument");
+        IBIM_REQUIRE(targets == nullptr || nt > 0, "targets given with nt <= 0");
+        bind(src->t->ctx);
+        Plan *P = make_plan(src->t, targets == nullptr, targets, targets ? nt : 0, order, maxpoint, maxlevel, precision);
+        *out = new ibim_plan_s{P};
+    });
+}
+
+int ibim_plan_destroy(ibim_plan p) {
+    return guard([&] {
+        if (!p) return;
+        bind(p->p->ctx);
+        delete p->p;
+        delete p;
+    });
+}
+
+int ibim_plan_stats(ibim_plan p, long stats[8]) {
+    return guard([&] {
+        IBIM_REQUIRE(p && stats, "null argument");
+        const Plan &P = *p->p;
+        const TargetSet &S = *P.targets[0];
+        long leaves = 0;
+        for (int i = 0; i < P.tree.nnodes; ++i) leaves += P.tree.leaf[i];
+        stats[0] = P.tree.nnodes;
+        stats[1] = P.tree.nlevels;
+        stats[2] = leaves;
+        stats[3] = S.nvpairs;
+        stats[4] = S.nxpairs;
+        stats[5] = S.near_pairs;
+        stats[6] = P.nops;
+        stats[7] = S.ntleaves;
+    });
+}
+
+int ibim_plan_lists(ibim_plan p, int which, int *buf, long cap, long *needed) {
+    return guard([&] {
+        IBIM_REQUIRE(p && which == 0, "invalid argument");
+        encode_lists(p->p->tree, buf, cap, needed);
+    });
+}
+
+int ibim_tree_lists_host(const double *points, long n, int maxpoint, int maxlevel, int *buf, long cap, long *needed) {
+    return guard([&] {
+        IBIM_REQUIRE(points && n > 0, "null or empty points");
+        TreeHost T = build_tree(points, n, points, n, maxpoint, maxlevel);
+        encode_lists(T, buf, cap, needed);
+    });
+}
+
+int ibim_fmm_apply(ibim_plan p, int kernel, const ibim_kernel_params *kp, const double *in, double *out) {
+    return guard([&] {
+        IBIM_REQUIRE(p && kp && in && out, "null argument");
+        if (kernel < 0 || kernel > IBIM_KERNEL_BIE_FUSED)
+            throw Error(IBIM_ERR_UNSUPPORTED_KERNEL, "kernel id outside the reference's kernel set");
+        Plan &P = *p->p;
+        Ctx *c = P.ctx;
+        bind(c);
+        cudaStream_t s = c->stream;
+        const long ns = P.ns;
+        TargetSet &S = *P.targets[0];
+        const long nt = S.nt;
+        const int rows = kernel == IBIM_KERNEL_BIE_FUSED ? 4 : 1;
+        DevBuf<double> hin;
+        hin.alloc((size_t)rows * ns, s);
+        hin.upload(in, (size_t)rows * ns);
+        P.dens4.zero();
+        if (rows == 4) {
+            for (int d = 0; d < 4; ++d) permute(c, ns, P.src_perm.ptr, hin.ptr + d * ns, P.dens4.ptr + d * ns, false);
+        } else {
+            permute(c, ns, P.src_perm.ptr, hin.ptr, P.dens4.ptr + kKernelMap[kernel].slot * ns, false);
+        }
+        fmm_run(P, 0, *kp, P.dens4.ptr, S.out4.ptr, IBIM_PRECISION_FP64);
+        DevBuf<double> hout;
+        hout.alloc((size_t)rows * nt, s);
+        if (rows == 4) {
+            for (int d = 0; d < 4; ++d) permute(c, nt, S.perm_d.ptr, S.out4.ptr + d * nt, hout.ptr + d * nt, true);
+        } else {
+            permute(c, nt, S.perm_d.ptr, S.out4.ptr + kKernelMap[kernel].field * nt, hout.ptr, true);
+        }
+        hout.download(out, (size_t)rows * nt);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        if (rows == 1 && kKernelMap[kernel].sign < 0)
+            for (long i = 0; i < nt; ++i) out[i] = -out[i];
+    });
+}
+
+int ibim_bie_matvec(ibim_plan p, const ibim_kernel_params *kp, const double *x, double *y) {
+    return guard([&] {
+        IBIM_REQUIRE(p && kp && x && y, "null argument");
+        Plan &P = *p->p;
+        Ctx *c = P.ctx;
+        bind(c);
+        cudaStream_t s = c->stream;
+        const long n = P.ns;
+        DevBuf<double> hx, tx, ty, hy;
+        hx.alloc(2 * n, s);
+        tx.alloc(2 * n, s);
+        ty.alloc(2 * n, s);
+        hy.alloc(2 * n, s);
+        hx.upload(x, 2 * n);
+        permute(c, n, P.src_perm.ptr, hx.ptr, tx.ptr, false);
+        permute(c, n, P.src_perm.ptr, hx.ptr + n, tx.ptr + n, false);
+        bie_matvec(P, *kp, tx.ptr, ty.ptr, IBIM_PRECISION_FP64);
+        permute(c, n, P.src_perm.ptr, ty.ptr, hy.ptr, true);
+        permute(c, n, P.src_perm.ptr, ty.ptr + n, hy.ptr + n, true);
+        hy.download(y, 2 * n);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ibim_bie_rhs(ibim_plan p, const ibim_kernel_params *kp, const double *centers, const double *charges, int natoms,
+                 double *b) {
+    return guard([&] {
+        IBIM_REQUIRE(p && kp && centers && charges && b, "null argument");
+        Plan &P = *p->p;
+        Ctx *c = P.ctx;
+        bind(c);
+        cudaStream_t s = c->stream;
+        const long n = P.ns;
+        DevBuf<double> a4, tb, hb;
+        atoms_to_device(c, centers, charges, natoms, a4);
+        tb.alloc(2 * n, s);
+        hb.alloc(2 * n, s);
+        bie_rhs(P, *kp, a4.ptr, natoms, tb.ptr);
+        permute(c, n, P.src_perm.ptr, tb.ptr, hb.ptr, true);
+        permute(c, n, P.src_perm.ptr, tb.ptr + n, hb.ptr + n, true);
+        hb.download(b, 2 * n);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ibim_gmres_solve(ibim_plan p, const ibim_kernel_params *kp, const double *b, double *x, int restart, int maxiter,
+                     double tol, int precision, int *iters, int *gmres_status, double *residual) {
+    return guard([&] {
+        IBIM_REQUIRE(p && kp && b && x, "null argument");
+        IBIM_REQUIRE(restart > 0 && maxiter > 0, "restart and maxiter must be positive");
+        Plan &P = *p->p;
+        Ctx *c = P.ctx;
+        bind(c);
+        cudaStream_t s = c->stream;
+        const long n = P.ns;
+        DevBuf<double> hb, hx, tb, tx;
+        hb.alloc(2 * n, s);
+        hx.alloc(2 * n, s);
+        tb.alloc(2 * n, s);
+        tx.alloc(2 * n, s);
+        hb.upload(b, 2 * n);
+        hx.upload(x, 2 * n);
+        permute(c, n, P.src_perm.ptr, hb.ptr, tb.ptr, false);
+        permute(c, n, P.src_perm.ptr, hb.ptr + n, tb.ptr + n, false);
+        permute(c, n, P.src_perm.ptr, hx.ptr, tx.ptr, false);
+        permute(c, n, P.src_perm.ptr, hx.ptr + n, tx.ptr + n, false);
+        Krylov K(c, 2 * n, std::min(restart, 250));
+        GmresStats st;
+        auto A = [&](const double *in, double *o) { bie_matvec(P, *kp, in, o, precision); };
+        const int rc = K.solve(A, tx.ptr, tb.ptr, maxiter, tol, false, st);
+        permute(c, n, P.src_perm.ptr, tx.ptr, hx.ptr, true);
+        permute(c, n, P.src_perm.ptr, tx.ptr + n, hx.ptr + n, true);
+        hx.download(x, 2 * n);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        if (iters) *iters = st.iters;
+        if (gmres_status) *gmres_status = rc;
+        if (residual) *residual = st.residual;
+    });
+}
+
+int ibim_electric(ibim_tube tube, const double *centers, const double *charges, int natoms, const ibim_config *cfg,
+                  double *x, double *atom_potential, ibim_result *res) {
+    return guard([&] {
+        IBIM_REQUIRE(tube && centers && charges && cfg && res, "null argument");
+        IBIM_REQUIRE(natoms > 0, "need at least one atom");
+        check_config(*cfg);
+        Tube *T = tube->t;
+        Ctx *c = T->ctx;
+        bind(c);
+        cudaStream_t s = c->stream;
+        std::memset(res, 0, sizeof(*res));
+        res->n_points = T->n;
+        Plan *P = make_plan(T, true, centers, natoms, cfg->np, cfg->maxpoint, cfg->maxlevel, cfg->precision);
+        try {
+            std::vector<double> w(T->n);
+            P->sw.download(w.data(), T->n);
+            IBIM_CUDA(cudaStreamSynchronize(s));
+            double area = 0.;
+            for (long i = 0; i < T->n; ++i) area += w[i];
+            res->area = area;
+            DevBuf<double> a4, xt, xh;
+            atoms_to_device(c, centers, charges, natoms, a4);
+            xt.alloc(2 * T->n, s);
+            std::vector<double> pot;
+            electric_solve(*P, cfg->kp, a4.ptr, charges, natoms, cfg->restart, cfg->maxiter, cfg->tol, cfg->precision,
+                           xt.ptr, &pot, *res);
+            if (x) {
+                xh.alloc(2 * T->n, s);
+                permute(c, T->n, P->src_perm.ptr, xt.ptr, xh.ptr, true);
+                permute(c, T->n, P->src_perm.ptr, xt.ptr + T->n, xh.ptr + T->n, true);
+                xh.download(x, 2 * T->n);
+                IBIM_CUDA(cudaStreamSynchronize(s));
+            }
+            if (atom_potential) std::copy(pot.begin(), pot.end(), atom_potential);
+        } catch (...) {
+            delete P;
+            throw;
+        }
+        delete P;
+    });
+}
+
+int ibim_solve(ibim_ctx ctx, const double *centers, const double *charges, const double *radii, int natoms,
+               const ibim_config *cfg, ibim_result *res) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && centers && charges && radii && cfg && res, "null argument");
+        IBIM_REQUIRE(natoms > 0, "need at least one atom");
+        Ctx *c = &ctx->c;
+        bind(c);
+        DevBuf<double> dc, dr;
+        dc.alloc(3 * (size_t)natoms, c->stream);
+        dr.alloc(natoms, c->stream);
+        dc.upload(centers, 3 * (size_t)natoms);
+        dr.upload(radii, natoms);
+        solve_impl(c, dc.ptr, dr.ptr, centers, charges, natoms, *cfg, *res, nullptr);
+    });
+}
+
+int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charges_dev, const double *radii_dev,
+                   int natoms, const ibim_config *cfg, ibim_result *res) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && centers_dev && charges_dev && radii_dev && cfg && res, "null argument");
+        IBIM_REQUIRE(natoms > 0, "need at least one atom");
+        Ctx *c = &ctx->c;
+        bind(c);
+        // the tree build and the energy sum run on the host: bring the atoms over once
+        std::vector<double> hc(3 * (size_t)natoms), hq(natoms);
+        IBIM_CUDA(cudaMemcpyAsync(hc.data(), centers_dev, sizeof(double) * 3 * natoms, cudaMemcpyDeviceToHost, c->stream));
+        IBIM_CUDA(cudaMemcpyAsync(hq.data(), charges_dev, sizeof(double) * natoms, cudaMemcpyDeviceToHost, c->stream));
+        IBIM_CUDA(cudaStreamSynchronize(c->stream));
+        solve_impl(c, centers_dev, radii_dev, hc.data(), hq.data(), natoms, *cfg, *res, nullptr);
+    });
+}
+
+int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, ibim_result *res) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && pqr_path && cfg && res, "null argument");
+        std::ifstream f(pqr_path);
+        if (!f.is_open()) throw Error(IBIM_ERR_IO, std::string("cannot open ") + pqr_path);
+        std::vector<double> c, q, r;
+        std::string line;
+        // molecule.h:21-50: lines starting with ATOM; tokens 5..9 = x y z charge radius
+        while (std::getline(f, line)) {
+            if (line.rfind("ATOM", 0) != 0) continue;
+            std::istringstream ss(line);
+            std::vector<std::string> tok;
+            std::string t;
+            while (ss >> t) tok.push_back(t);
+            if (tok.size() < 10) throw Error(IBIM_ERR_IO, "malformed ATOM line: " + line);
+            try {
+                c.push_back(std::stod(tok[5]));
+                c.push_back(std::stod(tok[6]));
+                c.push_back(std::stod(tok[7]));
+                q.push_back(std::stod(tok[8]));
+                r.push_back(std::stod(tok[9]));
+            } catch (const std::exception &) {
+                throw Error(IBIM_ERR_IO, "malformed ATOM line: " + line);
+            }
+        }
+        if (q.empty()) throw Error(IBIM_ERR_IO, std::string("no ATOM lines in ") + pqr_path);
+        const int rc = ibim_solve(ctx, c.data(), q.data(), r.data(), (int)q.size(), cfg, res);
+        if (rc != IBIM_OK) throw Error(rc, g_last_error);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,762 @@
+// Black-box Chebyshev FMM on the GPU (sm_103a), FP64 path.
+//
+// Replaces bbfmm::kernel (bbfmm.h:200-624) for the reference's BIE kernel set.  One pass
+// computes the fused 4-density -> 4-field operator (the 16 scalar FMMs of one matvec,
+// electric.cpp:333-367, share one tree and one set of Chebyshev operators, so their sum is
+// one FMM with a 4x4 kernel block):
+//   inputs  m_x, m_y, m_z = phi n w,  psi = dphi w        (electric.cpp:324-329)
+//   outputs F   = K1 . m - K2 psi                           (-> out1, electric.cpp:382)
+//           G_a = sum_b H_ab m_b - K4_a psi, H = K3 block   (-> n . G = tmp1 - tmp2, :372-383)
+// Same approximation as the reference: Chebyshev order p, leaf P2M/L2P through the tensor
+// interpolant S_p (bbfmm.h:392-433), M2M/L2L through the 8 Kronecker operators (:305-367),
+// M2L for V and X lists with the kernel at Chebyshev node pairs (:547-561), direct U and W
+// lists (:577-595).
+//
+// Data layout in HBM: points SoA in tree order (each node owns a contiguous range);
+// multipole / local coefficients per node as [4][p^3] with index z*p^2 + y*p + x.
+// V-list M2L: the kernel at Chebyshev node pairs depends only on (level, source - target
+// lattice offset), so those (4p^3)^2 operators are built once per plan and applied as a
+// batched dense contraction (pairs grouped by operator).
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <tuple>
+
+#include "fmm_common.cuh"
+
+namespace ibim {
+
+// ----------------------------------------------------------------------------------------
+// Tables
+// ----------------------------------------------------------------------------------------
+
+static void cheb_tables_host(int p, ChebTables &T) {
+    std::memset(&T, 0, sizeof(T));
+    T.p = p;
+    T.R = p * p * p;
+    for (int i = 0; i < p; ++i) T.cheb[i] = -std::cos((i + 0.5) * M_PI / p);
+    auto poly = [&](double x, double *out) {
+        out[0] = 1.0;
+        if (p > 1) out[1] = x;
+        for (int k = 2; k < p; ++k) out[k] = 2.0 * x * out[k - 1] - out[k - 2];
+    };
+    for (int m = 0; m < p; ++m) poly(T.cheb[m], T.tnode[m]);
+    // parent -> child transfer S[bit][child node][parent node] (bbfmm.h:305-326)
+    for (int a = 0; a < 2 * p; ++a) {
+        const double x = a < p ? 0.5 * T.cheb[a] - 0.5 : 0.5 * T.cheb[a - p] + 0.5;
+        double tx[MAXP];
+        poly(x, tx);
+        for (int m = 0; m < p; ++m) {
+            double s = 0.;
+            for (int k = 0; k < p; ++k) s += tx[k] * T.tnode[m][k];
+            T.S[a / p][a % p][m] = (-1.0 + 2.0 * s) * (1.0 / p);
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------
+// FP64 kernels
+// ----------------------------------------------------------------------------------------
+
+namespace {
+
+// P2M (upPass leaf, bbfmm.h:507-519): mult[leaf][d][c] = sum_pts S(pt, c) dens[d][pt].
+__global__ void __launch_bounds__(128) k_p2m64(const ChebTables *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ sb, const int *__restrict__ se,
+                                               const double *__restrict__ ctr, const double *__restrict__ rad,
+                                               const double *__restrict__ x, const double *__restrict__ y,
+                                               const double *__restrict__ z, const double *__restrict__ dens, long ns,
+                                               double *mult) {
+    __shared__ ChebTables T;
+    __shared__ double Sp[32][3][MAXP];
+    __shared__ double D[4][32];
+    if (threadIdx.x < sizeof(ChebTables) / 8) reinterpret_cast<double *>(&T)[threadIdx.x] = reinterpret_cast<const double *>(tab)[threadIdx.x];
+    for (int t = threadIdx.x + 128; t < (int)(sizeof(ChebTables) / 8); t += 128)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    const int node = nodes[blockIdx.x];
+    const int b = sb[node], e = se[node];
+    const double c[3] = {ctr[3 * node], ctr[3 * node + 1], ctr[3 * node + 2]};
+    const double r[3] = {rad[3 * node], rad[3 * node + 1], rad[3 * node + 2]};
+    __syncthreads();
+    const int p = T.p, R = T.R;
+    double acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = 0.;
+    for (int base = b; base < e; base += 32) {
+        const int cnt = min(32, e - base);
+        if (threadIdx.x < 96) {
+            const int pt = threadIdx.x / 3, ax = threadIdx.x % 3;
+            if (pt < cnt) {
+                const double *X = ax == 0 ? x : (ax == 1 ? y : z);
+                interp1(T, (X[base + pt] - c[ax]) / r[ax], Sp[pt][ax]);
+            }
+        } else if (threadIdx.x < 128) {
+            const int pt = threadIdx.x - 96;
+            if (pt < cnt)
+                for (int d = 0; d < 4; ++d) D[d][pt] = dens[d * ns + base + pt];
+        }
+        __syncthreads();
+        for (int q = 0; q < 16; ++q) {
+            const int o = threadIdx.x + 128 * q;
+            if (o >= 4 * R) break;
+            const int d = o / R, cc = o % R;
+            const int i = cc % p, j = (cc / p) % p, l = cc / (p * p);
+            double s = acc[q];
+            for (int pt = 0; pt < cnt; ++pt) s += Sp[pt][0][i] * Sp[pt][1][j] * Sp[pt][2][l] * D[d][pt];
+            acc[q] = s;
+        }
+        __syncthreads();
+    }
+    for (int q = 0; q < 16; ++q) {
+        const int o = threadIdx.x + 128 * q;
+        if (o >= 4 * R) break;
+        mult[(long)node * 4 * R + o] = acc[q];
+    }
+}
+
+// One separable Kronecker transfer (R[id] = S[b2] (x) S[b1] (x) S[b0], bbfmm.h:345-366) on a
+// [4][p^3] block in shared memory.  up = true: child -> parent (R^T), else parent -> child (R).
+__device__ void kron_apply(const ChebTables &T, int id, bool up, double *buf, double *tmp, int nthreads) {
+    const int p = T.p, R = T.R;
+    const int b[3] = {id & 1, (id >> 1) & 1, (id >> 2) & 1};
+    // axis 0 (x, stride 1), axis 1 (y, stride p), axis 2 (z, stride p^2)
+    for (int ax = 0; ax < 3; ++ax) {
+        const int stride = ax == 0 ? 1 : (ax == 1 ? p : p * p);
+        double *src = (ax & 1) ? tmp : buf;
+        double *dst = (ax & 1) ? buf : tmp;
+        for (int o = threadIdx.x; o < 4 * R; o += nthreads) {
+            const int d = o / R, cc = o % R;
+            const int idx = (cc / stride) % p;
+            const int base = d * R + cc - idx * stride;
+            double s = 0.;
+            for (int k = 0; k < p; ++k) {
+                // up:   out[n] = sum_k S[b][k][n] in[k];   down: out[k] = sum_n S[b][k][n] in[n]
+                const double w = up ? T.S[b[ax]][k][idx] : T.S[b[ax]][idx][k];
+                s += w * src[base + k * stride];
+            }
+            dst[o] = s;
+        }
+        __syncthreads();
+    }
+    // after 3 passes the result is in tmp (passes wrote tmp, buf, tmp)
+}
+
+// M2M (upPass, bbfmm.h:530-534): parent = sum over non-empty children R[i]^T child.
+__global__ void __launch_bounds__(128) k_m2m64(const ChebTables *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ child_first, const int *__restrict__ empty,
+                                               double *mult) {
+    extern __shared__ double sm[];
+    __shared__ ChebTables T;
+    for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    __syncthreads();
+    const int R = T.R, n4 = 4 * R;
+    double *buf = sm, *tmp = sm + n4, *acc = sm + 2 * n4;
+    const int node = nodes[blockIdx.x];
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] = 0.;
+    const int c0 = child_first[node];
+    for (int c8 = 0; c8 < 8; ++c8) {
+        const int ch = c0 + c8;
+        if (empty[ch]) continue;
+        __syncthreads();
+        for (int o = threadIdx.x; o < n4; o += blockDim.x) buf[o] = mult[(long)ch * n4 + o];
+        __syncthreads();
+        kron_apply(T, c8, true, buf, tmp, blockDim.x);
+        for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] += tmp[o];
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) mult[(long)node * n4 + o] = acc[o];
+}
+
+// L2L (downPass, bbfmm.h:566-567): child += R[index8] parent.
+__global__ void __launch_bounds__(128) k_l2l64(const ChebTables *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ parent, const int *__restrict__ index8,
+                                               double *local) {
+    extern __shared__ double sm[];
+    __shared__ ChebTables T;
+    for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    __syncthreads();
+    const int R = T.R, n4 = 4 * R;
+    double *buf = sm, *tmp = sm + n4;
+    const int node = nodes[blockIdx.x];
+    const int par = parent[node];
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) buf[o] = local[(long)par * n4 + o];
+    __syncthreads();
+    kron_apply(T, index8[node], false, buf, tmp, blockDim.x);
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) local[(long)node * n4 + o] += tmp[o];
+}
+
+// Build the V-list M2L operators: op (level, ox, oy, oz) -> K[col * 4R + row],
+// row = out * R + ct, col = in * R + cs, entry = block(src_cheb(cs) - tgt_cheb(ct))[out][in].
+__global__ void k_make_ops64(const ChebTables *__restrict__ tab, const int *__restrict__ keys,
+                             const double *__restrict__ root_r, KParams kp, double *ops) {
+    const ChebTables &T = *tab;
+    const int op = blockIdx.y;
+    const int p = T.p, R = T.R, n4 = 4 * R;
+    const int lv = keys[4 * op];
+    double r[3];
+    for (int a = 0; a < 3; ++a) {
+        double v = root_r[a];
+        for (int l = 0; l < lv; ++l) v *= 0.5;
+        r[a] = v;
+    }
+    const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (pair >= (long)R * R) return;
+    const int ct = (int)(pair / R), cs = (int)(pair % R);
+    const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
+    const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
+    double d[3];
+    for (int a = 0; a < 3; ++a) {
+        const double off = keys[4 * op + 1 + a] * (2.0 * r[a]);
+        d[a] = (off + r[a] * T.cheb[si[a]]) - r[a] * T.cheb[ti[a]];
+    }
+    double b[16];
+    kblock64(kp, d[0], d[1], d[2], b);
+    double *K = ops + (long)op * n4 * n4;
+    for (int o = 0; o < 4; ++o)
+        for (int in = 0; in < 4; ++in) K[(long)(in * R + cs) * n4 + (o * R + ct)] = b[o * 4 + in];
+}
+
+// V-list M2L as a batched contraction: chunk = (op, first pair, count <= M2L_CH); every
+// thread owns rows r = tid + 256 q of the 4R outputs for all pairs of the chunk.
+constexpr int M2L_CH = 8;
+__global__ void __launch_bounds__(256) k_m2l_v64(int n4, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+                                                 const int *__restrict__ vtgt, const double *__restrict__ ops,
+                                                 const double *__restrict__ mult, double *local) {
+    extern __shared__ double Ms[];  // [M2L_CH][n4]
+    const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
+    for (int j = 0; j < cnt; ++j) {
+        const double *src = mult + (long)vsrc[b + j] * n4;
+        for (int o = threadIdx.x; o < n4; o += blockDim.x) Ms[j * n4 + o] = src[o];
+    }
+    __syncthreads();
+    const double *K = ops + (long)op * n4 * n4;
+    constexpr int MAXQ = 8;  // n4 <= 2048
+    double acc[MAXQ][M2L_CH];
+#pragma unroll
+    for (int q = 0; q < MAXQ; ++q)
+#pragma unroll
+        for (int j = 0; j < M2L_CH; ++j) acc[q][j] = 0.;
+    const int nq = (n4 + 255) / 256;
+    for (int col = 0; col < n4; ++col) {
+        const double *Kc = K + (long)col * n4;
+#pragma unroll
+        for (int q = 0; q < MAXQ; ++q) {
+            if (q >= nq) break;
+            const int row = threadIdx.x + 256 * q;
+            const double a = row < n4 ? __ldg(Kc + row) : 0.;
+#pragma unroll
+            for (int j = 0; j < M2L_CH; ++j) acc[q][j] += a * Ms[j * n4 + col];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < MAXQ; ++q) {
+        if (q >= nq) break;
+        const int row = threadIdx.x + 256 * q;
+        if (row >= n4) continue;
+#pragma unroll
+        for (int j = 0; j < M2L_CH; ++j)
+            if (j < cnt) atomicAdd(local + (long)vtgt[b + j] * n4 + row, acc[q][j]);
+    }
+}
+
+// X-list M2L (bbfmm.h:556-560): coarser leaf -> node, kernel evaluated on the fly.
+__global__ void __launch_bounds__(128) k_m2l_x64(const ChebTables *__restrict__ tab, KParams kp,
+                                                 const int *__restrict__ xsrc, const int *__restrict__ xtgt,
+                                                 const double *__restrict__ ctr, const double *__restrict__ rad,
+                                                 const double *__restrict__ mult, double *local) {
+    __shared__ ChebTables T;
+    __shared__ double M[4 * MAXR];
+    __shared__ double sp[3][MAXP], tp[3][MAXP];
+    for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    __syncthreads();
+    const int s = xsrc[blockIdx.x], t = xtgt[blockIdx.x];
+    const int p = T.p, R = T.R;
+    for (int o = threadIdx.x; o < 4 * R; o += blockDim.x) M[o] = mult[(long)s * 4 * R + o];
+    if (threadIdx.x < 3 * p) {
+        const int a = threadIdx.x / p, m = threadIdx.x % p;
+        sp[a][m] = ctr[3 * s + a] + rad[3 * s + a] * T.cheb[m];
+        tp[a][m] = ctr[3 * t + a] + rad[3 * t + a] * T.cheb[m];
+    }
+    __syncthreads();
+    for (int ct = threadIdx.x; ct < R; ct += blockDim.x) {
+        const double tx = tp[0][ct % p], ty = tp[1][(ct / p) % p], tz = tp[2][ct / (p * p)];
+        double acc[4] = {0., 0., 0., 0.};
+        for (int cs = 0; cs < R; ++cs) {
+            double b[16];
+            kblock64(kp, sp[0][cs % p] - tx, sp[1][(cs / p) % p] - ty, sp[2][cs / (p * p)] - tz, b);
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+#pragma unroll
+                for (int in = 0; in < 4; ++in) acc[o] += b[o * 4 + in] * M[in * R + cs];
+        }
+        for (int o = 0; o < 4; ++o) atomicAdd(local + (long)t * 4 * R + o * R + ct, acc[o]);
+    }
+}
+
+// Near field + L2P for one target leaf per block (downPass leaf, bbfmm.h:571-609): U and W
+// lists direct (source ranges in tree order), then the local expansion at the targets.
+// Threads = targets x source phases; sources staged in shared memory tiles.
+constexpr int NEAR_T = 128, NEAR_TILE = 128;
+__global__ void __launch_bounds__(NEAR_T) k_near64(const ChebTables *__restrict__ tab, KParams kp,
+                                                   const int *__restrict__ tleaf, const int *__restrict__ near_ptr,
+                                                   const int *__restrict__ near_range, const int *__restrict__ tb_,
+                                                   const int *__restrict__ te_, const double *__restrict__ ctr,
+                                                   const double *__restrict__ rad, const double *__restrict__ sx,
+                                                   const double *__restrict__ sy, const double *__restrict__ sz,
+                                                   const double *__restrict__ dens, long ns,
+                                                   const double *__restrict__ tx, const double *__restrict__ ty,
+                                                   const double *__restrict__ tz, long nt,
+                                                   const double *__restrict__ local, double *out) {
+    __shared__ ChebTables T;
+    __shared__ double S[7][NEAR_TILE];
+    __shared__ double red[NEAR_T][4];
+    for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    const int leaf = tleaf[blockIdx.x];
+    const int tb = tb_[leaf], te = te_[leaf];
+    const int r0 = near_ptr[blockIdx.x], r1 = near_ptr[blockIdx.x + 1];
+    __syncthreads();
+    for (int t0 = tb; t0 < te; t0 += NEAR_T) {
+        const int nT = min(NEAR_T, te - t0);
+        const int nph = NEAR_T / nT;
+        const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
+        const bool active = ph < nph;
+        double X = 0, Y = 0, Z = 0;
+        if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
+        double acc[4] = {0., 0., 0., 0.};
+        for (int rr = r0; rr < r1; ++rr) {
+            const int b = near_range[2 * rr], e = near_range[2 * rr + 1];
+            for (int s0 = b; s0 < e; s0 += NEAR_TILE) {
+                const int cnt = min(NEAR_TILE, e - s0);
+                __syncthreads();
+                for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+                    S[0][q] = sx[s0 + q];
+                    S[1][q] = sy[s0 + q];
+                    S[2][q] = sz[s0 + q];
+                    S[3][q] = dens[s0 + q];
+                    S[4][q] = dens[ns + s0 + q];
+                    S[5][q] = dens[2 * ns + s0 + q];
+                    S[6][q] = dens[3 * ns + s0 + q];
+                }
+                __syncthreads();
+                if (active)
+                    for (int q = ph; q < cnt; q += nph)
+                        near_pair64(kp, S[0][q] - X, S[1][q] - Y, S[2][q] - Z, S[3][q], S[4][q], S[5][q], S[6][q],
+                                    acc);
+            }
+        }
+        for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = acc[o];
+        __syncthreads();
+        if (threadIdx.x < nT) {
+            double f[4] = {0., 0., 0., 0.};
+            for (int q = 0; q < nph; ++q)
+                for (int o = 0; o < 4; ++o) f[o] += red[threadIdx.x + q * nT][o];
+            // L2P (bbfmm.h:600): local expansion at the target
+            double Sp[3][MAXP];
+            const double xyz[3] = {X, Y, Z};
+            for (int a = 0; a < 3; ++a) interp1(T, (xyz[a] - ctr[3 * leaf + a]) / rad[3 * leaf + a], Sp[a]);
+            const int p = T.p, R = T.R;
+            const double *L = local + (long)leaf * 4 * R;
+            double l2p[4] = {0., 0., 0., 0.};
+            for (int c = 0; c < R; ++c) {
+                const double w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                for (int o = 0; o < 4; ++o) l2p[o] += w * L[o * R + c];
+            }
+            for (int o = 0; o < 4; ++o) out[o * nt + t0 + threadIdx.x] = f[o] + l2p[o];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------
+// Plan
+// ----------------------------------------------------------------------------------------
+
+namespace {
+__global__ void k_gather(long n, const int *__restrict__ perm, const double *__restrict__ a, double *b, double scale) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        b[i] = a[perm[i]] * scale;
+}
+
+void up_int(DevBuf<int> &b, const std::vector<int> &v, cudaStream_t s) {
+    b.alloc(std::max<size_t>(1, v.size()), s);
+    b.upload(v.data(), v.size());
+}
+}  // namespace
+
+void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale) {
+    if (n <= 0) return;
+    k_gather<<<(int)std::min<long>(4L * c->num_sms, div_up(n, 256)), 256, 0, c->stream>>>(n, perm, a, b, scale);
+    IBIM_CHECK_LAUNCH();
+}
+
+// Work lists of one target set: which nodes need locals, V pairs by operator, X pairs, and
+// per target leaf the merged source ranges of its U and W lists.
+static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, int, int, int>, int> &opid) {
+    const TreeHost &T = P.tree;
+    cudaStream_t s = P.ctx->stream;
+    const int nn = T.nnodes;
+    auto has_t = [&](int i) { return S.end[i] > S.begin[i]; };
+    auto has_s = [&](int i) { return T.src_end[i] > T.src_begin[i]; };
+    std::vector<int> l2l, lb(T.nlevels + 1, 0);
+    for (int l = 0; l < T.nlevels; ++l) {
+        lb[l] = (int)l2l.size();
+        for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i)
+            if (l >= 3 && has_t(i)) l2l.push_back(i);
+    }
+    lb[T.nlevels] = (int)l2l.size();
+    S.l2l_level_begin = lb;
+    up_int(S.l2l_nodes, l2l, s);
+    std::vector<std::vector<std::pair<int, int>>> byop;
+    std::vector<int> xs, xt;
+    for (int l = 0; l < T.nlevels; ++l)
+        for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i) {
+            if (!has_t(i)) continue;
+            for (int sidx : T.V[i]) {
+                if (!has_s(sidx)) continue;
+                auto key = std::make_tuple(l, T.coord[3 * sidx] - T.coord[3 * i], T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
+                                           T.coord[3 * sidx + 2] - T.coord[3 * i + 2]);
+                auto it = opid.find(key);
+                int id;
+                if (it == opid.end()) {
+                    id = (int)opid.size();
+                    opid[key] = id;
+                } else {
+                    id = it->second;
+                }
+                if ((int)byop.size() <= id) byop.resize(id + 1);
+                byop[id].push_back({sidx, i});
+            }
+            for (int sidx : T.X[i]) {
+                if (!has_s(sidx)) continue;
+                xs.push_back(sidx);
+                xt.push_back(i);
+            }
+        }
+    std::vector<int> vs, vt, chunks;
+    for (int op = 0; op < (int)byop.size(); ++op) {
+        const int b = (int)vs.size();
+        for (auto &pr : byop[op]) {
+            vs.push_back(pr.first);
+            vt.push_back(pr.second);
+        }
+        for (int q = 0; q < (int)byop[op].size(); q += M2L_CH) {
+            chunks.push_back(op);
+            chunks.push_back(b + q);
+            chunks.push_back(std::min<int>(M2L_CH, (int)byop[op].size() - q));
+        }
+    }
+    S.nvpairs = (long)vs.size();
+    S.nchunks = (int)chunks.size() / 3;
+    up_int(S.v_src, vs, s);
+    up_int(S.v_tgt, vt, s);
+    up_int(S.v_chunk, chunks, s);
+    S.nxpairs = (long)xs.size();
+    up_int(S.x_src, xs, s);
+    up_int(S.x_tgt, xt, s);
+    std::vector<int> tl, nptr{0}, nr;
+    long npairs = 0;
+    for (int i = 0; i < nn; ++i) {
+        if (!T.leaf[i] || !has_t(i)) continue;
+        std::vector<std::pair<int, int>> rg;
+        for (int sidx : T.U[i])
+            if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
+        for (int sidx : T.W[i])
+            if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
+        std::sort(rg.begin(), rg.end());
+        std::vector<std::pair<int, int>> mg;
+        for (auto &r : rg) {
+            if (!mg.empty() && mg.back().second == r.first)
+                mg.back().second = r.second;
+            else
+                mg.push_back(r);
+        }
+        tl.push_back(i);
+        long nsrc = 0;
+        for (auto &r : mg) {
+            nr.push_back(r.first);
+            nr.push_back(r.second);
+            nsrc += r.second - r.first;
+        }
+        npairs += nsrc * (S.end[i] - S.begin[i]);
+        nptr.push_back((int)nr.size() / 2);
+    }
+    S.ntleaves = (int)tl.size();
+    S.near_pairs = npairs;
+    up_int(S.tleaf, tl, s);
+    up_int(S.near_ptr, nptr, s);
+    up_int(S.near_range, nr, s);
+    up_int(S.tbeg, S.begin, s);
+    up_int(S.tend, S.end, s);
+    S.out4.alloc((size_t)4 * std::max<long>(1, S.nt), s);
+}
+
+// Extra targets (e.g. atom centres): descend the source tree with the split rule of
+// assignChildren (bbfmm.cpp:121-131) and keep each node's targets contiguous in DFS order.
+static void bin_targets(Plan &P, TargetSet &S, const double *pts, long nt, const std::vector<int> &child_first) {
+    const TreeHost &T = P.tree;
+    const int nn = T.nnodes;
+    std::vector<int> dfs(nn, 0);
+    {
+        std::vector<int> stack{0};
+        int k = 0;
+        while (!stack.empty()) {
+            const int n = stack.back();
+            stack.pop_back();
+            dfs[n] = k++;
+            if (!T.leaf[n])
+                for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
+        }
+    }
+    std::vector<int> leaf_of(nt);
+    for (long i = 0; i < nt; ++i) {
+        const double *x = pts + 3 * i;
+        int n = 0;
+        while (!T.leaf[n]) {
+            const double *c = &T.center[3 * n];
+            const int ch = 4 * (x[2] < c[2] ? 0 : 1) + 2 * (x[1] < c[1] ? 0 : 1) + (x[0] < c[0] ? 0 : 1);
+            n = child_first[n] + ch;
+        }
+        leaf_of[i] = n;
+    }
+    S.perm.resize(nt);
+    for (long i = 0; i < nt; ++i) S.perm[i] = (int)i;
+    std::stable_sort(S.perm.begin(), S.perm.end(), [&](int a, int b) { return dfs[leaf_of[a]] < dfs[leaf_of[b]]; });
+    S.begin.assign(nn, 0);
+    S.end.assign(nn, 0);
+    std::vector<int> cnt(nn, 0);
+    for (long i = 0; i < nt; ++i) cnt[leaf_of[i]]++;
+    // leaves in DFS order get consecutive ranges; internal nodes span their children
+    std::vector<int> order(nn);
+    for (int i = 0; i < nn; ++i) order[dfs[i]] = i;
+    int off = 0;
+    for (int q = 0; q < nn; ++q) {
+        const int n = order[q];
+        if (T.leaf[n]) {
+            S.begin[n] = off;
+            S.end[n] = off + cnt[n];
+            off += cnt[n];
+        }
+    }
+    for (int n = nn - 1; n >= 0; --n)
+        if (!T.leaf[n]) {
+            S.begin[n] = S.begin[child_first[n]];
+            S.end[n] = S.end[child_first[n] + 7];
+        }
+}
+
+Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int order, int maxpoint, int maxlevel,
+                int precision) {
+    IBIM_REQUIRE(order >= 2 && order <= MAXP, "fmm_np must be in [2, 8]");
+    IBIM_REQUIRE(t && t->n > 0, "plan needs a non-empty tube");
+    IBIM_REQUIRE(with_self || (extra && n_extra > 0), "plan needs targets");
+    Ctx *c = t->ctx;
+    cudaStream_t s = c->stream;
+    const long ns = t->n;
+    std::vector<double> pts(3 * ns);
+    {
+        std::vector<double> hx(ns), hy(ns), hz(ns);
+        t->x.download(hx.data(), ns);
+        t->y.download(hy.data(), ns);
+        t->z.download(hz.data(), ns);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        for (long i = 0; i < ns; ++i) {
+            pts[3 * i] = hx[i];
+            pts[3 * i + 1] = hy[i];
+            pts[3 * i + 2] = hz[i];
+        }
+    }
+    Plan *P = new Plan();
+    P->ctx = c;
+    P->tube = t;
+    P->ns = ns;
+    P->p = order;
+    P->R = order * order * order;
+    P->maxpoint = maxpoint;
+    P->maxlevel = maxlevel;
+    P->precision = precision;
+    try {
+        P->tree = build_tree(pts.data(), ns, pts.data(), ns, maxpoint, maxlevel);
+        TreeHost &T = P->tree;
+        const int nn = T.nnodes, R = P->R, n4 = 4 * R;
+        T.p = order;
+        T.R = R;
+        P->src_perm.alloc(ns, s);
+        P->src_perm.upload(T.src_perm.data(), ns);
+        DevBuf<double> *dst[7] = {&P->sx, &P->sy, &P->sz, &P->snx, &P->sny, &P->snz, &P->sw};
+        const DevBuf<double> *srcs[7] = {&t->x, &t->y, &t->z, &t->nx, &t->ny, &t->nz, &t->w};
+        const double h3 = t->h * t->h * t->h;
+        for (int k = 0; k < 7; ++k) {
+            dst[k]->alloc(ns, s);
+            // quadrature weight = w * s * h^3 with s = 1 (electric.cpp:33)
+            plan_gather(c, ns, P->src_perm.ptr, srcs[k]->ptr, dst[k]->ptr, k == 6 ? h3 : 1.0);
+        }
+        P->ncenter.alloc(3 * nn, s);
+        P->ncenter.upload(T.center.data(), 3 * nn);
+        P->nradius.alloc(3 * nn, s);
+        P->nradius.upload(T.radius.data(), 3 * nn);
+        up_int(P->nsrc_begin, T.src_begin, s);
+        up_int(P->nsrc_end, T.src_end, s);
+        up_int(P->nparent, T.parent, s);
+        up_int(P->nindex8, T.index8, s);
+        up_int(P->nempty, T.empty, s);
+        std::vector<int> child_first(nn, -1);
+        for (int i = nn - 1; i >= 0; --i)
+            if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
+        up_int(P->nchild_first, child_first, s);
+        auto has_s = [&](int i) { return T.src_end[i] > T.src_begin[i]; };
+        std::vector<int> p2m, m2m, m2m_lb(T.nlevels + 1, 0);
+        for (int i = 0; i < nn; ++i)
+            if (T.leaf[i] && has_s(i)) p2m.push_back(i);
+        for (int l = 0; l < T.nlevels; ++l) {
+            m2m_lb[l] = (int)m2m.size();
+            for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i)
+                if (!T.leaf[i] && has_s(i)) m2m.push_back(i);
+        }
+        m2m_lb[T.nlevels] = (int)m2m.size();
+        up_int(P->p2m_nodes, p2m, s);
+        up_int(P->m2m_nodes, m2m, s);
+        P->m2m_level_begin = m2m_lb;
+        P->np2m = (int)p2m.size();
+        std::map<std::tuple<int, int, int, int>, int> opid;
+        if (with_self) {
+            TargetSet *S = new TargetSet();
+            P->targets.push_back(S);
+            S->self = true;
+            S->nt = ns;
+            S->begin = T.src_begin;
+            S->end = T.src_end;
+            S->perm = T.src_perm;
+            up_int(S->perm_d, S->perm, s);
+            build_target_lists(*P, *S, opid);
+        }
+        if (extra && n_extra > 0) {
+            TargetSet *S = new TargetSet();
+            P->targets.push_back(S);
+            S->nt = n_extra;
+            bin_targets(*P, *S, extra, n_extra, child_first);
+            std::vector<double> tq[3];
+            for (int a = 0; a < 3; ++a) {
+                tq[a].resize(n_extra);
+                for (long i = 0; i < n_extra; ++i) tq[a][i] = extra[3 * (long)S->perm[i] + a];
+            }
+            S->tx.alloc(n_extra, s);
+            S->ty.alloc(n_extra, s);
+            S->tz.alloc(n_extra, s);
+            S->tx.upload(tq[0].data(), n_extra);
+            S->ty.upload(tq[1].data(), n_extra);
+            S->tz.upload(tq[2].data(), n_extra);
+            up_int(S->perm_d, S->perm, s);
+            build_target_lists(*P, *S, opid);
+        }
+        P->nops = (int)opid.size();
+        P->op_key_h.assign(4 * std::max(1, P->nops), 0);
+        for (auto &kv : opid) {
+            P->op_key_h[4 * kv.second] = std::get<0>(kv.first);
+            P->op_key_h[4 * kv.second + 1] = std::get<1>(kv.first);
+            P->op_key_h[4 * kv.second + 2] = std::get<2>(kv.first);
+            P->op_key_h[4 * kv.second + 3] = std::get<3>(kv.first);
+        }
+        up_int(P->op_key, P->op_key_h, s);
+        ChebTables ht;
+        cheb_tables_host(order, ht);
+        P->tables.alloc(1, s);
+        P->tables.upload(&ht, 1);
+        P->root_r.alloc(3, s);
+        P->root_r.upload(T.radius.data(), 3);
+        P->mult.alloc((size_t)nn * n4, s);
+        P->local.alloc((size_t)nn * n4, s);
+        P->dens4.alloc((size_t)4 * ns, s);
+        const size_t smem_k = sizeof(double) * 3 * n4;
+        if (smem_k > 48 * 1024) {
+            IBIM_CUDA(cudaFuncSetAttribute(k_m2m64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+            IBIM_CUDA(cudaFuncSetAttribute(k_l2l64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+        }
+        const size_t sm = sizeof(double) * M2L_CH * n4;
+        if (sm > 48 * 1024)
+            IBIM_CUDA(cudaFuncSetAttribute(k_m2l_v64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        IBIM_CUDA(cudaStreamSynchronize(s));
+    } catch (...) {
+        delete P;
+        throw;
+    }
+    return P;
+}
+
+void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision) {
+    const double key[4] = {kp.kappa, kp.dE, kp.dI, kp.tau};
+    bool same = P.ops_precision == precision;
+    for (int i = 0; i < 4; ++i) same = same && P.kp_cache[i] == key[i];
+    if (same || P.nops == 0) return;
+    cudaStream_t s = P.ctx->stream;
+    const int R = P.R, n4 = 4 * R;
+    const KParams k = make_kparams(kp, P.tube->h);
+    if (precision == IBIM_PRECISION_FP64) {
+        P.ops64.alloc((size_t)P.nops * n4 * n4, s);
+        dim3 g(div_up((long)R * R, 256), P.nops);
+        k_make_ops64<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops64.ptr);
+        IBIM_CHECK_LAUNCH();
+    } else {
+        fmm_prepare_operators_mixed(P, k);
+    }
+    for (int i = 0; i < 4; ++i) P.kp_cache[i] = key[i];
+    P.ops_precision = precision;
+}
+
+// One FP64 FMM: dens (4 x ns, tree order) -> out (4 x nt of target set ts, tree order).
+void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out) {
+    IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
+    fmm_prepare_operators(P, kpp, IBIM_PRECISION_FP64);
+    const TargetSet &S = *P.targets[ts];
+    cudaStream_t s = P.ctx->stream;
+    const TreeHost &T = P.tree;
+    const int R = P.R, n4 = 4 * R;
+    const KParams kp = make_kparams(kpp, P.tube->h);
+    const size_t smem_k = sizeof(double) * 3 * n4;
+    if (P.np2m > 0)
+        k_p2m64<<<P.np2m, 128, 0, s>>>(P.tables.ptr, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
+                                       P.ncenter.ptr, P.nradius.ptr, P.sx.ptr, P.sy.ptr, P.sz.ptr, dens, P.ns,
+                                       P.mult.ptr);
+    for (int l = T.nlevels - 1; l >= 0; --l) {
+        const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
+        if (e > b)
+            k_m2m64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
+                                               P.mult.ptr);
+    }
+    P.local.zero();
+    if (S.nchunks > 0)
+        k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
+                                                                       P.ops64.ptr, P.mult.ptr, P.local.ptr);
+    if (S.nxpairs > 0)
+        k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
+                                                 P.nradius.ptr, P.mult.ptr, P.local.ptr);
+    for (int l = 3; l < T.nlevels; ++l) {
+        const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
+        if (e > b)
+            k_l2l64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
+                                               P.local.ptr);
+    }
+    const double *tx = S.self ? P.sx.ptr : S.tx.ptr;
+    const double *ty = S.self ? P.sy.ptr : S.ty.ptr;
+    const double *tz = S.self ? P.sz.ptr : S.tz.ptr;
+    if (S.ntleaves > 0)
+        k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
+                                               S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
+                                               P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out);
+    IBIM_CHECK_LAUNCH();
+}
+
+void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out, int precision) {
+    if (precision == IBIM_PRECISION_FP64)
+        fmm_run_fp64(P, ts, kp, dens, out);
+    else
+        fmm_run_mixed(P, ts, kp, dens, out);
+}
+
+}  // namespace ibim

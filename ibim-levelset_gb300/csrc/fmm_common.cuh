@@ -1,0 +1,111 @@
+// Device helpers shared by the FMM translation units: Chebyshev tables, the fused BIE kernel
+// block and the near-field pair update.
+#pragma once
+
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace ibim {
+
+constexpr int MAXP = 8;
+constexpr int MAXR = MAXP * MAXP * MAXP;
+
+// Chebyshev nodes, polynomials and parent -> child transfers for order p (bbfmm.h:273-326).
+struct ChebTables {
+    double cheb[MAXP];           // -cos((i + 1/2) pi / p)
+    double tnode[MAXP][MAXP];    // T_k(cheb_m): [m][k]
+    double S[2][MAXP][MAXP];     // S_p(child node, parent node) for the lower (0) / upper (1) half
+    int p, R;
+};
+
+// Kernel parameters, prepared once (electric.cpp:52-58, :96-97).
+struct KParams {
+    double kappa, eps, ieps, vr, k2in, q4pi;
+};
+
+inline KParams make_kparams(const ibim_kernel_params &kp, double h) {
+    KParams k;
+    k.kappa = kp.kappa;
+    k.eps = kp.dE / kp.dI;
+    k.ieps = kp.dI / kp.dE;
+    k.vr = kp.tau * h;
+    k.k2in = kp.kappa == 0. ? 0. : (std::exp(-kp.kappa * k.vr) - 1.0 + kp.kappa * k.vr) / kp.kappa / 2.0 / M_PI / k.vr / k.vr;
+    k.q4pi = 1.0 / (4.0 * M_PI);
+    return k;
+}
+
+// S_p(x, cheb_m), m < p: (-1 + 2 sum_k T_k(x) T_k(cheb_m)) / p (bbfmm.h:409-419).
+__device__ __forceinline__ void interp1(const ChebTables &T, double x, double *out) {
+    double Tk[MAXP];
+    Tk[0] = 1.0;
+    Tk[1] = x;
+    for (int k = 2; k < T.p; ++k) Tk[k] = 2.0 * x * Tk[k - 1] - Tk[k - 2];
+    for (int m = 0; m < T.p; ++m) {
+        double s = 0.;
+        for (int k = 0; k < T.p; ++k) s += Tk[k] * T.tnode[m][k];
+        out[m] = (-1.0 + 2.0 * s) * (1.0 / T.p);
+    }
+}
+
+// Fused 4x4 block of the 16 BIE kernels (electric.cpp:67-291) at d = source - target.
+// Rows: F, Gx, Gy, Gz.  Columns: m_x, m_y, m_z, psi.
+__device__ __forceinline__ void kblock64(const KParams &k, double dx, double dy, double dz, double b[16]) {
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double r = sqrt(d2);
+    if (r < k.vr) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) b[i] = 0.;
+        b[3] = -k.k2in;
+        return;
+    }
+    const double t = k.kappa * r;
+    const double e = exp(-t);
+    const double ir3 = 1.0 / (r * d2);
+    const double et1 = e * (t + 1);
+    const double c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
+    const double c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
+    const double k2 = (1.0 - e) / r * k.q4pi;
+    const double hd = (1 - et1) * ir3;
+    const double ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 / d2;
+    const double dd[3] = {dx, dy, dz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b[a] = dd[a] * c1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) b[4 * (a + 1) + c] = ho * dd[a] * dd[c] + (a == c ? hd : 0.);
+        b[4 * (a + 1) + 3] = -dd[a] * c4;
+    }
+    b[3] = -k2;
+}
+
+// One near-field source -> target update of the fused block (same formulas as kblock64).
+__device__ __forceinline__ void near_pair64(const KParams &k, double dx, double dy, double dz, double m0, double m1,
+                                            double m2, double psi, double acc[4]) {
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double r = sqrt(d2);
+    if (r < k.vr) {
+        acc[0] -= k.k2in * psi;
+        return;
+    }
+    const double t = k.kappa * r;
+    const double e = exp(-t);
+    const double ir3 = 1.0 / (r * d2);
+    const double et1 = e * (t + 1);
+    const double c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
+    const double c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
+    const double k2 = (1.0 - e) / r * k.q4pi;
+    const double hd = (1 - et1) * ir3;
+    const double ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 / d2;
+    const double dm = dx * m0 + dy * m1 + dz * m2;
+    acc[0] += c1 * dm - k2 * psi;
+    const double cm = ho * dm - c4 * psi;
+    acc[1] += hd * m0 + dx * cm;
+    acc[2] += hd * m1 + dy * cm;
+    acc[3] += hd * m2 + dz * cm;
+}
+
+void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale);
+void fmm_prepare_operators_mixed(Plan &P, const KParams &k);
+
+}  // namespace ibim

@@ -1,0 +1,213 @@
+// Internal types shared by the translation units of libibim_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ibim.h"
+
+namespace ibim {
+
+// Thrown inside the library, converted to a status at the C ABI.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define IBIM_CUDA(call)                                                                                       \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                \
+            throw ::ibim::Error(e_ == cudaErrorMemoryAllocation ? IBIM_ERR_OUT_OF_MEMORY : IBIM_ERR_CUDA,     \
+                                std::string(#call) + ": " + cudaGetErrorString(e_) + " at " + __FILE__ + ":" + \
+                                    std::to_string(__LINE__));                                                \
+    } while (0)
+
+#define IBIM_CHECK_LAUNCH() IBIM_CUDA(cudaGetLastError())
+
+#define IBIM_REQUIRE(cond, msg)                                                   \
+    do {                                                                          \
+        if (!(cond)) throw ::ibim::Error(IBIM_ERR_INVALID_ARGUMENT, (msg));       \
+    } while (0)
+
+// Stream-ordered device buffer owned by a context.
+template <typename T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t n = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), n(o.n), stream(o.stream) { o.ptr = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept {
+        if (this != &o) { release(); ptr = o.ptr; n = o.n; stream = o.stream; o.ptr = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count, cudaStream_t s) {
+        release();
+        stream = s;
+        n = count;
+        if (count) IBIM_CUDA(cudaMallocAsync((void **)&ptr, sizeof(T) * count, s));
+    }
+    void release() {
+        if (ptr) cudaFreeAsync(ptr, stream);
+        ptr = nullptr;
+        n = 0;
+    }
+    void zero() { if (n) IBIM_CUDA(cudaMemsetAsync(ptr, 0, sizeof(T) * n, stream)); }
+    void upload(const T *h, size_t count) {
+        if (count > n) alloc(count, stream);
+        if (count) IBIM_CUDA(cudaMemcpyAsync(ptr, h, sizeof(T) * count, cudaMemcpyHostToDevice, stream));
+    }
+    void upload(const std::vector<T> &v) { if (v.size() > n || !ptr) alloc(v.size(), stream); upload(v.data(), v.size()); }
+    void download(T *h, size_t count) const {
+        if (count) IBIM_CUDA(cudaMemcpyAsync(h, ptr, sizeof(T) * count, cudaMemcpyDeviceToHost, stream));
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    cudaEvent_t ev[8];
+};
+
+struct Grid {
+    Ctx *ctx;
+    int nx, ny, nz;
+    double sx, sy, sz, dx;
+    DevBuf<double> data;
+    long cells() const { return (long)nx * ny * nz; }
+};
+
+// Tube points, SoA, in the reference's (i, j, k) extraction order.
+struct Tube {
+    Ctx *ctx;
+    long n = 0;
+    double h = 0;
+    DevBuf<double> x, y, z, nx, ny, nz, w;  // w = raw cosine weight (levelset.cpp:576)
+};
+
+// Octree + interaction lists, host side (tree.cpp).  Node ids are level-ordered.
+struct TreeHost {
+    int p = 0, R = 0;
+    int nnodes = 0, nlevels = 0;
+    std::vector<int> level_begin;        // size nlevels + 1
+    std::vector<double> center, radius;  // 3 per node
+    std::vector<int> parent, index8, leaf, empty, coord;  // coord: 3 ints per node
+    std::vector<int> src_begin, src_end, tgt_begin, tgt_end;
+    std::vector<int> src_perm, tgt_perm;  // tree position -> caller index
+    std::vector<int> ref_id;              // node id in the reference's numbering (bbfmm.cpp:88-91)
+    // lists (sorted node ids per node)
+    std::vector<std::vector<int>> U, V, W, X;
+};
+
+TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int maxpoint, int maxlevel);
+
+struct ChebTables;
+
+// Targets binned into a plan's tree, with the work lists that depend on them.
+struct TargetSet {
+    long nt = 0;
+    bool self = false;                 // the plan's sources
+    std::vector<int> begin, end;       // per node, range in tree-ordered targets
+    std::vector<int> perm;             // tree position -> caller index
+    DevBuf<double> tx, ty, tz;         // tree order (self: unused, the source arrays are used)
+    DevBuf<int> perm_d, tbeg, tend;
+    std::vector<int> l2l_level_begin;
+    DevBuf<int> l2l_nodes;
+    DevBuf<int> v_src, v_tgt, v_chunk; // V pairs sorted by operator; chunks (op, begin, count)
+    int nchunks = 0;
+    long nvpairs = 0;
+    DevBuf<int> x_src, x_tgt;
+    long nxpairs = 0;
+    DevBuf<int> tleaf, near_ptr, near_range;
+    int ntleaves = 0;
+    long near_pairs = 0;
+    DevBuf<double> out4;               // 4 x nt workspace
+    DevBuf<float> txf, tyf, tzf;       // target coordinates relative to their leaf centre (mixed)
+};
+
+// Tree over the sources + operators + target sets.
+struct Plan {
+    Ctx *ctx;
+    Tube *tube;                 // sources
+    long ns;
+    int p, R, maxpoint, maxlevel, precision;
+    TreeHost tree;
+    // sources in tree order
+    DevBuf<double> sx, sy, sz, snx, sny, snz, sw;  // sw = w * h^3
+    DevBuf<int> src_perm;       // tree pos -> tube index
+    // nodes
+    DevBuf<double> ncenter, nradius;  // 3 per node
+    DevBuf<int> nsrc_begin, nsrc_end, nparent, nindex8, nempty, nchild_first;
+    int np2m = 0;
+    DevBuf<int> p2m_nodes;
+    std::vector<int> m2m_level_begin;
+    DevBuf<int> m2m_nodes;
+    // M2L operators keyed by (level, source - target lattice offset), union over target sets
+    int nops = 0;
+    std::vector<int> op_key_h;
+    DevBuf<int> op_key;
+    DevBuf<double> ops64;          // nops * (4R)^2, column-major per operator
+    DevBuf<float> ops32;
+    std::vector<TargetSet *> targets;
+    // tables and workspaces
+    DevBuf<ChebTables> tables;
+    DevBuf<double> root_r;
+    DevBuf<double> mult, local, dens4;
+    DevBuf<float> mult32, local32, dens32;
+    DevBuf<float> sxf, syf, szf;   // source coordinates relative to their leaf centre (mixed)
+    double kp_cache[4] = {-1, -1, -1, -1};
+    int ops_precision = -1;
+    ~Plan() { for (auto *t : targets) delete t; }
+};
+
+// FMM engine.  dens: 4 x ns (tree order), out: 4 x nt of target set `ts` (tree order).
+void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision);
+void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
+void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
+void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out, int precision);
+
+// Plan creation (fmm.cu): target set 0 = the tube points when with_self, then `extra` (host
+// (n, 3)) when n_extra > 0.
+Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int order, int maxpoint, int maxlevel,
+                int precision);
+
+// Level set (levelset.cu)
+Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value);
+void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band);
+void levelset_evolve(Grid &g, double final_t, double vel, double cfl);
+int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,
+                          double thres);
+void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc);
+void grid_scale(Grid &g, double s);
+void grid_copy(Grid &dst, const Grid &src);
+Tube *surface_extract(Grid &g, int thickness, long *inclusion);
+
+// Timing helper
+struct Timer {
+    cudaEvent_t a, b;
+    cudaStream_t s;
+    explicit Timer(cudaStream_t st) : s(st) { cudaEventCreate(&a); cudaEventCreate(&b); cudaEventRecord(a, s); }
+    ~Timer() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    double ms() { cudaEventRecord(b, s); cudaEventSynchronize(b); float m = 0; cudaEventElapsedTime(&m, a, b); return m; }
+};
+
+inline int div_up(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace ibim
+
+struct ibim_ctx_s { ibim::Ctx c; };
+struct ibim_grid_s { ibim::Grid *g; };
+struct ibim_tube_s { ibim::Tube *t; };
+struct ibim_plan_s { ibim::Plan *p; };

@@ -1,0 +1,441 @@
+// BIE operator, right-hand side, restarted GMRES, polarization energy and the whole solve.
+//
+//   bie_matvec     dmapping (electric.cpp:294-388): densities -> fused FMM -> combine
+//   k_rhs          load (electric.cpp:395-412), direct atom sums
+//   gmres          GMRES (gmres.cpp:50-164): modified Gram-Schmidt Arnoldi on the device with
+//                  fixed-order (deterministic) reductions; Givens rotations and the small
+//                  triangular solve on the host in FP64, as in the reference
+//   polarize       polarizeMap + energy (electric.cpp:442-505)
+//   solve          main.cpp:45-77 for an explicit geometry
+// Mixed precision (IBIM_PRECISION_MIXED): the same GMRES runs on the FP32 operator inside an
+// FP64 iterative-refinement loop whose residual uses the FP64 operator.
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+#include "solve.cuh"
+
+namespace ibim {
+
+namespace {
+
+constexpr int RED_BLOCKS = 512;  // fixed reduction width: results independent of the GPU size
+constexpr int RED_THREADS = 256;
+
+// m_a = x n_a w, psi = x' w (electric.cpp:324-329), tree order.
+__global__ void k_densities(long n, const double *__restrict__ x, const double *__restrict__ nx,
+                            const double *__restrict__ ny, const double *__restrict__ nz,
+                            const double *__restrict__ w, double *dens) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double xi = x[i], wi = w[i];
+        dens[i] = xi * nx[i] * wi;
+        dens[n + i] = xi * ny[i] * wi;
+        dens[2 * n + i] = xi * nz[i] * wi;
+        dens[3 * n + i] = x[n + i] * wi;
+    }
+}
+
+// out1 = phi + F / (1/2 (1 + eE/eI)); out2 = dphi + n.G / (1/2 (1 + eI/eE)) (electric.cpp:369-384).
+__global__ void k_combine(long n, const double *__restrict__ x, const double *__restrict__ f,
+                          const double *__restrict__ nx, const double *__restrict__ ny, const double *__restrict__ nz,
+                          double e1, double e2, double *y) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double ng = nx[i] * f[n + i] + ny[i] * f[2 * n + i] + nz[i] * f[3 * n + i];
+        y[i] = x[i] + f[i] / e1;
+        y[n + i] = x[n + i] + ng / e2;
+    }
+}
+
+// Right-hand side (electric.cpp:395-412) at tree-ordered tube points; atoms staged in shared memory.
+__global__ void __launch_bounds__(256) k_rhs(long n, const double *__restrict__ px, const double *__restrict__ py,
+                                             const double *__restrict__ pz, const double *__restrict__ nx,
+                                             const double *__restrict__ ny, const double *__restrict__ nz,
+                                             const double *__restrict__ atoms, int natoms, double c1, double c2,
+                                             double *b) {
+    __shared__ double A[4][256];
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    double X = 0, Y = 0, Z = 0, NX = 0, NY = 0, NZ = 0;
+    if (i < n) { X = px[i]; Y = py[i]; Z = pz[i]; NX = nx[i]; NY = ny[i]; NZ = nz[i]; }
+    double b1 = 0., b2 = 0.;
+    for (int a0 = 0; a0 < natoms; a0 += 256) {
+        const int cnt = min(256, natoms - a0);
+        __syncthreads();
+        if (threadIdx.x < cnt)
+            for (int q = 0; q < 4; ++q) A[q][threadIdx.x] = atoms[4 * (a0 + threadIdx.x) + q];
+        __syncthreads();
+        if (i < n)
+            for (int a = 0; a < cnt; ++a) {
+                const double dx = X - A[0][a], dy = Y - A[1][a], dz = Z - A[2][a];
+                const double d = dx * dx + dy * dy + dz * dz;
+                const double r = sqrt(d);
+                const double ir = 1.0 / r;
+                b1 += A[3][a] * c1 * ir;
+                b2 -= A[3][a] * c2 * (ir / d) * (NX * dx + NY * dy + NZ * dz);
+            }
+    }
+    if (i < n) {
+        b[i] = b1;
+        b[n + i] = b2;
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double sh[RED_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < RED_THREADS / 32; ++w) s += sh[w];
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+// Reduce RED_BLOCKS partials in a fixed order; every block computes the same value.
+__device__ __forceinline__ double reduce_partials(const double *__restrict__ part) {
+    __shared__ double v;
+    double s = 0.;
+    for (int q = threadIdx.x; q < RED_BLOCKS; q += RED_THREADS) s += part[q];
+    s = block_sum(s);
+    if (threadIdx.x == 0) v = s;
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_dot(long n, const double *__restrict__ a, const double *__restrict__ b,
+                                                     double *part) {
+    double s = 0.;
+    for (long i = blockIdx.x * (long)RED_THREADS + threadIdx.x; i < n; i += (long)RED_BLOCKS * RED_THREADS)
+        s += a[i] * b[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// MGS step: h = <w, v_prev> (from the partials), w -= h v_prev, then partial <w, v_next>
+// (or <w, w> when v_next is null).  h is stored in hcol[slot].
+__global__ void __launch_bounds__(RED_THREADS) k_mgs(long n, const double *__restrict__ part_in, double *w,
+                                                     const double *__restrict__ v_prev,
+                                                     const double *__restrict__ v_next, double *part_out,
+                                                     double *hcol, int slot) {
+    const double h = reduce_partials(part_in);
+    if (blockIdx.x == 0 && threadIdx.x == 0) hcol[slot] = h;
+    double s = 0.;
+    for (long i = blockIdx.x * (long)RED_THREADS + threadIdx.x; i < n; i += (long)RED_BLOCKS * RED_THREADS) {
+        const double wi = w[i] - h * v_prev[i];
+        w[i] = wi;
+        s += wi * (v_next ? v_next[i] : wi);
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) part_out[blockIdx.x] = s;
+}
+
+// v = w / ||w|| with ||w|| from the partials of <w, w>; ||w|| stored in hcol[slot].
+__global__ void __launch_bounds__(RED_THREADS) k_normalize(long n, const double *__restrict__ part_in,
+                                                           const double *__restrict__ w, double *v, double *hcol,
+                                                           int slot) {
+    const double nr = sqrt(reduce_partials(part_in));
+    if (blockIdx.x == 0 && threadIdx.x == 0) hcol[slot] = nr;
+    const double s = 1.0 / nr;
+    for (long i = blockIdx.x * (long)RED_THREADS + threadIdx.x; i < n; i += (long)RED_BLOCKS * RED_THREADS)
+        v[i] = w[i] * s;
+}
+
+// x += sum_j y_j v_j (gmres.cpp:19-20, one daxpy per j in order).
+__global__ void k_update(long n, int k, const double *__restrict__ y, const double *__restrict__ V, double *x) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        double s = x[i];
+        for (int j = 0; j < k; ++j) s += y[j] * V[(long)j * n + i];
+        x[i] = s;
+    }
+}
+
+__global__ void k_sub(long n, const double *__restrict__ a, const double *__restrict__ b, double *c) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) c[i] = a[i] - b[i];
+}
+
+__global__ void k_axpy(long n, double a, const double *__restrict__ x, double *y) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] += a * x[i];
+}
+
+__global__ void k_permute(long n, const int *__restrict__ perm, const double *__restrict__ in, double *out, int scatter) {
+    // scatter: out[perm[i]] = in[i]; gather: out[i] = in[perm[i]]
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        if (scatter)
+            out[perm[i]] = in[i];
+        else
+            out[i] = in[perm[i]];
+    }
+}
+
+inline int ew_grid(Ctx *c, long n) { return (int)std::max<long>(1, std::min<long>(8L * c->num_sms, div_up(n, 256))); }
+
+}  // namespace
+
+void permute(Ctx *c, long n, const int *perm, const double *in, double *out, bool scatter) {
+    if (n <= 0) return;
+    k_permute<<<ew_grid(c, n), 256, 0, c->stream>>>(n, perm, in, out, scatter ? 1 : 0);
+    IBIM_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------------------
+// BIE operator
+// ---------------------------------------------------------------------------------------
+
+void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision) {
+    Ctx *c = P.ctx;
+    const long n = P.ns;
+    IBIM_REQUIRE(!P.targets.empty() && P.targets[0]->self, "BIE operator needs a plan over the tube points");
+    k_densities<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr, P.dens4.ptr);
+    IBIM_CHECK_LAUNCH();
+    TargetSet &S = *P.targets[0];
+    fmm_run(P, 0, kp, P.dens4.ptr, S.out4.ptr, precision);
+    const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
+    k_combine<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, S.out4.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, e1, e2, y);
+    IBIM_CHECK_LAUNCH();
+}
+
+void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b) {
+    Ctx *c = P.ctx;
+    const long n = P.ns;
+    const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
+    const double c1 = 1.0 / (kp.dI * 4.0 * M_PI * e1), c2 = 1.0 / (kp.dI * 4.0 * M_PI * e2);
+    k_rhs<<<div_up(n, 256), 256, 0, c->stream>>>(n, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr,
+                                                 atoms4_dev, natoms, c1, c2, b);
+    IBIM_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------------------
+// GMRES
+// ---------------------------------------------------------------------------------------
+
+namespace {
+
+// gmres.cpp:23-43
+void gen_rot(double dx, double dy, double &cs, double &sn) {
+    if (dy == 0.0) {
+        cs = 1.0;
+        sn = 0.0;
+    } else if (std::fabs(dy) > std::fabs(dx)) {
+        const double t = dx / dy;
+        sn = 1.0 / std::sqrt(1.0 + t * t);
+        cs = t * sn;
+    } else {
+        const double t = dy / dx;
+        cs = 1.0 / std::sqrt(1.0 + t * t);
+        sn = t * cs;
+    }
+}
+void apply_rot(double &dx, double &dy, double cs, double sn) {
+    const double t = cs * dx + sn * dy;
+    dy = -sn * dx + cs * dy;
+    dx = t;
+}
+
+}  // namespace
+
+Krylov::Krylov(Ctx *c, long n_, int m_) : ctx(c), n(n_), m(m_) {
+    cudaStream_t s = c->stream;
+    V.alloc((size_t)(m + 1) * n, s);
+    w.alloc(n, s);
+    r.alloc(n, s);
+    part.alloc(2 * RED_BLOCKS, s);
+    hcol.alloc(m + 2, s);
+    ydev.alloc(m + 1, s);
+    IBIM_CUDA(cudaMallocHost((void **)&hpin, sizeof(double) * (2 * m + 4)));
+}
+
+Krylov::~Krylov() { if (hpin) cudaFreeHost(hpin); }
+
+double Krylov::norm(const double *a) {
+    cudaStream_t s = ctx->stream;
+    k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, a, part.ptr);
+    k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0);
+    IBIM_CHECK_LAUNCH();
+    IBIM_CUDA(cudaMemcpyAsync(hpin, hcol.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    return hpin[0];
+}
+
+// Restarted GMRES(m) of gmres.cpp:50-164 on the device.  x (in/out) and b are device vectors of
+// length n.  `x_is_zero` skips the initial A x (it is exactly zero for a linear operator).
+int Krylov::solve(const std::function<void(const double *, double *)> &A, double *x, const double *b, int max_iter,
+                  double tol, bool x_is_zero, GmresStats &st) {
+    cudaStream_t s = ctx->stream;
+    const int eg = ew_grid(ctx, n);
+    double normb = norm(b);
+    if (x_is_zero) {
+        IBIM_CUDA(cudaMemcpyAsync(r.ptr, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+        A(x, w.ptr);
+        st.matvecs++;
+        k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr);
+        IBIM_CHECK_LAUNCH();
+    }
+    double beta = norm(r.ptr);
+    if (normb == 0.0) normb = 1;
+    double resid = beta / normb;
+    st.residual = resid;
+    if (resid <= tol) return 0;
+    std::vector<double> H((size_t)(m + 1) * (m + 1), 0.), sv(m + 1), cs(m + 1), sn(m + 1), y(m + 1);
+    auto Hm = [&](int i, int j) -> double & { return H[(size_t)i * (m + 1) + j]; };
+    int j = 1, i = 0;
+    auto update = [&](int k) {
+        // back substitution (gmres.cpp:9-21), then x += V y on the device
+        if (k < 0) return;
+        for (int q = 0; q <= k; ++q) y[q] = sv[q];
+        for (int q = k; q >= 0; --q) {
+            y[q] /= Hm(q, q);
+            for (int l = q - 1; l >= 0; --l) y[l] -= Hm(l, q) * y[q];
+        }
+        std::copy(y.begin(), y.begin() + k + 1, hpin + m + 2);
+        IBIM_CUDA(cudaMemcpyAsync(ydev.ptr, hpin + m + 2, sizeof(double) * (k + 1), cudaMemcpyHostToDevice, s));
+        k_update<<<eg, 256, 0, s>>>(n, k + 1, ydev.ptr, V.ptr, x);
+        IBIM_CHECK_LAUNCH();
+        IBIM_CUDA(cudaStreamSynchronize(s));  // hpin reused next step
+    };
+    while (j <= max_iter) {
+        // v0 = r / beta
+        k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, part.ptr, r.ptr, V.ptr, hcol.ptr, 0);
+        std::fill(sv.begin(), sv.end(), 0.);
+        sv[0] = beta;
+        for (i = 0; i < m && j <= max_iter; i++, j++) {
+            double *vi = V.ptr + (size_t)i * n;
+            A(vi, w.ptr);
+            st.matvecs++;
+            st.iters++;
+            double *pa = part.ptr, *pb = part.ptr + RED_BLOCKS;
+            k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, w.ptr, V.ptr, pa);
+            for (int k = 1; k <= i + 1; ++k) {
+                const double *vnext = k <= i ? V.ptr + (size_t)k * n : nullptr;
+                k_mgs<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(k - 1) * n, vnext, pb,
+                                                         hcol.ptr, k - 1);
+                std::swap(pa, pb);
+            }
+            k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(i + 1) * n, hcol.ptr, i + 1);
+            IBIM_CHECK_LAUNCH();
+            if (pa != part.ptr) {
+                // keep the <w,w> partials where the next restart's k_normalize does not look
+            }
+            IBIM_CUDA(cudaMemcpyAsync(hpin, hcol.ptr, sizeof(double) * (i + 2), cudaMemcpyDeviceToHost, s));
+            IBIM_CUDA(cudaStreamSynchronize(s));
+            for (int k = 0; k <= i + 1; ++k) Hm(k, i) = hpin[k];
+            for (int k = 0; k < i; ++k) apply_rot(Hm(k, i), Hm(k + 1, i), cs[k], sn[k]);
+            gen_rot(Hm(i, i), Hm(i + 1, i), cs[i], sn[i]);
+            apply_rot(Hm(i, i), Hm(i + 1, i), cs[i], sn[i]);
+            apply_rot(sv[i], sv[i + 1], cs[i], sn[i]);
+            resid = std::fabs(sv[i + 1]) / normb;
+            st.history.push_back(resid);
+            if (resid < tol) {
+                update(i);
+                st.residual = resid;
+                return 0;
+            }
+        }
+        update(i - 1);
+        A(x, w.ptr);
+        st.matvecs++;
+        k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr);
+        IBIM_CHECK_LAUNCH();
+        // ||r||: partials of <r, r> land in part[0..) for the k_normalize of the next cycle
+        k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r.ptr, r.ptr, part.ptr);
+        k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0);
+        IBIM_CHECK_LAUNCH();
+        IBIM_CUDA(cudaMemcpyAsync(hpin, hcol.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        beta = hpin[0];
+        resid = beta / normb;
+        st.residual = resid;
+        if (resid < tol) return 0;
+    }
+    return 1;
+}
+
+// The first k_normalize of each cycle reads the <r, r> partials from part[0..RED_BLOCKS).
+// norm() leaves them there; so does the restart above.
+
+// ---------------------------------------------------------------------------------------
+// Whole BIE solve on a plan: RHS, GMRES (FP64 or mixed with FP64 refinement), polarize, energy
+// ---------------------------------------------------------------------------------------
+
+void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, const double *charges_host,
+                    int natoms, int restart, int maxiter, double tol, int precision, double *x_tree_out,
+                    std::vector<double> *atom_pot, ibim_result &res) {
+    Ctx *c = P.ctx;
+    cudaStream_t s = c->stream;
+    const long n2 = 2 * P.ns;
+    DevBuf<double> b, x;
+    b.alloc(n2, s);
+    x.alloc(n2, s);
+    x.zero();
+    Timer tm(s);
+    bie_rhs(P, kp, atoms4_dev, natoms, b.ptr);
+    Krylov K(c, n2, std::max(1, std::min(restart, 250)));
+    GmresStats st;
+    int status = 1;
+    if (precision == IBIM_PRECISION_FP64) {
+        auto A = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_FP64); };
+        status = K.solve(A, x.ptr, b.ptr, maxiter, tol, true, st);
+        res.matvecs_fp64 = st.matvecs;
+        res.refinements = 0;
+    } else {
+        // FP64 iterative refinement around the mixed-precision GMRES
+        auto A32 = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_MIXED); };
+        auto A64 = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_FP64); };
+        DevBuf<double> r, d;
+        r.alloc(n2, s);
+        d.alloc(n2, s);
+        IBIM_CUDA(cudaMemcpyAsync(r.ptr, b.ptr, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
+        const double normb = K.norm(b.ptr);
+        int fp64 = 0, outer = 0, left = maxiter;
+        double rel = 1.0;
+        for (outer = 0; outer < 8 && left > 0; ++outer) {
+            d.zero();
+            GmresStats si;
+            K.solve(A32, d.ptr, r.ptr, left, std::max(tol * normb / std::max(rel * normb, 1e-300), tol), true, si);
+            st.iters += si.iters;
+            st.matvecs += si.matvecs;
+            left -= si.iters;
+            k_axpy<<<ew_grid(c, n2), 256, 0, s>>>(n2, 1.0, d.ptr, x.ptr);
+            A64(x.ptr, K.w.ptr);
+            fp64++;
+            k_sub<<<ew_grid(c, n2), 256, 0, s>>>(n2, b.ptr, K.w.ptr, r.ptr);
+            IBIM_CHECK_LAUNCH();
+            rel = K.norm(r.ptr) / (normb == 0 ? 1 : normb);
+            st.history.push_back(rel);
+            if (rel < tol) break;
+        }
+        st.residual = rel;
+        status = rel < tol ? 0 : 1;
+        res.matvecs_fp64 = fp64;
+        res.refinements = outer + (outer < 8 ? 1 : 0);
+    }
+    res.gmres_iters = st.iters;
+    res.matvecs = st.matvecs + (precision == IBIM_PRECISION_FP64 ? 0 : res.matvecs_fp64);
+    res.gmres_status = status;
+    res.residual = st.residual;
+    res.t_solve_ms = tm.ms();
+    // polarizeMap + energy (electric.cpp:442-505): targets = atoms (target set 1)
+    Timer te(s);
+    if (natoms > 0 && P.targets.size() > 1) {
+        TargetSet &A = *P.targets[1];
+        k_densities<<<ew_grid(c, P.ns), 256, 0, s>>>(P.ns, x.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr,
+                                                      P.dens4.ptr);
+        IBIM_CHECK_LAUNCH();
+        fmm_run(P, 1, kp, P.dens4.ptr, A.out4.ptr, IBIM_PRECISION_FP64);
+        std::vector<double> F(A.nt);
+        A.out4.download(F.data(), A.nt);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> pot(natoms, 0.);
+        for (long q = 0; q < A.nt; ++q) pot[A.perm[q]] = -F[q];  // ret2 - (ret1x + ret1y + ret1z)
+        double E = 0.;
+        for (int a = 0; a < natoms; ++a) E += pot[a] * charges_host[a];
+        res.energy = 0.5 * E;
+        if (atom_pot) *atom_pot = pot;
+    }
+    res.t_energy_ms = te.ms();
+    if (x_tree_out) IBIM_CUDA(cudaMemcpyAsync(x_tree_out, x.ptr, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
+    IBIM_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace ibim

@@ -1,0 +1,38 @@
+// BIE operator and GMRES (solve.cu).
+#pragma once
+
+#include <functional>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace ibim {
+
+struct GmresStats {
+    int iters = 0, matvecs = 0;
+    double residual = 0.;
+    std::vector<double> history;
+};
+
+// Device Krylov workspace for GMRES(m) on vectors of length n.
+struct Krylov {
+    Ctx *ctx;
+    long n;
+    int m;
+    DevBuf<double> V, w, r, part, hcol, ydev;
+    double *hpin = nullptr;
+    Krylov(Ctx *c, long n, int m);
+    ~Krylov();
+    double norm(const double *a);
+    int solve(const std::function<void(const double *, double *)> &A, double *x, const double *b, int max_iter,
+              double tol, bool x_is_zero, GmresStats &st);
+};
+
+void permute(Ctx *c, long n, const int *perm, const double *in, double *out, bool scatter);
+void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision);
+void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b);
+void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, const double *charges_host,
+                    int natoms, int restart, int maxiter, double tol, int precision, double *x_tree_out,
+                    std::vector<double> *atom_pot, ibim_result &res);
+
+}  // namespace ibim

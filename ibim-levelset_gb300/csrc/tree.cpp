@@ -1,0 +1,283 @@
+// Octree and U/V/W/X interaction lists of the reference's black-box FMM (host C++).
+//
+// Same tree as bbfmm::tree::populate (bbfmm.cpp:8-138):
+//   root = anisotropic bounding box of the sources (getCenterRadius, bbfmm.cpp:43-65);
+//   a node splits while nSource > maxPoint and level < maxLevel (bbfmm.cpp:81); all 8
+//   children are created, child id = 4z + 2y + x with `coordinate < centre ? 0 : 1`;
+//   child centre = c + (bit - 1/2) r, child radius = r / 2 (bbfmm.cpp:88-101).
+// Same lists as tree::buildNode (bbfmm.cpp:158-241): the 6x6x6 same-level candidates around
+// the parent, findNode (bbfmm.cpp:244-258) and isAdjacent (bbfmm.cpp:260-280).  Here nodes
+// carry integer lattice coordinates, so findNode is a descent on coordinate bits and
+// isAdjacent an interval test; the reference's EPS = 1e-12 tolerances only absorb rounding of
+// the same lattice, so the lists are identical (checked against the reference's own trees).
+//
+// Points are kept in a stable per-node partition (the order the reference's sourceIndex
+// vectors hold), so every node owns one contiguous range of the tree-ordered points.
+
+#include <algorithm>
+#include <cstdint>
+#include <unordered_map>
+
+#include "internal.cuh"
+
+namespace ibim {
+
+namespace {
+
+struct BNode {
+    int level, parent, index8, leaf = 0, empty = 0;
+    int child[8];
+    double c[3], r[3];
+    int coord[3];
+    int sb, se, tb, te;  // ranges into the source / target permutations
+};
+
+struct Builder {
+    const double *src, *tgt;
+    int maxpoint, maxlevel;
+    std::vector<BNode> nodes;
+    std::vector<int> sp, tp, tmp;
+
+    // assignChildren (bbfmm.cpp:67-138)
+    void split(int id) {
+        BNode &n0 = nodes[id];
+        const int ns = n0.se - n0.sb;
+        if (ns == 0) {
+            nodes[id].leaf = 1;
+            nodes[id].empty = 1;
+            return;
+        }
+        if (ns <= maxpoint || n0.level == maxlevel) {
+            nodes[id].leaf = 1;
+            return;
+        }
+        int first = (int)nodes.size();
+        for (int i = 0; i < 8; ++i) {
+            BNode q;
+            const BNode &p = nodes[id];
+            q.level = p.level + 1;
+            q.parent = id;
+            q.index8 = i;
+            for (int a = 0; a < 8; ++a) q.child[a] = -1;
+            q.c[0] = p.c[0] + ((i & 1) - 0.5) * p.r[0];
+            q.c[1] = p.c[1] + (((i >> 1) & 1) - 0.5) * p.r[1];
+            q.c[2] = p.c[2] + ((i >> 2) - 0.5) * p.r[2];
+            q.r[0] = p.r[0] * 0.5;
+            q.r[1] = p.r[1] * 0.5;
+            q.r[2] = p.r[2] * 0.5;
+            q.coord[0] = 2 * p.coord[0] + (i & 1);
+            q.coord[1] = 2 * p.coord[1] + ((i >> 1) & 1);
+            q.coord[2] = 2 * p.coord[2] + (i >> 2);
+            nodes.push_back(q);
+        }
+        for (int i = 0; i < 8; ++i) nodes[id].child[i] = first + i;
+        partition(nodes[id], first, sp, src, true);
+        partition(nodes[id], first, tp, tgt, false);
+        for (int i = 0; i < 8; ++i) split(first + i);
+    }
+
+    // stable 8-way partition of a node's range by octant
+    void partition(const BNode &p, int first, std::vector<int> &perm, const double *pts, bool is_src) {
+        const int b = is_src ? p.sb : p.tb, e = is_src ? p.se : p.te;
+        int cnt[8] = {0};
+        auto oct = [&](int idx) {
+            const double *x = pts + 3 * (long)idx;
+            return 4 * (x[2] < p.c[2] ? 0 : 1) + 2 * (x[1] < p.c[1] ? 0 : 1) + (x[0] < p.c[0] ? 0 : 1);
+        };
+        tmp.resize(std::max<size_t>(tmp.size(), (size_t)(e - b)));
+        for (int i = b; i < e; ++i) cnt[oct(perm[i])]++;
+        int off[8], o = b;
+        for (int i = 0; i < 8; ++i) {
+            off[i] = o;
+            BNode &q = nodes[first + i];
+            if (is_src) { q.sb = o; q.se = o + cnt[i]; } else { q.tb = o; q.te = o + cnt[i]; }
+            o += cnt[i];
+        }
+        for (int i = b; i < e; ++i) tmp[off[oct(perm[i])]++ - b] = perm[i];
+        std::copy(tmp.begin(), tmp.begin() + (e - b), perm.begin() + b);
+    }
+};
+
+inline uint64_t key_of(int level, int x, int y, int z) {
+    return ((uint64_t)level << 60) | ((uint64_t)x << 40) | ((uint64_t)y << 20) | (uint64_t)z;
+}
+
+}  // namespace
+
+TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int maxpoint, int maxlevel) {
+    IBIM_REQUIRE(ns > 0, "FMM tree needs at least one source point");
+    IBIM_REQUIRE(maxpoint > 0, "fmm_maxpoint must be positive");
+    IBIM_REQUIRE(maxlevel >= 0 && maxlevel <= 18, "fmm_maxlevel must be in [0, 18]");
+    Builder B;
+    B.src = src;
+    B.tgt = tgt;
+    B.maxpoint = maxpoint;
+    B.maxlevel = maxlevel;
+    // getCenterRadius (bbfmm.cpp:43-65)
+    double mx[3], mn[3];
+    for (int a = 0; a < 3; ++a) mx[a] = mn[a] = src[a];
+    for (long i = 0; i < ns; ++i)
+        for (int a = 0; a < 3; ++a) {
+            mx[a] = std::max(mx[a], src[3 * i + a]);
+            mn[a] = std::min(mn[a], src[3 * i + a]);
+        }
+    BNode root;
+    root.level = 0;
+    root.parent = -1;
+    root.index8 = 0;
+    for (int a = 0; a < 8; ++a) root.child[a] = -1;
+    for (int a = 0; a < 3; ++a) {
+        root.c[a] = (mx[a] + mn[a]) / 2.0;
+        root.r[a] = (mx[a] - mn[a]) / 2.0;
+        root.coord[a] = 0;
+    }
+    root.sb = 0;
+    root.se = (int)ns;
+    root.tb = 0;
+    root.te = (int)nt;
+    B.sp.resize(ns);
+    B.tp.resize(nt);
+    for (long i = 0; i < ns; ++i) B.sp[i] = (int)i;
+    for (long i = 0; i < nt; ++i) B.tp[i] = (int)i;
+    B.nodes.reserve(1024);
+    B.nodes.push_back(root);
+    B.split(0);
+
+    const int nn = (int)B.nodes.size();
+    int depth = 0;
+    for (auto &n : B.nodes) depth = std::max(depth, n.level);
+    std::unordered_map<uint64_t, int> lookup;
+    lookup.reserve(nn * 2);
+    for (int i = 0; i < nn; ++i) {
+        const BNode &n = B.nodes[i];
+        lookup[key_of(n.level, n.coord[0], n.coord[1], n.coord[2])] = i;
+    }
+    // findNode: the node at the candidate's level if it exists, else the leaf that contains it
+    auto find_node = [&](int level, const int c[3]) {
+        int id = 0;
+        while (B.nodes[id].level < level && !B.nodes[id].leaf) {
+            const int sh = level - B.nodes[id].level - 1;
+            const int ch = ((c[2] >> sh) & 1) * 4 + ((c[1] >> sh) & 1) * 2 + ((c[0] >> sh) & 1);
+            id = B.nodes[id].child[ch];
+        }
+        return id;
+    };
+    // isAdjacent: touching in one axis, overlapping or touching in the other two
+    auto adjacent = [&](int a, int b) {
+        const BNode &A = B.nodes[a], &Bn = B.nodes[b];
+        bool touch[3], ot[3];
+        for (int d = 0; d < 3; ++d) {
+            const long la = (long)A.coord[d] << (depth - A.level), ha = (long)(A.coord[d] + 1) << (depth - A.level);
+            const long lb = (long)Bn.coord[d] << (depth - Bn.level), hb = (long)(Bn.coord[d] + 1) << (depth - Bn.level);
+            touch[d] = (ha == lb) || (hb == la);
+            ot[d] = la <= hb && lb <= ha;
+        }
+        return (touch[0] && ot[1] && ot[2]) || (touch[1] && ot[0] && ot[2]) || (touch[2] && ot[0] && ot[1]);
+    };
+    std::vector<std::vector<int>> U(nn), V(nn), W(nn), X(nn);
+    std::vector<int> queue;
+    for (int id = 0; id < nn; ++id) {
+        const BNode &n = B.nodes[id];
+        if (n.parent != -1) {
+            const BNode &pn = B.nodes[n.parent];
+            const int side = 1 << n.level;
+            for (int xi = -2; xi < 4; ++xi)
+                for (int yi = -2; yi < 4; ++yi)
+                    for (int zi = -2; zi < 4; ++zi) {
+                        const int c[3] = {2 * pn.coord[0] + xi, 2 * pn.coord[1] + yi, 2 * pn.coord[2] + zi};
+                        if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= side || c[1] >= side || c[2] >= side) continue;
+                        if (c[0] == n.coord[0] && c[1] == n.coord[1] && c[2] == n.coord[2]) continue;
+                        const int cid = find_node(n.level, c);
+                        const bool adj = adjacent(id, cid);
+                        const BNode &cn = B.nodes[cid];
+                        if (cn.level < n.level) {
+                            if (adj) {
+                                if (cn.leaf) U[id].push_back(cid);
+                            } else {
+                                X[id].push_back(cid);
+                            }
+                        }
+                        if (cn.level == n.level) {
+                            if (!adj) {
+                                V[id].push_back(cid);
+                            } else if (n.leaf) {
+                                queue.clear();
+                                queue.push_back(cid);
+                                for (size_t q = 0; q < queue.size(); ++q) {
+                                    const int f = queue[q];
+                                    if (!adjacent(f, id)) {
+                                        W[id].push_back(f);
+                                    } else if (B.nodes[f].leaf) {
+                                        U[id].push_back(f);
+                                    } else {
+                                        for (int ch = 0; ch < 8; ++ch) queue.push_back(B.nodes[f].child[ch]);
+                                    }
+                                }
+                            }
+                        }
+                    }
+        }
+        if (n.leaf) U[id].push_back(id);
+    }
+    // level-ordered renumbering
+    std::vector<int> order(nn);
+    for (int i = 0; i < nn; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return B.nodes[a].level < B.nodes[b].level; });
+    std::vector<int> newid(nn);
+    for (int i = 0; i < nn; ++i) newid[order[i]] = i;
+
+    TreeHost T;
+    T.nnodes = nn;
+    T.nlevels = depth + 1;
+    T.level_begin.assign(T.nlevels + 1, 0);
+    T.center.resize(3 * nn);
+    T.radius.resize(3 * nn);
+    T.coord.resize(3 * nn);
+    T.parent.resize(nn);
+    T.index8.resize(nn);
+    T.leaf.resize(nn);
+    T.empty.resize(nn);
+    T.src_begin.resize(nn);
+    T.src_end.resize(nn);
+    T.tgt_begin.resize(nn);
+    T.tgt_end.resize(nn);
+    T.ref_id.resize(nn);
+    T.U.resize(nn);
+    T.V.resize(nn);
+    T.W.resize(nn);
+    T.X.resize(nn);
+    for (int i = 0; i < nn; ++i) {
+        const BNode &n = B.nodes[order[i]];
+        T.level_begin[n.level + 1]++;
+        for (int a = 0; a < 3; ++a) {
+            T.center[3 * i + a] = n.c[a];
+            T.radius[3 * i + a] = n.r[a];
+            T.coord[3 * i + a] = n.coord[a];
+        }
+        T.parent[i] = n.parent < 0 ? -1 : newid[n.parent];
+        T.index8[i] = n.index8;
+        T.leaf[i] = n.leaf;
+        T.empty[i] = n.empty;
+        T.src_begin[i] = n.sb;
+        T.src_end[i] = n.se;
+        T.tgt_begin[i] = n.tb;
+        T.tgt_end[i] = n.te;
+        T.ref_id[i] = order[i];
+        auto remap = [&](const std::vector<int> &in, std::vector<int> &out) {
+            out.reserve(in.size());
+            for (int v : in) out.push_back(newid[v]);
+            std::sort(out.begin(), out.end());
+            out.erase(std::unique(out.begin(), out.end()), out.end());
+        };
+        remap(U[order[i]], T.U[i]);
+        remap(V[order[i]], T.V[i]);
+        remap(W[order[i]], T.W[i]);
+        remap(X[order[i]], T.X[i]);
+    }
+    for (int l = 0; l < T.nlevels; ++l) T.level_begin[l + 1] += T.level_begin[l];
+    T.src_perm = std::move(B.sp);
+    T.tgt_perm = std::move(B.tp);
+    return T;
+}
+
+}  // namespace ibim

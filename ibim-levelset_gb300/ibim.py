@@ -1,0 +1,445 @@
+"""Python binding of libibim_gb300.so (the C ABI in include/ibim.h).
+
+Mirrors the reference's interfaces for the IBIM Poisson-Boltzmann path:
+  Grid / levelset (levelset.h:12-60)  -> Context.grid(), Grid.expand/evolve/reinitialize/...
+  Surface (levelset.h:62-72)          -> Grid.surface() -> Tube
+  bbfmm::kernel (bbfmm.h:200-270)     -> Tube.plan() -> Plan.apply(kernel, ...)
+  GMRES (gmres.h:20-21)               -> Plan.gmres()
+  electric (electric.h:13)            -> Tube.electric()
+  main.cpp:45-77                      -> Context.solve()
+The library has no CPU fallback: without a GPU, every compute call raises IbimError.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libibim_gb300.so")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_UNSUPPORTED_KERNEL = 4
+ERR_LIMIT = 5
+ERR_IO = 6
+
+KERNELS = ["K1x", "K1y", "K1z", "K2", "K3xx", "K3yy", "K3zz", "K3xy", "K3yz", "K3zx", "K3yx", "K3zy", "K3xz",
+           "K4x", "K4y", "K4z"]
+KERNEL_BIE_FUSED = 16
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+# every symbol include/ibim.h declares
+EXPORTS = [
+    "ibim_ctx_create", "ibim_ctx_destroy", "ibim_last_error", "ibim_status_string", "ibim_config_default",
+    "ibim_grid_create", "ibim_grid_destroy", "ibim_grid_upload", "ibim_grid_download", "ibim_grid_scale",
+    "ibim_grid_copy", "ibim_levelset_expand", "ibim_levelset_evolve", "ibim_levelset_reinitialize",
+    "ibim_levelset_count_gradient", "ibim_levelset_build", "ibim_surface_extract", "ibim_tube_create",
+    "ibim_tube_destroy", "ibim_tube_size", "ibim_tube_download", "ibim_fmm_plan", "ibim_plan_destroy",
+    "ibim_plan_stats", "ibim_plan_lists", "ibim_fmm_apply", "ibim_bie_matvec", "ibim_bie_rhs", "ibim_gmres_solve",
+    "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host",
+]
+
+
+class IbimError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class KernelParams(C.Structure):
+    _fields_ = [("kappa", C.c_double), ("dE", C.c_double), ("dI", C.c_double), ("tau", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("h", C.c_double), ("n", C.c_int * 3), ("band", C.c_int),
+                ("init", C.c_double), ("probe", C.c_double), ("reinit_t", C.c_double), ("thickness", C.c_int),
+                ("thres", C.c_double), ("np", C.c_int), ("maxpoint", C.c_int), ("maxlevel", C.c_int),
+                ("kp", KernelParams), ("restart", C.c_int), ("maxiter", C.c_int), ("tol", C.c_double),
+                ("precision", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("energy", C.c_double), ("area", C.c_double), ("n_points", C.c_long), ("inclusion", C.c_long),
+                ("reinit_steps", C.c_int * 2), ("gmres_iters", C.c_int), ("matvecs", C.c_int),
+                ("matvecs_fp64", C.c_int), ("gmres_status", C.c_int), ("refinements", C.c_int),
+                ("residual", C.c_double), ("t_levelset_ms", C.c_double), ("t_surface_ms", C.c_double),
+                ("t_plan_ms", C.c_double), ("t_solve_ms", C.c_double), ("t_energy_ms", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["reinit_steps"] = list(self.reinit_steps)
+        return d
+
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_long)
+_vp = C.c_void_p
+
+
+def lib():
+    """Load the shared library (built by build.py; fails loudly when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libibim_gb300.so not built ({LIB_PATH}); run ibim-levelset_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    sig = {
+        "ibim_ctx_create": ([C.c_int, C.POINTER(_vp)], C.c_int),
+        "ibim_ctx_destroy": ([_vp], C.c_int),
+        "ibim_last_error": ([], C.c_char_p),
+        "ibim_status_string": ([C.c_int], C.c_char_p),
+        "ibim_config_default": ([C.POINTER(Config)], None),
+        "ibim_grid_create": ([_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                              C.c_double, C.POINTER(_vp)], C.c_int),
+        "ibim_grid_destroy": ([_vp], C.c_int),
+        "ibim_grid_upload": ([_vp, _dp], C.c_int),
+        "ibim_grid_download": ([_vp, _dp], C.c_int),
+        "ibim_grid_scale": ([_vp, C.c_double], C.c_int),
+        "ibim_grid_copy": ([_vp, _vp], C.c_int),
+        "ibim_levelset_expand": ([_vp, _dp, _dp, C.c_int, C.c_double, C.c_int], C.c_int),
+        "ibim_levelset_evolve": ([_vp, C.c_double, C.c_double, C.c_double], C.c_int),
+        "ibim_levelset_reinitialize": ([_vp, _vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _ip],
+                                       C.c_int),
+        "ibim_levelset_count_gradient": ([_vp, C.c_double, C.c_double, _lp, _lp, _dp], C.c_int),
+        "ibim_levelset_build": ([_vp, _dp, _dp, C.c_int, C.POINTER(Config), C.POINTER(_vp), _ip], C.c_int),
+        "ibim_surface_extract": ([_vp, C.c_int, C.POINTER(_vp), _lp, _lp], C.c_int),
+        "ibim_tube_create": ([_vp, _dp, _dp, _dp, C.c_long, C.c_double, C.POINTER(_vp)], C.c_int),
+        "ibim_tube_destroy": ([_vp], C.c_int),
+        "ibim_tube_size": ([_vp], C.c_long),
+        "ibim_tube_download": ([_vp, _dp, _dp, _dp], C.c_int),
+        "ibim_fmm_plan": ([_vp, _dp, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
+        "ibim_plan_destroy": ([_vp], C.c_int),
+        "ibim_plan_stats": ([_vp, _lp], C.c_int),
+        "ibim_plan_lists": ([_vp, C.c_int, _ip, C.c_long, _lp], C.c_int),
+        "ibim_fmm_apply": ([_vp, C.c_int, C.POINTER(KernelParams), _dp, _dp], C.c_int),
+        "ibim_bie_matvec": ([_vp, C.POINTER(KernelParams), _dp, _dp], C.c_int),
+        "ibim_bie_rhs": ([_vp, C.POINTER(KernelParams), _dp, _dp, C.c_int, _dp], C.c_int),
+        "ibim_gmres_solve": ([_vp, C.POINTER(KernelParams), _dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
+                              _ip, _dp], C.c_int),
+        "ibim_electric": ([_vp, _dp, _dp, C.c_int, C.POINTER(Config), _dp, _dp, C.POINTER(Result)], C.c_int),
+        "ibim_solve": ([_vp, _dp, _dp, _dp, C.c_int, C.POINTER(Config), C.POINTER(Result)], C.c_int),
+        "ibim_solve_dev": ([_vp, _vp, _vp, _vp, C.c_int, C.POINTER(Config), C.POINTER(Result)], C.c_int),
+        "ibim_solve_pqr": ([_vp, C.c_char_p, C.POINTER(Config), C.POINTER(Result)], C.c_int),
+        "ibim_tree_lists_host": ([_dp, C.c_long, C.c_int, C.c_int, _ip, C.c_long, _lp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _check(st: int):
+    if st != OK:
+        raise IbimError(st, lib().ibim_last_error().decode())
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    lib().ibim_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if k == "lo":
+            cfg.lo = (C.c_double * 3)(*v)
+        elif k == "n":
+            cfg.n = (C.c_int * 3)(*v)
+        elif k in ("kappa", "dE", "dI", "tau"):
+            setattr(cfg.kp, k, v)
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+def kernel_params(kappa=0.0, dE=80.0, dI=1.0, tau=1.0) -> KernelParams:
+    return KernelParams(kappa, dE, dI, tau)
+
+
+class Context:
+    """One GPU, one stream (ibim_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = _vp()
+        _check(lib().ibim_ctx_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibim_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def grid(self, n, lo, h, value=0.0) -> "Grid":
+        g = _vp()
+        _check(lib().ibim_grid_create(self.h, int(n[0]), int(n[1]), int(n[2]), lo[0], lo[1], lo[2], h, value,
+                                      C.byref(g)))
+        return Grid(self, g, tuple(int(v) for v in n))
+
+    def levelset(self, centers, radii, cfg: Config):
+        """main.cpp:45-60: returns (Grid, reinit steps (2,))."""
+        c = _c(centers).reshape(-1, 3)
+        r = _c(radii)
+        g = _vp()
+        steps = (C.c_int * 2)()
+        _check(lib().ibim_levelset_build(self.h, _p(c), _p(r), len(r), C.byref(cfg), C.byref(g), steps))
+        return Grid(self, g, tuple(cfg.n)), list(steps)
+
+    def tube(self, points, normals, weights, h) -> "Tube":
+        p = _c(points).reshape(-1, 3)
+        n = _c(normals).reshape(-1, 3)
+        w = _c(weights)
+        t = _vp()
+        _check(lib().ibim_tube_create(self.h, _p(p), _p(n), _p(w), len(w), h, C.byref(t)))
+        return Tube(self, t)
+
+    def solve(self, centers, charges, radii, cfg: Config) -> dict:
+        c = _c(centers).reshape(-1, 3)
+        q = _c(charges)
+        r = _c(radii)
+        res = Result()
+        _check(lib().ibim_solve(self.h, _p(c), _p(q), _p(r), len(q), C.byref(cfg), C.byref(res)))
+        return res.as_dict()
+
+    def solve_dev(self, centers_ptr: int, charges_ptr: int, radii_ptr: int, natoms: int, cfg: Config) -> dict:
+        res = Result()
+        _check(lib().ibim_solve_dev(self.h, _vp(centers_ptr), _vp(charges_ptr), _vp(radii_ptr), natoms, C.byref(cfg),
+                                    C.byref(res)))
+        return res.as_dict()
+
+    def solve_pqr(self, path: str, cfg: Config) -> dict:
+        res = Result()
+        _check(lib().ibim_solve_pqr(self.h, path.encode(), C.byref(cfg), C.byref(res)))
+        return res.as_dict()
+
+
+class Grid:
+    """levelset.h:12-60 (Grid + levelset) on the device."""
+
+    def __init__(self, ctx, h, n):
+        self.ctx, self.h, self.n = ctx, h, n
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibim_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def upload(self, a):
+        a = _c(a)
+        assert a.size == int(np.prod(self.n))
+        _check(lib().ibim_grid_upload(self.h, _p(a)))
+
+    def download(self):
+        out = np.empty(self.n)
+        _check(lib().ibim_grid_download(self.h, _p(out)))
+        return out
+
+    def scale(self, s):
+        _check(lib().ibim_grid_scale(self.h, s))
+
+    def copy_from(self, other: "Grid"):
+        _check(lib().ibim_grid_copy(self.h, other.h))
+
+    def expand(self, centers, radii, probe=1.4, band=8):
+        c = _c(centers).reshape(-1, 3)
+        r = _c(radii)
+        _check(lib().ibim_levelset_expand(self.h, _p(c), _p(r), len(r), probe, band))
+
+    def evolve(self, final_t, vel=1.0, cfl=0.2):
+        _check(lib().ibim_levelset_evolve(self.h, final_t, vel, cfl))
+
+    def reinitialize(self, phi0: "Grid", final_t, vel=1.0, cfl=0.5, thickness=2, thres=1e-4) -> int:
+        st = C.c_int(0)
+        _check(lib().ibim_levelset_reinitialize(self.h, phi0.h, final_t, vel, cfl, thickness, thres, C.byref(st)))
+        return st.value
+
+    def count_gradient(self, thickness, thres):
+        bad, tot, acc = C.c_long(0), C.c_long(0), C.c_double(0)
+        _check(lib().ibim_levelset_count_gradient(self.h, float(thickness), thres, C.byref(bad), C.byref(tot),
+                                                  C.byref(acc)))
+        return bad.value, tot.value, acc.value
+
+    def surface(self, thickness) -> "Tube":
+        t = _vp()
+        n, inc = C.c_long(0), C.c_long(0)
+        _check(lib().ibim_surface_extract(self.h, thickness, C.byref(t), C.byref(n), C.byref(inc)))
+        tb = Tube(self.ctx, t)
+        tb.inclusion = inc.value
+        return tb
+
+
+class Tube:
+    """Surface (levelset.h:62-72): tube points, normals and cosine weights on the device."""
+
+    def __init__(self, ctx, h):
+        self.ctx, self.h = ctx, h
+        self.inclusion = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibim_tube_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __len__(self):
+        return int(lib().ibim_tube_size(self.h))
+
+    def download(self):
+        n = len(self)
+        p = np.empty((n, 3))
+        q = np.empty((n, 3))
+        w = np.empty(n)
+        _check(lib().ibim_tube_download(self.h, _p(p), _p(q), _p(w)))
+        return p, q, w
+
+    def surface7(self):
+        p, q, w = self.download()
+        return np.concatenate([p, q, w[:, None]], axis=1)
+
+    def plan(self, order, maxpoint, maxlevel=10, targets=None, precision=PRECISION_FP64) -> "Plan":
+        pl = _vp()
+        if targets is None:
+            _check(lib().ibim_fmm_plan(self.h, None, 0, order, maxpoint, maxlevel, precision, C.byref(pl)))
+            nt = len(self)
+        else:
+            t = _c(targets).reshape(-1, 3)
+            _check(lib().ibim_fmm_plan(self.h, _p(t), len(t), order, maxpoint, maxlevel, precision, C.byref(pl)))
+            nt = len(t)
+        return Plan(self, pl, len(self), nt)
+
+    def electric(self, centers, charges, cfg: Config, want_x=False):
+        c = _c(centers).reshape(-1, 3)
+        q = _c(charges)
+        res = Result()
+        n = len(self)
+        x = np.empty(2 * n) if want_x else None
+        pot = np.empty(len(q))
+        _check(lib().ibim_electric(self.h, _p(c), _p(q), len(q), C.byref(cfg), _p(x) if want_x else None, _p(pot),
+                                   C.byref(res)))
+        d = res.as_dict()
+        d["atom_potential"] = pot
+        if want_x:
+            d["x"] = x
+        return d
+
+
+class Plan:
+    """bbfmm tree + lists + operators over a tube (bbfmm.h:149-270)."""
+
+    def __init__(self, tube, h, ns, nt):
+        self.tube, self.h, self.ns, self.nt = tube, h, ns, nt
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibim_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def stats(self):
+        s = (C.c_long * 8)()
+        _check(lib().ibim_plan_stats(self.h, s))
+        keys = ["nodes", "levels", "leaves", "v_pairs", "x_pairs", "near_pairs", "operators", "target_leaves"]
+        return dict(zip(keys, list(s)))
+
+    def apply(self, kernel: int, kp: KernelParams, dens):
+        rows = 4 if kernel == KERNEL_BIE_FUSED else 1
+        d = _c(dens).reshape(rows, self.ns)
+        out = np.empty((rows, self.nt))
+        _check(lib().ibim_fmm_apply(self.h, kernel, C.byref(kp), _p(d), _p(out)))
+        return out if rows == 4 else out[0]
+
+    def matvec(self, kp: KernelParams, x):
+        x = _c(x)
+        y = np.empty_like(x)
+        _check(lib().ibim_bie_matvec(self.h, C.byref(kp), _p(x), _p(y)))
+        return y
+
+    def rhs(self, kp: KernelParams, centers, charges):
+        c = _c(centers).reshape(-1, 3)
+        q = _c(charges)
+        b = np.empty(2 * self.ns)
+        _check(lib().ibim_bie_rhs(self.h, C.byref(kp), _p(c), _p(q), len(q), _p(b)))
+        return b
+
+    def gmres(self, kp: KernelParams, b, x0=None, restart=30, maxiter=100, tol=1e-6, precision=PRECISION_FP64):
+        b = _c(b)
+        x = np.zeros_like(b) if x0 is None else _c(x0).copy()
+        it, st, res = C.c_int(0), C.c_int(0), C.c_double(0)
+        _check(lib().ibim_gmres_solve(self.h, C.byref(kp), _p(b), _p(x), restart, maxiter, tol, precision,
+                                      C.byref(it), C.byref(st), C.byref(res)))
+        return x, dict(iters=it.value, status=st.value, residual=res.value)
+
+    def lists(self):
+        """Tree + U/V/W/X lists in the reference's node numbering (inspection)."""
+        return _read_lists(lambda buf, cap, need: lib().ibim_plan_lists(self.h, 0, buf, cap, need))
+
+
+def _read_lists(call):
+    need = C.c_long(0)
+    st = call(None, 0, C.byref(need))
+    if st != OK:
+        raise IbimError(st, lib().ibim_last_error().decode())
+    buf = np.zeros(need.value, np.int32)
+    _check(call(buf.ctypes.data_as(_ip), need.value, C.byref(need)))
+    return decode_lists(buf)
+
+
+def decode_lists(buf):
+    """Layout of ibim_plan_lists: nnodes, then per node (reference numbering):
+    level, parent, leaf, empty, nsrc, then |U| U..., |V| V..., |W| W..., |X| X..."""
+    nn = int(buf[0])
+    pos = 1
+    nodes = []
+    for _ in range(nn):
+        level, parent, leaf, empty, nsrc = (int(v) for v in buf[pos:pos + 5])
+        pos += 5
+        L = []
+        for _w in range(4):
+            k = int(buf[pos])
+            L.append(buf[pos + 1:pos + 1 + k].copy())
+            pos += 1 + k
+        nodes.append(dict(level=level, parent=parent, leaf=leaf, empty=empty, nsrc=nsrc, U=L[0], V=L[1], W=L[2],
+                          X=L[3]))
+    return nodes
+
+
+def tree_lists_host(points, maxpoint, maxlevel=10):
+    """The host tree builder on (n,3) points, without a GPU (for inspection and tests)."""
+    p = _c(points).reshape(-1, 3)
+    return _read_lists(lambda buf, cap, need: lib().ibim_tree_lists_host(_p(p), len(p), maxpoint, maxlevel, buf, cap,
+                                                                         need))
+
+
+@dataclass
+class Workload:
+    """A solve request: atoms + config."""
+
+    centers: np.ndarray
+    charges: np.ndarray
+    radii: np.ndarray
+    cfg: Config

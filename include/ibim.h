@@ -1,0 +1,189 @@
+/*
+ * ibim-levelset GB300 — C ABI of the implicit-boundary-integral Poisson–Boltzmann path.
+ *
+ * One shared library (libibim_gb300.so, sm_103a) implements the reference's hot path
+ * (GaZ3ll3/ibim-levelset) on one GPU: level-set tube quadrature (levelset.h/.cpp),
+ * the black-box Chebyshev FMM (bbfmm.h/.cpp), restarted GMRES (gmres.h/.cpp) and the BIE
+ * operator and solvation energy (electric.h/.cpp).  The C++ headers under include/ibim/
+ * keep the reference's class interfaces on top of these entry points.
+ *
+ * Conventions
+ *   - every entry point returns an int status (IBIM_OK = 0); ibim_last_error() gives text;
+ *   - no exception crosses the ABI; no CPU fallback: a missing GPU is IBIM_ERR_CUDA;
+ *   - handles are owned by the caller and released with the matching *_destroy;
+ *   - "host" pointers are ordinary host memory; "_dev" entry points take device pointers;
+ *   - lengths in Angstrom (the reference's electric() with rescale s = 1);
+ *   - one CUDA stream per context; calls on one context are serialised by the caller.
+ */
+#ifndef IBIM_GB300_H
+#define IBIM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define IBIM_OK 0
+#define IBIM_ERR_INVALID_ARGUMENT 1 /* bad size, null pointer, inconsistent handles */
+#define IBIM_ERR_CUDA 2             /* CUDA runtime error (includes "no GPU") */
+#define IBIM_ERR_OUT_OF_MEMORY 3    /* device allocation refused or above the context budget */
+#define IBIM_ERR_UNSUPPORTED_KERNEL 4 /* kernel id outside the reference's kernel set */
+#define IBIM_ERR_LIMIT 5            /* a bounded device loop (flood fill) hit its iteration cap */
+#define IBIM_ERR_IO 6               /* unreadable or malformed input file */
+
+/* ---- kernel ids: the 16 kernels of electric.cpp:67-291, plus the fused forms ---- */
+#define IBIM_K1X 0
+#define IBIM_K1Y 1
+#define IBIM_K1Z 2
+#define IBIM_K2 3
+#define IBIM_K3XX 4
+#define IBIM_K3YY 5
+#define IBIM_K3ZZ 6
+#define IBIM_K3XY 7
+#define IBIM_K3YZ 8
+#define IBIM_K3ZX 9
+#define IBIM_K3YX 10
+#define IBIM_K3ZY 11
+#define IBIM_K3XZ 12
+#define IBIM_K4X 13
+#define IBIM_K4Y 14
+#define IBIM_K4Z 15
+/* 4 densities (phi n_x w, phi n_y w, phi n_z w, dphi w) -> 4 fields
+ * (F = K1.m - K2 dphi, G = H m - K4 dphi, H the K3 block): all 16 FMMs of one matvec
+ * (electric.cpp:333-367) in one pass. */
+#define IBIM_KERNEL_BIE_FUSED 16
+
+/* ---- precision modes ---- */
+#define IBIM_PRECISION_FP64 0  /* reference-exact FP64 path */
+#define IBIM_PRECISION_MIXED 1 /* FP32 far/near field inside FP64 iterative refinement */
+
+typedef struct ibim_ctx_s *ibim_ctx;
+typedef struct ibim_grid_s *ibim_grid;
+typedef struct ibim_tube_s *ibim_tube;
+typedef struct ibim_plan_s *ibim_plan;
+
+/* Solvent / kernel parameters (electric.cpp:52-58: solvent_kappa, solvent_dE, solvent_dI, tau). */
+typedef struct {
+    double kappa, dE, dI, tau;
+} ibim_kernel_params;
+
+/* Everything input.cfg carries for this path, with the geometry explicit. */
+typedef struct {
+    double lo[3];      /* grid origin (levelset sx, sy, sz) */
+    double h;          /* grid spacing (levelset dx) */
+    int n[3];          /* grid size (Nx, Ny, Nz) */
+    int band;          /* expand band in cells (main.cpp:45: 8) */
+    double init;       /* initial grid value (main.cpp:47: -2 * size) */
+    double probe;      /* probe radius (main.cpp:35: 1.4) */
+    double reinit_t;   /* reinit pseudo-time, input.cfg `reinit_step` (main.cpp:56,60) */
+    int thickness;     /* lvlset_thickness */
+    double thres;      /* lvlset_thres */
+    int np;            /* fmm_np (Chebyshev order) */
+    int maxpoint;      /* fmm_maxpoint */
+    int maxlevel;      /* fmm_maxlevel */
+    ibim_kernel_params kp;
+    int restart;       /* gmres_restart */
+    int maxiter;       /* gmres_maxiter */
+    double tol;        /* gmres_tol */
+    int precision;     /* IBIM_PRECISION_* */
+} ibim_config;
+
+typedef struct {
+    double energy;        /* polarized (solvation) energy, e^2/A (electric.cpp:499-505) */
+    double area;          /* sum of quadrature weights, A^2 (electric.cpp:60) */
+    long n_points;        /* tube points (POINTS NUM) */
+    long inclusion;       /* cavity cells removed (INCLUSION) */
+    int reinit_steps[2];  /* pseudo-time steps taken by the two reinitialisations */
+    int gmres_iters;      /* Arnoldi steps */
+    int matvecs;          /* operator applications (all precisions) */
+    int matvecs_fp64;     /* FP64 operator applications */
+    int gmres_status;     /* 0 converged, 1 not (gmres.cpp:186) */
+    int refinements;      /* outer iterative-refinement passes (mixed precision) */
+    double residual;      /* final relative residual ||b - A x|| / ||b|| */
+    double t_levelset_ms, t_surface_ms, t_plan_ms, t_solve_ms, t_energy_ms;
+} ibim_result;
+
+/* ---- context ---- */
+int ibim_ctx_create(int device, ibim_ctx *out);
+int ibim_ctx_destroy(ibim_ctx ctx);
+const char *ibim_last_error(void);
+const char *ibim_status_string(int status);
+/* Fill a config with the reference defaults (data/input.cfg, main.cpp). */
+void ibim_config_default(ibim_config *cfg);
+
+/* ---- level set: replaces Grid and levelset (levelset.h:12-60, levelset.cpp:9-432) ---- */
+int ibim_grid_create(ibim_ctx ctx, int nx, int ny, int nz, double sx, double sy, double sz, double dx,
+                     double value, ibim_grid *out);                          /* Grid(val, Nx, Ny, Nz) */
+int ibim_grid_destroy(ibim_grid g);
+int ibim_grid_upload(ibim_grid g, const double *host);                       /* row-major, k fastest */
+int ibim_grid_download(ibim_grid g, double *host);
+int ibim_grid_scale(ibim_grid g, double s);                                  /* Grid::operator*= */
+int ibim_grid_copy(ibim_grid dst, ibim_grid src);                            /* Grid::operator= */
+int ibim_levelset_expand(ibim_grid g, const double *centers, const double *radii, int natoms,
+                         double probe, int band);                            /* levelset::expand */
+int ibim_levelset_evolve(ibim_grid g, double final_t, double vel, double cfl); /* levelset::evolve */
+int ibim_levelset_reinitialize(ibim_grid g, ibim_grid phi0, double final_t, double vel, double cfl,
+                               int thickness, double thres, int *steps);    /* levelset::reinitialize */
+int ibim_levelset_count_gradient(ibim_grid g, double thickness, double thres, long *bad, long *total,
+                                 double *accum_error);                      /* levelset::countGradient */
+/* main.cpp:45-60 in one call: expand, evolve inward by the probe, flip sign, reinit twice. */
+int ibim_levelset_build(ibim_ctx ctx, const double *centers, const double *radii, int natoms,
+                        const ibim_config *cfg, ibim_grid *out, int steps[2]);
+
+/* ---- tube quadrature: replaces Surface (levelset.h:62-72, levelset.cpp:437-586) ---- */
+int ibim_surface_extract(ibim_grid g, int thickness, ibim_tube *out, long *n_points, long *inclusion);
+/* A tube from host arrays (points (n,3), normals (n,3), raw cosine weights (n)) on spacing h. */
+int ibim_tube_create(ibim_ctx ctx, const double *points, const double *normals, const double *weights, long n,
+                     double h, ibim_tube *out);
+int ibim_tube_destroy(ibim_tube t);
+long ibim_tube_size(ibim_tube t);
+/* Download in the reference's (i, j, k) order; any pointer may be NULL. */
+int ibim_tube_download(ibim_tube t, double *points, double *normals, double *weights);
+
+/* ---- black-box FMM: replaces bbfmm::tree / bbfmm::kernel (bbfmm.h:149-270) ---- */
+/* Tree and interaction lists over the tube points (sources); targets = the tube points when
+ * `targets` is NULL, else the nt host points given (e.g. atom centres, electric.cpp:432-489). */
+int ibim_fmm_plan(ibim_tube src, const double *targets, long nt, int order, int maxpoint, int maxlevel,
+                  int precision, ibim_plan *out);
+int ibim_plan_destroy(ibim_plan p);
+/* counts: nodes, levels, leaves, V pairs, X pairs, near-field pairs (source-target) */
+int ibim_plan_stats(ibim_plan p, long stats[8]);
+/* The tree and its U/V/W/X lists in the reference's node numbering (bbfmm.cpp:88-91), for
+ * inspection: buf gets nnodes, then per node level, parent, leaf, empty, nsrc, and for each
+ * list its length followed by its sorted node ids.  *needed receives the int count; call with
+ * cap = 0 first to size buf.  `which` is reserved (0). */
+int ibim_plan_lists(ibim_plan p, int which, int *buf, long cap, long *needed);
+/* The same tree and lists built on the host from n points (n, 3), without a GPU. */
+int ibim_tree_lists_host(const double *points, long n, int maxpoint, int maxlevel, int *buf, long cap, long *needed);
+/* One FMM.  kernel in [IBIM_K1X, IBIM_K4Z]: in is (ns), out is (nt);
+ * IBIM_KERNEL_BIE_FUSED: in is (4, ns), out is (4, nt).  Host buffers, caller point order. */
+int ibim_fmm_apply(ibim_plan p, int kernel, const ibim_kernel_params *kp, const double *in, double *out);
+
+/* ---- BIE operator, GMRES, energy: replaces GMRES (gmres.h:20-21) and electric (electric.h:13) ---- */
+/* y = dmapping(x) (electric.cpp:294-388), x, y of length 2N, host buffers, reference order. */
+int ibim_bie_matvec(ibim_plan p, const ibim_kernel_params *kp, const double *x, double *y);
+/* load (electric.cpp:395-412): b of length 2N. */
+int ibim_bie_rhs(ibim_plan p, const ibim_kernel_params *kp, const double *centers, const double *charges,
+                 int natoms, double *b);
+/* GMRES(m, max_iter, tol) on the BIE operator from x (in/out, 2N) (gmres.cpp:50-164). */
+int ibim_gmres_solve(ibim_plan p, const ibim_kernel_params *kp, const double *b, double *x, int restart,
+                     int maxiter, double tol, int precision, int *iters, int *gmres_status, double *residual);
+/* electric() after Surface: RHS, GMRES, polarizeMap, energy (electric.cpp:9-505).
+ * x (2N) and atom_potential (natoms) may be NULL. */
+int ibim_electric(ibim_tube tube, const double *centers, const double *charges, int natoms,
+                  const ibim_config *cfg, double *x, double *atom_potential, ibim_result *res);
+
+/* ---- whole path: main.cpp:45-77 for explicit geometry ---- */
+/* Host atom arrays (centers (n,3), charges, radii). */
+int ibim_solve(ibim_ctx ctx, const double *centers, const double *charges, const double *radii, int natoms,
+               const ibim_config *cfg, ibim_result *res);
+/* Same with the atoms already resident on the device (centers (n,3), charges, radii). */
+int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charges_dev, const double *radii_dev,
+                   int natoms, const ibim_config *cfg, ibim_result *res);
+/* PQR file (molecule.h:21-50: ATOM lines, tokens 5..9 = x y z q r). */
+int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, ibim_result *res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,91 @@
+"""CUDA level set and tube quadrature against the oracle and the reference's golden outputs."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import config_for, grid_stats
+
+pytestmark = pytest.mark.gpu
+CASES = ["born", "synth30", "cavity", "p1hje"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_levelset_build_matches_oracle(ctx, golden, case):
+    G = golden(case)
+    P = G["params"]
+    g, steps = ctx.levelset(G["centers"], G["radii"], config_for(P))
+    a = g.download()
+    ref, rsteps = O.levelset(G["centers"], G["radii"], P["lo"], P["h"], P["n"], reinit_t=P["reinit_t"],
+                             thickness=P["thickness"], thres=P["thres"], init=P["init"])
+    assert list(steps) == list(rsteps)
+    # FP64 stencils; FMA contraction on the GPU changes the last bits only (relative to the
+    # value: the far plateau sits near |init| and its band-edge jump amplifies rounding)
+    assert np.all(np.abs(a - ref) <= 1e-9 * np.maximum(1.0, np.abs(ref)))
+    np.testing.assert_allclose(grid_stats(a), G["gridstats_reinit2"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_surface_matches_reference(ctx, golden, case):
+    G = golden(case)
+    P = G["params"]
+    g, _ = ctx.levelset(G["centers"], G["radii"], config_for(P))
+    t = g.surface(P["thickness"])
+    s = t.surface7()
+    assert t.inclusion == P["scalars"].get("INCLUSION", 0)
+    assert len(s) == len(G["surface"])
+    assert np.abs(s - G["surface"]).max() < 1e-9
+    np.testing.assert_allclose(grid_stats(g.download()), G["gridstats_surface"], rtol=1e-9)
+
+
+def test_stages_match_oracle(ctx, golden):
+    G = golden("synth30")
+    P = G["params"]
+    n, lo, h = P["n"], P["lo"], P["h"]
+    g = ctx.grid(n, lo, h, P["init"])
+    g.expand(G["centers"], G["radii"])
+    ref = np.full(tuple(n), P["init"])
+    O.expand(ref, G["centers"], G["radii"], lo, h)
+    np.testing.assert_allclose(g.download(), ref, rtol=0, atol=1e-13)
+    g.evolve(1.4, 1.0, 0.2)
+    O.evolve(ref, h, 1.4, 1.0, 0.2)
+    assert np.abs(g.download() - ref).max() < 1e-10
+    g.scale(-1.0)
+    ref *= -1.0
+    phi0 = ctx.grid(n, lo, h, 0.0)
+    phi0.copy_from(g)
+    bad, tot, acc = g.count_gradient(P["thickness"], P["thres"])
+    rb, rt, ra = O.count_gradient(ref, h, P["thickness"], P["thres"])
+    assert (bad, tot) == (rb, rt)
+    assert abs(acc - ra) < 1e-9 * max(1.0, abs(ra))
+    st = g.reinitialize(phi0, 2.0, 1.0, 0.5, P["thickness"], P["thres"])
+    rst = O.reinitialize(ref, ref.copy(), h, 2.0, thickness=P["thickness"], thres=P["thres"])
+    assert st == rst
+    assert np.abs(g.download() - ref).max() < 1e-10
+
+
+def test_upload_download_roundtrip(ctx):
+    a = np.random.default_rng(0).standard_normal((7, 9, 11))
+    g = ctx.grid(a.shape, (0, 0, 0), 0.5)
+    g.upload(a)
+    assert np.array_equal(g.download(), a)
+
+
+def test_expand_clips_at_grid_edge(ctx):
+    """Cells of an atom's band cube outside the grid are skipped (Grid::set does not clamp)."""
+    c = np.array([[0.2, 0.1, -0.3]])
+    r = np.array([1.5])
+    n, lo, h = (24, 20, 22), (-2.0, -2.0, -2.0), 0.25
+    g = ctx.grid(n, lo, h, -50.0)
+    g.expand(c, r)
+    ref = np.full(n, -50.0)
+    O.expand(ref, c, r, lo, h)
+    np.testing.assert_allclose(g.download(), ref, rtol=0, atol=1e-13)
+
+
+def test_no_tube_points(ctx):
+    """An atom far outside the grid leaves no tube points."""
+    g = ctx.grid((16, 16, 16), (0, 0, 0), 0.5, -30.0)
+    g.expand(np.array([[100.0, 100.0, 100.0]]), np.array([1.0]))
+    t = g.surface(2)
+    assert len(t) == 0
