@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Benchmark of the IBIM Poisson-Boltzmann path on GB300: FMM-GMRES solves/sec, p50/p99 latency.
+
+One step = one whole solve of the workload (level set -> tube quadrature -> octree plan ->
+GMRES on the fused BIE FMM -> polarization energy) through the C ABI.
+
+  value   solves/sec with the atoms already in HBM (ibim_solve_dev), device time from CUDA events
+          on the library's stream, L2 flushed (256 MB write) between steps
+  e2e     the same through ibim_solve with host buffers (host->device copies inside the region)
+  roofline  the dominant kernel category of the timed region: algorithmic flops (or bytes) of its
+          launches / their CUDA-event time, against the measured peak of its bound
+  cpu_baseline  the oracle (plain-C restatement of the reference, reference-structured: 16 scalar
+          FMMs per matvec with on-the-fly M2L, as electric.cpp/bbfmm.h do) timed on a bounded
+          sample of the same workload on the host cores, extrapolated to one solve
+
+--impl reference runs only that CPU path and prints its line.
+Multi-GPU: replicas only (independent solves per rank, no collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ibim-levelset_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+import workloads  # noqa: E402
+
+METRIC = "FMM-GMRES solves/sec (whole IBIM PB solve) at <=1e-4 rel. energy err vs FP64 path"
+UNIT = "solves/s"
+# Arnoldi steps + 1 (the reference also applies the operator to x0 = 0) of the FP64 path on
+# protein2000, measured on GB300; the FP64 GPU path reproduces the reference's iteration counts
+# on every golden case, so the CPU baseline extrapolates with it.
+REF_MATVECS = {"synthetic_protein_2000_atoms_h0.5": None}
+FMM_STRIDE = 8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--workload", choices=["protein2000", "born"], default="protein2000")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def get_workload(name):
+    return workloads.protein2000() if name == "protein2000" else workloads.born()
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU baseline: bounded sample of the reference's CPU algorithm (the oracle restatement)
+# ---------------------------------------------------------------------------------------------
+
+def cpu_sample(W, grid_reinit=None, tube7=None, matvecs=None, stages=None):
+    """Time one bounded sample; return (extrapolated seconds per solve, parts dict).
+
+    Sample: one TVD-RK3 step (3 stages) of the level set on the full grid, the tube extraction,
+    the direct right-hand side, and one scalar FMM (kernel K1x, tree built per FMM) on the full
+    tube.  A solve = stages/3 level-set steps + tube + RHS + 16 FMMs per matvec + 4 (polarize).
+    """
+    import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    geo = W.geo
+    parts = {}
+    if grid_reinit is None or tube7 is None:
+        g, steps = O.levelset(W.mol.centers, W.mol.radii, geo.lo, geo.h, geo.n, reinit_t=W.reinit_t,
+                              thickness=W.thickness, thres=W.thres, init=W.init)
+        if stages is None:
+            stages = 3 * (int(1.4 / (0.2 * geo.h)) + 1 + int(steps[0]) + int(steps[1]))
+        grid_reinit = g.copy()
+        t0 = time.perf_counter()
+        tube7, _ = O.surface(g, geo.lo, geo.h, W.thickness)
+        parts["surface_s"] = time.perf_counter() - t0
+    else:
+        g = grid_reinit.copy()
+        t0 = time.perf_counter()
+        O.surface(g, geo.lo, geo.h, W.thickness)
+        parts["surface_s"] = time.perf_counter() - t0
+    # one level-set step (3 full-grid stages): evolve with final_t < dt takes exactly one step
+    g = grid_reinit.copy()
+    t0 = time.perf_counter()
+    O.evolve(g, geo.h, 0.5 * 0.2 * geo.h, 1.0, 0.2)
+    parts["levelset_step_s"] = time.perf_counter() - t0
+    bp = O.bie_params(W.np_, W.maxpoint, W.maxlevel, W.restart, W.maxiter, W.kappa, W.dE, W.dI, W.tau, W.tol, 1)
+    t0 = time.perf_counter()
+    O.rhs(tube7, W.mol.centers, W.mol.charges, bp)
+    parts["rhs_s"] = time.perf_counter() - t0
+    N = len(tube7)
+    dens = np.sin(0.37 * np.arange(N)) * tube7[:, 3] * tube7[:, 6] * geo.h ** 3
+    # one scalar FMM (K1x) with its own tree, as electric.cpp:333-367 does per kernel; the
+    # downward pass is sampled on every FMM_STRIDE-th node and scaled back
+    t0 = time.perf_counter()
+    T = O.Tree(tube7[:, :3], tube7[:, :3], W.maxpoint, W.maxlevel)
+    t_tree = time.perf_counter() - t0
+    kp = O.KParams(W.kappa, W.dE, W.dI, W.tau * geo.h)
+    t0 = time.perf_counter()
+    T.fmm(W.np_, kp, 0, dens, sample_stride=FMM_STRIDE)
+    t_sampled = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    T.fmm(W.np_, kp, 0, dens, sample_stride=1 << 30)
+    t_up = time.perf_counter() - t0  # upward pass alone (node 0 only downward)
+    parts["fmm_scalar_s"] = t_tree + t_up + (t_sampled - t_up) * FMM_STRIDE
+    del T
+    if matvecs is None:
+        matvecs = REF_MATVECS.get(W.name) or 31
+    if stages is None:
+        stages = 3 * (int(1.4 / (0.2 * geo.h)) + 1 + 2 * W.reinit_steps)
+    solve_s = (parts["levelset_step_s"] * stages / 3.0 + parts["surface_s"] + parts["rhs_s"] +
+               parts["fmm_scalar_s"] * (16 * matvecs + 4))
+    parts.update(threads=threads, matvecs=matvecs, stages=stages, points=N)
+    return solve_s, parts
+
+
+def cpu_baseline_object(solve_s, parts, kind="port"):
+    sample = (f"oracle port (reference-structured) on {parts['threads']} host threads: one level-set step "
+              f"(3 full-grid stages) x {parts['stages'] // 3}, tube extraction, direct RHS, one scalar FMM "
+              f"(K1x, own tree; downward pass timed on every {FMM_STRIDE}th node and scaled) x "
+              f"(16 x {parts['matvecs']} matvecs + 4 polarize FMMs) on {parts['points']} tube points")
+    return {"value": 1.0 / solve_s, "unit": UNIT, "cores": parts["threads"], "kind": kind, "sample": sample,
+            "seconds_per_solve": solve_s, "parts_s": {k: round(v, 4) for k, v in parts.items() if k.endswith("_s")}}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    W = get_workload(args.workload)
+    import oracle as O
+
+    O.build()
+    geo = W.geo
+    g, steps = O.levelset(W.mol.centers, W.mol.radii, geo.lo, geo.h, geo.n, reinit_t=W.reinit_t,
+                          thickness=W.thickness, thres=W.thres, init=W.init)
+    stages = 3 * (int(1.4 / (0.2 * geo.h)) + 1 + int(steps[0]) + int(steps[1]))
+    gg = g.copy()
+    tube7, _ = O.surface(gg, geo.lo, geo.h, W.thickness)
+    times, parts = [], None
+    for i in range(args.warmup + args.steps):
+        s, parts = cpu_sample(W, grid_reinit=g, tube7=tube7, stages=stages)
+        if i >= args.warmup:
+            times.append(s)
+    solve_s = statistics.mean(times)
+    value = 1.0 / solve_s
+    cb = cpu_baseline_object(solve_s, parts, kind="port")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "config": W.describe(), "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms",
+                                       "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for ln in fh:
+                c = [v.strip() for v in ln.split(",")]
+                if len(c) >= 9:
+                    rows.append(c)
+        os.unlink(self.f.name)
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        mine = [r for r in rows if r[0] == dev] or rows
+        sm = [float(r[1]) for r in mine if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in mine if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in mine for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(mine)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def committed_traffic(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary (profiles/traffic_per_launch.txt)."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    try:
+        with open(path) as f:
+            for ln in f:
+                t = ln.split()
+                if len(t) >= 3 and t[0] == kernel and t[1] == workload:
+                    return float(t[2])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+
+    import ibim
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    W = get_workload(args.workload)
+    precision = ibim.PRECISION_FP64 if args.precision == "fp64" else ibim.PRECISION_MIXED
+    cfg = W.config(precision)
+    ctx = ibim.Context(local)
+    ext = torch.cuda.ExternalStream(ctx.stream)
+    dev = torch.device("cuda", local)
+    centers = torch.tensor(W.mol.centers, dtype=torch.float64, device=dev).contiguous()
+    charges = torch.tensor(W.mol.charges, dtype=torch.float64, device=dev).contiguous()
+    radii = torch.tensor(W.mol.radii, dtype=torch.float64, device=dev).contiguous()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step_dev():
+        return ctx.solve_dev(centers.data_ptr(), charges.data_ptr(), radii.data_ptr(), W.mol.n, cfg)
+
+    def timed(fn, n):
+        out, ms = [], []
+        for _ in range(n):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            r = fn()
+            b.record(ext)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            out.append(r)
+        return out, ms
+
+    for _ in range(args.warmup):
+        step_dev()
+    ctx.profile(ibim.PROFILE_CATEGORIES)
+    ctx.profile_read()
+    sampler = ClockSampler()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    l0 = ibim.launch_count()
+    results, step_ms = timed(step_dev, args.steps)
+    launches = ibim.launch_count() - l0
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    prof = ctx.profile_read()
+    ctx.profile([])
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+    r0 = results[-1]
+
+    # end to end through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        _, e2e_ms = timed(lambda: ctx.solve(W.mol.centers, W.mol.charges, W.mol.radii, cfg), args.steps)
+        e2e = {"value": world * args.steps / (sum(e2e_ms) / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": int(W.mol.n * 5 * 8), "d2h_bytes_per_step": int(ctypes.sizeof(ibim.Result)),
+               "ms_per_step": statistics.mean(e2e_ms)}
+
+    # roofline of the dominant kernel category
+    peaks = measured_peaks()
+    fp64_peak = ctx.measure_peak("fp64")
+    fp32_peak = ctx.measure_peak("fp32")
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else None
+    roofline = None
+    if dom:
+        name, d = dom
+        fp_bound = {"m2l_v": "fp64", "m2l_x": "fp64", "near_l2p": "fp64", "weno_stage": "fp64", "p2m": "fp64"}
+        if precision == ibim.PRECISION_MIXED and name in ("near_l2p", "m2l_v", "m2l_x", "p2m"):
+            fp_bound = {name: "fp32"}
+        bound = fp_bound.get(name, "hbm")
+        per_launch_ms = d["ms"] / d["launches"]
+        if bound == "hbm":
+            ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
+            peak, unit, src = peaks.get("hbm_gbs", 6800.0), "GB/s", "MEASURED_PEAKS.json hbm_gbs (of measured)"
+        else:
+            ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
+            peak = fp64_peak if bound == "fp64" else fp32_peak
+            unit, src = "TFLOP/s", f"{bound.upper()} FMA-chain microkernel measured in this run (of measured)"
+        roofline = {"bound": bound, "kernel": name, "achieved": ach, "peak": peak, "unit": unit,
+                    "frac": ach / peak if peak else None, "peak_source": src,
+                    "traffic": committed_traffic(name, W.name), "launches": d["launches"],
+                    "avg_launch_ms": per_launch_ms,
+                    "algorithmic_per_launch": d["flops"] / d["launches"] if bound != "hbm" else d["bytes"] / d["launches"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            g, _ = ctx.levelset(W.mol.centers, W.mol.radii, cfg)
+            grid = g.download()
+            tube7 = g.surface(W.thickness).surface7()
+            g.close()
+            ref_mv = r0["matvecs"] + 1 if precision == ibim.PRECISION_FP64 else None
+            solve_s, parts = cpu_sample(W, grid_reinit=grid, tube7=tube7, matvecs=ref_mv,
+                                        stages=r0["levelset_stages"])
+            cpu = cpu_baseline_object(solve_s, parts)
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"error": str(e)}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f32+f64",
+           "data": "synthetic (seeded generator, same shapes as the configuration)",
+           "config": dict(W.describe(), precision=args.precision, parallelism=f"replicas{world}",
+                          l2="flushed (256 MB write) between steps", tube_points=r0["n_points"]),
+           "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+           "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
+           "solve": {k: r0[k] for k in ("energy", "area", "n_points", "gmres_iters", "matvecs", "matvecs_fp64",
+                                        "refinements", "residual", "gmres_status", "reinit_steps", "t_levelset_ms",
+                                        "t_surface_ms", "t_plan_ms", "t_solve_ms", "t_energy_ms", "fmm_nodes",
+                                        "fmm_v_pairs", "fmm_x_pairs", "fmm_near_pairs", "fmm_operators")},
+           "kernels_ms_per_step": {k: round(v["ms"] / args.steps, 3) for k, v in prof.items()},
+           "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak,
+                              "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")}}
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

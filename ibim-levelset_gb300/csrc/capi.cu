@@ -2,6 +2,7 @@
 // Every entry point catches library errors and returns a status; ibim_last_error() gives text.
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -14,8 +15,41 @@
 namespace ibim {
 
 static thread_local std::string g_last_error;
+static thread_local Ctx *g_current = nullptr;
+static std::atomic<long> g_launches{0};
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(); }
+Ctx *current_ctx() { return g_current; }
+void set_current_ctx(Ctx *c) { g_current = c; }
+
+cudaEvent_t Ctx::take_event() {
+    if (ev_pool.empty()) {
+        cudaEvent_t e;
+        IBIM_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+    cudaEvent_t e = ev_pool.back();
+    ev_pool.pop_back();
+    return e;
+}
+
+// FMA chains (8 independent per thread) to measure the FP64 / FP32 issue rate of the device.
+template <typename T>
+__global__ void k_fma_chain(T *out, int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = (T)(threadIdx.x + q) * (T)1e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = x[q] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += x[q];
+    if (s == (T)1234.5) out[blockIdx.x] = s;
+}
 
 template <class F>
 static int guard(F &&f) {
@@ -34,7 +68,10 @@ static int guard(F &&f) {
     }
 }
 
-static void bind(Ctx *c) { IBIM_CUDA(cudaSetDevice(c->device)); }
+static void bind(Ctx *c) {
+    IBIM_CUDA(cudaSetDevice(c->device));
+    set_current_ctx(c);
+}
 
 // Single-kernel FMMs through the fused block: (input density slot, output field, sign) per
 // reference kernel (electric.cpp:67-291); H is symmetric, so K3ab reads slot b, field G_a.
@@ -76,6 +113,15 @@ static void check_config(const ibim_config &cfg) {
     IBIM_REQUIRE(cfg.precision == IBIM_PRECISION_FP64 || cfg.precision == IBIM_PRECISION_MIXED, "unknown precision");
 }
 
+static void fill_plan_stats(const Plan &P, ibim_result &res) {
+    const TargetSet &S = *P.targets[0];
+    res.fmm_nodes = P.tree.nnodes;
+    res.fmm_v_pairs = S.nvpairs;
+    res.fmm_x_pairs = S.nxpairs;
+    res.fmm_near_pairs = S.near_pairs;
+    res.fmm_operators = P.nops;
+}
+
 // main.cpp:45-60 with s = 1
 static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *radii_dev, int natoms,
                                const ibim_config &cfg, int steps[2]) {
@@ -109,6 +155,8 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     Timer t0(s);
     Grid *g = levelset_pipeline(c, centers_dev, radii_dev, natoms, cfg, res.reinit_steps);
     res.t_levelset_ms = t0.ms();
+    res.grid_cells = (long)cfg.n[0] * cfg.n[1] * cfg.n[2];
+    res.levelset_stages = 3 * ((int)(cfg.probe / (0.2 * cfg.h)) + 1 + res.reinit_steps[0] + res.reinit_steps[1]);
     Timer t1(s);
     Tube *tube = nullptr;
     try {
@@ -144,6 +192,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         }
         electric_solve(*P, cfg.kp, atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol, cfg.precision,
                        nullptr, nullptr, res);
+        fill_plan_stats(*P, res);
     } catch (...) {
         delete P;
         delete tube;
@@ -252,6 +301,78 @@ int ibim_ctx_destroy(ibim_ctx ctx) {
         cudaStreamSynchronize(ctx->c.stream);
         cudaStreamDestroy(ctx->c.stream);
         delete ctx;
+    });
+}
+
+void *ibim_ctx_stream(ibim_ctx ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+long ibim_launch_count(void) { return launch_count(); }
+
+int ibim_profile_enable(ibim_ctx ctx, unsigned mask) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx, "null handle");
+        ctx->c.prof_mask = mask;
+    });
+}
+
+int ibim_profile_work(ibim_ctx ctx, double *flops, double *bytes, int ncat) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && flops && bytes, "null argument");
+        for (int k = 0; k < ncat && k < PROF_NCAT; ++k) {
+            flops[k] = ctx->c.prof_flops[k];
+            bytes[k] = ctx->c.prof_bytes[k];
+        }
+    });
+}
+
+int ibim_profile_read(ibim_ctx ctx, double *ms, long *launches, int ncat) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && ms && launches, "null argument");
+        Ctx &c = ctx->c;
+        bind(&c);
+        IBIM_CUDA(cudaStreamSynchronize(c.stream));
+        for (int k = 0; k < PROF_NCAT; ++k) {
+            double t = 0.;
+            for (auto &pr : c.prof_ev[k]) {
+                float m = 0.f;
+                IBIM_CUDA(cudaEventElapsedTime(&m, pr.first, pr.second));
+                t += m;
+                c.ev_pool.push_back(pr.first);
+                c.ev_pool.push_back(pr.second);
+            }
+            if (k < ncat) {
+                ms[k] = t;
+                launches[k] = (long)c.prof_ev[k].size();
+            }
+            c.prof_ev[k].clear();
+            c.prof_flops[k] = c.prof_bytes[k] = 0.;
+        }
+    });
+}
+
+int ibim_measure_peak(ibim_ctx ctx, int kind, double *tflops) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && tflops && (kind == 0 || kind == 1), "invalid argument");
+        Ctx &c = ctx->c;
+        bind(&c);
+        const int blocks = c.num_sms * 8, threads = 256, iters = kind == 0 ? 2048 : 16384;
+        DevBuf<double> out;
+        out.alloc(blocks, c.stream);
+        auto launch = [&] {
+            if (kind == 0)
+                (count_launch(), k_fma_chain<double><<<blocks, threads, 0, c.stream>>>(out.ptr, iters, 0.999999, 1e-7));
+            else
+                (count_launch(), k_fma_chain<float><<<blocks, threads, 0, c.stream>>>((float *)out.ptr, iters, 0.999999f, 1e-7f));
+            IBIM_CHECK_LAUNCH();
+        };
+        launch();
+        double best = 1e30;
+        for (int r = 0; r < 5; ++r) {
+            Timer t(c.stream);
+            launch();
+            best = std::min(best, t.ms());
+        }
+        *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
     });
 }
 

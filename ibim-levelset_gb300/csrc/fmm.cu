@@ -392,7 +392,7 @@ void up_int(DevBuf<int> &b, const std::vector<int> &v, cudaStream_t s) {
 
 void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale) {
     if (n <= 0) return;
-    k_gather<<<(int)std::min<long>(4L * c->num_sms, div_up(n, 256)), 256, 0, c->stream>>>(n, perm, a, b, scale);
+    (count_launch(), k_gather<<<(int)std::min<long>(4L * c->num_sms, div_up(n, 256)), 256, 0, c->stream>>>(n, perm, a, b, scale));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -700,7 +700,7 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
     if (precision == IBIM_PRECISION_FP64) {
         P.ops64.alloc((size_t)P.nops * n4 * n4, s);
         dim3 g(div_up((long)R * R, 256), P.nops);
-        k_make_ops64<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops64.ptr);
+        { ProfScope ps_(PROF_OPS); (count_launch(), k_make_ops64<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops64.ptr)); }
         IBIM_CHECK_LAUNCH();
     } else {
         fmm_prepare_operators_mixed(P, k);
@@ -720,35 +720,35 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
     const KParams kp = make_kparams(kpp, P.tube->h);
     const size_t smem_k = sizeof(double) * 3 * n4;
     if (P.np2m > 0)
-        k_p2m64<<<P.np2m, 128, 0, s>>>(P.tables.ptr, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
+        { ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 56.0 * P.ns); (count_launch(), k_p2m64<<<P.np2m, 128, 0, s>>>(P.tables.ptr, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
                                        P.ncenter.ptr, P.nradius.ptr, P.sx.ptr, P.sy.ptr, P.sz.ptr, dens, P.ns,
-                                       P.mult.ptr);
+                                       P.mult.ptr)); }
     for (int l = T.nlevels - 1; l >= 0; --l) {
         const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
         if (e > b)
-            k_m2m64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
-                                               P.mult.ptr);
+            { ProfScope ps_(PROF_M2M); (count_launch(), k_m2m64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
+                                               P.mult.ptr)); }
     }
     P.local.zero();
     if (S.nchunks > 0)
-        k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
-                                                                       P.ops64.ptr, P.mult.ptr, P.local.ptr);
+        { ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
+                                                                       P.ops64.ptr, P.mult.ptr, P.local.ptr)); }
     if (S.nxpairs > 0)
-        k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
-                                                 P.nradius.ptr, P.mult.ptr, P.local.ptr);
+        { ProfScope ps_(PROF_M2L_X, 102.0 * R * (double)R * S.nxpairs, 16.0 * n4 * S.nxpairs); (count_launch(), k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
+                                                 P.nradius.ptr, P.mult.ptr, P.local.ptr)); }
     for (int l = 3; l < T.nlevels; ++l) {
         const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
         if (e > b)
-            k_l2l64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
-                                               P.local.ptr);
+            { ProfScope ps_(PROF_L2L); (count_launch(), k_l2l64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
+                                               P.local.ptr)); }
     }
     const double *tx = S.self ? P.sx.ptr : S.tx.ptr;
     const double *ty = S.self ? P.sy.ptr : S.ty.ptr;
     const double *tz = S.self ? P.sz.ptr : S.tz.ptr;
     if (S.ntleaves > 0)
-        k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
+        { ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
                                                S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
-                                               P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out);
+                                               P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out)); }
     IBIM_CHECK_LAUNCH();
 }
 

@@ -74,11 +74,51 @@ struct DevBuf {
     }
 };
 
+// Kernel categories timed with CUDA events when profiling is enabled on a context.
+enum ProfCat {
+    PROF_EXPAND = 0, PROF_WENO, PROF_COUNT, PROF_FLOOD, PROF_TUBE, PROF_OPS, PROF_P2M, PROF_M2M, PROF_M2L_V,
+    PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_NCAT
+};
+
+// Number of kernels this library launched (all contexts).
+void count_launch();
+long launch_count();
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 0;
-    cudaEvent_t ev[8];
+    unsigned prof_mask = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[PROF_NCAT];
+    double prof_flops[PROF_NCAT] = {0}, prof_bytes[PROF_NCAT] = {0};  // algorithmic work of profiled launches
+    std::vector<cudaEvent_t> ev_pool;
+    cudaEvent_t take_event();
+};
+
+// The context bound by the current C-ABI call on this thread.
+Ctx *current_ctx();
+void set_current_ctx(Ctx *c);
+
+// Records CUDA events around the launches of one category when the context profiles it.
+struct ProfScope {
+    Ctx *c;
+    int cat;
+    cudaEvent_t a = nullptr;
+    explicit ProfScope(int category, double flops = 0., double bytes = 0.) : c(current_ctx()), cat(category) {
+        if (c && (c->prof_mask & (1u << cat))) {
+            a = c->take_event();
+            cudaEventRecord(a, c->stream);
+            c->prof_flops[cat] += flops;
+            c->prof_bytes[cat] += bytes;
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = c->take_event();
+            cudaEventRecord(b, c->stream);
+            c->prof_ev[cat].push_back({a, b});
+        }
+    }
 };
 
 struct Grid {

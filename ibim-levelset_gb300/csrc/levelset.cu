@@ -373,7 +373,7 @@ Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double s
     g->sx = sx; g->sy = sy; g->sz = sz; g->dx = dx;
     try {
         g->data.alloc(g->cells(), c->stream);
-        k_fill<<<4 * c->num_sms, 256, 0, c->stream>>>(g->data.ptr, g->cells(), value);
+        (count_launch(), k_fill<<<4 * c->num_sms, 256, 0, c->stream>>>(g->data.ptr, g->cells(), value));
         IBIM_CHECK_LAUNCH();
     } catch (...) {
         delete g;
@@ -387,15 +387,15 @@ void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev
     IBIM_REQUIRE(natoms <= 65535 * 64, "too many atoms");
     cudaStream_t s = g.ctx->stream;
     const long n = g.cells();
-    k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, +1);
+    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, +1)); }
     // atoms beyond gridDim.y's limit are processed in slices
     for (int a0 = 0; a0 < natoms; a0 += 65535) {
         const int na = std::min(65535, natoms - a0);
         dim3 grid(8, na);
-        k_expand<<<grid, 256, 0, s>>>(reinterpret_cast<unsigned long long *>(g.data.ptr), dims_of(g), g.sx, g.sy,
-                                      g.sz, g.dx, centers_dev + 3 * (long)a0, radii_dev + a0, probe, band);
+        { ProfScope ps_(PROF_EXPAND); (count_launch(), k_expand<<<grid, 256, 0, s>>>(reinterpret_cast<unsigned long long *>(g.data.ptr), dims_of(g), g.sx, g.sy,
+                                      g.sz, g.dx, centers_dev + 3 * (long)a0, radii_dev + a0, probe, band)); }
     }
-    k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, -1);
+    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, -1)); }
     IBIM_CHECK_LAUNCH();
 }
 
@@ -412,9 +412,9 @@ void levelset_evolve(Grid &g, double final_t, double vel, double cfl) {
     const dim3 gr = stencil_grid(g), bl = stencil_block();
     const double dtv = dt * vel, ih = g.dx;
     for (int st = 0; st < steps; ++st) {
-        k_weno_stage<0, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., g.data.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr);
-        k_weno_stage<0, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u1.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr);
-        k_weno_stage<0, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u2.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr);
+        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., g.data.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u1.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u2.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
     }
     IBIM_CHECK_LAUNCH();
 }
@@ -427,8 +427,8 @@ void levelset_count_gradient(const Grid &g, double thickness, double thres, long
     a.alloc(1, s);
     cnt.zero();
     a.zero();
-    k_count_grad<<<stencil_grid(g), stencil_block(), 0, s>>>(dims_of(g), g.dx, thickness * g.dx, thres,
-                                                             g.data.ptr, cnt.ptr, a.ptr);
+    { ProfScope ps_(PROF_COUNT, 0., 8.0 * g.cells()); (count_launch(), k_count_grad<<<stencil_grid(g), stencil_block(), 0, s>>>(dims_of(g), g.dx, thickness * g.dx, thres,
+                                                             g.data.ptr, cnt.ptr, a.ptr)); }
     IBIM_CHECK_LAUNCH();
     unsigned long long h[2];
     double ha;
@@ -462,7 +462,7 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
     const double dtv = dt * vel, ih = g.dx, band = thickness * g.dx;
     auto count = [&]() -> unsigned long long {
         cnt.zero();
-        k_count_grad<<<gr, bl, 0, s>>>(dm, ih, band, thres, g.data.ptr, cnt.ptr, acc.ptr);
+        { ProfScope ps_(PROF_COUNT, 0., 8.0 * g.cells()); (count_launch(), k_count_grad<<<gr, bl, 0, s>>>(dm, ih, band, thres, g.data.ptr, cnt.ptr, acc.ptr)); }
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaMemcpyAsync(hcnt, cnt.ptr, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         IBIM_CUDA(cudaStreamSynchronize(s));
@@ -473,12 +473,12 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
         unsigned long long bad = count();
         while (bad != 0 && step < steps) {
             step++;
-            k_weno_stage<1, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, g.data.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr);
-            k_weno_stage<1, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u1.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr);
-            k_weno_stage<1, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u2.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr);
+            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, g.data.ptr, g.data.ptr, u1.ptr, u2.ptr,
+                                                 phi0.data.ptr)); }
+            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u1.ptr, g.data.ptr, u1.ptr, u2.ptr,
+                                                 phi0.data.ptr)); }
+            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u2.ptr, g.data.ptr, u1.ptr, u2.ptr,
+                                                 phi0.data.ptr)); }
             bad = count();
         }
     } catch (...) {
@@ -491,7 +491,7 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
 
 // Grid::operator*= (levelset.cpp:54-59)
 void grid_scale(Grid &g, double sc) {
-    k_scale<<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(g.data.ptr, g.cells(), sc);
+    (count_launch(), k_scale<<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(g.data.ptr, g.cells(), sc));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -525,7 +525,7 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     try {
         for (;;) {
             changed.zero();
-            for (int r = 0; r < 4; ++r) k_flood_tile<<<fg, fb, 0, s>>>(dm, -tw, g.data.ptr, vis.ptr, changed.ptr);
+            for (int r = 0; r < 4; ++r) { ProfScope ps_(PROF_FLOOD); (count_launch(), k_flood_tile<<<fg, fb, 0, s>>>(dm, -tw, g.data.ptr, vis.ptr, changed.ptr)); }
             IBIM_CHECK_LAUNCH();
             IBIM_CUDA(cudaMemcpyAsync(hflag, changed.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
             IBIM_CUDA(cudaStreamSynchronize(s));
@@ -546,8 +546,8 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     offsets.alloc(nb + 1, s);
     ninc.alloc(1, s);
     ninc.zero();
-    k_tube_count<<<nb, TUBE_BLOCK, 0, s>>>(n, tw, g.data.ptr, vis.ptr, counts.ptr, ninc.ptr);
-    k_scan_counts<<<1, 1024, 0, s>>>(counts.ptr, nb, offsets.ptr);
+    { ProfScope ps_(PROF_TUBE); (count_launch(), k_tube_count<<<nb, TUBE_BLOCK, 0, s>>>(n, tw, g.data.ptr, vis.ptr, counts.ptr, ninc.ptr)); }
+    { ProfScope ps_(PROF_TUBE); (count_launch(), k_scan_counts<<<1, 1024, 0, s>>>(counts.ptr, nb, offsets.ptr)); }
     IBIM_CHECK_LAUNCH();
     long total = 0;
     unsigned long long hinc = 0;
@@ -561,8 +561,8 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     try {
         DevBuf<double> *arrs[7] = {&t->x, &t->y, &t->z, &t->nx, &t->ny, &t->nz, &t->w};
         for (auto *a : arrs) a->alloc(total > 0 ? total : 1, s);
-        k_tube_emit<<<nb, TUBE_BLOCK, 0, s>>>(dm, g.sx, g.sy, g.sz, g.dx, tw, g.data.ptr, offsets.ptr, t->x.ptr,
-                                             t->y.ptr, t->z.ptr, t->nx.ptr, t->ny.ptr, t->nz.ptr, t->w.ptr);
+        { ProfScope ps_(PROF_TUBE); (count_launch(), k_tube_emit<<<nb, TUBE_BLOCK, 0, s>>>(dm, g.sx, g.sy, g.sz, g.dx, tw, g.data.ptr, offsets.ptr, t->x.ptr,
+                                             t->y.ptr, t->z.ptr, t->nx.ptr, t->ny.ptr, t->nz.ptr, t->w.ptr)); }
         IBIM_CHECK_LAUNCH();
     } catch (...) {
         delete t;

@@ -174,7 +174,7 @@ inline int ew_grid(Ctx *c, long n) { return (int)std::max<long>(1, std::min<long
 
 void permute(Ctx *c, long n, const int *perm, const double *in, double *out, bool scatter) {
     if (n <= 0) return;
-    k_permute<<<ew_grid(c, n), 256, 0, c->stream>>>(n, perm, in, out, scatter ? 1 : 0);
+    (count_launch(), k_permute<<<ew_grid(c, n), 256, 0, c->stream>>>(n, perm, in, out, scatter ? 1 : 0));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -186,12 +186,12 @@ void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *
     Ctx *c = P.ctx;
     const long n = P.ns;
     IBIM_REQUIRE(!P.targets.empty() && P.targets[0]->self, "BIE operator needs a plan over the tube points");
-    k_densities<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr, P.dens4.ptr);
+    (count_launch(), k_densities<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr, P.dens4.ptr));
     IBIM_CHECK_LAUNCH();
     TargetSet &S = *P.targets[0];
     fmm_run(P, 0, kp, P.dens4.ptr, S.out4.ptr, precision);
     const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
-    k_combine<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, S.out4.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, e1, e2, y);
+    (count_launch(), k_combine<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, S.out4.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, e1, e2, y));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -200,8 +200,8 @@ void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, in
     const long n = P.ns;
     const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
     const double c1 = 1.0 / (kp.dI * 4.0 * M_PI * e1), c2 = 1.0 / (kp.dI * 4.0 * M_PI * e2);
-    k_rhs<<<div_up(n, 256), 256, 0, c->stream>>>(n, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr,
-                                                 atoms4_dev, natoms, c1, c2, b);
+    { ProfScope ps_(PROF_RHS); (count_launch(), k_rhs<<<div_up(n, 256), 256, 0, c->stream>>>(n, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr,
+                                                 atoms4_dev, natoms, c1, c2, b)); }
     IBIM_CHECK_LAUNCH();
 }
 
@@ -249,8 +249,8 @@ Krylov::~Krylov() { if (hpin) cudaFreeHost(hpin); }
 
 double Krylov::norm(const double *a) {
     cudaStream_t s = ctx->stream;
-    k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, a, part.ptr);
-    k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0);
+    { ProfScope ps_(PROF_GMRES); (count_launch(), k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, a, a, part.ptr)); }
+    { ProfScope ps_(PROF_GMRES); (count_launch(), k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0)); }
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaMemcpyAsync(hpin, hcol.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
     IBIM_CUDA(cudaStreamSynchronize(s));
@@ -269,7 +269,7 @@ int Krylov::solve(const std::function<void(const double *, double *)> &A, double
     } else {
         A(x, w.ptr);
         st.matvecs++;
-        k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr);
+        (count_launch(), k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr));
         IBIM_CHECK_LAUNCH();
     }
     double beta = norm(r.ptr);
@@ -290,13 +290,13 @@ int Krylov::solve(const std::function<void(const double *, double *)> &A, double
         }
         std::copy(y.begin(), y.begin() + k + 1, hpin + m + 2);
         IBIM_CUDA(cudaMemcpyAsync(ydev.ptr, hpin + m + 2, sizeof(double) * (k + 1), cudaMemcpyHostToDevice, s));
-        k_update<<<eg, 256, 0, s>>>(n, k + 1, ydev.ptr, V.ptr, x);
+        { ProfScope ps_(PROF_GMRES); (count_launch(), k_update<<<eg, 256, 0, s>>>(n, k + 1, ydev.ptr, V.ptr, x)); }
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaStreamSynchronize(s));  // hpin reused next step
     };
     while (j <= max_iter) {
         // v0 = r / beta
-        k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, part.ptr, r.ptr, V.ptr, hcol.ptr, 0);
+        { ProfScope ps_(PROF_GMRES); (count_launch(), k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, part.ptr, r.ptr, V.ptr, hcol.ptr, 0)); }
         std::fill(sv.begin(), sv.end(), 0.);
         sv[0] = beta;
         for (i = 0; i < m && j <= max_iter; i++, j++) {
@@ -305,14 +305,14 @@ int Krylov::solve(const std::function<void(const double *, double *)> &A, double
             st.matvecs++;
             st.iters++;
             double *pa = part.ptr, *pb = part.ptr + RED_BLOCKS;
-            k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, w.ptr, V.ptr, pa);
+            { ProfScope ps_(PROF_GMRES); (count_launch(), k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, w.ptr, V.ptr, pa)); }
             for (int k = 1; k <= i + 1; ++k) {
                 const double *vnext = k <= i ? V.ptr + (size_t)k * n : nullptr;
-                k_mgs<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(k - 1) * n, vnext, pb,
-                                                         hcol.ptr, k - 1);
+                { ProfScope ps_(PROF_GMRES); (count_launch(), k_mgs<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(k - 1) * n, vnext, pb,
+                                                         hcol.ptr, k - 1)); }
                 std::swap(pa, pb);
             }
-            k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(i + 1) * n, hcol.ptr, i + 1);
+            { ProfScope ps_(PROF_GMRES); (count_launch(), k_normalize<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, pa, w.ptr, V.ptr + (size_t)(i + 1) * n, hcol.ptr, i + 1)); }
             IBIM_CHECK_LAUNCH();
             if (pa != part.ptr) {
                 // keep the <w,w> partials where the next restart's k_normalize does not look
@@ -335,11 +335,11 @@ int Krylov::solve(const std::function<void(const double *, double *)> &A, double
         update(i - 1);
         A(x, w.ptr);
         st.matvecs++;
-        k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr);
+        (count_launch(), k_sub<<<eg, 256, 0, s>>>(n, b, w.ptr, r.ptr));
         IBIM_CHECK_LAUNCH();
         // ||r||: partials of <r, r> land in part[0..) for the k_normalize of the next cycle
-        k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r.ptr, r.ptr, part.ptr);
-        k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0);
+        { ProfScope ps_(PROF_GMRES); (count_launch(), k_dot<<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, r.ptr, r.ptr, part.ptr)); }
+        { ProfScope ps_(PROF_GMRES); (count_launch(), k_normalize<<<1, RED_THREADS, 0, s>>>(0, part.ptr, nullptr, nullptr, hcol.ptr, 0)); }
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaMemcpyAsync(hpin, hcol.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
         IBIM_CUDA(cudaStreamSynchronize(s));
@@ -396,10 +396,10 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
             st.iters += si.iters;
             st.matvecs += si.matvecs;
             left -= si.iters;
-            k_axpy<<<ew_grid(c, n2), 256, 0, s>>>(n2, 1.0, d.ptr, x.ptr);
+            (count_launch(), k_axpy<<<ew_grid(c, n2), 256, 0, s>>>(n2, 1.0, d.ptr, x.ptr));
             A64(x.ptr, K.w.ptr);
             fp64++;
-            k_sub<<<ew_grid(c, n2), 256, 0, s>>>(n2, b.ptr, K.w.ptr, r.ptr);
+            (count_launch(), k_sub<<<ew_grid(c, n2), 256, 0, s>>>(n2, b.ptr, K.w.ptr, r.ptr));
             IBIM_CHECK_LAUNCH();
             rel = K.norm(r.ptr) / (normb == 0 ? 1 : normb);
             st.history.push_back(rel);
@@ -419,8 +419,8 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
     Timer te(s);
     if (natoms > 0 && P.targets.size() > 1) {
         TargetSet &A = *P.targets[1];
-        k_densities<<<ew_grid(c, P.ns), 256, 0, s>>>(P.ns, x.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr,
-                                                      P.dens4.ptr);
+        (count_launch(), k_densities<<<ew_grid(c, P.ns), 256, 0, s>>>(P.ns, x.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr,
+                                                      P.dens4.ptr));
         IBIM_CHECK_LAUNCH();
         fmm_run(P, 1, kp, P.dens4.ptr, A.out4.ptr, IBIM_PRECISION_FP64);
         std::vector<double> F(A.nt);

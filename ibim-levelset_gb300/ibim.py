@@ -43,8 +43,11 @@ EXPORTS = [
     "ibim_levelset_count_gradient", "ibim_levelset_build", "ibim_surface_extract", "ibim_tube_create",
     "ibim_tube_destroy", "ibim_tube_size", "ibim_tube_download", "ibim_fmm_plan", "ibim_plan_destroy",
     "ibim_plan_stats", "ibim_plan_lists", "ibim_fmm_apply", "ibim_bie_matvec", "ibim_bie_rhs", "ibim_gmres_solve",
-    "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host",
+    "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host", "ibim_ctx_stream",
+    "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
 ]
+PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
+                      "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors"]
 
 
 class IbimError(RuntimeError):
@@ -70,7 +73,10 @@ class Result(C.Structure):
                 ("reinit_steps", C.c_int * 2), ("gmres_iters", C.c_int), ("matvecs", C.c_int),
                 ("matvecs_fp64", C.c_int), ("gmres_status", C.c_int), ("refinements", C.c_int),
                 ("residual", C.c_double), ("t_levelset_ms", C.c_double), ("t_surface_ms", C.c_double),
-                ("t_plan_ms", C.c_double), ("t_solve_ms", C.c_double), ("t_energy_ms", C.c_double)]
+                ("t_plan_ms", C.c_double), ("t_solve_ms", C.c_double), ("t_energy_ms", C.c_double),
+                ("grid_cells", C.c_long), ("levelset_stages", C.c_int), ("fmm_nodes", C.c_long),
+                ("fmm_v_pairs", C.c_long), ("fmm_x_pairs", C.c_long), ("fmm_near_pairs", C.c_long),
+                ("fmm_operators", C.c_long)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -131,6 +137,12 @@ def lib():
         "ibim_solve_dev": ([_vp, _vp, _vp, _vp, C.c_int, C.POINTER(Config), C.POINTER(Result)], C.c_int),
         "ibim_solve_pqr": ([_vp, C.c_char_p, C.POINTER(Config), C.POINTER(Result)], C.c_int),
         "ibim_tree_lists_host": ([_dp, C.c_long, C.c_int, C.c_int, _ip, C.c_long, _lp], C.c_int),
+        "ibim_ctx_stream": ([_vp], _vp),
+        "ibim_launch_count": ([], C.c_long),
+        "ibim_profile_enable": ([_vp, C.c_uint], C.c_int),
+        "ibim_profile_read": ([_vp, _dp, _lp, C.c_int], C.c_int),
+        "ibim_profile_work": ([_vp, _dp, _dp, C.c_int], C.c_int),
+        "ibim_measure_peak": ([_vp, C.c_int, _dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -138,6 +150,11 @@ def lib():
         fn.restype = res
     _lib = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().ibim_launch_count())
 
 
 def _check(st: int):
@@ -187,6 +204,35 @@ class Context:
 
     def __del__(self):
         self.close()
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        return int(lib().ibim_ctx_stream(self.h) or 0)
+
+    def profile(self, categories):
+        """Enable CUDA-event timing of the named kernel categories (PROFILE_CATEGORIES)."""
+        mask = 0
+        for c in categories:
+            mask |= 1 << PROFILE_CATEGORIES.index(c)
+        _check(lib().ibim_profile_enable(self.h, mask))
+
+    def profile_read(self) -> dict:
+        """{category: dict(ms, launches, flops, bytes)} since the last read; clears the counters."""
+        n = len(PROFILE_CATEGORIES)
+        ms = (C.c_double * n)()
+        ln = (C.c_long * n)()
+        fl = (C.c_double * n)()
+        by = (C.c_double * n)()
+        _check(lib().ibim_profile_work(self.h, fl, by, n))
+        _check(lib().ibim_profile_read(self.h, ms, ln, n))
+        return {c: dict(ms=ms[i], launches=ln[i], flops=fl[i], bytes=by[i]) for i, c in enumerate(PROFILE_CATEGORIES)
+                if ln[i]}
+
+    def measure_peak(self, kind: str) -> float:
+        v = C.c_double(0)
+        _check(lib().ibim_measure_peak(self.h, {"fp64": 0, "fp32": 1}[kind], C.byref(v)))
+        return v.value
 
     def grid(self, n, lo, h, value=0.0) -> "Grid":
         g = _vp()

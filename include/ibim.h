@@ -101,6 +101,9 @@ typedef struct {
     int refinements;      /* outer iterative-refinement passes (mixed precision) */
     double residual;      /* final relative residual ||b - A x|| / ||b|| */
     double t_levelset_ms, t_surface_ms, t_plan_ms, t_solve_ms, t_energy_ms;
+    long grid_cells;      /* level-set grid cells */
+    int levelset_stages;  /* TVD-RK3 stage sweeps (evolve + both reinitialisations) */
+    long fmm_nodes, fmm_v_pairs, fmm_x_pairs, fmm_near_pairs, fmm_operators; /* tree work counts */
 } ibim_result;
 
 /* ---- context ---- */
@@ -110,6 +113,22 @@ const char *ibim_last_error(void);
 const char *ibim_status_string(int status);
 /* Fill a config with the reference defaults (data/input.cfg, main.cpp). */
 void ibim_config_default(ibim_config *cfg);
+/* The context's CUDA stream (cudaStream_t), for callers that record events on it. */
+void *ibim_ctx_stream(ibim_ctx ctx);
+/* Kernels this library has launched since load (all contexts). */
+long ibim_launch_count(void);
+/* Per-category kernel timing with CUDA events on the context stream.  mask bit k enables
+ * category k: 0 expand, 1 WENO stage, 2 gradient count, 3 flood fill, 4 tube extraction,
+ * 5 M2L operators, 6 P2M, 7 M2M, 8 M2L (V list), 9 M2L (X list), 10 L2L, 11 near field + L2P,
+ * 12 right-hand side, 13 GMRES vector kernels.  ibim_profile_read returns (and clears) the
+ * summed milliseconds and launch counts of the first ncat categories. */
+int ibim_profile_enable(ibim_ctx ctx, unsigned mask);
+int ibim_profile_read(ibim_ctx ctx, double *ms, long *launches, int ncat);
+/* Algorithmic flops and bytes of the profiled launches per category since the last read (call
+ * before ibim_profile_read, which clears them). */
+int ibim_profile_work(ibim_ctx ctx, double *flops, double *bytes, int ncat);
+/* Measured FMA issue rate of the device: kind 0 = FP64, 1 = FP32 (TFLOP/s, 2 flops per FMA). */
+int ibim_measure_peak(ibim_ctx ctx, int kind, double *tflops);
 
 /* ---- level set: replaces Grid and levelset (levelset.h:12-60, levelset.cpp:9-432) ---- */
 int ibim_grid_create(ibim_ctx ctx, int nx, int ny, int nz, double sx, double sy, double sz, double dx,

@@ -702,7 +702,22 @@ static inline void kblock(const orc_kparams *kp, int kernel, const double dd[3],
         b[0] = kscalar(kp, kernel, dd);
 }
 
+static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                     int stride);
+
 void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out) {
+    fmm_impl(t, p, kp, kernel, dens, out, 1);
+}
+
+/* Timing sample: the upward pass in full, the downward pass (M2L, L2L, near field, L2P) only
+ * for nodes whose id is a multiple of `stride`; `out` is then incomplete. */
+void orc_fmm_sample(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                    int stride) {
+    fmm_impl(t, p, kp, kernel, dens, out, stride < 1 ? 1 : stride);
+}
+
+static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                     int stride) {
     const int nd = kernel == ORC_KERNEL_FUSED ? 4 : 1, no = nd, nb = nd * no;
     cheb_t ch;
     cheb_init(&ch, p);
@@ -762,7 +777,7 @@ void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const 
 #pragma omp parallel for schedule(dynamic, 1)
         for (int i = 0; i < nn; ++i) {
             const onode *n = &t->nd[i];
-            if (n->level != lv) continue;
+            if (n->level != lv || i % stride) continue;
             double *L = local + (size_t)i * no * R;
             double blk[16];
             for (int which = 1; which <= 3; which += 2) {
@@ -807,7 +822,7 @@ void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const 
 #pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < nn; ++i) {
         const onode *n = &t->nd[i];
-        if (!n->leaf || n->ntgt == 0) continue;
+        if (!n->leaf || n->ntgt == 0 || i % stride) continue;
         double *w = (double *)malloc(sizeof(double) * R);
         double blk[16];
         for (int tt = 0; tt < n->ntgt; ++tt) {

@@ -63,6 +63,9 @@ typedef struct {
 /* One FMM: dens is nd x ns (nd = 4 for the fused kernel, else 1), out is no x nt (no = 4 / 1),
  * both in the caller's point order.  `t` must have been built on the same src/tgt. */
 void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out);
+/* Timing sample of orc_fmm: full upward pass, downward pass only on nodes with id % stride == 0. */
+void orc_fmm_sample(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                    int stride);
 
 typedef struct {
     int np, maxpoint, maxlevel, restart, maxiter;

@@ -72,6 +72,7 @@ def lib():
         L.orc_tree_list.argtypes = [C.c_void_p, C.c_int, C.c_int, _ip, C.c_int]
         L.orc_tree_list.restype = C.c_int
         L.orc_fmm.argtypes = [C.c_void_p, C.c_int, C.POINTER(KParams), C.c_int, _dp, _dp]
+        L.orc_fmm_sample.argtypes = [C.c_void_p, C.c_int, C.POINTER(KParams), C.c_int, _dp, _dp, C.c_int]
         L.orc_rhs.argtypes = [_dp, C.c_long, _dp, _dp, C.c_int, C.POINTER(BieParams), _dp]
         L.orc_matvec.argtypes = [_dp, C.c_long, C.c_double, C.POINTER(BieParams), _dp, _dp]
         L.orc_solve.argtypes = [_dp, C.c_long, C.c_double, _dp, _dp, C.c_int, C.POINTER(BieParams), _dp, _dp, _dp,
@@ -172,11 +173,16 @@ class Tree:
             out.append(buf[:n].copy())
         return out
 
-    def fmm(self, p, kparams: KParams, kernel: int, dens):
+    def fmm(self, p, kparams: KParams, kernel: int, dens, sample_stride: int = 1):
+        """One FMM; sample_stride > 1 runs the downward pass on every stride-th node only
+        (a timing sample whose output is incomplete)."""
         nd = 4 if kernel == 16 else 1
         d = _c(dens).reshape(nd, len(self.src))
         out = np.zeros((nd, len(self.tgt)))
-        lib().orc_fmm(self.ptr, p, C.byref(kparams), kernel, _p(d), _p(out))
+        if sample_stride > 1:
+            lib().orc_fmm_sample(self.ptr, p, C.byref(kparams), kernel, _p(d), _p(out), sample_stride)
+        else:
+            lib().orc_fmm(self.ptr, p, C.byref(kparams), kernel, _p(d), _p(out))
         return out
 
 
