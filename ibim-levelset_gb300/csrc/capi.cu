@@ -125,13 +125,14 @@ static void fill_plan_stats(const Plan &P, ibim_result &res) {
 // main.cpp:45-60 with s = 1
 static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *radii_dev, int natoms,
                                const ibim_config &cfg, int steps[2]) {
-    Grid *g = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, cfg.init);
+    Grid *g = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, cfg.init,
+                          cfg.precision);
     Grid *phi0 = nullptr;
     try {
         levelset_expand(*g, centers_dev, radii_dev, natoms, cfg.probe, cfg.band);
         levelset_evolve(*g, cfg.probe, 1.0, 0.2);
         grid_scale(*g, -1.0);
-        phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0.);
+        phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0., cfg.precision);
         grid_copy(*phi0, *g);
         steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
         grid_copy(*phi0, *g);
@@ -398,18 +399,32 @@ int ibim_grid_destroy(ibim_grid g) {
 int ibim_grid_upload(ibim_grid g, const double *host) {
     return guard([&] {
         IBIM_REQUIRE(g && host, "null argument");
-        bind(g->g->ctx);
-        g->g->data.upload(host, g->g->cells());
-        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+        Grid &G = *g->g;
+        bind(G.ctx);
+        if (G.prec == IBIM_PRECISION_FP64) {
+            G.data.upload(host, G.cells());
+        } else {
+            std::vector<float> f(host, host + G.cells());
+            G.data32.upload(f.data(), G.cells());
+        }
+        IBIM_CUDA(cudaStreamSynchronize(G.ctx->stream));
     });
 }
 
 int ibim_grid_download(ibim_grid g, double *host) {
     return guard([&] {
         IBIM_REQUIRE(g && host, "null argument");
-        bind(g->g->ctx);
-        g->g->data.download(host, g->g->cells());
-        IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
+        Grid &G = *g->g;
+        bind(G.ctx);
+        if (G.prec == IBIM_PRECISION_FP64) {
+            G.data.download(host, G.cells());
+            IBIM_CUDA(cudaStreamSynchronize(G.ctx->stream));
+        } else {
+            std::vector<float> f(G.cells());
+            G.data32.download(f.data(), G.cells());
+            IBIM_CUDA(cudaStreamSynchronize(G.ctx->stream));
+            std::copy(f.begin(), f.end(), host);
+        }
     });
 }
 
@@ -655,7 +670,7 @@ int ibim_fmm_apply(ibim_plan p, int kernel, const ibim_kernel_params *kp, const 
         } else {
             permute(c, ns, P.src_perm.ptr, hin.ptr, P.dens4.ptr + kKernelMap[kernel].slot * ns, false);
         }
-        fmm_run(P, 0, *kp, P.dens4.ptr, S.out4.ptr, IBIM_PRECISION_FP64);
+        fmm_run(P, 0, *kp, P.dens4.ptr, S.out4.ptr, P.precision);
         DevBuf<double> hout;
         hout.alloc((size_t)rows * nt, s);
         if (rows == 4) {
@@ -686,7 +701,7 @@ int ibim_bie_matvec(ibim_plan p, const ibim_kernel_params *kp, const double *x, 
         hx.upload(x, 2 * n);
         permute(c, n, P.src_perm.ptr, hx.ptr, tx.ptr, false);
         permute(c, n, P.src_perm.ptr, hx.ptr + n, tx.ptr + n, false);
-        bie_matvec(P, *kp, tx.ptr, ty.ptr, IBIM_PRECISION_FP64);
+        bie_matvec(P, *kp, tx.ptr, ty.ptr, P.precision);
         permute(c, n, P.src_perm.ptr, ty.ptr, hy.ptr, true);
         permute(c, n, P.src_perm.ptr, ty.ptr + n, hy.ptr + n, true);
         hy.download(y, 2 * n);

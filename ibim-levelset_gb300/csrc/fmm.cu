@@ -439,7 +439,7 @@ static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, i
                 xt.push_back(i);
             }
         }
-    std::vector<int> vs, vt, chunks;
+    std::vector<int> vs, vt, chunks, chunks32;
     for (int op = 0; op < (int)byop.size(); ++op) {
         const int b = (int)vs.size();
         for (auto &pr : byop[op]) {
@@ -451,9 +451,16 @@ static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, i
             chunks.push_back(b + q);
             chunks.push_back(std::min<int>(M2L_CH, (int)byop[op].size() - q));
         }
+        for (int q = 0; q < (int)byop[op].size(); q += M2L_CH32) {
+            chunks32.push_back(op);
+            chunks32.push_back(b + q);
+            chunks32.push_back(std::min<int>(M2L_CH32, (int)byop[op].size() - q));
+        }
     }
     S.nvpairs = (long)vs.size();
     S.nchunks = (int)chunks.size() / 3;
+    S.nchunks32 = (int)chunks32.size() / 3;
+    up_int(S.v_chunk32, chunks32, s);
     up_int(S.v_src, vs, s);
     up_int(S.v_tgt, vt, s);
     up_int(S.v_chunk, chunks, s);
@@ -691,8 +698,10 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
 
 void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision) {
     const double key[4] = {kp.kappa, kp.dE, kp.dI, kp.tau};
-    bool same = P.ops_precision == precision;
-    for (int i = 0; i < 4; ++i) same = same && P.kp_cache[i] == key[i];
+    const bool is64 = precision == IBIM_PRECISION_FP64;
+    double *cache = is64 ? P.kp64 : P.kp32;
+    bool same = is64 ? P.ops64_ready : P.ops32_ready;
+    for (int i = 0; i < 4; ++i) same = same && cache[i] == key[i];
     if (same || P.nops == 0) return;
     cudaStream_t s = P.ctx->stream;
     const int R = P.R, n4 = 4 * R;
@@ -705,8 +714,8 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
     } else {
         fmm_prepare_operators_mixed(P, k);
     }
-    for (int i = 0; i < 4; ++i) P.kp_cache[i] = key[i];
-    P.ops_precision = precision;
+    for (int i = 0; i < 4; ++i) cache[i] = key[i];
+    (is64 ? P.ops64_ready : P.ops32_ready) = true;
 }
 
 // One FP64 FMM: dens (4 x ns, tree order) -> out (4 x nt of target set ts, tree order).

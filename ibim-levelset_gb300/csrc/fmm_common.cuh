@@ -10,6 +10,7 @@ namespace ibim {
 
 constexpr int MAXP = 8;
 constexpr int MAXR = MAXP * MAXP * MAXP;
+constexpr int M2L_CH32 = 32;  // V pairs per chunk of the FP32 contraction
 
 // Chebyshev nodes, polynomials and parent -> child transfers for order p (bbfmm.h:273-326).
 struct ChebTables {

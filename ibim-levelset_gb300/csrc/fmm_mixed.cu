@@ -1,14 +1,686 @@
-// Mixed-precision FMM (FP32 far and near field) used inside FP64 iterative refinement.
+// Mixed-precision FMM (sm_103a): the same tree, lists and Chebyshev approximation as the FP64
+// path (fmm.cu), evaluated in FP32 for use inside FP64 iterative refinement.
+//
+//   coordinates  FP32, relative to the centre of the point's leaf (|x| <= leaf size), plus an
+//                FP32 centre offset per (target leaf, source leaf) from an FP64 difference, so
+//                that close pairs keep ~1e-7 relative accuracy
+//   near field   FP32 pair kernel (rsqrt, exp on the SFU), per-tile sums added with Kahan
+//                compensation
+//   far field    P2M / M2M / L2L / L2P in FP32; V-list M2L as a batched FP32 contraction with
+//                FP32 operators; X-list M2L on the fly in FP32
+// Outputs are written as FP64 so the BIE combine and GMRES stay FP64.
+
+#include <algorithm>
+#include <cmath>
+
 #include "fmm_common.cuh"
 
 namespace ibim {
 
-void fmm_prepare_operators_mixed(Plan &, const KParams &) {
-    throw Error(IBIM_ERR_INVALID_ARGUMENT, "mixed precision is not available in this build");
+struct ChebTables32 {
+    float cheb[MAXP];
+    float tnode[MAXP][MAXP];
+    float S[2][MAXP][MAXP];
+    int p, R;
+};
+
+struct KParams32 {
+    float kappa, eps, ieps, vr2, k2in, q4pi;
+};
+
+static KParams32 to32(const KParams &k) {
+    return KParams32{(float)k.kappa, (float)k.eps, (float)k.ieps, (float)(k.vr * k.vr), (float)k.k2in,
+                     (float)k.q4pi};
 }
 
-void fmm_run_mixed(Plan &, int, const ibim_kernel_params &, const double *, double *) {
-    throw Error(IBIM_ERR_INVALID_ARGUMENT, "mixed precision is not available in this build");
+namespace {
+
+
+__device__ __forceinline__ void interp1f(const ChebTables32 &T, float x, float *out) {
+    float Tk[MAXP];
+    Tk[0] = 1.f;
+    Tk[1] = x;
+    for (int k = 2; k < T.p; ++k) Tk[k] = 2.f * x * Tk[k - 1] - Tk[k - 2];
+    const float ip = 1.f / T.p;
+    for (int m = 0; m < T.p; ++m) {
+        float s = 0.f;
+        for (int k = 0; k < T.p; ++k) s = fmaf(Tk[k], T.tnode[m][k], s);
+        out[m] = (-1.f + 2.f * s) * ip;
+    }
+}
+
+template <class TT>
+__device__ __forceinline__ void load_tables(TT &T, const TT *__restrict__ g) {
+    const int n = sizeof(TT) / 4;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) reinterpret_cast<int *>(&T)[t] = reinterpret_cast<const int *>(g)[t];
+}
+
+__global__ void k_rel_coords(int nleaf, const int *__restrict__ leaves, const int *__restrict__ b_,
+                             const int *__restrict__ e_, const double *__restrict__ ctr, const double *__restrict__ x,
+                             const double *__restrict__ y, const double *__restrict__ z, float *xf, float *yf,
+                             float *zf) {
+    const int L = blockIdx.x < nleaf ? leaves[blockIdx.x] : -1;
+    if (L < 0) return;
+    const double cx = ctr[3 * L], cy = ctr[3 * L + 1], cz = ctr[3 * L + 2];
+    for (int i = b_[L] + threadIdx.x; i < e_[L]; i += blockDim.x) {
+        xf[i] = (float)(x[i] - cx);
+        yf[i] = (float)(y[i] - cy);
+        zf[i] = (float)(z[i] - cz);
+    }
+}
+
+__global__ void k_to_f32(long n, const double *__restrict__ a, float *b) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+
+// P2M in FP32 (bbfmm.h:507-519); coordinates relative to the leaf centre.
+__global__ void __launch_bounds__(128) k_p2m32(const ChebTables32 *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ sb, const int *__restrict__ se,
+                                               const float *__restrict__ rad, const float *__restrict__ x,
+                                               const float *__restrict__ y, const float *__restrict__ z,
+                                               const float *__restrict__ dens, long ns, float *mult) {
+    __shared__ ChebTables32 T;
+    __shared__ float Sp[32][3][MAXP];
+    __shared__ float D[4][32];
+    load_tables(T, tab);
+    const int node = nodes[blockIdx.x];
+    const int b = sb[node], e = se[node];
+    const float ir[3] = {1.f / rad[3 * node], 1.f / rad[3 * node + 1], 1.f / rad[3 * node + 2]};
+    __syncthreads();
+    const int p = T.p, R = T.R;
+    float acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = 0.f;
+    for (int base = b; base < e; base += 32) {
+        const int cnt = min(32, e - base);
+        if (threadIdx.x < 96) {
+            const int pt = threadIdx.x / 3, ax = threadIdx.x % 3;
+            if (pt < cnt) {
+                const float *X = ax == 0 ? x : (ax == 1 ? y : z);
+                interp1f(T, X[base + pt] * ir[ax], Sp[pt][ax]);
+            }
+        } else {
+            const int pt = threadIdx.x - 96;
+            if (pt < cnt)
+                for (int d = 0; d < 4; ++d) D[d][pt] = dens[d * ns + base + pt];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int o = threadIdx.x + 128 * q;
+            if (o < 4 * R) {
+                const int d = o / R, cc = o % R;
+                const int i = cc % p, j = (cc / p) % p, l = cc / (p * p);
+                float s = acc[q];
+                for (int pt = 0; pt < cnt; ++pt) s = fmaf(Sp[pt][0][i] * Sp[pt][1][j] * Sp[pt][2][l], D[d][pt], s);
+                acc[q] = s;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const int o = threadIdx.x + 128 * q;
+        if (o < 4 * R) mult[(long)node * 4 * R + o] = acc[q];
+    }
+}
+
+__device__ void kron_apply32(const ChebTables32 &T, int id, bool up, float *buf, float *tmp) {
+    const int p = T.p, R = T.R;
+    const int b[3] = {id & 1, (id >> 1) & 1, (id >> 2) & 1};
+    for (int ax = 0; ax < 3; ++ax) {
+        const int stride = ax == 0 ? 1 : (ax == 1 ? p : p * p);
+        float *src = (ax & 1) ? tmp : buf;
+        float *dst = (ax & 1) ? buf : tmp;
+        for (int o = threadIdx.x; o < 4 * R; o += blockDim.x) {
+            const int d = o / R, cc = o % R;
+            const int idx = (cc / stride) % p;
+            const int base = d * R + cc - idx * stride;
+            float s = 0.f;
+            for (int k = 0; k < p; ++k) s = fmaf(up ? T.S[b[ax]][k][idx] : T.S[b[ax]][idx][k], src[base + k * stride], s);
+            dst[o] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(128) k_m2m32(const ChebTables32 *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ child_first, const int *__restrict__ empty,
+                                               float *mult) {
+    extern __shared__ float smf[];
+    __shared__ ChebTables32 T;
+    load_tables(T, tab);
+    __syncthreads();
+    const int n4 = 4 * T.R;
+    float *buf = smf, *tmp = smf + n4, *acc = smf + 2 * n4;
+    const int node = nodes[blockIdx.x];
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] = 0.f;
+    const int c0 = child_first[node];
+    for (int c8 = 0; c8 < 8; ++c8) {
+        const int ch = c0 + c8;
+        if (empty[ch]) continue;
+        __syncthreads();
+        for (int o = threadIdx.x; o < n4; o += blockDim.x) buf[o] = mult[(long)ch * n4 + o];
+        __syncthreads();
+        kron_apply32(T, c8, true, buf, tmp);
+        for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] += tmp[o];
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) mult[(long)node * n4 + o] = acc[o];
+}
+
+__global__ void __launch_bounds__(128) k_l2l32(const ChebTables32 *__restrict__ tab, const int *__restrict__ nodes,
+                                               const int *__restrict__ parent, const int *__restrict__ index8,
+                                               float *local) {
+    extern __shared__ float smf[];
+    __shared__ ChebTables32 T;
+    load_tables(T, tab);
+    __syncthreads();
+    const int n4 = 4 * T.R;
+    float *buf = smf, *tmp = smf + n4;
+    const int node = nodes[blockIdx.x];
+    const int par = parent[node];
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) buf[o] = local[(long)par * n4 + o];
+    __syncthreads();
+    kron_apply32(T, index8[node], false, buf, tmp);
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) local[(long)node * n4 + o] += tmp[o];
+}
+
+// FP32 V-list operators, evaluated in FP64 and rounded (same layout as the FP64 operators).
+__global__ void k_make_ops32(const ChebTables *__restrict__ tab, const int *__restrict__ keys,
+                             const double *__restrict__ root_r, KParams kp, float *ops) {
+    const ChebTables &T = *tab;
+    const int op = blockIdx.y;
+    const int p = T.p, R = T.R, n4 = 4 * R;
+    const int lv = keys[4 * op];
+    double r[3];
+    for (int a = 0; a < 3; ++a) {
+        double v = root_r[a];
+        for (int l = 0; l < lv; ++l) v *= 0.5;
+        r[a] = v;
+    }
+    const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (pair >= (long)R * R) return;
+    const int ct = (int)(pair / R), cs = (int)(pair % R);
+    const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
+    const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
+    double d[3];
+    for (int a = 0; a < 3; ++a)
+        d[a] = (keys[4 * op + 1 + a] * (2.0 * r[a]) + r[a] * T.cheb[si[a]]) - r[a] * T.cheb[ti[a]];
+    double b[16];
+    kblock64(kp, d[0], d[1], d[2], b);
+    float *K = ops + (long)op * n4 * n4;
+    for (int o = 0; o < 4; ++o)
+        for (int in = 0; in < 4; ++in) K[(long)(in * R + cs) * n4 + (o * R + ct)] = (float)b[o * 4 + in];
+}
+
+// V-list M2L in FP32 as a register-tiled SIMT contraction.  Block = (row tile of 128 of the 4R
+// output rows, chunk of <= 32 pairs sharing one operator).  Per 32-column step the operator tile
+// (32 x 128, contiguous rows) and the pairs' multipole tile (32 x 32) are staged in shared
+// memory; each thread owns a 4 x 4 (rows x pairs) block of outputs; the next operator tile is
+// prefetched into registers while the current one is consumed.
+constexpr int GM_BM = 128, GM_BN = 32, GM_BK = 32;
+__global__ void __launch_bounds__(256) k_m2l_v32(int n4, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+                                                 const int *__restrict__ vtgt, const float *__restrict__ ops,
+                                                 const float *__restrict__ mult, float *local) {
+    __shared__ __align__(16) float As[GM_BK][GM_BM];
+    __shared__ __align__(16) float Bs[GM_BK][GM_BN];
+    __shared__ int src_s[GM_BN], tgt_s[GM_BN];
+    const int op = chunks[3 * blockIdx.y], b = chunks[3 * blockIdx.y + 1], cnt = chunks[3 * blockIdx.y + 2];
+    const int row0 = blockIdx.x * GM_BM;
+    const int tid = threadIdx.x;
+    if (tid < GM_BN) {
+        src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
+        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
+    }
+    const float *K = ops + (long)op * n4 * n4;
+    const int tr = tid / 8, tc = tid % 8;  // rows tr*4.., pairs tc*4..
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    // operator tile loader: 32 columns x 128 rows = 1024 float4, 4 per thread
+    float4 pre[4];
+    auto load_a = [&](int k0) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int idx = tid + 256 * v;      // 0..1023
+            const int col = idx / 32, r4 = (idx % 32) * 4;
+            const int gr = row0 + r4, gc = k0 + col;
+            float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (gc < n4) {
+                const float *src = K + (long)gc * n4 + gr;
+                if (gr + 3 < n4) {
+                    val = *reinterpret_cast<const float4 *>(src);
+                } else {
+                    if (gr < n4) val.x = src[0];
+                    if (gr + 1 < n4) val.y = src[1];
+                    if (gr + 2 < n4) val.z = src[2];
+                }
+            }
+            pre[v] = val;
+        }
+    };
+    __syncthreads();
+    load_a(0);
+    for (int k0 = 0; k0 < n4; k0 += GM_BK) {
+        __syncthreads();
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int idx = tid + 256 * v;
+            *reinterpret_cast<float4 *>(&As[idx / 32][(idx % 32) * 4]) = pre[v];
+        }
+        // multipole tile: Bs[col][pair] = mult[src_pair][k0 + col]
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int idx = tid + 256 * v;  // 0..1023
+            const int j = idx / 32, col = idx % 32;
+            const int sn = src_s[j];
+            Bs[col][j] = (sn >= 0 && k0 + col < n4) ? mult[(long)sn * n4 + k0 + col] : 0.f;
+        }
+        __syncthreads();
+        if (k0 + GM_BK < n4) load_a(k0 + GM_BK);
+#pragma unroll 8
+        for (int kk = 0; kk < GM_BK; ++kk) {
+            const float4 a = *reinterpret_cast<const float4 *>(&As[kk][tr * 4]);
+            const float4 bb = *reinterpret_cast<const float4 *>(&Bs[kk][tc * 4]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {bb.x, bb.y, bb.z, bb.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int t = tgt_s[tc * 4 + j];
+        if (t < 0) continue;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int row = row0 + tr * 4 + i;
+            if (row < n4) atomicAdd(local + (long)t * n4 + row, acc[i][j]);
+        }
+    }
+}
+
+// Fused 4x4 block in FP32 (same formulas as kblock64).
+__device__ __forceinline__ void kblock32(const KParams32 &k, float dx, float dy, float dz, float b[16]) {
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < k.vr2) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) b[i] = 0.f;
+        b[3] = -k.k2in;
+        return;
+    }
+    const float ir = rsqrtf(d2), r = d2 * ir, ir3 = ir * ir * ir;
+    const float t = k.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
+    const float c1 = (k.eps * et1 - 1.f) * ir3 * k.q4pi;
+    const float c4 = -(k.ieps * et1 - 1.f) * ir3 * k.q4pi;
+    const float k2 = (1.f - e) * ir * k.q4pi;
+    const float hd = (1.f - et1) * ir3;
+    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir;
+    const float dd[3] = {dx, dy, dz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b[a] = dd[a] * c1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) b[4 * (a + 1) + c] = ho * dd[a] * dd[c] + (a == c ? hd : 0.f);
+        b[4 * (a + 1) + 3] = -dd[a] * c4;
+    }
+    b[3] = -k2;
+}
+
+// X-list M2L in FP32, kernel on the fly; off = source centre - target centre.
+__global__ void __launch_bounds__(128) k_m2l_x32(const ChebTables32 *__restrict__ tab, KParams32 kp,
+                                                 const int *__restrict__ xsrc, const int *__restrict__ xtgt,
+                                                 const float *__restrict__ off, const float *__restrict__ rad,
+                                                 const float *__restrict__ mult, float *local) {
+    __shared__ ChebTables32 T;
+    __shared__ float M[4 * MAXR];
+    __shared__ float sp[3][MAXP], tp[3][MAXP];
+    load_tables(T, tab);
+    __syncthreads();
+    const int s = xsrc[blockIdx.x], t = xtgt[blockIdx.x];
+    const int p = T.p, R = T.R;
+    for (int o = threadIdx.x; o < 4 * R; o += blockDim.x) M[o] = mult[(long)s * 4 * R + o];
+    if (threadIdx.x < 3 * p) {
+        const int a = threadIdx.x / p, m = threadIdx.x % p;
+        sp[a][m] = off[3 * blockIdx.x + a] + rad[3 * s + a] * T.cheb[m];
+        tp[a][m] = rad[3 * t + a] * T.cheb[m];
+    }
+    __syncthreads();
+    for (int ct = threadIdx.x; ct < R; ct += blockDim.x) {
+        const float tx = tp[0][ct % p], ty = tp[1][(ct / p) % p], tz = tp[2][ct / (p * p)];
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int cs = 0; cs < R; ++cs) {
+            float b[16];
+            kblock32(kp, sp[0][cs % p] - tx, sp[1][(cs / p) % p] - ty, sp[2][cs / (p * p)] - tz, b);
+#pragma unroll
+            for (int o = 0; o < 4; ++o)
+#pragma unroll
+                for (int in = 0; in < 4; ++in) acc[o] = fmaf(b[o * 4 + in], M[in * R + cs], acc[o]);
+        }
+        for (int o = 0; o < 4; ++o) atomicAdd(local + (long)t * 4 * R + o * R + ct, acc[o]);
+    }
+}
+
+// Near field + L2P in FP32 for one target leaf per block: source leaves staged in shared memory
+// in the target leaf's frame; per-tile partial sums are added with Kahan compensation.
+constexpr int NT32 = 128, TILE32 = 256;
+__global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict__ tab, KParams32 kp,
+                                                 const int *__restrict__ tleaf, const int *__restrict__ nptr,
+                                                 const int *__restrict__ nrange, const float *__restrict__ noff,
+                                                 const int *__restrict__ tb_, const int *__restrict__ te_,
+                                                 const float *__restrict__ rad, const float *__restrict__ sx,
+                                                 const float *__restrict__ sy, const float *__restrict__ sz,
+                                                 const float *__restrict__ dens, long ns, const float *__restrict__ tx,
+                                                 const float *__restrict__ ty, const float *__restrict__ tz, long nt,
+                                                 const float *__restrict__ local, double *out) {
+    __shared__ ChebTables32 T;
+    __shared__ float S[7][TILE32];
+    __shared__ float red[NT32][4];
+    load_tables(T, tab);
+    const int leaf = tleaf[blockIdx.x];
+    const int tb = tb_[leaf], te = te_[leaf];
+    const int r0 = nptr[blockIdx.x], r1 = nptr[blockIdx.x + 1];
+    __syncthreads();
+    for (int t0 = tb; t0 < te; t0 += NT32) {
+        const int nT = min(NT32, te - t0);
+        const int nph = NT32 / nT;
+        const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
+        const bool active = ph < nph;
+        float X = 0.f, Y = 0.f, Z = 0.f;
+        if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
+        float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+        // fill tiles across consecutive source leaves
+        int rr = r0, pos = r1 > r0 ? nrange[2 * r0] : 0;
+        while (rr < r1) {
+            __syncthreads();
+            int filled = 0;
+            // sequentially pack up to TILE32 sources; each thread copies its slots
+            int lrr = rr, lpos = pos;
+            while (lrr < r1 && filled < TILE32) {
+                const int e = nrange[2 * lrr + 1];
+                const int take = min(TILE32 - filled, e - lpos);
+                const float ox = noff[3 * lrr], oy = noff[3 * lrr + 1], oz = noff[3 * lrr + 2];
+                for (int q = threadIdx.x; q < take; q += blockDim.x) {
+                    const int si = lpos + q;
+                    S[0][filled + q] = sx[si] + ox;
+                    S[1][filled + q] = sy[si] + oy;
+                    S[2][filled + q] = sz[si] + oz;
+                    S[3][filled + q] = dens[si];
+                    S[4][filled + q] = dens[ns + si];
+                    S[5][filled + q] = dens[2 * ns + si];
+                    S[6][filled + q] = dens[3 * ns + si];
+                }
+                filled += take;
+                lpos += take;
+                if (lpos >= e) {
+                    ++lrr;
+                    if (lrr < r1) lpos = nrange[2 * lrr];
+                }
+            }
+            rr = lrr;
+            pos = lpos;
+            __syncthreads();
+            if (active) {
+                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+                for (int q = ph; q < filled; q += nph) {
+                    const float dx = S[0][q] - X, dy = S[1][q] - Y, dz = S[2][q] - Z;
+                    const float m0 = S[3][q], m1 = S[4][q], m2 = S[5][q], psi = S[6][q];
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 < kp.vr2) {
+                        a0 -= kp.k2in * psi;
+                        continue;
+                    }
+                    const float ir = rsqrtf(d2), r = d2 * ir, ir3 = ir * ir * ir;
+                    const float t = kp.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
+                    const float c1 = (kp.eps * et1 - 1.f) * ir3 * kp.q4pi;
+                    const float c4 = -(kp.ieps * et1 - 1.f) * ir3 * kp.q4pi;
+                    const float k2 = (1.f - e) * ir * kp.q4pi;
+                    const float hd = (1.f - et1) * ir3;
+                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir;
+                    const float dm = dx * m0 + dy * m1 + dz * m2;
+                    a0 += c1 * dm - k2 * psi;
+                    const float cm = ho * dm - c4 * psi;
+                    a1 += hd * m0 + dx * cm;
+                    a2 += hd * m1 + dy * cm;
+                    a3 += hd * m2 + dz * cm;
+                }
+                const float part[4] = {a0, a1, a2, a3};
+#pragma unroll
+                for (int o = 0; o < 4; ++o) {  // Kahan: sum += part
+                    const float yk = part[o] - cmp[o];
+                    const float tk = sum[o] + yk;
+                    cmp[o] = (tk - sum[o]) - yk;
+                    sum[o] = tk;
+                }
+            }
+        }
+        __syncthreads();
+        for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = sum[o] - cmp[o];
+        __syncthreads();
+        if (threadIdx.x < nT) {
+            double f[4] = {0., 0., 0., 0.};
+            for (int q = 0; q < nph; ++q)
+                for (int o = 0; o < 4; ++o) f[o] += (double)red[threadIdx.x + q * nT][o];
+            float Sp[3][MAXP];
+            const float xyz[3] = {X, Y, Z};
+            for (int a = 0; a < 3; ++a) interp1f(T, xyz[a] / rad[3 * leaf + a], Sp[a]);
+            const int p = T.p, R = T.R;
+            const float *L = local + (long)leaf * 4 * R;
+            float l2p[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int c = 0; c < R; ++c) {
+                const float w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, L[o * R + c], l2p[o]);
+            }
+            for (int o = 0; o < 4; ++o) out[o * nt + t0 + threadIdx.x] = f[o] + (double)l2p[o];
+        }
+        __syncthreads();
+    }
+}
+
+inline int ew(Ctx *c, long n) { return (int)std::max<long>(1, std::min<long>(8L * c->num_sms, div_up(n, 256))); }
+
+void up_i(DevBuf<int> &b, const std::vector<int> &v, cudaStream_t s) {
+    b.alloc(std::max<size_t>(1, v.size()), s);
+    b.upload(v.data(), v.size());
+}
+void up_f(DevBuf<float> &b, const std::vector<float> &v, cudaStream_t s) {
+    b.alloc(std::max<size_t>(1, v.size()), s);
+    b.upload(v.data(), v.size());
+}
+
+// Leaf-relative FP32 coordinates, FP32 tables, and the FP32 near and X lists of a target set.
+void prepare_mixed(Plan &P, TargetSet &S) {
+    cudaStream_t s = P.ctx->stream;
+    const TreeHost &T = P.tree;
+    const int nn = T.nnodes;
+    if (!P.mixed_ready) {
+        ChebTables h64;
+        P.tables.download(&h64, 1);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        ChebTables32 h;
+        std::memset(&h, 0, sizeof(h));
+        h.p = h64.p;
+        h.R = h64.R;
+        for (int i = 0; i < MAXP; ++i) {
+            h.cheb[i] = (float)h64.cheb[i];
+            for (int j = 0; j < MAXP; ++j) {
+                h.tnode[i][j] = (float)h64.tnode[i][j];
+                h.S[0][i][j] = (float)h64.S[0][i][j];
+                h.S[1][i][j] = (float)h64.S[1][i][j];
+            }
+        }
+        P.tables32.alloc(sizeof(ChebTables32), s);
+        P.tables32.upload(reinterpret_cast<unsigned char *>(&h), sizeof(h));
+        std::vector<float> r32(3 * nn);
+        for (int i = 0; i < 3 * nn; ++i) r32[i] = (float)T.radius[i];
+        up_f(P.nrad32, r32, s);
+        P.sxf.alloc(P.ns, s);
+        P.syf.alloc(P.ns, s);
+        P.szf.alloc(P.ns, s);
+        std::vector<int> leaves;
+        for (int i = 0; i < nn; ++i)
+            if (T.leaf[i] && T.src_end[i] > T.src_begin[i]) leaves.push_back(i);
+        DevBuf<int> dl;
+        up_i(dl, leaves, s);
+        if (!leaves.empty())
+            (count_launch(), k_rel_coords<<<(int)leaves.size(), 128, 0, s>>>((int)leaves.size(), dl.ptr, P.nsrc_begin.ptr,
+                                                                       P.nsrc_end.ptr, P.ncenter.ptr, P.sx.ptr, P.sy.ptr,
+                                                                       P.sz.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr));
+        IBIM_CHECK_LAUNCH();
+        const int n4 = 4 * P.R;
+        P.mult32.alloc((size_t)nn * n4, s);
+        P.local32.alloc((size_t)nn * n4, s);
+        P.dens32.alloc((size_t)4 * P.ns, s);
+        const size_t smk = sizeof(float) * 3 * n4;
+        if (smk > 48 * 1024) {
+            IBIM_CUDA(cudaFuncSetAttribute(k_m2m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk));
+            IBIM_CUDA(cudaFuncSetAttribute(k_l2l32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk));
+        }
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        P.mixed_ready = true;
+    }
+    if (S.mixed_ready) return;
+    // target coordinates relative to their leaf
+    if (S.self) {
+        // the source arrays are used
+    } else {
+        std::vector<int> leaves;
+        for (int i = 0; i < nn; ++i)
+            if (T.leaf[i] && S.end[i] > S.begin[i]) leaves.push_back(i);
+        S.txf.alloc(std::max<long>(1, S.nt), s);
+        S.tyf.alloc(std::max<long>(1, S.nt), s);
+        S.tzf.alloc(std::max<long>(1, S.nt), s);
+        DevBuf<int> dl;
+        up_i(dl, leaves, s);
+        if (!leaves.empty())
+            (count_launch(), k_rel_coords<<<(int)leaves.size(), 128, 0, s>>>((int)leaves.size(), dl.ptr, S.tbeg.ptr,
+                                                                       S.tend.ptr, P.ncenter.ptr, S.tx.ptr, S.ty.ptr,
+                                                                       S.tz.ptr, S.txf.ptr, S.tyf.ptr, S.tzf.ptr));
+        IBIM_CHECK_LAUNCH();
+        IBIM_CUDA(cudaStreamSynchronize(s));
+    }
+    // near lists: U and W nodes expanded into their non-empty leaves, with centre offsets
+    std::vector<int> ptr{0}, rng;
+    std::vector<float> off;
+    std::vector<int> child_first(nn, -1);
+    for (int i = nn - 1; i >= 0; --i)
+        if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
+    std::vector<int> stack;
+    for (int i = 0; i < nn; ++i) {
+        if (!T.leaf[i] || S.end[i] <= S.begin[i]) continue;
+        auto add_leaves = [&](int root) {
+            stack.clear();
+            stack.push_back(root);
+            while (!stack.empty()) {
+                const int n = stack.back();
+                stack.pop_back();
+                if (T.src_end[n] <= T.src_begin[n]) continue;
+                if (T.leaf[n]) {
+                    rng.push_back(T.src_begin[n]);
+                    rng.push_back(T.src_end[n]);
+                    for (int a = 0; a < 3; ++a) off.push_back((float)(T.center[3 * n + a] - T.center[3 * i + a]));
+                } else {
+                    for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
+                }
+            }
+        };
+        for (int u : T.U[i]) add_leaves(u);
+        for (int w : T.W[i]) add_leaves(w);
+        ptr.push_back((int)rng.size() / 2);
+    }
+    up_i(S.near32_ptr, ptr, s);
+    up_i(S.near32_range, rng, s);
+    up_f(S.near32_off, off, s);
+    S.near32_entries = (int)rng.size() / 2;
+    // X pair centre offsets (FP64 difference, rounded)
+    std::vector<int> xs(std::max<long>(1, S.nxpairs)), xt(std::max<long>(1, S.nxpairs));
+    if (S.nxpairs > 0) {
+        S.x_src.download(xs.data(), S.nxpairs);
+        S.x_tgt.download(xt.data(), S.nxpairs);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+    }
+    std::vector<float> xo(3 * std::max<long>(1, S.nxpairs));
+    for (long q = 0; q < S.nxpairs; ++q)
+        for (int a = 0; a < 3; ++a) xo[3 * q + a] = (float)(T.center[3 * xs[q] + a] - T.center[3 * xt[q] + a]);
+    up_f(S.x_off32, xo, s);
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    S.mixed_ready = true;
+}
+
+}  // namespace
+
+void fmm_prepare_operators_mixed(Plan &P, const KParams &k) {
+    cudaStream_t s = P.ctx->stream;
+    const int R = P.R, n4 = 4 * R;
+    P.ops32.alloc((size_t)P.nops * n4 * n4, s);
+    dim3 g(div_up((long)R * R, 256), P.nops);
+    { ProfScope ps_(PROF_OPS); (count_launch(), k_make_ops32<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops32.ptr)); }
+    IBIM_CHECK_LAUNCH();
+}
+
+void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out) {
+    IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
+    TargetSet &S = *P.targets[ts];
+    prepare_mixed(P, S);
+    fmm_prepare_operators(P, kpp, IBIM_PRECISION_MIXED);
+    Ctx *c = P.ctx;
+    cudaStream_t s = c->stream;
+    const TreeHost &T = P.tree;
+    const int R = P.R, n4 = 4 * R;
+    const KParams kp = make_kparams(kpp, P.tube->h);
+    const KParams32 k32 = to32(kp);
+    const ChebTables32 *tab = reinterpret_cast<const ChebTables32 *>(P.tables32.ptr);
+    (count_launch(), k_to_f32<<<ew(c, 4 * P.ns), 256, 0, s>>>(4 * P.ns, dens, P.dens32.ptr));
+    if (P.np2m > 0) {
+        ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 28.0 * P.ns);
+        (count_launch(), k_p2m32<<<P.np2m, 128, 0, s>>>(tab, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
+                                                        P.nrad32.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr,
+                                                        P.ns, P.mult32.ptr));
+    }
+    const size_t smk = sizeof(float) * 3 * n4;
+    for (int l = T.nlevels - 1; l >= 0; --l) {
+        const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
+        if (e > b) {
+            ProfScope ps_(PROF_M2M);
+            (count_launch(), k_m2m32<<<e - b, 128, smk, s>>>(tab, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
+                                                             P.mult32.ptr));
+        }
+    }
+    P.local32.zero();
+    if (S.nchunks32 > 0) {
+        ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 4.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));
+        const dim3 grid(div_up(n4, GM_BM), S.nchunks32);
+        (count_launch(), k_m2l_v32<<<grid, 256, 0, s>>>(n4, S.v_chunk32.ptr, S.v_src.ptr, S.v_tgt.ptr, P.ops32.ptr,
+                                                        P.mult32.ptr, P.local32.ptr));
+    }
+    if (S.nxpairs > 0) {
+        ProfScope ps_(PROF_M2L_X, 102.0 * R * (double)R * S.nxpairs, 8.0 * n4 * S.nxpairs);
+        (count_launch(), k_m2l_x32<<<(int)S.nxpairs, 128, 0, s>>>(tab, k32, S.x_src.ptr, S.x_tgt.ptr, S.x_off32.ptr,
+                                                                  P.nrad32.ptr, P.mult32.ptr, P.local32.ptr));
+    }
+    for (int l = 3; l < T.nlevels; ++l) {
+        const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
+        if (e > b) {
+            ProfScope ps_(PROF_L2L);
+            (count_launch(), k_l2l32<<<e - b, 128, smk, s>>>(tab, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
+                                                             P.local32.ptr));
+        }
+    }
+    const float *tx = S.self ? P.sxf.ptr : S.txf.ptr;
+    const float *ty = S.self ? P.syf.ptr : S.tyf.ptr;
+    const float *tz = S.self ? P.szf.ptr : S.tzf.ptr;
+    if (S.ntleaves > 0) {
+        ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 28.0 * P.ns + 40.0 * S.nt);
+        (count_launch(), k_near32<<<S.ntleaves, NT32, 0, s>>>(tab, k32, S.tleaf.ptr, S.near32_ptr.ptr, S.near32_range.ptr,
+                                                              S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr, P.nrad32.ptr,
+                                                              P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr, P.ns, tx, ty,
+                                                              tz, S.nt, P.local32.ptr, out));
+    }
+    IBIM_CHECK_LAUNCH();
 }
 
 }  // namespace ibim

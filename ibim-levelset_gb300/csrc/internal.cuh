@@ -125,7 +125,9 @@ struct Grid {
     Ctx *ctx;
     int nx, ny, nz;
     double sx, sy, sz, dx;
+    int prec = IBIM_PRECISION_FP64;  // storage and stencil arithmetic: FP64, or FP32 (mixed path)
     DevBuf<double> data;
+    DevBuf<float> data32;
     long cells() const { return (long)nx * ny * nz; }
 };
 
@@ -167,6 +169,8 @@ struct TargetSet {
     DevBuf<int> l2l_nodes;
     DevBuf<int> v_src, v_tgt, v_chunk; // V pairs sorted by operator; chunks (op, begin, count)
     int nchunks = 0;
+    DevBuf<int> v_chunk32;             // chunks of the FP32 contraction (larger)
+    int nchunks32 = 0;
     long nvpairs = 0;
     DevBuf<int> x_src, x_tgt;
     long nxpairs = 0;
@@ -174,7 +178,13 @@ struct TargetSet {
     int ntleaves = 0;
     long near_pairs = 0;
     DevBuf<double> out4;               // 4 x nt workspace
-    DevBuf<float> txf, tyf, tzf;       // target coordinates relative to their leaf centre (mixed)
+    // mixed precision
+    bool mixed_ready = false;
+    DevBuf<float> txf, tyf, tzf;       // target coordinates relative to their leaf centre
+    DevBuf<int> near32_ptr, near32_range;  // per target leaf: source leaves (begin, end)
+    DevBuf<float> near32_off;          // per source leaf entry: source leaf centre - target leaf centre
+    int near32_entries = 0;
+    DevBuf<float> x_off32;             // per X pair: source centre - target centre
 };
 
 // Tree over the sources + operators + target sets.
@@ -207,8 +217,11 @@ struct Plan {
     DevBuf<double> mult, local, dens4;
     DevBuf<float> mult32, local32, dens32;
     DevBuf<float> sxf, syf, szf;   // source coordinates relative to their leaf centre (mixed)
-    double kp_cache[4] = {-1, -1, -1, -1};
-    int ops_precision = -1;
+    DevBuf<float> nrad32;          // per node radius (mixed)
+    DevBuf<unsigned char> tables32;  // ChebTables32
+    bool mixed_ready = false;
+    double kp64[4] = {-1, -1, -1, -1}, kp32[4] = {-1, -1, -1, -1};
+    bool ops64_ready = false, ops32_ready = false;
     ~Plan() { for (auto *t : targets) delete t; }
 };
 
@@ -224,7 +237,8 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
                 int precision);
 
 // Level set (levelset.cu)
-Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value);
+Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value,
+                  int prec = IBIM_PRECISION_FP64);
 void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band);
 void levelset_evolve(Grid &g, double final_t, double vel, double cfl);
 int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,

@@ -1,4 +1,4 @@
-// Level set and tube quadrature on the GPU (sm_103a), FP64.
+// Level set and tube quadrature on the GPU (sm_103a).
 //
 // Replaces the reference's Grid / levelset / Surface (levelset.h:12-72, levelset.cpp:9-586):
 //   k_expand        levelset::expand       (levelset.cpp:91-109)   atom-parallel ordered atomicMax
@@ -7,12 +7,16 @@
 //   k_flood_tile    Surface BFS from cell 0 (levelset.cpp:444-524) as tiled label propagation
 //   k_tube_*        cavity removal + tube points (levelset.cpp:529-583) as an ordered compaction
 //
-// Grid layout (same as the reference): FP64, row-major, index i*Ny*Nz + j*Nz + k, k fastest.
+// Grid layout (same as the reference): row-major, index i*Ny*Nz + j*Nz + k, k fastest.
 // Stencil reads clamp indices to the grid (Grid::get, levelset.cpp:28-33).
+// Every kernel is instantiated for an FP64 grid (the reference-exact path) and an FP32 grid
+// (the mixed-precision path: storage and WENO arithmetic in FP32; tube points are emitted in
+// FP64 from the FP32 values).
 
 #include "internal.cuh"
 
 #include <cmath>
+#include <string>
 
 namespace ibim {
 
@@ -29,38 +33,54 @@ struct Dims {
     }
 };
 
-// Order-preserving map between doubles and unsigned 64-bit integers (for atomicMax).
-__device__ __forceinline__ unsigned long long d2o(double v) {
+// Order-preserving maps to unsigned integers (for atomicMax on either precision).
+__device__ __forceinline__ unsigned long long ord(double v) {
     unsigned long long u = (unsigned long long)__double_as_longlong(v);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
-__device__ __forceinline__ double o2d(unsigned long long u) {
+__device__ __forceinline__ unsigned ord(float v) {
+    unsigned u = __float_as_uint(v);
+    return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ double unord(unsigned long long u) {
     u = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
     return __longlong_as_double((long long)u);
 }
+__device__ __forceinline__ float unord(unsigned u) {
+    u = (u >> 31) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(u);
+}
+template <class T> struct OrdT;
+template <> struct OrdT<double> { using type = unsigned long long; };
+template <> struct OrdT<float> { using type = unsigned; };
 
-__global__ void k_fill(double *g, long n, double v) {
+template <class T>
+__global__ void k_fill(T *g, long n, T v) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) g[i] = v;
 }
 
-__global__ void k_scale(double *g, long n, double s) {
+template <class T>
+__global__ void k_scale(T *g, long n, T s) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) g[i] *= s;
 }
 
-__global__ void k_encode(double *g, long n, int dir) {
-    unsigned long long *u = reinterpret_cast<unsigned long long *>(g);
+template <class T>
+__global__ void k_encode(T *g, long n, int dir) {
+    using U = typename OrdT<T>::type;
+    U *u = reinterpret_cast<U *>(g);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         if (dir > 0)
-            u[i] = d2o(g[i]);
+            u[i] = ord(g[i]);
         else
-            g[i] = o2d(u[i]);
+            g[i] = unord(u[i]);
     }
 }
 
 // levelset::expand: g = max(g, (R_a + probe) - |x - c_a|) over the cube of +-r cells around
 // each atom, r = (int)((R_a + probe)/dx) + band.  blockIdx.y = atom.  Cells outside the grid
 // are skipped (the reference's Grid::set does not clamp).
-__global__ void k_expand(unsigned long long *g, Dims d, double sx, double sy, double sz, double dx,
+template <class T>
+__global__ void k_expand(typename OrdT<T>::type *g, Dims d, double sx, double sy, double sz, double dx,
                          const double *__restrict__ centers, const double *__restrict__ radii, double probe,
                          int band) {
     const int a = blockIdx.y;
@@ -77,43 +97,45 @@ __global__ void k_expand(unsigned long long *g, Dims d, double sx, double sy, do
         if (ia < 0 || b < 0 || c < 0 || ia >= d.nx || b >= d.ny || c >= d.nz) continue;
         const double px = (sx + ia * dx) - cx, py = (sy + b * dx) - cy, pz = (sz + c * dx) - cz;
         const double dist = R - sqrt(px * px + py * py + pz * pz);
-        atomicMax(g + d.idx(ia, b, c), d2o(dist));
+        atomicMax(g + d.idx(ia, b, c), ord((T)dist));
     }
 }
 
 // WENO5 one-sided derivatives along one axis from the 7 values w[0..6] centred on w[3]
 // (levelset::setGradient, levelset.cpp:330-388; Jiang-Peng smoothness indicators, eps 1e-6).
-__device__ __forceinline__ void weno5(const double w[7], double h, double &up, double &un) {
-    const double EPS_LS = 1e-6;
-    double a = w[1] - w[0], b = w[2] - w[1], c = w[3] - w[2], d = w[4] - w[3], e = w[5] - w[4], f = w[6] - w[5];
-    const double df = (-b + 7.0 * (c + d) - e) / 12.0;
+template <class T>
+__device__ __forceinline__ void weno5(const T w[7], T h, T &up, T &un) {
+    const T EPS_LS = (T)1e-6;
+    T a = w[1] - w[0], b = w[2] - w[1], c = w[3] - w[2], d = w[4] - w[3], e = w[5] - w[4], f = w[6] - w[5];
+    const T df = (-b + (T)7.0 * (c + d) - e) / (T)12.0;
     a = b - a;
     b = c - b;
     c = d - c;
     d = e - d;
     e = f - e;
-    double s0 = 13.0 * (e - d) * (e - d) + 3.0 * (e - 3.0 * d) * (e - 3.0 * d);
-    double s1 = 13.0 * (d - c) * (d - c) + 3.0 * (d + c) * (d + c);
-    double s2 = 13.0 * (c - b) * (c - b) + 3.0 * (3.0 * c - b) * (3.0 * c - b);
-    double a0 = 1.0 / ((EPS_LS + s0) * (EPS_LS + s0)), a1 = 6.0 / ((EPS_LS + s1) * (EPS_LS + s1)),
-           a2 = 3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
-    double w1 = 1.0 / (a0 + a1 + a2), w0 = a0 * w1, w2 = a2 * w1;
-    up = (df + w0 * (e - 2 * d + c) / 3.0 + (w2 - 0.5) * (d - 2.0 * c + b) / 6.0) / h;
-    s0 = 13.0 * (a - b) * (a - b) + 3.0 * (a - 3.0 * b) * (a - 3.0 * b);
-    s1 = 13.0 * (b - c) * (b - c) + 3.0 * (b + c) * (b + c);
-    s2 = 13.0 * (c - d) * (c - d) + 3.0 * (3.0 * c - d) * (3.0 * c - d);
-    a0 = 1.0 / ((EPS_LS + s0) * (EPS_LS + s0));
-    a1 = 6.0 / ((EPS_LS + s1) * (EPS_LS + s1));
-    a2 = 3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
-    w1 = 1.0 / (a0 + a1 + a2);
+    T s0 = (T)13.0 * (e - d) * (e - d) + (T)3.0 * (e - (T)3.0 * d) * (e - (T)3.0 * d);
+    T s1 = (T)13.0 * (d - c) * (d - c) + (T)3.0 * (d + c) * (d + c);
+    T s2 = (T)13.0 * (c - b) * (c - b) + (T)3.0 * ((T)3.0 * c - b) * ((T)3.0 * c - b);
+    T a0 = (T)1.0 / ((EPS_LS + s0) * (EPS_LS + s0)), a1 = (T)6.0 / ((EPS_LS + s1) * (EPS_LS + s1)),
+      a2 = (T)3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
+    T w1 = (T)1.0 / (a0 + a1 + a2), w0 = a0 * w1, w2 = a2 * w1;
+    up = (df + w0 * (e - 2 * d + c) / (T)3.0 + (w2 - (T)0.5) * (d - (T)2.0 * c + b) / (T)6.0) / h;
+    s0 = (T)13.0 * (a - b) * (a - b) + (T)3.0 * (a - (T)3.0 * b) * (a - (T)3.0 * b);
+    s1 = (T)13.0 * (b - c) * (b - c) + (T)3.0 * (b + c) * (b + c);
+    s2 = (T)13.0 * (c - d) * (c - d) + (T)3.0 * ((T)3.0 * c - d) * ((T)3.0 * c - d);
+    a0 = (T)1.0 / ((EPS_LS + s0) * (EPS_LS + s0));
+    a1 = (T)6.0 / ((EPS_LS + s1) * (EPS_LS + s1));
+    a2 = (T)3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
+    w1 = (T)1.0 / (a0 + a1 + a2);
     w0 = a0 * w1;
     w2 = a2 * w1;
-    un = (df - w0 * (a - 2 * b + c) / 3.0 - (w2 - 0.5) * (b - 2 * c + d) / 6.0) / h;
+    un = (df - w0 * (a - 2 * b + c) / (T)3.0 - (w2 - (T)0.5) * (b - 2 * c + d) / (T)6.0) / h;
 }
 
-__device__ __forceinline__ void gradients(const double *__restrict__ g, const Dims &dm, int i, int j, int k,
-                                          double h, double up[3], double un[3]) {
-    double w[7];
+template <class T>
+__device__ __forceinline__ void gradients(const T *__restrict__ g, const Dims &dm, int i, int j, int k, T h, T up[3],
+                                          T un[3]) {
+    T w[7];
 #pragma unroll
     for (int l = 0; l < 7; ++l) w[l] = __ldg(g + dm.cidx(i - 3 + l, j, k));
     weno5(w, h, up[0], un[0]);
@@ -126,11 +148,12 @@ __device__ __forceinline__ void gradients(const double *__restrict__ g, const Di
 }
 
 // levelset::getNorm(Dun, Dup) (levelset.cpp:294-301).
-__device__ __forceinline__ double godunov(const double n[3], const double p[3]) {
-    double v = 0.;
+template <class T>
+__device__ __forceinline__ T godunov(const T n[3], const T p[3]) {
+    T v = 0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double m = fmax(n[a] > 0. ? n[a] : 0., p[a] < 0. ? -p[a] : 0.);
+        const T m = fmax(n[a] > (T)0 ? n[a] : (T)0, p[a] < (T)0 ? -p[a] : (T)0);
         v += m * m;
     }
     return sqrt(v);
@@ -139,52 +162,50 @@ __device__ __forceinline__ double godunov(const double n[3], const double p[3]) 
 // One TVD-RK3 stage over the whole grid.  MODE 0: evolve (phi_t + vel|grad phi| = 0);
 // MODE 1: reinitialize (phi_t + S(phi0)(|grad phi| - 1) = 0, S = phi0/sqrt(phi0^2 + dx^2)).
 // STAGE 0: u1 = g - L(g); 1: u2 = (3g + u1 - L(u1))/4; 2: g = (g + 2(u2 - L(u2)))/3.
-template <int MODE, int STAGE>
-__global__ void __launch_bounds__(256) k_weno_stage(Dims dm, double h, double dtv, double eps,
-                                                    const double *__restrict__ src, double *g, double *u1,
-                                                    double *u2, const double *__restrict__ phi0) {
+template <int MODE, int STAGE, class T>
+__global__ void __launch_bounds__(256) k_weno_stage(Dims dm, T h, T dtv, T eps, const T *__restrict__ src, T *g, T *u1,
+                                                    T *u2, const T *__restrict__ phi0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z * blockDim.z + threadIdx.z;
     if (i >= dm.nx || j >= dm.ny || k >= dm.nz) return;
-    double up[3], un[3];
+    T up[3], un[3];
     gradients(src, dm, i, j, k, h, up, un);
     const long I = dm.idx(i, j, k);
-    double L;
+    T L;
     if (MODE == 0) {
         L = dtv * godunov(un, up);
     } else {
-        const double p0 = phi0[I];
-        const double sign = p0 / sqrt(p0 * p0 + eps);
-        const double nd = sign > 0. ? godunov(un, up) : godunov(up, un);
-        L = dtv * sign * (nd - 1.0);
+        const T p0 = phi0[I];
+        const T sign = p0 / sqrt(p0 * p0 + eps);
+        const T nd = sign > (T)0 ? godunov(un, up) : godunov(up, un);
+        L = dtv * sign * (nd - (T)1.0);
     }
     if (STAGE == 0)
         u1[I] = g[I] - L;
     else if (STAGE == 1)
-        u2[I] = (3 * g[I] + u1[I] - L) / 4.0;
+        u2[I] = (3 * g[I] + u1[I] - L) / (T)4.0;
     else
-        g[I] = (g[I] + 2 * (u2[I] - L)) / 3.0;
+        g[I] = (g[I] + 2 * (u2[I] - L)) / (T)3.0;
 }
 
 // levelset::countGradient: among cells with |g| < thickness*dx, count | |grad g| - 1 | > thres.
-__global__ void __launch_bounds__(256) k_count_grad(Dims dm, double h, double band, double thres,
-                                                    const double *__restrict__ g, unsigned long long *counts,
-                                                    double *accum) {
+template <class T>
+__global__ void __launch_bounds__(256) k_count_grad(Dims dm, T h, T band, T thres, const T *__restrict__ g,
+                                                    unsigned long long *counts, double *accum) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z * blockDim.z + threadIdx.z;
     unsigned bad = 0, tot = 0;
     double acc = 0.;
     if (i < dm.nx && j < dm.ny && k < dm.nz && fabs(g[dm.idx(i, j, k)]) < band) {
-        double up[3], un[3];
+        T up[3], un[3];
         gradients(g, dm, i, j, k, h, up, un);
-        const double nr = godunov(un, up);
+        const T nr = godunov(un, up);
         tot = 1;
-        bad = fabs(nr - 1.0) > thres ? 1u : 0u;
-        acc = fabs(nr - 1.0);
+        bad = fabs(nr - (T)1.0) > thres ? 1u : 0u;
+        acc = fabs((double)nr - 1.0);
     }
-    // warp then block reduction, one atomic per block
     for (int o = 16; o > 0; o >>= 1) {
         bad += __shfl_down_sync(0xffffffffu, bad, o);
         tot += __shfl_down_sync(0xffffffffu, tot, o);
@@ -196,13 +217,13 @@ __global__ void __launch_bounds__(256) k_count_grad(Dims dm, double h, double ba
     if ((tid & 31) == 0) { sb[tid >> 5] = bad; st[tid >> 5] = tot; sa[tid >> 5] = acc; }
     __syncthreads();
     if (tid == 0) {
-        unsigned B = 0, T = 0;
+        unsigned B = 0, Tt = 0;
         double A = 0;
         const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
-        for (int w = 0; w < nw; ++w) { B += sb[w]; T += st[w]; A += sa[w]; }
-        if (T) {
+        for (int w = 0; w < nw; ++w) { B += sb[w]; Tt += st[w]; A += sa[w]; }
+        if (Tt) {
             atomicAdd(counts, (unsigned long long)B);
-            atomicAdd(counts + 1, (unsigned long long)T);
+            atomicAdd(counts + 1, (unsigned long long)Tt);
             atomicAdd(accum, A);
         }
     }
@@ -213,7 +234,8 @@ __global__ void __launch_bounds__(256) k_count_grad(Dims dm, double h, double ba
 // rule to a fixed point in shared memory (halo = neighbours' state at launch), writes back and
 // raises `changed` if it reached new cells.  The host relaunches until nothing changes.
 constexpr int FT_K = 32, FT_J = 8, FT_I = 4;
-__global__ void __launch_bounds__(FT_K *FT_J *FT_I) k_flood_tile(Dims dm, double neg_tw, const double *__restrict__ g,
+template <class T>
+__global__ void __launch_bounds__(FT_K *FT_J *FT_I) k_flood_tile(Dims dm, T neg_tw, const T *__restrict__ g,
                                                                  unsigned char *vis, int *changed) {
     __shared__ unsigned char sv[FT_I + 2][FT_J + 2][FT_K + 2];
     __shared__ unsigned char sp[FT_I + 2][FT_J + 2][FT_K + 2];
@@ -257,16 +279,17 @@ __global__ void __launch_bounds__(FT_K *FT_J *FT_I) k_flood_tile(Dims dm, double
 constexpr int TUBE_BLOCK = 1024;
 
 // Cavity removal (levelset.cpp:529-537) and per-block tube counts in linear cell order.
-__global__ void __launch_bounds__(TUBE_BLOCK) k_tube_count(long n, double tw, double *g,
-                                                           const unsigned char *__restrict__ vis,
-                                                           int *block_counts, unsigned long long *ninc) {
+template <class T>
+__global__ void __launch_bounds__(TUBE_BLOCK) k_tube_count(long n, T tw, T cavity, T *g,
+                                                           const unsigned char *__restrict__ vis, int *block_counts,
+                                                           unsigned long long *ninc) {
     const long I = blockIdx.x * (long)TUBE_BLOCK + threadIdx.x;
     int in = 0;
     unsigned inc = 0;
     if (I < n) {
-        double v = g[I];
+        T v = g[I];
         if (!vis[I] && fabs(v) < tw) {
-            v = -(tw + 1e-15);
+            v = cavity;
             g[I] = v;
             inc = 1;
         }
@@ -289,7 +312,6 @@ __global__ void k_scan_counts(const int *counts, int nb, long *offsets) {
     for (int base = 0; base < nb; base += blockDim.x) {
         const int i = base + threadIdx.x;
         long v = i < nb ? counts[i] : 0;
-        // inclusive warp scan
         long x = v;
         for (int o = 1; o < 32; o <<= 1) {
             long y = __shfl_up_sync(0xffffffffu, x, o);
@@ -316,14 +338,15 @@ __global__ void k_scan_counts(const int *counts, int nb, long *offsets) {
 }
 
 // Tube points in (i, j, k) order (levelset.cpp:540-583): normal = (D- + D+)/2 (not normalised),
-// projection P = x - n*phi, weight = (1 + cos(pi phi / tw)) / (2 tw).
-__global__ void __launch_bounds__(TUBE_BLOCK) k_tube_emit(Dims dm, double sx, double sy, double sz, double dx,
-                                                          double tw, const double *__restrict__ g,
-                                                          const long *__restrict__ offsets, double *px, double *py,
-                                                          double *pz, double *qx, double *qy, double *qz, double *w) {
+// projection P = x - n*phi, weight = (1 + cos(pi phi / tw)) / (2 tw); emitted in FP64.
+template <class T>
+__global__ void __launch_bounds__(TUBE_BLOCK) k_tube_emit(Dims dm, double sx, double sy, double sz, double dx, T tw,
+                                                          const T *__restrict__ g, const long *__restrict__ offsets,
+                                                          double *px, double *py, double *pz, double *qx, double *qy,
+                                                          double *qz, double *w) {
     const long n = (long)dm.nx * dm.ny * dm.nz;
     const long I = blockIdx.x * (long)TUBE_BLOCK + threadIdx.x;
-    const double v = I < n ? g[I] : 0.;
+    const T v = I < n ? g[I] : (T)0;
     const bool in = I < n && fabs(v) < tw;
     __shared__ int wcount[TUBE_BLOCK / 32];
     const unsigned bal = __ballot_sync(0xffffffffu, in);
@@ -336,22 +359,24 @@ __global__ void __launch_bounds__(TUBE_BLOCK) k_tube_emit(Dims dm, double sx, do
             int y = __shfl_up_sync(0xffffffffu, s, o);
             if (threadIdx.x >= o) s += y;
         }
-        wcount[threadIdx.x] = s;  // inclusive
+        wcount[threadIdx.x] = s;
     }
     __syncthreads();
     if (!in) return;
     const long pos = offsets[blockIdx.x] + (warp ? wcount[warp - 1] : 0) + __popc(bal & ((1u << lane) - 1));
     const int k = (int)(I % dm.nz), j = (int)((I / dm.nz) % dm.ny), i = (int)(I / ((long)dm.ny * dm.nz));
-    double up[3], un[3];
-    gradients(g, dm, i, j, k, dx, up, un);
-    const double nxv = (un[0] + up[0]) * 0.5, nyv = (un[1] + up[1]) * 0.5, nzv = (un[2] + up[2]) * 0.5;
-    px[pos] = (sx + i * dx) - nxv * v;
-    py[pos] = (sy + j * dx) - nyv * v;
-    pz[pos] = (sz + k * dx) - nzv * v;
+    T up[3], un[3];
+    gradients(g, dm, i, j, k, (T)dx, up, un);
+    const double nxv = (double)((un[0] + up[0]) * (T)0.5), nyv = (double)((un[1] + up[1]) * (T)0.5),
+                 nzv = (double)((un[2] + up[2]) * (T)0.5);
+    const double vd = (double)v, twd = (double)tw;
+    px[pos] = (sx + i * dx) - nxv * vd;
+    py[pos] = (sy + j * dx) - nyv * vd;
+    pz[pos] = (sz + k * dx) - nzv * vd;
     qx[pos] = nxv;
     qy[pos] = nyv;
     qz[pos] = nzv;
-    w[pos] = 0.5 * (1.0 + cos(M_PI * v / tw)) / tw;
+    w[pos] = 0.5 * (1.0 + cos(M_PI * vd / twd)) / twd;
 }
 
 inline dim3 stencil_block() { return dim3(32, 4, 2); }
@@ -361,95 +386,67 @@ inline dim3 stencil_grid(const Grid &g) {
 }
 inline Dims dims_of(const Grid &g) { return Dims{g.nx, g.ny, g.nz}; }
 
-}  // namespace
+template <class T> T *gdata(Grid &g);
+template <> double *gdata<double>(Grid &g) { return g.data.ptr; }
+template <> float *gdata<float>(Grid &g) { return g.data32.ptr; }
+template <class T> const T *gdata(const Grid &g) { return gdata<T>(const_cast<Grid &>(g)); }
 
-Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value) {
-    IBIM_REQUIRE(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
-    IBIM_REQUIRE(dx > 0, "grid spacing must be positive");
-    IBIM_REQUIRE((double)nx * ny * nz < 4.0e9, "grid too large");
-    Grid *g = new Grid();
-    g->ctx = c;
-    g->nx = nx; g->ny = ny; g->nz = nz;
-    g->sx = sx; g->sy = sy; g->sz = sz; g->dx = dx;
-    try {
-        g->data.alloc(g->cells(), c->stream);
-        (count_launch(), k_fill<<<4 * c->num_sms, 256, 0, c->stream>>>(g->data.ptr, g->cells(), value));
-        IBIM_CHECK_LAUNCH();
-    } catch (...) {
-        delete g;
-        throw;
-    }
-    return g;
-}
-
-void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band) {
-    if (natoms <= 0) return;
-    IBIM_REQUIRE(natoms <= 65535 * 64, "too many atoms");
+template <class T>
+void expand_t(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band) {
     cudaStream_t s = g.ctx->stream;
     const long n = g.cells();
-    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, +1)); }
-    // atoms beyond gridDim.y's limit are processed in slices
+    T *d = gdata<T>(g);
+    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<T><<<4 * g.ctx->num_sms, 256, 0, s>>>(d, n, +1)); }
     for (int a0 = 0; a0 < natoms; a0 += 65535) {
         const int na = std::min(65535, natoms - a0);
         dim3 grid(8, na);
-        { ProfScope ps_(PROF_EXPAND); (count_launch(), k_expand<<<grid, 256, 0, s>>>(reinterpret_cast<unsigned long long *>(g.data.ptr), dims_of(g), g.sx, g.sy,
-                                      g.sz, g.dx, centers_dev + 3 * (long)a0, radii_dev + a0, probe, band)); }
+        ProfScope ps_(PROF_EXPAND);
+        (count_launch(), k_expand<T><<<grid, 256, 0, s>>>(reinterpret_cast<typename OrdT<T>::type *>(d), dims_of(g),
+                                                           g.sx, g.sy, g.sz, g.dx, centers_dev + 3 * (long)a0,
+                                                           radii_dev + a0, probe, band));
     }
-    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<<<4 * g.ctx->num_sms, 256, 0, s>>>(g.data.ptr, n, -1)); }
+    { ProfScope ps_(PROF_EXPAND); (count_launch(), k_encode<T><<<4 * g.ctx->num_sms, 256, 0, s>>>(d, n, -1)); }
     IBIM_CHECK_LAUNCH();
 }
 
-void levelset_evolve(Grid &g, double final_t, double vel, double cfl) {
-    IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "evolve: invalid time step parameters");
+template <class T>
+void evolve_t(Grid &g, double final_t, double vel, double cfl) {
     double dt = cfl * g.dx / vel;
     const int steps = (int)(final_t / dt) + 1;
     dt = final_t / (double)steps;
     cudaStream_t s = g.ctx->stream;
-    DevBuf<double> u1, u2;
+    DevBuf<T> u1, u2;
     u1.alloc(g.cells(), s);
     u2.alloc(g.cells(), s);
     const Dims dm = dims_of(g);
     const dim3 gr = stencil_grid(g), bl = stencil_block();
-    const double dtv = dt * vel, ih = g.dx;
+    const T dtv = (T)(dt * vel), h = (T)g.dx;
+    T *G = gdata<T>(g);
+    const double fl = 350.0 * g.cells(), by = 3.0 * sizeof(T) * g.cells();
     for (int st = 0; st < steps; ++st) {
-        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., g.data.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
-        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u1.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
-        { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<0, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, 0., u2.ptr, g.data.ptr, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, G, G, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, u1.ptr, G, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, u2.ptr, G, u1.ptr, u2.ptr, nullptr)); }
     }
     IBIM_CHECK_LAUNCH();
 }
 
-void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc) {
-    cudaStream_t s = g.ctx->stream;
-    DevBuf<unsigned long long> cnt;
-    DevBuf<double> a;
-    cnt.alloc(2, s);
-    a.alloc(1, s);
-    cnt.zero();
-    a.zero();
-    { ProfScope ps_(PROF_COUNT, 0., 8.0 * g.cells()); (count_launch(), k_count_grad<<<stencil_grid(g), stencil_block(), 0, s>>>(dims_of(g), g.dx, thickness * g.dx, thres,
-                                                             g.data.ptr, cnt.ptr, a.ptr)); }
-    IBIM_CHECK_LAUNCH();
-    unsigned long long h[2];
-    double ha;
-    cnt.download(h, 2);
-    a.download(&ha, 1);
-    IBIM_CUDA(cudaStreamSynchronize(s));
-    if (bad) *bad = (long)h[0];
-    if (total) *total = (long)h[1];
-    if (acc) *acc = ha;
+template <class T>
+void count_t(const Grid &g, double thickness, double thres, unsigned long long *cnt, double *acc) {
+    ProfScope ps_(PROF_COUNT, 0., (double)sizeof(T) * g.cells());
+    (count_launch(), k_count_grad<T><<<stencil_grid(g), stencil_block(), 0, g.ctx->stream>>>(
+                         dims_of(g), (T)g.dx, (T)(thickness * g.dx), (T)thres, gdata<T>(g), cnt, acc));
 }
 
-int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,
-                          double thres) {
-    IBIM_REQUIRE(phi0.nx == g.nx && phi0.ny == g.ny && phi0.nz == g.nz, "reinitialize: phi0 size mismatch");
-    IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "reinitialize: invalid time step parameters");
+template <class T>
+int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness, double thres) {
     double dt = cfl * g.dx / vel;
     const double eps = g.dx * g.dx;
     const int steps = (int)(final_t / dt) + 1;
     dt = final_t / (double)steps;
     cudaStream_t s = g.ctx->stream;
-    DevBuf<double> u1, u2, acc;
+    DevBuf<T> u1, u2;
+    DevBuf<double> acc;
     DevBuf<unsigned long long> cnt;
     u1.alloc(g.cells(), s);
     u2.alloc(g.cells(), s);
@@ -459,10 +456,13 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
     IBIM_CUDA(cudaMallocHost((void **)&hcnt, 2 * sizeof(unsigned long long)));
     const Dims dm = dims_of(g);
     const dim3 gr = stencil_grid(g), bl = stencil_block();
-    const double dtv = dt * vel, ih = g.dx, band = thickness * g.dx;
+    const T dtv = (T)(dt * vel), h = (T)g.dx;
+    T *G = gdata<T>(g);
+    const T *P0 = gdata<T>(phi0);
+    const double fl = 350.0 * g.cells(), by = 4.0 * sizeof(T) * g.cells();
     auto count = [&]() -> unsigned long long {
         cnt.zero();
-        { ProfScope ps_(PROF_COUNT, 0., 8.0 * g.cells()); (count_launch(), k_count_grad<<<gr, bl, 0, s>>>(dm, ih, band, thres, g.data.ptr, cnt.ptr, acc.ptr)); }
+        count_t<T>(g, (double)thickness, thres, cnt.ptr, acc.ptr);
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaMemcpyAsync(hcnt, cnt.ptr, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         IBIM_CUDA(cudaStreamSynchronize(s));
@@ -473,12 +473,9 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
         unsigned long long bad = count();
         while (bad != 0 && step < steps) {
             step++;
-            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 0><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, g.data.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr)); }
-            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 1><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u1.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr)); }
-            { ProfScope ps_(PROF_WENO, 350.0 * g.cells(), 24.0 * g.cells()); (count_launch(), k_weno_stage<1, 2><<<gr, bl, 0, s>>>(dm, ih, dtv, eps, u2.ptr, g.data.ptr, u1.ptr, u2.ptr,
-                                                 phi0.data.ptr)); }
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, G, G, u1.ptr, u2.ptr, P0)); }
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u1.ptr, G, u1.ptr, u2.ptr, P0)); }
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u2.ptr, G, u1.ptr, u2.ptr, P0)); }
             bad = count();
         }
     } catch (...) {
@@ -489,25 +486,14 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
     return step;
 }
 
-// Grid::operator*= (levelset.cpp:54-59)
-void grid_scale(Grid &g, double sc) {
-    (count_launch(), k_scale<<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(g.data.ptr, g.cells(), sc));
-    IBIM_CHECK_LAUNCH();
-}
-
-void grid_copy(Grid &dst, const Grid &src) {
-    IBIM_REQUIRE(dst.cells() == src.cells(), "grid copy: size mismatch");
-    IBIM_CUDA(cudaMemcpyAsync(dst.data.ptr, src.data.ptr, sizeof(double) * src.cells(), cudaMemcpyDeviceToDevice,
-                              dst.ctx->stream));
-}
-
-Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
-    IBIM_REQUIRE(thickness > 0, "thickness must be positive");
+template <class T>
+Tube *surface_t(Grid &g, int thickness, long *inclusion) {
     Ctx *c = g.ctx;
     cudaStream_t s = c->stream;
     const double tw = thickness * g.dx;
     const long n = g.cells();
     const Dims dm = dims_of(g);
+    T *G = gdata<T>(g);
     DevBuf<unsigned char> vis;
     DevBuf<int> changed;
     vis.alloc(n, s);
@@ -525,7 +511,10 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     try {
         for (;;) {
             changed.zero();
-            for (int r = 0; r < 4; ++r) { ProfScope ps_(PROF_FLOOD); (count_launch(), k_flood_tile<<<fg, fb, 0, s>>>(dm, -tw, g.data.ptr, vis.ptr, changed.ptr)); }
+            for (int r = 0; r < 4; ++r) {
+                ProfScope ps_(PROF_FLOOD);
+                (count_launch(), k_flood_tile<T><<<fg, fb, 0, s>>>(dm, (T)(-tw), G, vis.ptr, changed.ptr));
+            }
             IBIM_CHECK_LAUNCH();
             IBIM_CUDA(cudaMemcpyAsync(hflag, changed.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
             IBIM_CUDA(cudaStreamSynchronize(s));
@@ -546,7 +535,10 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     offsets.alloc(nb + 1, s);
     ninc.alloc(1, s);
     ninc.zero();
-    { ProfScope ps_(PROF_TUBE); (count_launch(), k_tube_count<<<nb, TUBE_BLOCK, 0, s>>>(n, tw, g.data.ptr, vis.ptr, counts.ptr, ninc.ptr)); }
+    // the cavity value -(tw + 1e-15) (levelset.cpp:529) rounds to -tw in FP32; one ulp below
+    // keeps such cells outside the tube in either precision
+    const T cavity = sizeof(T) == 8 ? (T)(-(tw + 1e-15)) : (T)std::nextafter(-(float)tw, -1e30f);
+    { ProfScope ps_(PROF_TUBE); (count_launch(), k_tube_count<T><<<nb, TUBE_BLOCK, 0, s>>>(n, (T)tw, cavity, G, vis.ptr, counts.ptr, ninc.ptr)); }
     { ProfScope ps_(PROF_TUBE); (count_launch(), k_scan_counts<<<1, 1024, 0, s>>>(counts.ptr, nb, offsets.ptr)); }
     IBIM_CHECK_LAUNCH();
     long total = 0;
@@ -561,8 +553,10 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     try {
         DevBuf<double> *arrs[7] = {&t->x, &t->y, &t->z, &t->nx, &t->ny, &t->nz, &t->w};
         for (auto *a : arrs) a->alloc(total > 0 ? total : 1, s);
-        { ProfScope ps_(PROF_TUBE); (count_launch(), k_tube_emit<<<nb, TUBE_BLOCK, 0, s>>>(dm, g.sx, g.sy, g.sz, g.dx, tw, g.data.ptr, offsets.ptr, t->x.ptr,
-                                             t->y.ptr, t->z.ptr, t->nx.ptr, t->ny.ptr, t->nz.ptr, t->w.ptr)); }
+        ProfScope ps_(PROF_TUBE);
+        (count_launch(), k_tube_emit<T><<<nb, TUBE_BLOCK, 0, s>>>(dm, g.sx, g.sy, g.sz, g.dx, (T)tw, G, offsets.ptr,
+                                                                  t->x.ptr, t->y.ptr, t->z.ptr, t->nx.ptr, t->ny.ptr,
+                                                                  t->nz.ptr, t->w.ptr));
         IBIM_CHECK_LAUNCH();
     } catch (...) {
         delete t;
@@ -572,4 +566,104 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
     return t;
 }
 
+}  // namespace
+
+Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value, int prec) {
+    IBIM_REQUIRE(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
+    IBIM_REQUIRE(dx > 0, "grid spacing must be positive");
+    IBIM_REQUIRE((double)nx * ny * nz < 4.0e9, "grid too large");
+    Grid *g = new Grid();
+    g->ctx = c;
+    g->nx = nx; g->ny = ny; g->nz = nz;
+    g->sx = sx; g->sy = sy; g->sz = sz; g->dx = dx;
+    g->prec = prec;
+    try {
+        if (prec == IBIM_PRECISION_FP64) {
+            g->data.alloc(g->cells(), c->stream);
+            (count_launch(), k_fill<double><<<4 * c->num_sms, 256, 0, c->stream>>>(g->data.ptr, g->cells(), value));
+        } else {
+            g->data32.alloc(g->cells(), c->stream);
+            (count_launch(), k_fill<float><<<4 * c->num_sms, 256, 0, c->stream>>>(g->data32.ptr, g->cells(), (float)value));
+        }
+        IBIM_CHECK_LAUNCH();
+    } catch (...) {
+        delete g;
+        throw;
+    }
+    return g;
+}
+
+void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band) {
+    if (natoms <= 0) return;
+    if (g.prec == IBIM_PRECISION_FP64)
+        expand_t<double>(g, centers_dev, radii_dev, natoms, probe, band);
+    else
+        expand_t<float>(g, centers_dev, radii_dev, natoms, probe, band);
+}
+
+void levelset_evolve(Grid &g, double final_t, double vel, double cfl) {
+    IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "evolve: invalid time step parameters");
+    if (g.prec == IBIM_PRECISION_FP64)
+        evolve_t<double>(g, final_t, vel, cfl);
+    else
+        evolve_t<float>(g, final_t, vel, cfl);
+}
+
+void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc) {
+    cudaStream_t s = g.ctx->stream;
+    DevBuf<unsigned long long> cnt;
+    DevBuf<double> a;
+    cnt.alloc(2, s);
+    a.alloc(1, s);
+    cnt.zero();
+    a.zero();
+    if (g.prec == IBIM_PRECISION_FP64)
+        count_t<double>(g, thickness, thres, cnt.ptr, a.ptr);
+    else
+        count_t<float>(g, thickness, thres, cnt.ptr, a.ptr);
+    IBIM_CHECK_LAUNCH();
+    unsigned long long h[2];
+    double ha;
+    cnt.download(h, 2);
+    a.download(&ha, 1);
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    if (bad) *bad = (long)h[0];
+    if (total) *total = (long)h[1];
+    if (acc) *acc = ha;
+}
+
+int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,
+                          double thres) {
+    IBIM_REQUIRE(phi0.nx == g.nx && phi0.ny == g.ny && phi0.nz == g.nz && phi0.prec == g.prec,
+                 "reinitialize: phi0 size or precision mismatch");
+    IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "reinitialize: invalid time step parameters");
+    return g.prec == IBIM_PRECISION_FP64 ? reinit_t<double>(g, phi0, final_t, vel, cfl, thickness, thres)
+                                         : reinit_t<float>(g, phi0, final_t, vel, cfl, thickness, thres);
+}
+
+// Grid::operator*= (levelset.cpp:54-59)
+void grid_scale(Grid &g, double sc) {
+    if (g.prec == IBIM_PRECISION_FP64)
+        (count_launch(), k_scale<double><<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(g.data.ptr, g.cells(), sc));
+    else
+        (count_launch(), k_scale<float><<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(g.data32.ptr, g.cells(), (float)sc));
+    IBIM_CHECK_LAUNCH();
+}
+
+// Grid::operator= (levelset.cpp:61-73)
+void grid_copy(Grid &dst, const Grid &src) {
+    IBIM_REQUIRE(dst.cells() == src.cells() && dst.prec == src.prec, "grid copy: size or precision mismatch");
+    const size_t bytes = (src.prec == IBIM_PRECISION_FP64 ? sizeof(double) : sizeof(float)) * src.cells();
+    IBIM_CUDA(cudaMemcpyAsync(src.prec == IBIM_PRECISION_FP64 ? (void *)dst.data.ptr : (void *)dst.data32.ptr,
+                              src.prec == IBIM_PRECISION_FP64 ? (const void *)src.data.ptr : (const void *)src.data32.ptr,
+                              bytes, cudaMemcpyDeviceToDevice, dst.ctx->stream));
+}
+
+Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
+    IBIM_REQUIRE(thickness > 0, "thickness must be positive");
+    return g.prec == IBIM_PRECISION_FP64 ? surface_t<double>(g, thickness, inclusion)
+                                         : surface_t<float>(g, thickness, inclusion);
+}
+
 }  // namespace ibim
+

@@ -145,7 +145,8 @@ int ibim_levelset_reinitialize(ibim_grid g, ibim_grid phi0, double final_t, doub
                                int thickness, double thres, int *steps);    /* levelset::reinitialize */
 int ibim_levelset_count_gradient(ibim_grid g, double thickness, double thres, long *bad, long *total,
                                  double *accum_error);                      /* levelset::countGradient */
-/* main.cpp:45-60 in one call: expand, evolve inward by the probe, flip sign, reinit twice. */
+/* main.cpp:45-60 in one call: expand, evolve inward by the probe, flip sign, reinit twice.
+ * cfg->precision selects an FP64 grid or (IBIM_PRECISION_MIXED) an FP32 grid. */
 int ibim_levelset_build(ibim_ctx ctx, const double *centers, const double *radii, int natoms,
                         const ibim_config *cfg, ibim_grid *out, int steps[2]);
 
@@ -174,12 +175,13 @@ int ibim_plan_stats(ibim_plan p, long stats[8]);
 int ibim_plan_lists(ibim_plan p, int which, int *buf, long cap, long *needed);
 /* The same tree and lists built on the host from n points (n, 3), without a GPU. */
 int ibim_tree_lists_host(const double *points, long n, int maxpoint, int maxlevel, int *buf, long cap, long *needed);
-/* One FMM.  kernel in [IBIM_K1X, IBIM_K4Z]: in is (ns), out is (nt);
+/* One FMM in the plan's precision.  kernel in [IBIM_K1X, IBIM_K4Z]: in is (ns), out is (nt);
  * IBIM_KERNEL_BIE_FUSED: in is (4, ns), out is (4, nt).  Host buffers, caller point order. */
 int ibim_fmm_apply(ibim_plan p, int kernel, const ibim_kernel_params *kp, const double *in, double *out);
 
 /* ---- BIE operator, GMRES, energy: replaces GMRES (gmres.h:20-21) and electric (electric.h:13) ---- */
-/* y = dmapping(x) (electric.cpp:294-388), x, y of length 2N, host buffers, reference order. */
+/* y = dmapping(x) (electric.cpp:294-388) in the plan's precision, x, y of length 2N, host buffers,
+ * reference order. */
 int ibim_bie_matvec(ibim_plan p, const ibim_kernel_params *kp, const double *x, double *y);
 /* load (electric.cpp:395-412): b of length 2N. */
 int ibim_bie_rhs(ibim_plan p, const ibim_kernel_params *kp, const double *centers, const double *charges,
