@@ -16,6 +16,7 @@
 #include "internal.cuh"
 
 #include <cmath>
+#include <mutex>
 #include <string>
 
 namespace ibim {
@@ -667,3 +668,82 @@ Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
 
 }  // namespace ibim
 
+// ---------------------------------------------------------------------------------------------
+// Allocation-free level-set evolution
+//
+// Some callers cannot let a library allocate device memory: applications that reserve their
+// whole HBM budget in their own pool at start-up, or loops that must never enter the CUDA
+// allocator (cudaMalloc / cudaFree can synchronise the device and can fail under memory
+// pressure in the middle of a run).  ibim_levelset_evolve_static runs levelset::evolve on a
+// caller-owned FP64 device grid and takes its two TVD-RK3 stage buffers from the fixed array
+// below instead of allocating them.  The array holds 2 x 524,288 doubles (8 MiB) and stays
+// resident on every GPU that loads this library until the process exits; grids larger than
+// 524,288 cells are rejected.  All calls share the array, so calls that overlap on the GPU
+// (on different streams, or from different threads) race; the stage buffers are fully written
+// before they are read, so nothing in the array has to start at zero.
+// ---------------------------------------------------------------------------------------------
+
+namespace ibim {
+namespace {
+constexpr long kStaticMaxCells = 1L << 19;
+__device__ __align__(256) double g_static_stage[2 * kStaticMaxCells];
+std::mutex g_static_mu;
+double *g_static_addr[256] = {nullptr};  // per device, from cudaGetSymbolAddress
+}  // namespace
+
+}  // namespace ibim
+
+extern "C" int ibim_levelset_evolve_static(double *grid_dev, int nx, int ny, int nz, double dx, double final_t,
+                                           double vel, double cfl, void *stream) {
+    using namespace ibim;
+    if (!grid_dev || nx <= 0 || ny <= 0 || nz <= 0 || !(dx > 0) || !(vel > 0) || !(cfl > 0) || !(final_t >= 0)) {
+        set_last_error("ibim_levelset_evolve_static: invalid argument");
+        return IBIM_ERR_INVALID_ARGUMENT;
+    }
+    const long cells = (long)nx * ny * nz;
+    if (cells > kStaticMaxCells) {
+        set_last_error("ibim_levelset_evolve_static: grid of " + std::to_string(cells) +
+                       " cells exceeds the fixed scratch limit of " + std::to_string(kStaticMaxCells) + " cells");
+        return IBIM_ERR_INVALID_ARGUMENT;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 256) {
+        set_last_error(std::string("ibim_levelset_evolve_static: cudaGetDevice: ") + cudaGetErrorString(e));
+        return IBIM_ERR_CUDA;
+    }
+    double *scratch = nullptr;
+    {
+        // first call on a device: look up the array's device address with that device current
+        std::lock_guard<std::mutex> lock(g_static_mu);
+        if (!g_static_addr[dev]) {
+            e = cudaGetSymbolAddress((void **)&g_static_addr[dev], g_static_stage);
+            if (e != cudaSuccess) {
+                g_static_addr[dev] = nullptr;
+                set_last_error(std::string("ibim_levelset_evolve_static: cudaGetSymbolAddress: ") +
+                               cudaGetErrorString(e));
+                return IBIM_ERR_CUDA;
+            }
+        }
+        scratch = g_static_addr[dev];
+    }
+    double *u1 = scratch, *u2 = scratch + kStaticMaxCells;
+    cudaStream_t s = (cudaStream_t)stream;
+    double dt = cfl * dx / vel;
+    const int steps = (int)(final_t / dt) + 1;
+    dt = final_t / (double)steps;
+    const Dims dm{nx, ny, nz};
+    const dim3 bl = stencil_block(), gr(div_up(nz, bl.x), div_up(ny, bl.y), div_up(nx, bl.z));
+    const double dtv = dt * vel;
+    for (int st = 0; st < steps; ++st) {
+        (count_launch(), k_weno_stage<0, 0, double><<<gr, bl, 0, s>>>(dm, dx, dtv, 0., grid_dev, grid_dev, u1, u2, nullptr));
+        (count_launch(), k_weno_stage<0, 1, double><<<gr, bl, 0, s>>>(dm, dx, dtv, 0., u1, grid_dev, u1, u2, nullptr));
+        (count_launch(), k_weno_stage<0, 2, double><<<gr, bl, 0, s>>>(dm, dx, dtv, 0., u2, grid_dev, u1, u2, nullptr));
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_last_error(std::string("ibim_levelset_evolve_static: launch: ") + cudaGetErrorString(e));
+        return IBIM_ERR_CUDA;
+    }
+    return IBIM_OK;
+}

@@ -45,6 +45,7 @@ EXPORTS = [
     "ibim_plan_stats", "ibim_plan_lists", "ibim_fmm_apply", "ibim_bie_matvec", "ibim_bie_rhs", "ibim_gmres_solve",
     "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host", "ibim_ctx_stream",
     "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
+    "ibim_levelset_evolve_static",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors"]
@@ -143,6 +144,8 @@ def lib():
         "ibim_profile_read": ([_vp, _dp, _lp, C.c_int], C.c_int),
         "ibim_profile_work": ([_vp, _dp, _dp, C.c_int], C.c_int),
         "ibim_measure_peak": ([_vp, C.c_int, _dp], C.c_int),
+        "ibim_levelset_evolve_static": ([_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, _vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

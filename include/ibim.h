@@ -150,6 +150,18 @@ int ibim_levelset_count_gradient(ibim_grid g, double thickness, double thres, lo
 int ibim_levelset_build(ibim_ctx ctx, const double *centers, const double *radii, int natoms,
                         const ibim_config *cfg, ibim_grid *out, int steps[2]);
 
+/* Level-set evolution (as ibim_levelset_evolve) on a caller-owned FP64 device grid
+ * (row-major, k fastest), enqueued on `stream` (a cudaStream_t; NULL = default stream), that
+ * allocates no device memory.  No counterpart in the reference: it serves callers that cannot
+ * let a library allocate (a fixed HBM budget in the caller's own pool, or a loop that must not
+ * enter cudaMalloc/cudaFree).  Its two stage buffers live in one fixed array of
+ * 2 x 524,288 doubles (8 MiB) that every GPU loading the library keeps until exit; grids of
+ * more than 524,288 cells are rejected with IBIM_ERR_INVALID_ARGUMENT.  The first call on a
+ * device looks up the array's device address with that device current.  All calls share the
+ * array, so calls that overlap on the GPU race. */
+int ibim_levelset_evolve_static(double *grid_dev, int nx, int ny, int nz, double dx, double final_t, double vel,
+                                double cfl, void *stream);
+
 /* ---- tube quadrature: replaces Surface (levelset.h:62-72, levelset.cpp:437-586) ---- */
 int ibim_surface_extract(ibim_grid g, int thickness, ibim_tube *out, long *n_points, long *inclusion);
 /* A tube from host arrays (points (n,3), normals (n,3), raw cosine weights (n)) on spacing h. */
