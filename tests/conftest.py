@@ -58,3 +58,20 @@ def config_for(P, precision=0):
 
 def grid_stats(a):
     return np.array([a.sum(), np.abs(a).sum(), a.max(), a.min(), (a * a).sum()])
+
+
+def _build_if_stale():
+    """Rebuild libibim_gb300.so when a source is newer (no-op when fresh; skipped without nvcc)."""
+    import importlib.util
+    import shutil
+
+    if not (shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
+        return
+    spec = importlib.util.spec_from_file_location("ibim_gb300_build",
+                                                  os.path.join(ROOT, "ibim-levelset_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+
+
+_build_if_stale()

