@@ -321,14 +321,19 @@ def run_ours(args):
     roofline = None
     if dom:
         name, d = dom
-        fp_bound = {"m2l_v": "fp64", "m2l_x": "fp64", "near_l2p": "fp64", "weno_stage": "fp64", "p2m": "fp64"}
-        if precision == ibim.PRECISION_MIXED and name in ("near_l2p", "m2l_v", "m2l_x", "p2m"):
-            fp_bound = {name: "fp32"}
+        fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
+                    "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if precision == ibim.PRECISION_MIXED else "fp64",
+                    "weno_stage": "fp64" if precision == ibim.PRECISION_FP64 else "fp32", "p2m": "fp32"}
         bound = fp_bound.get(name, "hbm")
         per_launch_ms = d["ms"] / d["launches"]
         if bound == "hbm":
             ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
             peak, unit, src = peaks.get("hbm_gbs", 6800.0), "GB/s", "MEASURED_PEAKS.json hbm_gbs (of measured)"
+        elif bound.startswith("tf32"):
+            # 3 TF32 MMAs per algorithmic multiply-add; peak: half the measured dense BF16 rate
+            ach = 3 * d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
+            peak = 0.5 * peaks.get("bf16_tflops", 1909.5)
+            unit, src = "TFLOP/s", "TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 3 MMAs"
         else:
             ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
             peak = fp64_peak if bound == "fp64" else fp32_peak

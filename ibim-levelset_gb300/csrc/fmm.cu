@@ -398,7 +398,23 @@ void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, do
 
 // Work lists of one target set: which nodes need locals, V pairs by operator, X pairs, and
 // per target leaf the merged source ranges of its U and W lists.
-static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, int, int, int>, int> &opid) {
+// Dense index of the V-list operators: (level, source - target lattice offset in [-3, 3]^3).
+struct OpIndex {
+    std::vector<int> dense;  // level * 343 + offset -> operator id, -1 when absent
+    std::vector<int> keys;   // 4 ints per operator: level, ox, oy, oz
+    explicit OpIndex(int nlevels) : dense((size_t)std::max(1, nlevels) * 343, -1) {}
+    int get(int l, int ox, int oy, int oz) {
+        IBIM_REQUIRE(ox >= -3 && ox <= 3 && oy >= -3 && oy <= 3 && oz >= -3 && oz <= 3, "V-list offset out of range");
+        int &id = dense[(size_t)l * 343 + (ox + 3) * 49 + (oy + 3) * 7 + (oz + 3)];
+        if (id < 0) {
+            id = (int)keys.size() / 4;
+            keys.insert(keys.end(), {l, ox, oy, oz});
+        }
+        return id;
+    }
+};
+
+static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     const TreeHost &T = P.tree;
     cudaStream_t s = P.ctx->stream;
     const int nn = T.nnodes;
@@ -420,16 +436,8 @@ static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, i
             if (!has_t(i)) continue;
             for (int sidx : T.V[i]) {
                 if (!has_s(sidx)) continue;
-                auto key = std::make_tuple(l, T.coord[3 * sidx] - T.coord[3 * i], T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
-                                           T.coord[3 * sidx + 2] - T.coord[3 * i + 2]);
-                auto it = opid.find(key);
-                int id;
-                if (it == opid.end()) {
-                    id = (int)opid.size();
-                    opid[key] = id;
-                } else {
-                    id = it->second;
-                }
+                const int id = opid.get(l, T.coord[3 * sidx] - T.coord[3 * i], T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
+                                        T.coord[3 * sidx + 2] - T.coord[3 * i + 2]);
                 if ((int)byop.size() <= id) byop.resize(id + 1);
                 byop[id].push_back({sidx, i});
             }
@@ -439,7 +447,7 @@ static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, i
                 xt.push_back(i);
             }
         }
-    std::vector<int> vs, vt, chunks, chunks32;
+    std::vector<int> vs, vt, chunks, chunks32, chunks_tc;
     for (int op = 0; op < (int)byop.size(); ++op) {
         const int b = (int)vs.size();
         for (auto &pr : byop[op]) {
@@ -456,11 +464,18 @@ static void build_target_lists(Plan &P, TargetSet &S, std::map<std::tuple<int, i
             chunks32.push_back(b + q);
             chunks32.push_back(std::min<int>(M2L_CH32, (int)byop[op].size() - q));
         }
+        for (int q = 0; q < (int)byop[op].size(); q += M2L_CHTC) {
+            chunks_tc.push_back(op);
+            chunks_tc.push_back(b + q);
+            chunks_tc.push_back(std::min<int>(M2L_CHTC, (int)byop[op].size() - q));
+        }
     }
     S.nvpairs = (long)vs.size();
     S.nchunks = (int)chunks.size() / 3;
     S.nchunks32 = (int)chunks32.size() / 3;
     up_int(S.v_chunk32, chunks32, s);
+    S.nchunks_tc = (int)chunks_tc.size() / 3;
+    up_int(S.v_chunk_tc, chunks_tc, s);
     up_int(S.v_src, vs, s);
     up_int(S.v_tgt, vt, s);
     up_int(S.v_chunk, chunks, s);
@@ -631,7 +646,7 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
         up_int(P->m2m_nodes, m2m, s);
         P->m2m_level_begin = m2m_lb;
         P->np2m = (int)p2m.size();
-        std::map<std::tuple<int, int, int, int>, int> opid;
+        OpIndex opid(T.nlevels);
         if (with_self) {
             TargetSet *S = new TargetSet();
             P->targets.push_back(S);
@@ -662,14 +677,9 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
             up_int(S->perm_d, S->perm, s);
             build_target_lists(*P, *S, opid);
         }
-        P->nops = (int)opid.size();
-        P->op_key_h.assign(4 * std::max(1, P->nops), 0);
-        for (auto &kv : opid) {
-            P->op_key_h[4 * kv.second] = std::get<0>(kv.first);
-            P->op_key_h[4 * kv.second + 1] = std::get<1>(kv.first);
-            P->op_key_h[4 * kv.second + 2] = std::get<2>(kv.first);
-            P->op_key_h[4 * kv.second + 3] = std::get<3>(kv.first);
-        }
+        P->nops = (int)opid.keys.size() / 4;
+        P->op_key_h = opid.keys;
+        if (P->op_key_h.empty()) P->op_key_h.assign(4, 0);
         up_int(P->op_key, P->op_key_h, s);
         ChebTables ht;
         cheb_tables_host(order, ht);
@@ -740,10 +750,10 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
     }
     P.local.zero();
     if (S.nchunks > 0)
-        { ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
+        { ProfScope ps_(PROF_M2L_V64, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
                                                                        P.ops64.ptr, P.mult.ptr, P.local.ptr)); }
     if (S.nxpairs > 0)
-        { ProfScope ps_(PROF_M2L_X, 102.0 * R * (double)R * S.nxpairs, 16.0 * n4 * S.nxpairs); (count_launch(), k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
+        { ProfScope ps_(PROF_M2L_X64, 102.0 * R * (double)R * S.nxpairs, 16.0 * n4 * S.nxpairs); (count_launch(), k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
                                                  P.nradius.ptr, P.mult.ptr, P.local.ptr)); }
     for (int l = 3; l < T.nlevels; ++l) {
         const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
@@ -755,7 +765,7 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
     const double *ty = S.self ? P.sy.ptr : S.ty.ptr;
     const double *tz = S.self ? P.sz.ptr : S.tz.ptr;
     if (S.ntleaves > 0)
-        { ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
+        { ProfScope ps_(PROF_NEAR64, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
                                                S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
                                                P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out)); }
     IBIM_CHECK_LAUNCH();

@@ -11,6 +11,7 @@ namespace ibim {
 constexpr int MAXP = 8;
 constexpr int MAXR = MAXP * MAXP * MAXP;
 constexpr int M2L_CH32 = 32;  // V pairs per chunk of the FP32 contraction
+constexpr int M2L_CHTC = 128; // V pairs per chunk of the tensor-core contraction (MMA N)
 
 // Chebyshev nodes, polynomials and parent -> child transfers for order p (bbfmm.h:273-326).
 struct ChebTables {

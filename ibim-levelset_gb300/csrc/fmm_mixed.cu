@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "fmm_common.cuh"
 
@@ -226,8 +227,8 @@ __global__ void __launch_bounds__(256) k_m2l_v32(int n4, const int *__restrict__
     __shared__ __align__(16) float As[GM_BK][GM_BM];
     __shared__ __align__(16) float Bs[GM_BK][GM_BN];
     __shared__ int src_s[GM_BN], tgt_s[GM_BN];
-    const int op = chunks[3 * blockIdx.y], b = chunks[3 * blockIdx.y + 1], cnt = chunks[3 * blockIdx.y + 2];
-    const int row0 = blockIdx.x * GM_BM;
+    const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
+    const int row0 = blockIdx.y * GM_BM;
     const int tid = threadIdx.x;
     if (tid < GM_BN) {
         src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
@@ -651,9 +652,13 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
         }
     }
     P.local32.zero();
-    if (S.nchunks32 > 0) {
+    static const bool simt_m2l = std::getenv("IBIM_M2L_SIMT") != nullptr;
+    if (!simt_m2l && m2l_tc_supported()) {
+        m2l_tc_prepare(P);
+        m2l_tc_run(P, S);
+    } else if (S.nchunks32 > 0) {
         ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 4.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));
-        const dim3 grid(div_up(n4, GM_BM), S.nchunks32);
+        const dim3 grid(S.nchunks32, div_up(n4, GM_BM));
         (count_launch(), k_m2l_v32<<<grid, 256, 0, s>>>(n4, S.v_chunk32.ptr, S.v_src.ptr, S.v_tgt.ptr, P.ops32.ptr,
                                                         P.mult32.ptr, P.local32.ptr));
     }

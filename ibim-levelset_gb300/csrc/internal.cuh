@@ -77,7 +77,7 @@ struct DevBuf {
 // Kernel categories timed with CUDA events when profiling is enabled on a context.
 enum ProfCat {
     PROF_EXPAND = 0, PROF_WENO, PROF_COUNT, PROF_FLOOD, PROF_TUBE, PROF_OPS, PROF_P2M, PROF_M2M, PROF_M2L_V,
-    PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_NCAT
+    PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_M2L_V64, PROF_M2L_X64, PROF_NEAR64, PROF_NCAT
 };
 
 // Number of kernels this library launched (all contexts).
@@ -171,6 +171,8 @@ struct TargetSet {
     int nchunks = 0;
     DevBuf<int> v_chunk32;             // chunks of the FP32 contraction (larger)
     int nchunks32 = 0;
+    DevBuf<int> v_chunk_tc;            // chunks of the tensor-core contraction (<= 128 pairs)
+    int nchunks_tc = 0;
     long nvpairs = 0;
     DevBuf<int> x_src, x_tgt;
     long nxpairs = 0;
@@ -220,6 +222,11 @@ struct Plan {
     DevBuf<float> nrad32;          // per node radius (mixed)
     DevBuf<unsigned char> tables32;  // ChebTables32
     bool mixed_ready = false;
+    // tensor-core V-list M2L (m2l_tc.cu): 3xTF32 operands, padded
+    bool tc_ready = false;
+    int tc_kpad = 0, tc_mpad = 0;
+    DevBuf<float> tc_a_hi, tc_a_lo, tc_b_hi, tc_b_lo;
+    DevBuf<int> tc_err;
     double kp64[4] = {-1, -1, -1, -1}, kp32[4] = {-1, -1, -1, -1};
     bool ops64_ready = false, ops32_ready = false;
     ~Plan() { for (auto *t : targets) delete t; }
@@ -230,6 +237,12 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
 void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
 void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
 void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out, int precision);
+
+// Tensor-core V-list M2L (m2l_tc.cu)
+bool m2l_tc_supported();
+void m2l_tc_prepare(Plan &P);
+void m2l_tc_run(Plan &P, TargetSet &S);
+int m2l_tc_error(Plan &P);
 
 // Plan creation (fmm.cu): target set 0 = the tube points when with_self, then `extra` (host
 // (n, 3)) when n_extra > 0.

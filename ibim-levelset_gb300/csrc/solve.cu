@@ -436,6 +436,7 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
         if (atom_pot) *atom_pot = pot;
     }
     res.t_energy_ms = te.ms();
+    if (m2l_tc_error(P)) throw Error(IBIM_ERR_LIMIT, "tensor-core M2L: an MMA completion wait exceeded its bound");
     if (x_tree_out) IBIM_CUDA(cudaMemcpyAsync(x_tree_out, x.ptr, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
     IBIM_CUDA(cudaStreamSynchronize(s));
 }

@@ -98,10 +98,6 @@ struct Builder {
     }
 };
 
-inline uint64_t key_of(int level, int x, int y, int z) {
-    return ((uint64_t)level << 60) | ((uint64_t)x << 40) | ((uint64_t)y << 20) | (uint64_t)z;
-}
-
 }  // namespace
 
 TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int maxpoint, int maxlevel) {
@@ -146,12 +142,6 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     const int nn = (int)B.nodes.size();
     int depth = 0;
     for (auto &n : B.nodes) depth = std::max(depth, n.level);
-    std::unordered_map<uint64_t, int> lookup;
-    lookup.reserve(nn * 2);
-    for (int i = 0; i < nn; ++i) {
-        const BNode &n = B.nodes[i];
-        lookup[key_of(n.level, n.coord[0], n.coord[1], n.coord[2])] = i;
-    }
     // findNode: the node at the candidate's level if it exists, else the leaf that contains it
     auto find_node = [&](int level, const int c[3]) {
         int id = 0;
@@ -175,9 +165,12 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         return (touch[0] && ot[1] && ot[2]) || (touch[1] && ot[0] && ot[2]) || (touch[2] && ot[0] && ot[1]);
     };
     std::vector<std::vector<int>> U(nn), V(nn), W(nn), X(nn);
-    std::vector<int> queue;
+    // nodes are independent: build their lists in parallel
+#pragma omp parallel for schedule(dynamic, 64)
     for (int id = 0; id < nn; ++id) {
+        std::vector<int> queue;
         const BNode &n = B.nodes[id];
+        V[id].reserve(64);
         if (n.parent != -1) {
             const BNode &pn = B.nodes[n.parent];
             const int side = 1 << n.level;
@@ -246,9 +239,10 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     T.V.resize(nn);
     T.W.resize(nn);
     T.X.resize(nn);
+    for (int i = 0; i < nn; ++i) T.level_begin[B.nodes[order[i]].level + 1]++;
+#pragma omp parallel for schedule(dynamic, 64)
     for (int i = 0; i < nn; ++i) {
         const BNode &n = B.nodes[order[i]];
-        T.level_begin[n.level + 1]++;
         for (int a = 0; a < 3; ++a) {
             T.center[3 * i + a] = n.c[a];
             T.radius[3 * i + a] = n.r[a];

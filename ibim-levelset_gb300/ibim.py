@@ -48,7 +48,8 @@ EXPORTS = [
     "ibim_levelset_evolve_static",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
-                      "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors"]
+                      "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
+                      "near_l2p_fp64"]
 
 
 class IbimError(RuntimeError):

@@ -120,7 +120,8 @@ long ibim_launch_count(void);
 /* Per-category kernel timing with CUDA events on the context stream.  mask bit k enables
  * category k: 0 expand, 1 WENO stage, 2 gradient count, 3 flood fill, 4 tube extraction,
  * 5 M2L operators, 6 P2M, 7 M2M, 8 M2L (V list), 9 M2L (X list), 10 L2L, 11 near field + L2P,
- * 12 right-hand side, 13 GMRES vector kernels.  ibim_profile_read returns (and clears) the
+ * 12 right-hand side, 13 GMRES vector kernels; FP64 versions of 8, 9 and 11 are categories 14, 15
+ * and 16 (categories 6-11 then count the mixed-precision kernels).  ibim_profile_read returns (and clears) the
  * summed milliseconds and launch counts of the first ncat categories. */
 int ibim_profile_enable(ibim_ctx ctx, unsigned mask);
 int ibim_profile_read(ibim_ctx ctx, double *ms, long *launches, int ncat);
