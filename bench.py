@@ -2,13 +2,19 @@
 """Benchmark of the IBIM Poisson-Boltzmann path on GB300: FMM-GMRES solves/sec, p50/p99 latency.
 
 One step = one whole solve of the workload (level set -> tube quadrature -> octree plan ->
-GMRES on the fused BIE FMM -> polarization energy) through the C ABI.
+GMRES on the fused BIE FMM -> polarization energy) through the C ABI.  The default precision is
+the mixed path (FP32 level set, TF32x3 tensor-core M2L, FP32 near field, FP64 iterative
+refinement); --precision fp64 times the reference-exact FP64 path.
 
   value   solves/sec with the atoms already in HBM (ibim_solve_dev), device time from CUDA events
           on the library's stream, L2 flushed (256 MB write) between steps
   e2e     the same through ibim_solve with host buffers (host->device copies inside the region)
   roofline  the dominant kernel category of the timed region: algorithmic flops (or bytes) of its
           launches / their CUDA-event time, against the measured peak of its bound
+          (rooflines: the same for every category with counted work)
+  accuracy  mixed path only: one untimed FP64 solve of the same workload after the timed region;
+          the energy's relative error against it (the metric's 1e-4 bound) and the FP64 path's
+          own solves/s
   cpu_baseline  the oracle (plain-C restatement of the reference, reference-structured: 16 scalar
           FMMs per matvec with on-the-fly M2L, as electric.cpp/bbfmm.h do) timed on a bounded
           sample of the same workload on the host cores, extrapolated to one solve
@@ -52,15 +58,23 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--workload", choices=["protein2000", "born"], default="protein2000")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="skip the untimed FP64 solve that states the mixed path's energy error")
+    ap.add_argument("--order", type=int, default=None,
+                    help="override the workload's Chebyshev order (smaller operator storage for profiler captures)")
     return ap.parse_args()
 
 
-def get_workload(name):
-    return workloads.protein2000() if name == "protein2000" else workloads.born()
+def get_workload(name, order=None):
+    W = workloads.protein2000() if name == "protein2000" else workloads.born()
+    if order is not None:
+        W.np_ = order
+        W.name = f"{W.name}_p{order}"
+    return W
 
 
 # ---------------------------------------------------------------------------------------------
@@ -142,7 +156,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    W = get_workload(args.workload)
+    W = get_workload(args.workload, args.order)
     import oracle as O
 
     O.build()
@@ -252,7 +266,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    W = get_workload(args.workload)
+    W = get_workload(args.workload, args.order)
     precision = ibim.PRECISION_FP64 if args.precision == "fp64" else ibim.PRECISION_MIXED
     cfg = W.config(precision)
     ctx = ibim.Context(local)
@@ -313,36 +327,81 @@ def run_ours(args):
                "h2d_bytes_per_step": int(W.mol.n * 5 * 8), "d2h_bytes_per_step": int(ctypes.sizeof(ibim.Result)),
                "ms_per_step": statistics.mean(e2e_ms)}
 
-    # roofline of the dominant kernel category
+    # roofline of every kernel category with counted work; the headline one is the dominant
     peaks = measured_peaks()
     fp64_peak = ctx.measure_peak("fp64")
     fp32_peak = ctx.measure_peak("fp32")
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else None
-    roofline = None
-    if dom:
-        name, d = dom
-        fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
-                    "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if precision == ibim.PRECISION_MIXED else "fp64",
-                    "weno_stage": "fp64" if precision == ibim.PRECISION_FP64 else "fp32", "p2m": "fp32"}
+    mixed = precision == ibim.PRECISION_MIXED
+    fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
+                "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if mixed else "fp64", "rhs": "fp64",
+                "weno_stage": "fp32" if mixed else "fp64", "p2m": "fp32" if mixed else "fp64",
+                "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": "bf16x28 tensor"}
+
+    def roofline_of(name, d):
         bound = fp_bound.get(name, "hbm")
         per_launch_ms = d["ms"] / d["launches"]
         if bound == "hbm":
+            if d["bytes"] <= 0:
+                return None
             ach = d["bytes"] / d["launches"] / (per_launch_ms * 1e-3) / 1e9
             peak, unit, src = peaks.get("hbm_gbs", 6800.0), "GB/s", "MEASURED_PEAKS.json hbm_gbs (of measured)"
-        elif bound.startswith("tf32"):
-            # 3 TF32 MMAs per algorithmic multiply-add; peak: half the measured dense BF16 rate
-            ach = 3 * d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
-            peak = 0.5 * peaks.get("bf16_tflops", 1909.5)
-            unit, src = "TFLOP/s", "TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 3 MMAs"
+            alg = d["bytes"] / d["launches"]
         else:
-            ach = d["flops"] / d["launches"] / (per_launch_ms * 1e-3) / 1e12
-            peak = fp64_peak if bound == "fp64" else fp32_peak
-            unit, src = "TFLOP/s", f"{bound.upper()} FMA-chain microkernel measured in this run (of measured)"
-        roofline = {"bound": bound, "kernel": name, "achieved": ach, "peak": peak, "unit": unit,
-                    "frac": ach / peak if peak else None, "peak_source": src,
-                    "traffic": committed_traffic(name, W.name), "launches": d["launches"],
-                    "avg_launch_ms": per_launch_ms,
-                    "algorithmic_per_launch": d["flops"] / d["launches"] if bound != "hbm" else d["bytes"] / d["launches"]}
+            if d["flops"] <= 0:
+                return None
+            alg = d["flops"] / d["launches"]
+            if bound.startswith("tf32"):
+                # 3 TF32 MMAs per algorithmic multiply-add; peak: half the measured dense BF16 rate
+                ach = 3 * alg / (per_launch_ms * 1e-3) / 1e12
+                peak = 0.5 * peaks.get("bf16_tflops", 1909.5)
+                unit = "TFLOP/s"
+                src = "TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 3 MMAs"
+            elif bound.startswith("bf16"):
+                # 28 BF16 digit-pair MMAs per algorithmic multiply-add (7 digits, pairs i + l <= 6)
+                ach = 28 * alg / (per_launch_ms * 1e-3) / 1e12
+                peak = peaks.get("bf16_tflops", 1909.5)
+                unit = "TFLOP/s"
+                src = "MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 28 digit MMAs"
+            else:
+                ach = alg / (per_launch_ms * 1e-3) / 1e12
+                peak = fp64_peak if bound == "fp64" else fp32_peak
+                unit, src = "TFLOP/s", f"{bound.upper()} FMA-chain microkernel measured in this run (of measured)"
+        return {"bound": bound, "kernel": name, "achieved": ach, "peak": peak, "unit": unit,
+                "frac": ach / peak if peak else None, "peak_source": src,
+                "traffic": committed_traffic(name, W.name), "launches": d["launches"],
+                "avg_launch_ms": per_launch_ms, "algorithmic_per_launch": alg}
+
+    rooflines = {}
+    for name, d in (prof or {}).items():
+        if d["launches"] > 0 and d["ms"] > 0:
+            r = roofline_of(name, d)
+            if r is not None:
+                rooflines[name] = r
+    roofline = max(rooflines.values(), key=lambda r: r["launches"] * r["avg_launch_ms"]) if rooflines else None
+    # per-solve ideal time: sum over the categories of (algorithmic work / peak of their bound)
+    ideal_ms = sum(r["launches"] * r["avg_launch_ms"] * r["frac"] for r in rooflines.values() if r["frac"])
+    solve_roofline = {"ideal_ms_per_step": ideal_ms / args.steps, "ms_per_step": total_ms / args.steps,
+                      "frac": ideal_ms / total_ms if total_ms else None,
+                      "categories": sorted(rooflines),
+                      "note": "ideal = sum over counted kernel categories of work / measured peak of the bound"}
+
+    # the mixed path's energy error against the FP64 path, from one untimed FP64 solve
+    accuracy = None
+    if mixed and not args.no_fp64_check:
+        cfg64 = W.config(ibim.PRECISION_FP64)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(ext)
+        r64 = ctx.solve_dev(centers.data_ptr(), charges.data_ptr(), radii.data_ptr(), W.mol.n, cfg64)
+        b.record(ext)
+        b.synchronize()
+        ms64 = a.elapsed_time(b)
+        rel = abs(r0["energy"] - r64["energy"]) / abs(r64["energy"])
+        accuracy = {"energy": r0["energy"], "energy_fp64": r64["energy"], "rel_err_vs_fp64": rel, "tolerance": 1e-4,
+                    "within_tolerance": rel <= 1e-4, "fp64_ms_per_solve": ms64,
+                    "fp64_solves_per_s": 1e3 / ms64, "speedup_vs_fp64": value / world * ms64 / 1e3,
+                    "fp64_gmres_iters": r64["gmres_iters"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -366,6 +425,9 @@ def run_ours(args):
                           l2="flushed (256 MB write) between steps", tube_points=r0["n_points"]),
            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
            "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
+           "accuracy": accuracy, "solve_roofline": solve_roofline,
+           "rooflines": {k: {f: v[f] for f in ("bound", "achieved", "peak", "unit", "frac", "avg_launch_ms")}
+                         for k, v in rooflines.items()},
            "solve": {k: r0[k] for k in ("energy", "area", "n_points", "gmres_iters", "matvecs", "matvecs_fp64",
                                         "refinements", "residual", "gmres_status", "reinit_steps", "t_levelset_ms",
                                         "t_surface_ms", "t_plan_ms", "t_solve_ms", "t_energy_ms", "fmm_nodes",

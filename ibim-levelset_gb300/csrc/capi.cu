@@ -116,8 +116,8 @@ static void check_config(const ibim_config &cfg) {
 static void fill_plan_stats(const Plan &P, ibim_result &res) {
     const TargetSet &S = *P.targets[0];
     res.fmm_nodes = P.tree.nnodes;
-    res.fmm_v_pairs = S.nvpairs;
-    res.fmm_x_pairs = S.nxpairs;
+    res.fmm_v_pairs = S.nv_list;
+    res.fmm_x_pairs = S.nx_list;
     res.fmm_near_pairs = S.near_pairs;
     res.fmm_operators = P.nops;
 }
@@ -171,13 +171,27 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     res.t_surface_ms = t1.ms();
     IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
     Plan *P = nullptr;
+    DevBuf<double> a4, b_tube;
     try {
+        const double *atoms4 = atoms4_dev;
+        if (!atoms4) {
+            atoms_to_device(c, centers_host, charges_host, natoms, a4);
+            atoms4 = a4.ptr;
+        }
+        // the right-hand side needs only the tube and the atoms: it runs on the second stream
+        // while the host builds the octree and its lists
+        b_tube.alloc(2 * (size_t)tube->n, s);
+        IBIM_CUDA(cudaEventRecord(c->ev_fork, s));
+        IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
+        bie_rhs_tube(*tube, cfg.kp, atoms4, natoms, b_tube.ptr, c->aux);
+        IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
         auto w0 = std::chrono::steady_clock::now();
         P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
         fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
         if (cfg.precision != IBIM_PRECISION_FP64) fmm_prepare_operators(*P, cfg.kp, cfg.precision);
         IBIM_CUDA(cudaStreamSynchronize(s));
         res.t_plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+        IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
         // area = sum of quadrature weights (electric.cpp:60)
         std::vector<double> w(tube->n);
         P->sw.download(w.data(), tube->n);
@@ -185,16 +199,11 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         double area = 0.;
         for (long i = 0; i < tube->n; ++i) area += w[i];
         res.area = area;
-        DevBuf<double> a4;
-        const double *atoms4 = atoms4_dev;
-        if (!atoms4) {
-            atoms_to_device(c, centers_host, charges_host, natoms, a4);
-            atoms4 = a4.ptr;
-        }
         electric_solve(*P, cfg.kp, atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol, cfg.precision,
-                       nullptr, nullptr, res);
+                       nullptr, nullptr, res, b_tube.ptr);
         fill_plan_stats(*P, res);
     } catch (...) {
+        cudaStreamSynchronize(c->aux);  // the right-hand side may still read the tube and atoms
         delete P;
         delete tube;
         throw;
@@ -287,6 +296,9 @@ int ibim_ctx_create(int device, ibim_ctx *out) {
             IBIM_CUDA(cudaSetDevice(device));
             IBIM_CUDA(cudaDeviceGetAttribute(&h->c.num_sms, cudaDevAttrMultiProcessorCount, device));
             IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
+            IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.aux, cudaStreamNonBlocking));
+            IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_fork, cudaEventDisableTiming));
+            IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_join, cudaEventDisableTiming));
         } catch (...) {
             delete h;
             throw;
@@ -300,6 +312,12 @@ int ibim_ctx_destroy(ibim_ctx ctx) {
         if (!ctx) return;
         cudaSetDevice(ctx->c.device);
         cudaStreamSynchronize(ctx->c.stream);
+        if (ctx->c.aux) {
+            cudaStreamSynchronize(ctx->c.aux);
+            cudaStreamDestroy(ctx->c.aux);
+        }
+        if (ctx->c.ev_fork) cudaEventDestroy(ctx->c.ev_fork);
+        if (ctx->c.ev_join) cudaEventDestroy(ctx->c.ev_join);
         cudaStreamDestroy(ctx->c.stream);
         delete ctx;
     });
@@ -625,8 +643,8 @@ int ibim_plan_stats(ibim_plan p, long stats[8]) {
         stats[0] = P.tree.nnodes;
         stats[1] = P.tree.nlevels;
         stats[2] = leaves;
-        stats[3] = S.nvpairs;
-        stats[4] = S.nxpairs;
+        stats[3] = S.nv_list;
+        stats[4] = S.nx_list;
         stats[5] = S.near_pairs;
         stats[6] = P.nops;
         stats[7] = S.ntleaves;

@@ -19,7 +19,9 @@
 // batched dense contraction (pairs grouped by operator).
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <tuple>
 
@@ -188,30 +190,38 @@ __global__ void __launch_bounds__(128) k_l2l64(const ChebTables *__restrict__ ta
     for (int o = threadIdx.x; o < n4; o += blockDim.x) local[(long)node * n4 + o] += tmp[o];
 }
 
-// Build the V-list M2L operators: op (level, ox, oy, oz) -> K[col * 4R + row],
-// row = out * R + ct, col = in * R + cs, entry = block(src_cheb(cs) - tgt_cheb(ct))[out][in].
+// Build the M2L operators: op (target level, source level, centre offset D in target half-widths)
+// -> K[col * 4R + row], row = out * R + ct, col = in * R + cs,
+// entry = block(src_cheb(cs) - tgt_cheb(ct))[out][in], node positions D r_t + r_s cheb - r_t cheb.
+// V operators (same level, D = 2 o) and X operators (coarser source leaf) share the layout.
+__device__ __forceinline__ void op_geometry(const int *keys, int op, const double *root_r, double rt[3], double rs[3],
+                                            int D[3]) {
+    const int lt = keys[5 * op], ls = keys[5 * op + 1];
+    for (int a = 0; a < 3; ++a) {
+        double vt = root_r[a], vs = root_r[a];
+        for (int l = 0; l < lt; ++l) vt *= 0.5;
+        for (int l = 0; l < ls; ++l) vs *= 0.5;
+        rt[a] = vt;
+        rs[a] = vs;
+        D[a] = keys[5 * op + 2 + a];
+    }
+}
+
 __global__ void k_make_ops64(const ChebTables *__restrict__ tab, const int *__restrict__ keys,
                              const double *__restrict__ root_r, KParams kp, double *ops) {
     const ChebTables &T = *tab;
     const int op = blockIdx.y;
     const int p = T.p, R = T.R, n4 = 4 * R;
-    const int lv = keys[4 * op];
-    double r[3];
-    for (int a = 0; a < 3; ++a) {
-        double v = root_r[a];
-        for (int l = 0; l < lv; ++l) v *= 0.5;
-        r[a] = v;
-    }
+    double rt[3], rs[3];
+    int D[3];
+    op_geometry(keys, op, root_r, rt, rs, D);
     const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (pair >= (long)R * R) return;
     const int ct = (int)(pair / R), cs = (int)(pair % R);
     const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
     const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
     double d[3];
-    for (int a = 0; a < 3; ++a) {
-        const double off = keys[4 * op + 1 + a] * (2.0 * r[a]);
-        d[a] = (off + r[a] * T.cheb[si[a]]) - r[a] * T.cheb[ti[a]];
-    }
+    for (int a = 0; a < 3; ++a) d[a] = (D[a] * rt[a] + rs[a] * T.cheb[si[a]]) - rt[a] * T.cheb[ti[a]];
     double b[16];
     kblock64(kp, d[0], d[1], d[2], b);
     double *K = ops + (long)op * n4 * n4;
@@ -399,17 +409,31 @@ void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, do
 // Work lists of one target set: which nodes need locals, V pairs by operator, X pairs, and
 // per target leaf the merged source ranges of its U and W lists.
 // Dense index of the V-list operators: (level, source - target lattice offset in [-3, 3]^3).
+// M2L operator keys, 5 ints: target level, source level, and the source-minus-target centre offset
+// in units of the target node's half-width (per axis).  V pairs (same level, lattice offset o in
+// [-3, 3]^3) have offset 2 o and a dense index; X pairs (a coarser source leaf) are hashed.
 struct OpIndex {
     std::vector<int> dense;  // level * 343 + offset -> operator id, -1 when absent
-    std::vector<int> keys;   // 4 ints per operator: level, ox, oy, oz
+    std::vector<int> keys;   // 5 ints per operator
+    std::map<std::array<int, 5>, int> xmap;
     explicit OpIndex(int nlevels) : dense((size_t)std::max(1, nlevels) * 343, -1) {}
+    int add(const std::array<int, 5> &k) {
+        const int id = (int)keys.size() / 5;
+        keys.insert(keys.end(), k.begin(), k.end());
+        return id;
+    }
     int get(int l, int ox, int oy, int oz) {
         IBIM_REQUIRE(ox >= -3 && ox <= 3 && oy >= -3 && oy <= 3 && oz >= -3 && oz <= 3, "V-list offset out of range");
         int &id = dense[(size_t)l * 343 + (ox + 3) * 49 + (oy + 3) * 7 + (oz + 3)];
-        if (id < 0) {
-            id = (int)keys.size() / 4;
-            keys.insert(keys.end(), {l, ox, oy, oz});
-        }
+        if (id < 0) id = add({l, l, 2 * ox, 2 * oy, 2 * oz});
+        return id;
+    }
+    int get_x(int lt, int ls, int dx, int dy, int dz) {
+        const std::array<int, 5> k{lt, ls, dx, dy, dz};
+        auto it = xmap.find(k);
+        if (it != xmap.end()) return it->second;
+        const int id = add(k);
+        xmap.emplace(k, id);
         return id;
     }
 };
@@ -436,6 +460,7 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             if (!has_t(i)) continue;
             for (int sidx : T.V[i]) {
                 if (!has_s(sidx)) continue;
+                ++S.nv_list;
                 const int id = opid.get(l, T.coord[3 * sidx] - T.coord[3 * i], T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
                                         T.coord[3 * sidx + 2] - T.coord[3 * i + 2]);
                 if ((int)byop.size() <= id) byop.resize(id + 1);
@@ -443,11 +468,25 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             }
             for (int sidx : T.X[i]) {
                 if (!has_s(sidx)) continue;
-                xs.push_back(sidx);
-                xt.push_back(i);
+                ++S.nx_list;
+                if (P.x_as_ops) {
+                    // centre offset in target half-widths: (2 c_s + 1) 2^(lt - ls) - (2 c_t + 1)
+                    const int ls = (int)(std::upper_bound(T.level_begin.begin(), T.level_begin.end(), sidx) -
+                                         T.level_begin.begin()) - 1;
+                    const int sh = l - ls;
+                    int d[3];
+                    for (int a = 0; a < 3; ++a)
+                        d[a] = (2 * T.coord[3 * sidx + a] + 1) * (1 << sh) - (2 * T.coord[3 * i + a] + 1);
+                    const int id = opid.get_x(l, ls, d[0], d[1], d[2]);
+                    if ((int)byop.size() <= id) byop.resize(id + 1);
+                    byop[id].push_back({sidx, i});
+                } else {
+                    xs.push_back(sidx);
+                    xt.push_back(i);
+                }
             }
         }
-    std::vector<int> vs, vt, chunks, chunks32, chunks_tc;
+    std::vector<int> vs, vt, chunks, chunks32, chunks_tc, chunks_oz;
     for (int op = 0; op < (int)byop.size(); ++op) {
         const int b = (int)vs.size();
         for (auto &pr : byop[op]) {
@@ -469,6 +508,11 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             chunks_tc.push_back(b + q);
             chunks_tc.push_back(std::min<int>(M2L_CHTC, (int)byop[op].size() - q));
         }
+        for (int q = 0; q < (int)byop[op].size(); q += M2L_CHOZ) {
+            chunks_oz.push_back(op);
+            chunks_oz.push_back(b + q);
+            chunks_oz.push_back(std::min<int>(M2L_CHOZ, (int)byop[op].size() - q));
+        }
     }
     S.nvpairs = (long)vs.size();
     S.nchunks = (int)chunks.size() / 3;
@@ -476,6 +520,8 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     up_int(S.v_chunk32, chunks32, s);
     S.nchunks_tc = (int)chunks_tc.size() / 3;
     up_int(S.v_chunk_tc, chunks_tc, s);
+    S.nchunks_oz = (int)chunks_oz.size() / 3;
+    up_int(S.v_chunk_oz, chunks_oz, s);
     up_int(S.v_src, vs, s);
     up_int(S.v_tgt, vt, s);
     up_int(S.v_chunk, chunks, s);
@@ -576,6 +622,9 @@ static void bin_targets(Plan &P, TargetSet &S, const double *pts, long nt, const
 Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int order, int maxpoint, int maxlevel,
                 int precision) {
     IBIM_REQUIRE(order >= 2 && order <= MAXP, "fmm_np must be in [2, 8]");
+    IBIM_REQUIRE(precision == IBIM_PRECISION_FP64 || precision == IBIM_PRECISION_MIXED ||
+                     precision == IBIM_PRECISION_FP64_TC,
+                 "unknown precision");
     IBIM_REQUIRE(t && t->n > 0, "plan needs a non-empty tube");
     IBIM_REQUIRE(with_self || (extra && n_extra > 0), "plan needs targets");
     Ctx *c = t->ctx;
@@ -597,6 +646,9 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
     Plan *P = new Plan();
     P->ctx = c;
     P->tube = t;
+    // X pairs join the operator contraction; IBIM_X_ONTHEFLY keeps the on-the-fly X kernels
+    // (kernel evaluated per pair, no operator storage)
+    P->x_as_ops = std::getenv("IBIM_X_ONTHEFLY") == nullptr;
     P->ns = ns;
     P->p = order;
     P->R = order * order * order;
@@ -677,9 +729,9 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
             up_int(S->perm_d, S->perm, s);
             build_target_lists(*P, *S, opid);
         }
-        P->nops = (int)opid.keys.size() / 4;
+        P->nops = (int)opid.keys.size() / 5;
         P->op_key_h = opid.keys;
-        if (P->op_key_h.empty()) P->op_key_h.assign(4, 0);
+        if (P->op_key_h.empty()) P->op_key_h.assign(5, 0);
         up_int(P->op_key, P->op_key_h, s);
         ChebTables ht;
         cheb_tables_host(order, ht);
@@ -726,10 +778,11 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
     }
     for (int i = 0; i < 4; ++i) cache[i] = key[i];
     (is64 ? P.ops64_ready : P.ops32_ready) = true;
+    if (is64) P.ops64_gen++;
 }
 
 // One FP64 FMM: dens (4 x ns, tree order) -> out (4 x nt of target set ts, tree order).
-void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out) {
+void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out, bool m2l_sliced) {
     IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
     fmm_prepare_operators(P, kpp, IBIM_PRECISION_FP64);
     const TargetSet &S = *P.targets[ts];
@@ -749,7 +802,10 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
                                                P.mult.ptr)); }
     }
     P.local.zero();
-    if (S.nchunks > 0)
+    if (m2l_sliced && S.nchunks_oz > 0 && (n4 + 15) / 16 * 16 <= M2L_OZ_MAXK) {
+        m2l_oz_prepare(P);
+        m2l_oz_run(P, S);
+    } else if (S.nchunks > 0)
         { ProfScope ps_(PROF_M2L_V64, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
                                                                        P.ops64.ptr, P.mult.ptr, P.local.ptr)); }
     if (S.nxpairs > 0)
@@ -773,7 +829,9 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
 
 void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out, int precision) {
     if (precision == IBIM_PRECISION_FP64)
-        fmm_run_fp64(P, ts, kp, dens, out);
+        fmm_run_fp64(P, ts, kp, dens, out, false);
+    else if (precision == IBIM_PRECISION_FP64_TC)
+        fmm_run_fp64(P, ts, kp, dens, out, m2l_tc_supported());
     else
         fmm_run_mixed(P, ts, kp, dens, out);
 }

@@ -12,6 +12,10 @@ constexpr int MAXP = 8;
 constexpr int MAXR = MAXP * MAXP * MAXP;
 constexpr int M2L_CH32 = 32;  // V pairs per chunk of the FP32 contraction
 constexpr int M2L_CHTC = 128; // V pairs per chunk of the tensor-core contraction (MMA N)
+constexpr int M2L_CHOZ = 64;  // V pairs per chunk of the sliced FP64-class contraction (MMA N)
+// Largest padded contraction length whose digit-group sums stay below 2^24 (exact in FP32):
+// K * (2 * 64 * 32 + 5 * 32 * 32) < 2^24, i.e. orders p <= 7.
+constexpr int M2L_OZ_MAXK = 1792;
 
 // Chebyshev nodes, polynomials and parent -> child transfers for order p (bbfmm.h:273-326).
 struct ChebTables {
@@ -23,7 +27,7 @@ struct ChebTables {
 
 // Kernel parameters, prepared once (electric.cpp:52-58, :96-97).
 struct KParams {
-    double kappa, eps, ieps, vr, k2in, q4pi;
+    double kappa, eps, ieps, vr, k2in, q4pi, vr2;
 };
 
 inline KParams make_kparams(const ibim_kernel_params &kp, double h) {
@@ -34,6 +38,7 @@ inline KParams make_kparams(const ibim_kernel_params &kp, double h) {
     k.vr = kp.tau * h;
     k.k2in = kp.kappa == 0. ? 0. : (std::exp(-kp.kappa * k.vr) - 1.0 + kp.kappa * k.vr) / kp.kappa / 2.0 / M_PI / k.vr / k.vr;
     k.q4pi = 1.0 / (4.0 * M_PI);
+    k.vr2 = k.vr * k.vr;
     return k;
 }
 
@@ -50,26 +55,47 @@ __device__ __forceinline__ void interp1(const ChebTables &T, double x, double *o
     }
 }
 
+// 1 / sqrt(x) for x > 0 in FP64: the FP32 reciprocal square root as seed (relative error below
+// 2^-22) and two Newton steps y <- y (3 - x y^2) / 2, each squaring the error (2^-44, then below
+// FP64 rounding).  This replaces the FP64 square root and three divisions of the formulas below,
+// whose multi-instruction sequences dominated the FP64 pipe.
+__device__ __forceinline__ double rsqrt64(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y;
+}
+
+// Shared radial factors of the 16 kernels (electric.cpp:67-291) at squared distance d2 >= vr^2:
+// c1 (K1), c4 (K4), k2 (K2), hd and ho (K3: hd delta_ab + ho d_a d_b).  With kappa = 0 the
+// Yukawa factor e^{-kappa r} is 1 and the exponential is skipped (uniform branch).
+__device__ __forceinline__ void radial64(const KParams &k, double d2, double &c1, double &c4, double &k2, double &hd,
+                                         double &ho) {
+    const double ir = rsqrt64(d2);
+    const double r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
+    const double t = k.kappa * r;
+    const double e = k.kappa == 0.0 ? 1.0 : exp(-t);
+    const double et1 = e * (t + 1);
+    c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
+    c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
+    k2 = (1.0 - e) * ir * k.q4pi;
+    hd = (1 - et1) * ir3;
+    ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 * ir2;
+}
+
 // Fused 4x4 block of the 16 BIE kernels (electric.cpp:67-291) at d = source - target.
-// Rows: F, Gx, Gy, Gz.  Columns: m_x, m_y, m_z, psi.
+// Rows: F, Gx, Gy, Gz.  Columns: m_x, m_y, m_z, psi.  Inside the cutoff r < tau h only the
+// regularised K2 value remains (electric.cpp:96-97).
 __device__ __forceinline__ void kblock64(const KParams &k, double dx, double dy, double dz, double b[16]) {
     const double d2 = dx * dx + dy * dy + dz * dz;
-    const double r = sqrt(d2);
-    if (r < k.vr) {
+    if (d2 < k.vr2) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) b[i] = 0.;
         b[3] = -k.k2in;
         return;
     }
-    const double t = k.kappa * r;
-    const double e = exp(-t);
-    const double ir3 = 1.0 / (r * d2);
-    const double et1 = e * (t + 1);
-    const double c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
-    const double c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
-    const double k2 = (1.0 - e) / r * k.q4pi;
-    const double hd = (1 - et1) * ir3;
-    const double ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 / d2;
+    double c1, c4, k2, hd, ho;
+    radial64(k, d2, c1, c4, k2, hd, ho);
     const double dd[3] = {dx, dy, dz};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -85,20 +111,12 @@ __device__ __forceinline__ void kblock64(const KParams &k, double dx, double dy,
 __device__ __forceinline__ void near_pair64(const KParams &k, double dx, double dy, double dz, double m0, double m1,
                                             double m2, double psi, double acc[4]) {
     const double d2 = dx * dx + dy * dy + dz * dz;
-    const double r = sqrt(d2);
-    if (r < k.vr) {
+    if (d2 < k.vr2) {
         acc[0] -= k.k2in * psi;
         return;
     }
-    const double t = k.kappa * r;
-    const double e = exp(-t);
-    const double ir3 = 1.0 / (r * d2);
-    const double et1 = e * (t + 1);
-    const double c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
-    const double c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
-    const double k2 = (1.0 - e) / r * k.q4pi;
-    const double hd = (1 - et1) * ir3;
-    const double ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 / d2;
+    double c1, c4, k2, hd, ho;
+    radial64(k, d2, c1, c4, k2, hd, ho);
     const double dm = dx * m0 + dy * m1 + dz * m2;
     acc[0] += c1 * dm - k2 * psi;
     const double cm = ho * dm - c4 * psi;

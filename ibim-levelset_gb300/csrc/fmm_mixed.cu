@@ -70,8 +70,20 @@ __global__ void k_rel_coords(int nleaf, const int *__restrict__ leaves, const in
     }
 }
 
-__global__ void k_to_f32(long n, const double *__restrict__ a, float *b) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (float)a[i];
+// Densities to FP32: [4][ns] for P2M, and per source the near-field record
+// {x, y, z, m_x | m_y, m_z, psi, 0} (leaf-relative coordinates) as two float4.
+__global__ void k_pack_src32(long ns, const double *__restrict__ dens, const float *__restrict__ sx,
+                             const float *__restrict__ sy, const float *__restrict__ sz, float *d32, float4 *src8) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ns; i += (long)gridDim.x * blockDim.x) {
+        const float m0 = (float)dens[i], m1 = (float)dens[ns + i], m2 = (float)dens[2 * ns + i],
+                    psi = (float)dens[3 * ns + i];
+        d32[i] = m0;
+        d32[ns + i] = m1;
+        d32[2 * ns + i] = m2;
+        d32[3 * ns + i] = psi;
+        src8[2 * i] = make_float4(sx[i], sy[i], sz[i], m0);
+        src8[2 * i + 1] = make_float4(m1, m2, psi, 0.f);
+    }
 }
 
 // P2M in FP32 (bbfmm.h:507-519); coordinates relative to the leaf centre.
@@ -187,18 +199,21 @@ __global__ void __launch_bounds__(128) k_l2l32(const ChebTables32 *__restrict__ 
     for (int o = threadIdx.x; o < n4; o += blockDim.x) local[(long)node * n4 + o] += tmp[o];
 }
 
-// FP32 V-list operators, evaluated in FP64 and rounded (same layout as the FP64 operators).
+// FP32 M2L operators (V and X keys), evaluated in FP64 and rounded (same layout as the FP64
+// operators).
 __global__ void k_make_ops32(const ChebTables *__restrict__ tab, const int *__restrict__ keys,
                              const double *__restrict__ root_r, KParams kp, float *ops) {
     const ChebTables &T = *tab;
     const int op = blockIdx.y;
     const int p = T.p, R = T.R, n4 = 4 * R;
-    const int lv = keys[4 * op];
-    double r[3];
+    const int lt = keys[5 * op], ls = keys[5 * op + 1];
+    double rt[3], rs[3];
     for (int a = 0; a < 3; ++a) {
-        double v = root_r[a];
-        for (int l = 0; l < lv; ++l) v *= 0.5;
-        r[a] = v;
+        double vt = root_r[a], vs = root_r[a];
+        for (int l = 0; l < lt; ++l) vt *= 0.5;
+        for (int l = 0; l < ls; ++l) vs *= 0.5;
+        rt[a] = vt;
+        rs[a] = vs;
     }
     const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (pair >= (long)R * R) return;
@@ -207,7 +222,7 @@ __global__ void k_make_ops32(const ChebTables *__restrict__ tab, const int *__re
     const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
     double d[3];
     for (int a = 0; a < 3; ++a)
-        d[a] = (keys[4 * op + 1 + a] * (2.0 * r[a]) + r[a] * T.cheb[si[a]]) - r[a] * T.cheb[ti[a]];
+        d[a] = (keys[5 * op + 2 + a] * rt[a] + rs[a] * T.cheb[si[a]]) - rt[a] * T.cheb[ti[a]];
     double b[16];
     kblock64(kp, d[0], d[1], d[2], b);
     float *K = ops + (long)op * n4 * n4;
@@ -367,16 +382,16 @@ __global__ void __launch_bounds__(128) k_m2l_x32(const ChebTables32 *__restrict_
 }
 
 // Near field + L2P in FP32 for one target leaf per block: source leaves staged in shared memory
-// in the target leaf's frame; per-tile partial sums are added with Kahan compensation.
+// in the target leaf's frame (two 16-byte loads per source record); per-tile partial sums are
+// added with Kahan compensation.
 constexpr int NT32 = 128, TILE32 = 256;
 __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict__ tab, KParams32 kp,
                                                  const int *__restrict__ tleaf, const int *__restrict__ nptr,
                                                  const int *__restrict__ nrange, const float *__restrict__ noff,
                                                  const int *__restrict__ tb_, const int *__restrict__ te_,
-                                                 const float *__restrict__ rad, const float *__restrict__ sx,
-                                                 const float *__restrict__ sy, const float *__restrict__ sz,
-                                                 const float *__restrict__ dens, long ns, const float *__restrict__ tx,
-                                                 const float *__restrict__ ty, const float *__restrict__ tz, long nt,
+                                                 const float *__restrict__ rad, const float4 *__restrict__ src8,
+                                                 const float *__restrict__ tx, const float *__restrict__ ty,
+                                                 const float *__restrict__ tz, long nt,
                                                  const float *__restrict__ local, double *out) {
     __shared__ ChebTables32 T;
     __shared__ float S[7][TILE32];
@@ -407,13 +422,14 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                 const float ox = noff[3 * lrr], oy = noff[3 * lrr + 1], oz = noff[3 * lrr + 2];
                 for (int q = threadIdx.x; q < take; q += blockDim.x) {
                     const int si = lpos + q;
-                    S[0][filled + q] = sx[si] + ox;
-                    S[1][filled + q] = sy[si] + oy;
-                    S[2][filled + q] = sz[si] + oz;
-                    S[3][filled + q] = dens[si];
-                    S[4][filled + q] = dens[ns + si];
-                    S[5][filled + q] = dens[2 * ns + si];
-                    S[6][filled + q] = dens[3 * ns + si];
+                    const float4 A = __ldg(src8 + 2 * si), B = __ldg(src8 + 2 * si + 1);
+                    S[0][filled + q] = A.x + ox;
+                    S[1][filled + q] = A.y + oy;
+                    S[2][filled + q] = A.z + oz;
+                    S[3][filled + q] = A.w;
+                    S[4][filled + q] = B.x;
+                    S[5][filled + q] = B.y;
+                    S[6][filled + q] = B.z;
                 }
                 filled += take;
                 lpos += take;
@@ -536,6 +552,7 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         P.mult32.alloc((size_t)nn * n4, s);
         P.local32.alloc((size_t)nn * n4, s);
         P.dens32.alloc((size_t)4 * P.ns, s);
+        P.src8.alloc((size_t)2 * P.ns, s);
         const size_t smk = sizeof(float) * 3 * n4;
         if (smk > 48 * 1024) {
             IBIM_CUDA(cudaFuncSetAttribute(k_m2m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk));
@@ -635,7 +652,8 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     const KParams kp = make_kparams(kpp, P.tube->h);
     const KParams32 k32 = to32(kp);
     const ChebTables32 *tab = reinterpret_cast<const ChebTables32 *>(P.tables32.ptr);
-    (count_launch(), k_to_f32<<<ew(c, 4 * P.ns), 256, 0, s>>>(4 * P.ns, dens, P.dens32.ptr));
+    (count_launch(), k_pack_src32<<<ew(c, P.ns), 256, 0, s>>>(P.ns, dens, P.sxf.ptr, P.syf.ptr, P.szf.ptr,
+                                                               P.dens32.ptr, P.src8.ptr));
     if (P.np2m > 0) {
         ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 28.0 * P.ns);
         (count_launch(), k_p2m32<<<P.np2m, 128, 0, s>>>(tab, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
@@ -682,8 +700,7 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
         ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 28.0 * P.ns + 40.0 * S.nt);
         (count_launch(), k_near32<<<S.ntleaves, NT32, 0, s>>>(tab, k32, S.tleaf.ptr, S.near32_ptr.ptr, S.near32_range.ptr,
                                                               S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr, P.nrad32.ptr,
-                                                              P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr, P.ns, tx, ty,
-                                                              tz, S.nt, P.local32.ptr, out));
+                                                              P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out));
     }
     IBIM_CHECK_LAUNCH();
 }

@@ -77,7 +77,8 @@ struct DevBuf {
 // Kernel categories timed with CUDA events when profiling is enabled on a context.
 enum ProfCat {
     PROF_EXPAND = 0, PROF_WENO, PROF_COUNT, PROF_FLOOD, PROF_TUBE, PROF_OPS, PROF_P2M, PROF_M2M, PROF_M2L_V,
-    PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_M2L_V64, PROF_M2L_X64, PROF_NEAR64, PROF_NCAT
+    PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_M2L_V64, PROF_M2L_X64, PROF_NEAR64, PROF_M2L_VOZ,
+    PROF_NCAT
 };
 
 // Number of kernels this library launched (all contexts).
@@ -87,6 +88,10 @@ long launch_count();
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // second stream for device work that overlaps host-side planning (the right-hand side),
+    // forked from and joined back to `stream` by the two events
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int num_sms = 0;
     unsigned prof_mask = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[PROF_NCAT];
@@ -104,10 +109,13 @@ struct ProfScope {
     Ctx *c;
     int cat;
     cudaEvent_t a = nullptr;
-    explicit ProfScope(int category, double flops = 0., double bytes = 0.) : c(current_ctx()), cat(category) {
+    cudaStream_t s = nullptr;
+    explicit ProfScope(int category, double flops = 0., double bytes = 0., cudaStream_t st = nullptr)
+        : c(current_ctx()), cat(category) {
         if (c && (c->prof_mask & (1u << cat))) {
+            s = st ? st : c->stream;
             a = c->take_event();
-            cudaEventRecord(a, c->stream);
+            cudaEventRecord(a, s);
             c->prof_flops[cat] += flops;
             c->prof_bytes[cat] += bytes;
         }
@@ -115,7 +123,7 @@ struct ProfScope {
     ~ProfScope() {
         if (a) {
             cudaEvent_t b = c->take_event();
-            cudaEventRecord(b, c->stream);
+            cudaEventRecord(b, s);
             c->prof_ev[cat].push_back({a, b});
         }
     }
@@ -167,15 +175,18 @@ struct TargetSet {
     DevBuf<int> perm_d, tbeg, tend;
     std::vector<int> l2l_level_begin;
     DevBuf<int> l2l_nodes;
-    DevBuf<int> v_src, v_tgt, v_chunk; // V pairs sorted by operator; chunks (op, begin, count)
+    DevBuf<int> v_src, v_tgt, v_chunk; // contraction pairs sorted by operator; chunks (op, begin, count)
     int nchunks = 0;
     DevBuf<int> v_chunk32;             // chunks of the FP32 contraction (larger)
     int nchunks32 = 0;
     DevBuf<int> v_chunk_tc;            // chunks of the tensor-core contraction (<= 128 pairs)
     int nchunks_tc = 0;
-    long nvpairs = 0;
-    DevBuf<int> x_src, x_tgt;
+    DevBuf<int> v_chunk_oz;            // chunks of the sliced FP64-class contraction (<= 64 pairs)
+    int nchunks_oz = 0;
+    long nvpairs = 0;                  // pairs of the operator contraction (V, plus X when x_as_ops)
+    DevBuf<int> x_src, x_tgt;          // X pairs evaluated on the fly (when not x_as_ops)
     long nxpairs = 0;
+    long nv_list = 0, nx_list = 0;     // V and X list sizes (bbfmm.cpp lists, pairs with sources)
     DevBuf<int> tleaf, near_ptr, near_range;
     int ntleaves = 0;
     long near_pairs = 0;
@@ -206,7 +217,9 @@ struct Plan {
     DevBuf<int> p2m_nodes;
     std::vector<int> m2m_level_begin;
     DevBuf<int> m2m_nodes;
-    // M2L operators keyed by (level, source - target lattice offset), union over target sets
+    // M2L operators keyed by (target level, source level, centre offset), union over target sets:
+    // the V list's, and (x_as_ops) the X list's, whose pairs then join the V contraction
+    bool x_as_ops = true;
     int nops = 0;
     std::vector<int> op_key_h;
     DevBuf<int> op_key;
@@ -218,6 +231,7 @@ struct Plan {
     DevBuf<double> root_r;
     DevBuf<double> mult, local, dens4;
     DevBuf<float> mult32, local32, dens32;
+    DevBuf<float4> src8;           // near-field source records (mixed): {x, y, z, m_x}, {m_y, m_z, psi, 0}
     DevBuf<float> sxf, syf, szf;   // source coordinates relative to their leaf centre (mixed)
     DevBuf<float> nrad32;          // per node radius (mixed)
     DevBuf<unsigned char> tables32;  // ChebTables32
@@ -227,6 +241,12 @@ struct Plan {
     int tc_kpad = 0, tc_mpad = 0;
     DevBuf<float> tc_a_hi, tc_a_lo, tc_b_hi, tc_b_lo;
     DevBuf<int> tc_err;
+    // FP64-class V-list M2L of the refinement residual (m2l_tc.cu): operators and multipoles as
+    // exact BF16 integer slices under power-of-two row / column scales
+    int ops64_gen = 0, oz_gen = -1;  // generation of ops64, and the one the slices were cut from
+    int oz_kpad = 0, oz_mtiles = 0;
+    DevBuf<uint16_t> oz_a, oz_b;
+    DevBuf<double> oz_sig, oz_tau;
     double kp64[4] = {-1, -1, -1, -1}, kp32[4] = {-1, -1, -1, -1};
     bool ops64_ready = false, ops32_ready = false;
     ~Plan() { for (auto *t : targets) delete t; }
@@ -234,7 +254,10 @@ struct Plan {
 
 // FMM engine.  dens: 4 x ns (tree order), out: 4 x nt of target set `ts` (tree order).
 void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision);
-void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
+// m2l_sliced: the V-list M2L on the tensor cores by exact BF16 slicing (FP64-class accuracy),
+// as used for the mixed path's refinement residual; false = FP64 pipe, the reference-exact path.
+void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out,
+                  bool m2l_sliced = false);
 void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out);
 void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, double *out, int precision);
 
@@ -243,6 +266,8 @@ bool m2l_tc_supported();
 void m2l_tc_prepare(Plan &P);
 void m2l_tc_run(Plan &P, TargetSet &S);
 int m2l_tc_error(Plan &P);
+void m2l_oz_prepare(Plan &P);
+void m2l_oz_run(Plan &P, const TargetSet &S);
 
 // Plan creation (fmm.cu): target set 0 = the tube points when with_self, then `extra` (host
 // (n, 3)) when n_extra > 0.

@@ -7,12 +7,15 @@
 // 3xTF32 split: A = A_hi + A_lo, B = B_hi + B_lo with hi = x rounded to TF32 and lo = x - hi, and
 // D accumulates A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the dropped A_lo.B_lo is below FP32 rounding).
 //
-// Operand staging: operator rows (padded to 128) and the pairs' multipoles (gathered by source
-// node) are copied with cp.async into shared memory in the canonical no-swizzle K-major layout
-// (8-row x 16-byte core matrices; K-direction core-matrix stride 128 B, row-group stride 1 KB),
-// 32 K-elements per stage.  One elected thread issues the MMAs and commits them to an mbarrier;
+// One CTA takes one chunk of up to 128 pairs of an operator against up to four 128-row tiles of
+// the operator (four FP32 accumulators of 128 x 128 = all 512 TMEM columns), so each gathered
+// multipole is read once per chunk rather than once per row tile.  Operands are copied with
+// cp.async into shared memory in the canonical no-swizzle K-major layout (8-row x 16-byte core
+// matrices; K-direction core-matrix stride 128 B, row-group stride 256 B), 8 K-elements per
+// stage, five stage buffers.  One elected thread issues the MMAs of a stage and commits them to
+// that stage's mbarrier; two stages of MMAs may be queued while three stages of copies are in flight;
 // every wait is bounded and reports through an error flag instead of hanging.  The epilogue
-// reads the accumulator with tcgen05.ld (each warp its 32 TMEM lanes) and adds it into the
+// reads the accumulators with tcgen05.ld (each warp its 32 TMEM lanes) and adds them into the
 // target nodes' local expansions.
 
 #include <cstdint>
@@ -23,10 +26,14 @@ namespace ibim {
 
 namespace {
 
-constexpr int TC_M = 128, TC_N = 128, TC_KS = 32;  // rows, pairs, K elements per stage
-constexpr int TC_THREADS = 128;
-constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 16 KB per operand tile
+constexpr int TC_M = 128, TC_N = 128, TC_KS = 8;   // rows per tile, pairs per chunk, K elements per stage
+constexpr int TC_NST = 5;                          // pipeline stages in shared memory
+constexpr int TC_QD = 2;                           // stages of MMAs allowed in flight
+constexpr int TC_RT = 4;                           // row tiles per CTA (4 x 128 TMEM columns)
+constexpr int TC_THREADS = 256;
+constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 4 KB per operand tile and stage
 constexpr long TC_WAIT_LIMIT = 1L << 20;           // bounded mbarrier polling
+constexpr int kTcSmemBytes = TC_NST * (2 * TC_RT + 2) * TC_TILE_BYTES;  // 200 KB
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -75,121 +82,195 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
-// Byte offset of element (row, k) of a 128 x 32 tile in the canonical no-swizzle K-major layout:
-// core matrix (row / 8, k / 4) at ((row / 8) * 8 + k / 4) * 128, row % 8 at 16 B, k % 4 at 4 B.
+// Byte offset of element (row, 4 * kchunk) of a 128 x 8 tile in the canonical no-swizzle
+// K-major layout: core matrix (row / 8, kchunk) at ((row / 8) * 2 + kchunk) * 128, row % 8 at 16 B.
+// Descriptor strides: 128 B between the two core matrices along K, 256 B between row groups.
 __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
-    return (uint32_t)((((row >> 3) << 3) + kchunk) * 128 + (row & 7) * 16);
+    return (uint32_t)((((row >> 3) << 1) + kchunk) * 128 + (row & 7) * 16);
 }
 
-__global__ void __launch_bounds__(TC_THREADS) k_m2l_tc(int n4, int kpad, int mpad, const int *__restrict__ chunks,
-                                                       const int *__restrict__ vsrc, const int *__restrict__ vtgt,
-                                                       const float *__restrict__ a_hi, const float *__restrict__ a_lo,
-                                                       const float *__restrict__ b_hi, const float *__restrict__ b_lo,
-                                                       float *local, int *err) {
+// One CTA: one chunk of <= 128 V pairs of a single operator x up to TC_RT row tiles of 128
+// operator rows.  Stage st holds K elements [8 st, 8 st + 8) of A_hi, A_lo (per row tile) and of
+// B_hi, B_lo in buffer st % TC_NST.  The operator tiles are pre-packed as contiguous 4 KB blocks
+// in the shared-memory layout and arrive by bulk asynchronous copies that complete on the
+// stage's "full" mbarrier; the gathered multipole rows arrive by cp.async.  The MMAs of stage st
+// are committed to the stage's "done" mbarrier; while they run, the copies of stages st + 1 ..
+// st + 3 are in flight, and the buffer of stage st - 2 (whose MMAs are waited for) is refilled
+// with stage st + 3.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+             const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
+             const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t done_bar[TC_NST], full_bar[TC_NST];
     __shared__ uint32_t tmem_base;
     __shared__ int src_s[TC_N], tgt_s[TC_N];
-    unsigned char *sAh = tc_smem, *sAl = tc_smem + TC_TILE_BYTES, *sBh = tc_smem + 2 * TC_TILE_BYTES,
-                  *sBl = tc_smem + 3 * TC_TILE_BYTES;
+    __shared__ int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
-    const int row0 = blockIdx.y * TC_M;
-    src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
-    tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
-    const uint32_t mb = smem_u32(&mbar);
+    const int tile0 = blockIdx.y * TC_RT;
+    const int rt = min(TC_RT, mtiles - tile0);
+    const int nstage = kpad / TC_KS;
+    constexpr int kStageBytes = (2 * TC_RT + 2) * TC_TILE_BYTES;
+    if (tid < TC_N) {
+        src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
+        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
+    }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+        abort_s = 0;
+        for (int i = 0; i < TC_NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done_bar[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[i])));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(TC_N));
+                     "r"(TC_RT * TC_N));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem_d = tmem_base;
-    const float *Ah = a_hi + ((long)op * mpad + row0) * kpad;
-    const float *Al = a_lo + ((long)op * mpad + row0) * kpad;
-    bool ok = true;
-    const int nstage = kpad / TC_KS;
-    for (int st = 0; st < nstage && ok; ++st) {
-        const int k0 = st * TC_KS;
-        // 4 tiles x 128 rows x 8 chunks of 16 B; thread tid copies rows tid (all chunks)
-        {
-            const int r = tid;
-            const float *ga_h = Ah + (long)r * kpad + k0, *ga_l = Al + (long)r * kpad + k0;
-            const int sn = src_s[r];
-            const float *gb_h = sn >= 0 ? b_hi + (long)sn * kpad + k0 : b_hi;
-            const float *gb_l = sn >= 0 ? b_lo + (long)sn * kpad + k0 : b_lo;
-            const uint32_t nb = sn >= 0 ? 16u : 0u;
-#pragma unroll
-            for (int c = 0; c < TC_KS / 4; ++c) {
-                const uint32_t o = tile_off(r, c);
-                cp_async16(smem_u32(sAh + o), ga_h + 4 * c, 16u);
-                cp_async16(smem_u32(sAl + o), ga_l + 4 * c, 16u);
-                cp_async16(smem_u32(sBh + o), sn >= 0 ? (const void *)(gb_h + 4 * c) : (const void *)gb_h, nb);
-                cp_async16(smem_u32(sBl + o), sn >= 0 ? (const void *)(gb_l + 4 * c) : (const void *)gb_l, nb);
+    // packed operator tiles: [op][row tile][stage][1024 floats]
+    const long atile0 = ((long)op * mtiles + tile0) * nstage;
+
+    auto load_stage = [&](int st) {
+        unsigned char *base = tc_smem + (st % TC_NST) * kStageBytes;
+        if (tid == 0) {
+            const uint32_t fb = smem_u32(&full_bar[st % TC_NST]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
+                         "r"(2 * rt * TC_TILE_BYTES)
+                         : "memory");
+            for (int t = 0; t < rt; ++t) {
+                const long g = (atile0 + (long)t * nstage + st) * (TC_TILE_BYTES / 4);
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(base + t * TC_TILE_BYTES)),
+                    "l"(a_hi + g), "r"(TC_TILE_BYTES), "r"(fb)
+                    : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(base + (rt + t) * TC_TILE_BYTES)),
+                    "l"(a_lo + g), "r"(TC_TILE_BYTES), "r"(fb)
+                    : "memory");
             }
         }
+        // multipole rows: 2 tiles x 128 rows x 2 pieces of 16 B
+        const int k0 = st * TC_KS;
+        for (int i = tid; i < 2 * 2 * TC_M; i += TC_THREADS) {
+            const int tile = i >> 8, row = (i >> 1) & (TC_M - 1), c = i & 1;
+            const uint32_t dst = smem_u32(base + (2 * rt + tile) * TC_TILE_BYTES + tile_off(row, c));
+            const int sn = src_s[row];
+            const float *B = tile == 0 ? b_hi : b_lo;
+            cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
+                       sn >= 0 ? 16u : 0u);
+        }
         asm volatile("cp.async.commit_group;");
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
+    };
+
+    int issued = -1;       // last stage whose copies were issued
+    int full_waited = -1;  // last stage whose operator tiles thread 0 waited for
+    for (int s = 0; s < TC_NST - TC_QD; ++s) {
+        if (s < nstage) {
+            load_stage(s);
+            issued = s;
+        } else {
+            asm volatile("cp.async.commit_group;");
+        }
+    }
+    bool ok = true;
+    int last = -1;  // last stage whose MMAs were committed
+    for (int st = 0; st < nstage; ++st) {
+        const int ld = st + TC_NST - TC_QD;  // stage loaded now, into the buffer stage st - TC_QD used
+        bool w = true;
+        if (ld < nstage && st >= TC_QD)
+            w = mbar_wait(smem_u32(&done_bar[(st - TC_QD) % TC_NST]), (uint32_t)(((st - TC_QD) / TC_NST) & 1));
+        if (!__syncthreads_and((w && !abort_s) ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+        if (ld < nstage) {
+            load_stage(ld);
+            issued = ld;
+        } else {
+            asm volatile("cp.async.commit_group;");
+        }
+        asm volatile("cp.async.wait_group %0;" ::"n"(TC_NST - TC_QD) : "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll
-            for (int s = 0; s < TC_KS / 8; ++s) {
-                // K = 8 TF32 = 2 core matrices along K: advance 256 B per step
-                const uint64_t ah = make_desc(smem_u32(sAh) + 256 * s, 128, 1024);
-                const uint64_t al = make_desc(smem_u32(sAl) + 256 * s, 128, 1024);
-                const uint64_t bh = make_desc(smem_u32(sBh) + 256 * s, 128, 1024);
-                const uint64_t bl = make_desc(smem_u32(sBl) + 256 * s, 128, 1024);
-                mma_tf32(tmem_d, ah, bh, (st > 0 || s > 0) ? 1u : 0u);
-                mma_tf32(tmem_d, ah, bl, 1u);
-                mma_tf32(tmem_d, al, bh, 1u);
+            const bool have = mbar_wait(smem_u32(&full_bar[st % TC_NST]), (uint32_t)((st / TC_NST) & 1));
+            if (have) {
+                full_waited = st;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(tc_smem + (st % TC_NST) * kStageBytes);
+                const uint64_t bh = make_desc(base + (2 * rt) * TC_TILE_BYTES, 128, 256);
+                const uint64_t bl = make_desc(base + (2 * rt + 1) * TC_TILE_BYTES, 128, 256);
+                for (int t = 0; t < rt; ++t) {
+                    const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
+                    const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
+                    const uint32_t d = tmem_d + (uint32_t)(t * TC_N);
+                    mma_tf32(d, ah, bh, st > 0 ? 1u : 0u);
+                    mma_tf32(d, ah, bl, 1u);
+                    mma_tf32(d, al, bh, 1u);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&done_bar[st % TC_NST]))
+                             : "memory");
+                last = st;
+            } else {
+                abort_s = 1;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
-                         : "memory");
-        }
-        // every thread waits for this stage's MMAs before the tiles are overwritten
-        ok = __syncthreads_and(mbar_wait(mb, (uint32_t)(st & 1)) ? 1 : 0) != 0;
-        if (!ok) {
-            if (tid == 0) atomicExch(err, 1);
-            // give the stage one more bounded wait before the accumulator is released
-            mbar_wait(mb, (uint32_t)(st & 1));
-            __syncthreads();
         }
     }
+    // drain: the multipole copies, then (thread 0) every operator-tile copy not yet waited for
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (tid == 0) {
+        for (int s = full_waited + 1; s <= issued; ++s)
+            if (!mbar_wait(smem_u32(&full_bar[s % TC_NST]), (uint32_t)((s / TC_NST) & 1))) ok = false;
+        if (last >= 0 && !mbar_wait(smem_u32(&done_bar[last % TC_NST]), (uint32_t)((last / TC_NST) & 1))) ok = false;
+        if (last != nstage - 1) ok = false;
+        if (!ok) {
+            abort_s = 1;
+            atomicExch(err, 1);
+        }
+    }
+    __syncthreads();
+    ok = !abort_s;
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ok) {
-        // epilogue: warp w owns TMEM lanes 32w..32w+31 = operator rows row0 + 32w + lane
-        const int row = row0 + 32 * warp + lane;
-        const uint32_t taddr = tmem_d + ((uint32_t)(32 * warp) << 16);
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (operator rows) of the row tiles t = w / 4, w / 4 + 2
+        const int lg = warp & 3;
+        for (int t = warp >> 2; t < rt; t += 2) {
+            const int row = (tile0 + t) * TC_M + 32 * lg + lane;
+            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(t * TC_N);
 #pragma unroll 1
-        for (int c0 = 0; c0 < TC_N; c0 += 16) {
-            uint32_t v[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                : "r"(taddr + (uint32_t)c0));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < n4) {
+            for (int c0 = 0; c0 < TC_N; c0 += 16) {
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr + (uint32_t)c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < n4) {
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int t = tgt_s[c0 + q];
-                    if (t >= 0) atomicAdd(local + (long)t * n4 + row, __uint_as_float(v[q]));
+                    for (int q = 0; q < 16; ++q) {
+                        const int tg = tgt_s[c0 + q];
+                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]));
+                    }
                 }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_N));
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * TC_N));
 }
 
 // hi = x rounded to TF32 (10 explicit mantissa bits, to nearest even), lo = x - hi.
@@ -201,15 +282,23 @@ __device__ __forceinline__ float tf32_round(float x) {
     return __uint_as_float(u);
 }
 
-// Operators (column-major n4 x n4 per op, FP32) -> row-major [mpad][kpad] hi / lo, zero padded.
-__global__ void k_pack_ops_tc(int n4, int mpad, int kpad, int nops, const float *__restrict__ ops, float *a_hi,
+// Operators (column-major n4 x n4 per op, FP32) -> hi / lo tiles in the shared-memory layout,
+// [op][row tile of 128][stage of 8 K][1024 floats]; float f of a tile holds row
+// (f / 64) * 8 + (f % 32) / 4 and K element ((f / 32) % 2) * 4 + f % 4 (core matrices of 8 rows
+// x 4 K, two per row group along K).  Rows and K beyond n4 are zero.
+__global__ void k_pack_ops_tc(int n4, int mtiles, int kpad, int nops, const float *__restrict__ ops, float *a_hi,
                               float *a_lo) {
-    const long total = (long)nops * mpad * kpad;
+    const int nstage = kpad / TC_KS;
+    const long total = (long)nops * mtiles * nstage * (TC_TILE_BYTES / 4);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const int k = (int)(i % kpad);
-        const long rr = i / kpad;
-        const int row = (int)(rr % mpad);
-        const int op = (int)(rr / mpad);
+        const int f = (int)(i % (TC_TILE_BYTES / 4));
+        const long tix = i / (TC_TILE_BYTES / 4);
+        const int st = (int)(tix % nstage);
+        const int t = (int)((tix / nstage) % mtiles);
+        const int op = (int)(tix / ((long)nstage * mtiles));
+        const int cm = f >> 5;  // core matrix: row group cm / 2, K half cm % 2
+        const int row = t * TC_M + (cm >> 1) * 8 + ((f & 31) >> 2);
+        const int k = st * TC_KS + (cm & 1) * 4 + (f & 3);
         float x = 0.f;
         if (row < n4 && k < n4) x = ops[(long)op * n4 * n4 + (long)k * n4 + row];
         const float h = tf32_round(x);
@@ -229,6 +318,297 @@ __global__ void k_split_mult_tc(long nnodes, int n4, int kpad, const float *__re
         hi[i] = h;
         lo[i] = x - h;
     }
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// FP64-class V-list M2L for the refinement residual: exact integer slices on the tensor cores.
+//
+// The Ozaki scheme (Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix
+// multiplication by using fast routines of matrix multiplication", Numer. Algorithms 59, 2012),
+// in its fixed-point form: each operator row r is scaled by a power of two s_r >= max |A_r.|,
+// each multipole column j by t_j >= max |B_.j|, and the scaled values (in [-1, 1]) are cut into
+// OZ_S signed 6-bit digits by repeated round-to-nearest,
+//     A_rk / s_r = sum_i a_i(r,k) 2^(-6(i+1)) + e,   |a_0| <= 64, |a_i>0| <= 32, |e| <= 2^-43.
+// Digits are small integers, exact in BF16; a digit product is an integer below 2^12 and a
+// K-term dot product of one digit pair below 2^21 (K <= 1024), so the FP32 tensor-core
+// accumulation of each group G_k = sum_{i+l=k} a_i b_l (at most 7 digit pairs, < 2^24) is exact.
+// The epilogue recombines sum_k G_k 2^(-6(k+2)) exactly in 64-bit integers, converts once to
+// FP64 and applies s_r t_j.  Digit pairs with i + l >= OZ_S are dropped: the result differs from
+// the FP64 product by about 2^-40 of s_r t_j per term (~1e-11 relative), far below the FP32
+// operator the refinement corrects.
+//
+// One CTA: one chunk of <= 64 pairs x one 128-row tile; accumulator k (k = 0..6) in TMEM
+// columns [64 k, 64 k + 64).  Stage st holds K elements [16 st, 16 st + 16): the 7 operator digit
+// tiles (128 x 16 BF16, 4 KB each, pre-packed contiguously: one bulk copy) and the 7 multipole
+// digit tiles (64 x 16 BF16, gathered by cp.async).
+// ---------------------------------------------------------------------------------------------
+
+constexpr int OZ_S = 7, OZ_M = 128, OZ_N = 64, OZ_KS = 16;
+constexpr int OZ_NST = 5, OZ_QD = 2, OZ_THREADS = 256;
+constexpr int OZ_ATILE = OZ_M * OZ_KS * 2;                 // 4 KB
+constexpr int OZ_BTILE = OZ_N * OZ_KS * 2;                 // 2 KB
+constexpr int OZ_STAGE = OZ_S * (OZ_ATILE + OZ_BTILE);      // 42 KB
+constexpr int kOzSmemBytes = OZ_NST * OZ_STAGE;             // 210 KB
+constexpr int OZ_SCALE_EXP = 6 * (OZ_S + 1);                // 2^-48 folded into the row scale
+
+// D FP32, A and B BF16, both K-major, M = 128, N = 64.
+constexpr uint32_t kIdescOz = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
+                              ((uint32_t)(OZ_M >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescOz), "r"(accumulate));
+}
+
+// BF16 bits of a small integer-valued float (exact: the low 16 bits are zero).
+__device__ __forceinline__ uint16_t bf16_bits_exact(float v) {
+    return (uint16_t)(__float_as_uint(v) >> 16);
+}
+
+// Cut x (|x| <= 1) into OZ_S digits.
+__device__ __forceinline__ void oz_digits(double x, uint16_t *dig) {
+#pragma unroll
+    for (int i = 0; i < OZ_S; ++i) {
+        const double v = x * 64.0;
+        const double a = rint(v);
+        dig[i] = bf16_bits_exact((float)a);
+        x = v - a;
+    }
+}
+
+// Power-of-two scale >= m (1 for m == 0), returned as its exponent.
+__device__ __forceinline__ int oz_scale_exp(double m) {
+    if (!(m > 0.0)) return 0;
+    int e;
+    frexp(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return e;
+}
+
+// Operators (FP64, column-major n4 x n4 per op) -> digit tiles [op][row tile][stage][digit][4 KB]
+// in the shared-memory layout (tile_off with 16 K elements of 2 bytes per row) and the row scales
+// sig[op][mtiles * 128] = s_r 2^-48.  One thread per (op, row).
+__global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const double *__restrict__ ops, uint16_t *a,
+                              double *sig) {
+    const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M;
+    const long total = (long)nops * mpad;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(i % mpad), op = (int)(i / mpad);
+        const double *col0 = ops + (long)op * n4 * n4 + r;
+        double m = 0.0;
+        if (r < n4)
+            for (int k = 0; k < n4; ++k) m = fmax(m, fabs(col0[(long)k * n4]));
+        const int e = oz_scale_exp(m);
+        sig[i] = ldexp(1.0, e - OZ_SCALE_EXP);
+        const int t = r / OZ_M, row = r % OZ_M;
+        for (int k = 0; k < kpad; ++k) {
+            const double x = (r < n4 && k < n4) ? ldexp(col0[(long)k * n4], -e) : 0.0;
+            uint16_t dig[OZ_S];
+            oz_digits(x, dig);
+            const int st = k / OZ_KS, kin = k % OZ_KS;
+            const long tbase = (((long)op * mtiles + t) * nstage + st) * OZ_S;
+            const uint32_t off = tile_off(row, kin >> 3) + 2 * (kin & 7);
+#pragma unroll
+            for (int d = 0; d < OZ_S; ++d) a[(tbase + d) * (OZ_ATILE / 2) + off / 2] = dig[d];
+        }
+    }
+}
+
+// Multipoles (FP64 [node][n4]) -> digits [node][stage][digit][16] and column scales tau = t_j.
+// One warp per node.
+__global__ void k_split_mult_oz(long nnodes, int n4, int kpad, const double *__restrict__ mult, uint16_t *b,
+                                double *tau) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+    const int nstage = kpad / OZ_KS;
+    for (long node = warp; node < nnodes; node += nwarps) {
+        const double *m = mult + node * n4;
+        double mx = 0.0;
+        for (int k = lane; k < n4; k += 32) mx = fmax(mx, fabs(m[k]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const int e = oz_scale_exp(mx);
+        if (lane == 0) tau[node] = ldexp(1.0, e);
+        for (int k = lane; k < kpad; k += 32) {
+            const double x = k < n4 ? ldexp(m[k], -e) : 0.0;
+            uint16_t dig[OZ_S];
+            oz_digits(x, dig);
+            const long base = ((node * nstage + k / OZ_KS) * OZ_S) * OZ_KS + (k % OZ_KS);
+#pragma unroll
+            for (int d = 0; d < OZ_S; ++d) b[base + (long)d * OZ_KS] = dig[d];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_m2l_oz(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+             const int *__restrict__ vtgt, const uint16_t *__restrict__ a, const double *__restrict__ sig,
+             const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err) {
+    extern __shared__ __align__(1024) unsigned char oz_smem[];
+    __shared__ __align__(8) uint64_t done_bar[OZ_NST], full_bar[OZ_NST];
+    __shared__ uint32_t tmem_base;
+    __shared__ int src_s[OZ_N], tgt_s[OZ_N];
+    __shared__ double tau_s[OZ_N];
+    __shared__ int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
+    const int t = blockIdx.y;
+    const int nstage = kpad / OZ_KS;
+    if (tid < OZ_N) {
+        const int sn = tid < cnt ? vsrc[b + tid] : -1;
+        src_s[tid] = sn;
+        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
+        tau_s[tid] = sn >= 0 ? tau[sn] : 0.0;
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        for (int i = 0; i < OZ_NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done_bar[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[i])));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem_d = tmem_base;
+    const long atile0 = ((long)op * mtiles + t) * nstage;
+
+    auto load_stage = [&](int st) {
+        unsigned char *base = oz_smem + (st % OZ_NST) * OZ_STAGE;
+        if (tid == 0) {
+            const uint32_t fb = smem_u32(&full_bar[st % OZ_NST]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(OZ_S * OZ_ATILE)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(base)),
+                "l"(a + (atile0 + st) * (long)(OZ_S * OZ_ATILE / 2)), "r"(OZ_S * OZ_ATILE), "r"(fb)
+                : "memory");
+        }
+        // multipole digits: 64 rows x 7 digits x 2 pieces of 16 B (224 contiguous bytes per row)
+        for (int i = tid; i < OZ_N * OZ_S * 2; i += OZ_THREADS) {
+            const int row = i / (OZ_S * 2), rem = i % (OZ_S * 2), d = rem >> 1, c = rem & 1;
+            const uint32_t dst = smem_u32(base + OZ_S * OZ_ATILE + d * OZ_BTILE + tile_off(row, c));
+            const int sn = src_s[row];
+            const uint16_t *g = sn >= 0 ? bdig + (((long)sn * nstage + st) * OZ_S + d) * OZ_KS + 8 * c : bdig;
+            cp_async16(dst, g, sn >= 0 ? 16u : 0u);
+        }
+        asm volatile("cp.async.commit_group;");
+    };
+
+    int issued = -1, full_waited = -1, last = -1;
+    for (int s = 0; s < OZ_NST - OZ_QD; ++s) {
+        if (s < nstage) {
+            load_stage(s);
+            issued = s;
+        } else {
+            asm volatile("cp.async.commit_group;");
+        }
+    }
+    bool ok = true;
+    for (int st = 0; st < nstage; ++st) {
+        const int ld = st + OZ_NST - OZ_QD;
+        bool w = true;
+        if (ld < nstage && st >= OZ_QD)
+            w = mbar_wait(smem_u32(&done_bar[(st - OZ_QD) % OZ_NST]), (uint32_t)(((st - OZ_QD) / OZ_NST) & 1));
+        if (!__syncthreads_and((w && !abort_s) ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+        if (ld < nstage) {
+            load_stage(ld);
+            issued = ld;
+        } else {
+            asm volatile("cp.async.commit_group;");
+        }
+        asm volatile("cp.async.wait_group %0;" ::"n"(OZ_NST - OZ_QD) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            if (mbar_wait(smem_u32(&full_bar[st % OZ_NST]), (uint32_t)((st / OZ_NST) & 1))) {
+                full_waited = st;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(oz_smem + (st % OZ_NST) * OZ_STAGE);
+#pragma unroll
+                for (int k = 0; k < OZ_S; ++k) {
+#pragma unroll
+                    for (int i = 0; i <= k; ++i) {
+                        const uint64_t ad = make_desc(base + i * OZ_ATILE, 128, 256);
+                        const uint64_t bd = make_desc(base + OZ_S * OZ_ATILE + (k - i) * OZ_BTILE, 128, 256);
+                        mma_bf16(tmem_d + (uint32_t)(k * OZ_N), ad, bd, (st > 0 || i > 0) ? 1u : 0u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&done_bar[st % OZ_NST]))
+                             : "memory");
+                last = st;
+            } else {
+                abort_s = 1;
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (tid == 0) {
+        for (int s = full_waited + 1; s <= issued; ++s)
+            if (!mbar_wait(smem_u32(&full_bar[s % OZ_NST]), (uint32_t)((s / OZ_NST) & 1))) ok = false;
+        if (last >= 0 && !mbar_wait(smem_u32(&done_bar[last % OZ_NST]), (uint32_t)((last / OZ_NST) & 1))) ok = false;
+        if (last != nstage - 1) ok = false;
+        if (!ok) {
+            abort_s = 1;
+            atomicExch(err, 1);
+        }
+    }
+    __syncthreads();
+    ok = !abort_s;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+        // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [32 (w / 4), + 32)
+        const int lg = warp & 3, h = warp >> 2;
+        const int row = t * OZ_M + 32 * lg + lane;
+        const double srow = row < n4 ? sig[(long)op * mtiles * OZ_M + row] : 0.0;
+#pragma unroll 1
+        for (int c0 = 32 * h; c0 < 32 * h + 32; c0 += 16) {
+            long long acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc[q] = 0;
+#pragma unroll 1
+            for (int k = 0; k < OZ_S; ++k) {
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(k * OZ_N + c0)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const long long wgt = 1LL << (6 * (OZ_S - 1 - k));
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc[q] += (long long)__float2int_rn(__uint_as_float(v[q])) * wgt;
+            }
+            if (row < n4) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int tg = tgt_s[c0 + q];
+                    if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, (double)acc[q] * srow * tau_s[c0 + q]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(512));
 }
 
 }  // namespace
@@ -251,14 +631,14 @@ void m2l_tc_prepare(Plan &P) {
     P.tc_a_hi.alloc(na, s);
     P.tc_a_lo.alloc(na, s);
     if (P.nops > 0)
-        (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, P.tc_mpad, P.tc_kpad, P.nops, P.ops32.ptr,
+        (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, P.tc_mpad / TC_M, P.tc_kpad, P.nops, P.ops32.ptr,
                                                                       P.tc_a_hi.ptr, P.tc_a_lo.ptr));
     P.tc_b_hi.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
     P.tc_b_lo.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
     P.tc_err.alloc(1, s);
     P.tc_err.zero();
     IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * TC_TILE_BYTES));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
     P.tc_ready = true;
 }
 
@@ -269,19 +649,62 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     const int n4 = 4 * P.R;
     (count_launch(), k_split_mult_tc<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr,
                                                                         P.tc_b_hi.ptr, P.tc_b_lo.ptr));
-    const dim3 grid(S.nchunks_tc, P.tc_mpad / TC_M);
+    const dim3 grid(S.nchunks_tc, (P.tc_mpad / TC_M + TC_RT - 1) / TC_RT);
     {
         ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                       4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-        (count_launch(), k_m2l_tc<<<grid, TC_THREADS, 4 * TC_TILE_BYTES, s>>>(
-                             n4, P.tc_kpad, P.tc_mpad, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+        (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
+                             n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }
 
+// Digit tiles of the FP64 operators, rebuilt whenever the FP64 operators are.
+void m2l_oz_prepare(Plan &P) {
+    if (P.oz_gen == P.ops64_gen || P.nops == 0) return;
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R;
+    P.oz_kpad = (n4 + OZ_KS - 1) / OZ_KS * OZ_KS;
+    P.oz_mtiles = (n4 + OZ_M - 1) / OZ_M;
+    const int nstage = P.oz_kpad / OZ_KS;
+    P.oz_a.alloc((size_t)P.nops * P.oz_mtiles * nstage * OZ_S * (OZ_ATILE / 2), s);
+    P.oz_sig.alloc((size_t)P.nops * P.oz_mtiles * OZ_M, s);
+    P.oz_b.alloc((size_t)P.tree.nnodes * nstage * OZ_S * OZ_KS, s);
+    P.oz_tau.alloc((size_t)P.tree.nnodes, s);
+    if (!P.tc_err.ptr) {
+        P.tc_err.alloc(1, s);
+        P.tc_err.zero();
+    }
+    const long rows = (long)P.nops * P.oz_mtiles * OZ_M;
+    (count_launch(), k_pack_ops_oz<<<(int)std::min<long>((rows + 127) / 128, 64L * P.ctx->num_sms), 128, 0, s>>>(
+                         n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, P.oz_a.ptr, P.oz_sig.ptr));
+    IBIM_CHECK_LAUNCH();
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmemBytes));
+    P.oz_gen = P.ops64_gen;
+}
+
+// V-list M2L of the FP64 operator by exact digit products on the tensor cores; mult -> local.
+void m2l_oz_run(Plan &P, const TargetSet &S) {
+    if (S.nchunks_oz == 0) return;
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R;
+    (count_launch(), k_split_mult_oz<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.oz_kpad, P.mult.ptr,
+                                                                        P.oz_b.ptr, P.oz_tau.ptr));
+    const dim3 grid(S.nchunks_oz, P.oz_mtiles);
+    {
+        const double nst = P.oz_kpad / OZ_KS;
+        ProfScope ps_(PROF_M2L_VOZ, 2.0 * n4 * (double)n4 * S.nvpairs,
+                      2.0 * OZ_S * nst * OZ_KS * ((double)P.oz_mtiles * OZ_M * P.nops + (double)S.nvpairs));
+        (count_launch(), k_m2l_oz<<<grid, OZ_THREADS, kOzSmemBytes, s>>>(
+                             n4, P.oz_kpad, P.oz_mtiles, S.v_chunk_oz.ptr, S.v_src.ptr, S.v_tgt.ptr, P.oz_a.ptr,
+                             P.oz_sig.ptr, P.oz_b.ptr, P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr));
+    }
+    IBIM_CHECK_LAUNCH();
+}
+
 int m2l_tc_error(Plan &P) {
-    if (!P.tc_ready) return 0;
+    if (!P.tc_err.ptr) return 0;
     int e = 0;
     P.tc_err.download(&e, 1);
     IBIM_CUDA(cudaStreamSynchronize(P.ctx->stream));

@@ -8,12 +8,16 @@
 //   polarize       polarizeMap + energy (electric.cpp:442-505)
 //   solve          main.cpp:45-77 for an explicit geometry
 // Mixed precision (IBIM_PRECISION_MIXED): the same GMRES runs on the FP32 operator inside an
-// FP64 iterative-refinement loop whose residual uses the FP64 operator.
+// FP64 iterative-refinement loop whose residual uses the FP64 operator (IBIM_PRECISION_FP64_TC:
+// FP64 near field and X list, V-list M2L as exact BF16 digit products on the tensor cores).
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
+#include <string>
 
+#include "fmm_common.cuh"
 #include "solve.cuh"
 
 namespace ibim {
@@ -68,10 +72,9 @@ __global__ void __launch_bounds__(256) k_rhs(long n, const double *__restrict__ 
             for (int a = 0; a < cnt; ++a) {
                 const double dx = X - A[0][a], dy = Y - A[1][a], dz = Z - A[2][a];
                 const double d = dx * dx + dy * dy + dz * dz;
-                const double r = sqrt(d);
-                const double ir = 1.0 / r;
+                const double ir = rsqrt64(d);  // 1 / r (electric.cpp:401-409 divides by r and r^3)
                 b1 += A[3][a] * c1 * ir;
-                b2 -= A[3][a] * c2 * (ir / d) * (NX * dx + NY * dy + NZ * dz);
+                b2 -= A[3][a] * c2 * (ir * ir * ir) * (NX * dx + NY * dy + NZ * dz);
             }
     }
     if (i < n) {
@@ -195,14 +198,24 @@ void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *
     IBIM_CHECK_LAUNCH();
 }
 
-void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b) {
-    Ctx *c = P.ctx;
-    const long n = P.ns;
+static void rhs_launch(Ctx *c, long n, const double *x, const double *y, const double *z, const double *nx,
+                       const double *ny, const double *nz, const ibim_kernel_params &kp, const double *atoms4_dev,
+                       int natoms, double *b, cudaStream_t st) {
     const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
     const double c1 = 1.0 / (kp.dI * 4.0 * M_PI * e1), c2 = 1.0 / (kp.dI * 4.0 * M_PI * e2);
-    { ProfScope ps_(PROF_RHS); (count_launch(), k_rhs<<<div_up(n, 256), 256, 0, c->stream>>>(n, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr,
-                                                 atoms4_dev, natoms, c1, c2, b)); }
+    ProfScope ps_(PROF_RHS, 20.0 * n * (double)natoms, 0., st);
+    (count_launch(), k_rhs<<<div_up(n, 256), 256, 0, st>>>(n, x, y, z, nx, ny, nz, atoms4_dev, natoms, c1, c2, b));
     IBIM_CHECK_LAUNCH();
+}
+
+void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b) {
+    rhs_launch(P.ctx, P.ns, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, kp, atoms4_dev, natoms, b,
+               P.ctx->stream);
+}
+
+void bie_rhs_tube(const Tube &t, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b,
+                  cudaStream_t st) {
+    rhs_launch(t.ctx, t.n, t.x.ptr, t.y.ptr, t.z.ptr, t.nx.ptr, t.ny.ptr, t.nz.ptr, kp, atoms4_dev, natoms, b, st);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -360,7 +373,7 @@ int Krylov::solve(const std::function<void(const double *, double *)> &A, double
 
 void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, const double *charges_host,
                     int natoms, int restart, int maxiter, double tol, int precision, double *x_tree_out,
-                    std::vector<double> *atom_pot, ibim_result &res) {
+                    std::vector<double> *atom_pot, ibim_result &res, const double *b_tube) {
     Ctx *c = P.ctx;
     cudaStream_t s = c->stream;
     const long n2 = 2 * P.ns;
@@ -369,7 +382,13 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
     x.alloc(n2, s);
     x.zero();
     Timer tm(s);
-    bie_rhs(P, kp, atoms4_dev, natoms, b.ptr);
+    if (b_tube) {
+        // right-hand side computed in tube order beforehand: into tree order
+        permute(c, P.ns, P.src_perm.ptr, b_tube, b.ptr, false);
+        permute(c, P.ns, P.src_perm.ptr, b_tube + P.ns, b.ptr + P.ns, false);
+    } else {
+        bie_rhs(P, kp, atoms4_dev, natoms, b.ptr);
+    }
     Krylov K(c, n2, std::max(1, std::min(restart, 250)));
     GmresStats st;
     int status = 1;
@@ -381,7 +400,11 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
     } else {
         // FP64 iterative refinement around the mixed-precision GMRES
         auto A32 = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_MIXED); };
-        auto A64 = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_FP64); };
+        // residual operator: FP64 with the V-list M2L as exact digit products on the tensor cores
+        // (IBIM_RESIDUAL_M2L=fp64 selects the FP64-pipe M2L, for comparison)
+        const char *rm = std::getenv("IBIM_RESIDUAL_M2L");
+        const int res_prec = (rm && std::string(rm) == "fp64") ? IBIM_PRECISION_FP64 : IBIM_PRECISION_FP64_TC;
+        auto A64 = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, res_prec); };
         DevBuf<double> r, d;
         r.alloc(n2, s);
         d.alloc(n2, s);

@@ -34,6 +34,7 @@ KERNELS = ["K1x", "K1y", "K1z", "K2", "K3xx", "K3yy", "K3zz", "K3xy", "K3yz", "K
 KERNEL_BIE_FUSED = 16
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_FP64_TC = 2
 
 # every symbol include/ibim.h declares
 EXPORTS = [
@@ -49,7 +50,7 @@ EXPORTS = [
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
-                      "near_l2p_fp64"]
+                      "near_l2p_fp64", "m2l_v_sliced"]
 
 
 class IbimError(RuntimeError):

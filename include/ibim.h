@@ -56,6 +56,12 @@ extern "C" {
 /* ---- precision modes ---- */
 #define IBIM_PRECISION_FP64 0  /* reference-exact FP64 path */
 #define IBIM_PRECISION_MIXED 1 /* FP32 far/near field inside FP64 iterative refinement */
+/* FP64 operator whose V-list M2L runs on the tensor cores as exact products of BF16 integer
+ * digits (Ozaki scheme, 7 digits of 6 bits under power-of-two row/column scales; ~1e-11 of the
+ * FP64 product): the operator of the mixed path's refinement residual.  Accepted by
+ * ibim_fmm_plan (hence ibim_fmm_apply / ibim_bie_matvec) and ibim_gmres_solve; not a whole-solve
+ * mode (ibim_config.precision is FP64 or MIXED). */
+#define IBIM_PRECISION_FP64_TC 2
 
 typedef struct ibim_ctx_s *ibim_ctx;
 typedef struct ibim_grid_s *ibim_grid;
@@ -121,8 +127,10 @@ long ibim_launch_count(void);
  * category k: 0 expand, 1 WENO stage, 2 gradient count, 3 flood fill, 4 tube extraction,
  * 5 M2L operators, 6 P2M, 7 M2M, 8 M2L (V list), 9 M2L (X list), 10 L2L, 11 near field + L2P,
  * 12 right-hand side, 13 GMRES vector kernels; FP64 versions of 8, 9 and 11 are categories 14, 15
- * and 16 (categories 6-11 then count the mixed-precision kernels).  ibim_profile_read returns (and clears) the
- * summed milliseconds and launch counts of the first ncat categories. */
+ * and 16 (categories 6-11 then count the mixed-precision kernels); 17 is the V-list M2L of the
+ * mixed path's refinement residual (BF16 integer slices on the tensor cores, FP64-class).
+ * ibim_profile_read returns (and clears) the summed milliseconds and launch counts of the first
+ * ncat categories. */
 int ibim_profile_enable(ibim_ctx ctx, unsigned mask);
 int ibim_profile_read(ibim_ctx ctx, double *ms, long *launches, int ncat);
 /* Algorithmic flops and bytes of the profiled launches per category since the last read (call

@@ -2,7 +2,7 @@
 // with an explicit box instead of the hard-wired [-300, 300]^3 rescaling: the same sequence of
 // calls, executed on the GPU.  Usage: main_dropin <input.cfg>
 // (keys: pqr_file, lo, h, n, reinit_step, plus the reference's lvlset_*, fmm_*, solvent_*, tau,
-// gmres_* keys).
+// gmres_*, potent_file, energy_file keys; optional grid_file / node_file).
 #include <cstdio>
 
 #include "ibim/dropin.hpp"
@@ -33,6 +33,9 @@ int main(int argc, char *argv[]) {
         phi0 = g;
         ls.reinitialize(g, phi0, cfg.num("reinit_step"), 1, 0.5);
         Surface surf(g, ls, 1.0);
+        // main.cpp:70-73 writes these under -DGRID; here when the config names the files
+        if (cfg.options.count("grid_file")) g.output(cfg.options["grid_file"]);
+        if (cfg.options.count("node_file")) surf.output(cfg.options["node_file"]);
         const double E = electric(g, ls, surf, mol, 1.0, cfg);
         std::printf("DROPIN_POINTS %zu\nDROPIN_ENERGY %.17e\n", surf.nodes.size(), E);
     } catch (const Error &e) {

@@ -1,12 +1,15 @@
 """The reference's main.cpp sequence written against the C++ drop-in classes
 (include/ibim/dropin.hpp) compiles against the library here, and on a GPU reproduces the
-reference's energy."""
+reference's energy and writes the reference's output files (electric.cpp:420-427 potent_file,
+2N lines; electric.cpp:491-497 energy_file, M lines; levelset.cpp:39-52 Grid::output, one value
+per line in i, j, k order; levelset.cpp:593-601 Surface::output, "x y z" per tube point)."""
 
 import os
 import shutil
 import subprocess
 import tempfile
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -53,7 +56,9 @@ def test_dropin_main_reproduces_reference(golden):
                     f"lvlset_thickness = {P['thickness']}\nlvlset_thres = {P['thres']}\nfmm_np = {P['np']}\n"
                     f"fmm_maxpoint = {P['maxpoint']}\nfmm_maxlevel = {P['maxlevel']}\ntau = {P['tau']}\n"
                     f"solvent_kappa = {P['kappa']!r}\nsolvent_dE = {P['dE']!r}\nsolvent_dI = {P['dI']!r}\n"
-                    f"gmres_restart = {P['restart']}\ngmres_maxiter = {P['maxiter']}\ngmres_tol = {P['tol']}\n")
+                    f"gmres_restart = {P['restart']}\ngmres_maxiter = {P['maxiter']}\ngmres_tol = {P['tol']}\n"
+                    f"potent_file = {td}/potential.txt\nenergy_file = {td}/energy.txt\n"
+                    f"grid_file = {td}/output.grid\nnode_file = {td}/output.node\n")
         r = subprocess.run([exe, cfg], capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr
         vals = dict(ln.split()[:2] for ln in r.stdout.splitlines() if ln.startswith("DROPIN_"))
@@ -69,3 +74,14 @@ def test_dropin_main_reproduces_reference(golden):
         ctx.close()
         assert int(vals["DROPIN_POINTS"]) == ref["n_points"]
         assert abs(E - ref["energy"]) / abs(ref["energy"]) < 1e-9
+        npts = ref["n_points"]
+        pot = np.loadtxt(os.path.join(td, "potential.txt"))
+        assert pot.shape == (2 * npts,) and np.all(np.isfinite(pot))
+        atom = np.loadtxt(os.path.join(td, "energy.txt"))
+        assert atom.shape == (len(G["charges"]),)
+        # the files carry 6 significant digits (default stream precision), as the reference's do
+        assert abs(0.5 * np.dot(atom, G["charges"]) - E) <= 1e-5 * np.sum(np.abs(0.5 * atom * G["charges"]))
+        grid = np.loadtxt(os.path.join(td, "output.grid"))
+        assert grid.shape == (n ** 3,)
+        nodes = np.loadtxt(os.path.join(td, "output.node"))
+        assert nodes.shape == (npts, 3)
