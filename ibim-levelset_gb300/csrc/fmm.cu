@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(128) k_m2l_x64(const ChebTables *__restrict__ 
 // Threads = targets x source phases; sources staged in shared memory tiles.
 constexpr int NEAR_T = 128, NEAR_TILE = 128;
 __global__ void __launch_bounds__(NEAR_T) k_near64(const ChebTables *__restrict__ tab, KParams kp,
-                                                   const int *__restrict__ tleaf, const int *__restrict__ near_ptr,
+                                                   const int4 *__restrict__ segs,
                                                    const int *__restrict__ near_range, const int *__restrict__ tb_,
                                                    const int *__restrict__ te_, const double *__restrict__ ctr,
                                                    const double *__restrict__ rad, const double *__restrict__ sx,
@@ -326,9 +326,9 @@ __global__ void __launch_bounds__(NEAR_T) k_near64(const ChebTables *__restrict_
     __shared__ double red[NEAR_T][4];
     for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
         reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
-    const int leaf = tleaf[blockIdx.x];
+    const int4 sg = segs[blockIdx.x];
+    const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
     const int tb = tb_[leaf], te = te_[leaf];
-    const int r0 = near_ptr[blockIdx.x], r1 = near_ptr[blockIdx.x + 1];
     __syncthreads();
     for (int t0 = tb; t0 < te; t0 += NEAR_T) {
         const int nT = min(NEAR_T, te - t0);
@@ -365,18 +365,24 @@ __global__ void __launch_bounds__(NEAR_T) k_near64(const ChebTables *__restrict_
             double f[4] = {0., 0., 0., 0.};
             for (int q = 0; q < nph; ++q)
                 for (int o = 0; o < 4; ++o) f[o] += red[threadIdx.x + q * nT][o];
-            // L2P (bbfmm.h:600): local expansion at the target
-            double Sp[3][MAXP];
-            const double xyz[3] = {X, Y, Z};
-            for (int a = 0; a < 3; ++a) interp1(T, (xyz[a] - ctr[3 * leaf + a]) / rad[3 * leaf + a], Sp[a]);
-            const int p = T.p, R = T.R;
-            const double *L = local + (long)leaf * 4 * R;
+            // L2P (bbfmm.h:600): local expansion at the target, by the leaf's first segment
             double l2p[4] = {0., 0., 0., 0.};
-            for (int c = 0; c < R; ++c) {
-                const double w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
-                for (int o = 0; o < 4; ++o) l2p[o] += w * L[o * R + c];
+            if (mode & 1) {
+                double Sp[3][MAXP];
+                const double xyz[3] = {X, Y, Z};
+                for (int a = 0; a < 3; ++a) interp1(T, (xyz[a] - ctr[3 * leaf + a]) / rad[3 * leaf + a], Sp[a]);
+                const int p = T.p, R = T.R;
+                const double *L = local + (long)leaf * 4 * R;
+                for (int c = 0; c < R; ++c) {
+                    const double w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                    for (int o = 0; o < 4; ++o) l2p[o] += w * L[o * R + c];
+                }
             }
-            for (int o = 0; o < 4; ++o) out[o * nt + t0 + threadIdx.x] = f[o] + l2p[o];
+            for (int o = 0; o < 4; ++o) {
+                double *dst = out + o * nt + t0 + threadIdx.x;
+                if (mode & 2) atomicAdd(dst, f[o] + l2p[o]);
+                else *dst = f[o] + l2p[o];
+            }
         }
         __syncthreads();
     }
@@ -404,6 +410,57 @@ void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, do
     if (n <= 0) return;
     (count_launch(), k_gather<<<(int)std::min<long>(4L * c->num_sms, div_up(n, 256)), 256, 0, c->stream>>>(n, perm, a, b, scale));
     IBIM_CHECK_LAUNCH();
+}
+
+constexpr long NEAR_SEG_PAIRS = 1L << 17;
+
+bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::vector<int> &ptr,
+                   std::vector<int> &rng, bool split_long, std::vector<int> &seg) {
+    const int nl = (int)tl.size();
+    if (split_long) {
+        std::vector<int> p2{0}, r2;
+        for (int k = 0; k < nl; ++k) {
+            const long cap = std::max<long>(256, NEAR_SEG_PAIRS / std::max(1, nt[k]));
+            for (int r = ptr[k]; r < ptr[k + 1]; ++r)
+                for (long b = rng[2 * r]; b < rng[2 * r + 1]; b += cap) {
+                    r2.push_back((int)b);
+                    r2.push_back((int)std::min<long>(b + cap, rng[2 * r + 1]));
+                }
+            p2.push_back((int)r2.size() / 2);
+        }
+        ptr.swap(p2);
+        rng.swap(r2);
+    }
+    struct Seg {
+        long work;
+        int leaf, r0, r1, mode;
+    };
+    std::vector<Seg> out;
+    bool atomic = false;
+    for (int k = 0; k < nl; ++k) {
+        const long cap = std::max<long>(256, NEAR_SEG_PAIRS / std::max(1, nt[k]));
+        const size_t first = out.size();
+        int r0 = ptr[k];
+        long acc = 0;
+        for (int r = ptr[k]; r < ptr[k + 1]; ++r) {
+            const long len = rng[2 * r + 1] - rng[2 * r];
+            if (acc > 0 && acc + len > cap) {
+                out.push_back({acc * nt[k], tl[k], r0, r, 0});
+                r0 = r;
+                acc = 0;
+            }
+            acc += len;
+        }
+        out.push_back({acc * nt[k], tl[k], r0, ptr[k + 1], 0});
+        const bool multi = out.size() - first > 1;
+        atomic = atomic || multi;
+        for (size_t q = first; q < out.size(); ++q) out[q].mode = (q == first ? 1 : 0) | (multi ? 2 : 0);
+    }
+    std::stable_sort(out.begin(), out.end(), [](const Seg &a, const Seg &b) { return a.work > b.work; });
+    seg.clear();
+    for (auto &g : out) seg.insert(seg.end(), {g.leaf, g.r0, g.r1, g.mode});
+    if (seg.empty()) seg.assign(4, 0);
+    return atomic;
 }
 
 // Work lists of one target set: which nodes need locals, V pairs by operator, X pairs, and
@@ -557,6 +614,13 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     }
     S.ntleaves = (int)tl.size();
     S.near_pairs = npairs;
+    {
+        std::vector<int> ntk(tl.size()), seg;
+        for (size_t k = 0; k < tl.size(); ++k) ntk[k] = (int)(S.end[tl[k]] - S.begin[tl[k]]);
+        S.near_atomic = near_segments(tl, ntk, nptr, nr, true, seg);
+        S.nnear_seg = tl.empty() ? 0 : (int)seg.size() / 4;
+        up_int(S.near_seg, seg, s);
+    }
     up_int(S.tleaf, tl, s);
     up_int(S.near_ptr, nptr, s);
     up_int(S.near_range, nr, s);
@@ -820,8 +884,9 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
     const double *tx = S.self ? P.sx.ptr : S.tx.ptr;
     const double *ty = S.self ? P.sy.ptr : S.ty.ptr;
     const double *tz = S.self ? P.sz.ptr : S.tz.ptr;
+    if (S.ntleaves > 0 && S.near_atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
     if (S.ntleaves > 0)
-        { ProfScope ps_(PROF_NEAR64, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, kp, S.tleaf.ptr, S.near_ptr.ptr, S.near_range.ptr,
+        { ProfScope ps_(PROF_NEAR64, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.nnear_seg, NEAR_T, 0, s>>>(P.tables.ptr, kp, reinterpret_cast<const int4 *>(S.near_seg.ptr), S.near_range.ptr,
                                                S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
                                                P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out)); }
     IBIM_CHECK_LAUNCH();

@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(128) k_m2l_x32(const ChebTables32 *__restrict_
 // added with Kahan compensation.
 constexpr int NT32 = 128, TILE32 = 256;
 __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict__ tab, KParams32 kp,
-                                                 const int *__restrict__ tleaf, const int *__restrict__ nptr,
+                                                 const int4 *__restrict__ segs,
                                                  const int *__restrict__ nrange, const float *__restrict__ noff,
                                                  const int *__restrict__ tb_, const int *__restrict__ te_,
                                                  const float *__restrict__ rad, const float4 *__restrict__ src8,
@@ -397,9 +397,9 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
     __shared__ float S[7][TILE32];
     __shared__ float red[NT32][4];
     load_tables(T, tab);
-    const int leaf = tleaf[blockIdx.x];
+    const int4 sg = segs[blockIdx.x];
+    const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
     const int tb = tb_[leaf], te = te_[leaf];
-    const int r0 = nptr[blockIdx.x], r1 = nptr[blockIdx.x + 1];
     __syncthreads();
     for (int t0 = tb; t0 < te; t0 += NT32) {
         const int nT = min(NT32, te - t0);
@@ -482,17 +482,23 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
             double f[4] = {0., 0., 0., 0.};
             for (int q = 0; q < nph; ++q)
                 for (int o = 0; o < 4; ++o) f[o] += (double)red[threadIdx.x + q * nT][o];
-            float Sp[3][MAXP];
-            const float xyz[3] = {X, Y, Z};
-            for (int a = 0; a < 3; ++a) interp1f(T, xyz[a] / rad[3 * leaf + a], Sp[a]);
-            const int p = T.p, R = T.R;
-            const float *L = local + (long)leaf * 4 * R;
             float l2p[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int c = 0; c < R; ++c) {
-                const float w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
-                for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, L[o * R + c], l2p[o]);
+            if (mode & 1) {  // L2P by the leaf's first segment
+                float Sp[3][MAXP];
+                const float xyz[3] = {X, Y, Z};
+                for (int a = 0; a < 3; ++a) interp1f(T, xyz[a] / rad[3 * leaf + a], Sp[a]);
+                const int p = T.p, R = T.R;
+                const float *L = local + (long)leaf * 4 * R;
+                for (int c = 0; c < R; ++c) {
+                    const float w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                    for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, L[o * R + c], l2p[o]);
+                }
             }
-            for (int o = 0; o < 4; ++o) out[o * nt + t0 + threadIdx.x] = f[o] + (double)l2p[o];
+            for (int o = 0; o < 4; ++o) {
+                double *dst = out + o * nt + t0 + threadIdx.x;
+                if (mode & 2) atomicAdd(dst, f[o] + (double)l2p[o]);
+                else *dst = f[o] + (double)l2p[o];
+            }
         }
         __syncthreads();
     }
@@ -587,9 +593,11 @@ void prepare_mixed(Plan &P, TargetSet &S) {
     std::vector<int> child_first(nn, -1);
     for (int i = nn - 1; i >= 0; --i)
         if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
-    std::vector<int> stack;
+    std::vector<int> stack, tl32, nt32;
     for (int i = 0; i < nn; ++i) {
         if (!T.leaf[i] || S.end[i] <= S.begin[i]) continue;
+        tl32.push_back(i);
+        nt32.push_back((int)(S.end[i] - S.begin[i]));
         auto add_leaves = [&](int root) {
             stack.clear();
             stack.push_back(root);
@@ -609,6 +617,12 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         for (int u : T.U[i]) add_leaves(u);
         for (int w : T.W[i]) add_leaves(w);
         ptr.push_back((int)rng.size() / 2);
+    }
+    {
+        std::vector<int> seg;
+        S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, seg);
+        S.nnear32_seg = tl32.empty() ? 0 : (int)seg.size() / 4;
+        up_i(S.near32_seg, seg, s);
     }
     up_i(S.near32_ptr, ptr, s);
     up_i(S.near32_range, rng, s);
@@ -698,7 +712,8 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     const float *tz = S.self ? P.szf.ptr : S.tzf.ptr;
     if (S.ntleaves > 0) {
         ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 28.0 * P.ns + 40.0 * S.nt);
-        (count_launch(), k_near32<<<S.ntleaves, NT32, 0, s>>>(tab, k32, S.tleaf.ptr, S.near32_ptr.ptr, S.near32_range.ptr,
+        if (S.near32_atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
+        (count_launch(), k_near32<<<S.nnear32_seg, NT32, 0, s>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr), S.near32_range.ptr,
                                                               S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr, P.nrad32.ptr,
                                                               P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out));
     }

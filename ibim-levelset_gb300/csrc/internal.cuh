@@ -190,6 +190,12 @@ struct TargetSet {
     DevBuf<int> tleaf, near_ptr, near_range;
     int ntleaves = 0;
     long near_pairs = 0;
+    // near-field work segments (one CTA each): {target leaf node, first range, end range, mode},
+    // mode bit 0 = this segment adds the L2P term, bit 1 = the leaf has several segments (atomic
+    // accumulation into a zeroed output); heaviest first
+    DevBuf<int> near_seg;
+    int nnear_seg = 0;
+    bool near_atomic = false;
     DevBuf<double> out4;               // 4 x nt workspace
     // mixed precision
     bool mixed_ready = false;
@@ -197,6 +203,9 @@ struct TargetSet {
     DevBuf<int> near32_ptr, near32_range;  // per target leaf: source leaves (begin, end)
     DevBuf<float> near32_off;          // per source leaf entry: source leaf centre - target leaf centre
     int near32_entries = 0;
+    DevBuf<int> near32_seg;            // work segments over the near32 ranges (as near_seg)
+    int nnear32_seg = 0;
+    bool near32_atomic = false;
     DevBuf<float> x_off32;             // per X pair: source centre - target centre
 };
 
@@ -268,6 +277,15 @@ void m2l_tc_run(Plan &P, TargetSet &S);
 int m2l_tc_error(Plan &P);
 void m2l_oz_prepare(Plan &P);
 void m2l_oz_run(Plan &P, const TargetSet &S);
+
+// Near-field work segments.  Target leaf k (node tl[k], nt[k] targets) owns source ranges
+// ptr[k] .. ptr[k+1] of `rng` (begin, end pairs); consecutive ranges are grouped into segments of
+// at most max(256, NEAR_SEG_PAIRS / nt[k]) sources, so no CTA carries more than about
+// NEAR_SEG_PAIRS pairs; ranges longer than that are split first (split_long).  Output: 4 ints per
+// segment (see TargetSet::near_seg), sorted by descending work; returns whether any leaf has
+// several segments.
+bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::vector<int> &ptr,
+                   std::vector<int> &rng, bool split_long, std::vector<int> &seg);
 
 // Plan creation (fmm.cu): target set 0 = the tube points when with_self, then `extra` (host
 // (n, 3)) when n_extra > 0.

@@ -19,6 +19,7 @@
 // target nodes' local expansions.
 
 #include <cstdint>
+#include <cstdlib>
 
 #include "fmm_common.cuh"
 
@@ -246,6 +247,197 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int t = warp >> 2; t < rt; t += 2) {
             const int row = (tile0 + t) * TC_M + 32 * lg + lane;
             const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(t * TC_N);
+#pragma unroll 1
+            for (int c0 = 0; c0 < TC_N; c0 += 16) {
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr + (uint32_t)c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < n4) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int tg = tgt_s[c0 + q];
+                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]));
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * TC_N));
+}
+
+// Warp-specialised form of the same contraction: warp 0 (one thread) issues the operator bulk
+// copies, warp 1 (one thread) issues the MMAs, warps 2-7 gather the multipole rows with cp.async.
+// Per stage buffer: full_a (bulk copies, transaction count), full_b (the 192 gathering threads,
+// each after its own copies of the stage have landed and been fenced to the async proxy), empty
+// (tcgen05.commit of the stage's MMAs).  No CTA-wide barrier inside the K loop; every wait is
+// bounded and an expired wait aborts the CTA through a shared flag and the error word.
+constexpr int TC_BPROD = 192, TC_LAG = 2;
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_m2l_tc_ws(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+                const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
+                const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full_a[TC_NST], full_b[TC_NST], empty_bar[TC_NST], acc_bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int src_s[TC_N], tgt_s[TC_N];
+    __shared__ volatile int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
+    const int tile0 = blockIdx.y * TC_RT;
+    const int rt = min(TC_RT, mtiles - tile0);
+    const int nstage = kpad / TC_KS;
+    constexpr int kStageBytes = (2 * TC_RT + 2) * TC_TILE_BYTES;
+    if (tid < TC_N) {
+        src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
+        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        for (int i = 0; i < TC_NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(TC_BPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TC_RT * TC_N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem_d = tmem_base;
+    const long atile0 = ((long)op * mtiles + tile0) * nstage;
+
+    if (warp == 0) {
+        if (lane == 0) {  // operator tiles: bulk copies
+            int issued = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % TC_NST;
+                if (st >= TC_NST &&
+                    !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / TC_NST) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                if (abort_s) break;
+                unsigned char *base = tc_smem + buf * kStageBytes;
+                const uint32_t fb = smem_u32(&full_a[buf]);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
+                             "r"(2 * rt * TC_TILE_BYTES)
+                             : "memory");
+                for (int t = 0; t < rt; ++t) {
+                    const long g = (atile0 + (long)t * nstage + st) * (TC_TILE_BYTES / 4);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            smem_u32(base + t * TC_TILE_BYTES)),
+                        "l"(a_hi + g), "r"(TC_TILE_BYTES), "r"(fb)
+                        : "memory");
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            smem_u32(base + (rt + t) * TC_TILE_BYTES)),
+                        "l"(a_lo + g), "r"(TC_TILE_BYTES), "r"(fb)
+                        : "memory");
+                }
+                issued = st;
+            }
+            // every issued copy lands before the CTA may exit (the last use of each buffer)
+            for (int s2 = max(0, issued - TC_NST + 1); s2 <= issued; ++s2)
+                if (!mbar_wait(smem_u32(&full_a[s2 % TC_NST]), (uint32_t)((s2 / TC_NST) & 1))) abort_s = 1;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issue
+            int last = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % TC_NST;
+                const uint32_t par = (uint32_t)((st / TC_NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(tc_smem + buf * kStageBytes);
+                const uint64_t bh = make_desc(base + (2 * rt) * TC_TILE_BYTES, 128, 256);
+                const uint64_t bl = make_desc(base + (2 * rt + 1) * TC_TILE_BYTES, 128, 256);
+                for (int t = 0; t < rt; ++t) {
+                    const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
+                    const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
+                    const uint32_t d = tmem_d + (uint32_t)(t * TC_N);
+                    mma_tf32(d, ah, bh, st > 0 ? 1u : 0u);
+                    mma_tf32(d, ah, bl, 1u);
+                    mma_tf32(d, al, bh, 1u);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&empty_bar[buf]))
+                             : "memory");
+                last = st;
+            }
+            if (last == nstage - 1) {
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&acc_bar))
+                             : "memory");
+            } else {
+                abort_s = 1;
+                if (last >= 0) mbar_wait(smem_u32(&empty_bar[last % TC_NST]), (uint32_t)((last / TC_NST) & 1));
+            }
+        }
+    } else {  // multipole rows: cp.async by 192 threads
+        const int t = tid - 64;
+        int issued = -1;
+        for (int st = 0; st < nstage; ++st) {
+            const int buf = st % TC_NST;
+            if (st >= TC_NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / TC_NST) - 1) & 1))) {
+                abort_s = 1;
+                break;
+            }
+            if (abort_s) break;
+            unsigned char *base = tc_smem + buf * kStageBytes;
+            const int k0 = st * TC_KS;
+            for (int i = t; i < 2 * 2 * TC_M; i += TC_BPROD) {
+                const int tile = i >> 8, row = (i >> 1) & (TC_M - 1), c = i & 1;
+                const uint32_t dst = smem_u32(base + (2 * rt + tile) * TC_TILE_BYTES + tile_off(row, c));
+                const int sn = src_s[row];
+                const float *B = tile == 0 ? b_hi : b_lo;
+                cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
+                           sn >= 0 ? 16u : 0u);
+            }
+            asm volatile("cp.async.commit_group;");
+            issued = st;
+            if (st >= TC_LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(TC_LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - TC_LAG) % TC_NST]))
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s2 = max(0, issued - TC_LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % TC_NST])) : "memory");
+    }
+    __syncthreads();
+    bool ok = !abort_s;
+    if (ok) ok = mbar_wait(smem_u32(&acc_bar), 0u);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (!ok && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+        const int lg = warp & 3;
+        for (int tt = warp >> 2; tt < rt; tt += 2) {
+            const int row = (tile0 + tt) * TC_M + 32 * lg + lane;
+            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * TC_N);
 #pragma unroll 1
             for (int c0 = 0; c0 < TC_N; c0 += 16) {
                 uint32_t v[16];
@@ -639,6 +831,7 @@ void m2l_tc_prepare(Plan &P) {
     P.tc_err.zero();
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
     P.tc_ready = true;
 }
 
@@ -653,9 +846,15 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     {
         ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                       4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-        (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
-                             n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
-                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        static const bool ws = std::getenv("IBIM_TC_NOWS") == nullptr;
+        if (ws)
+            (count_launch(), k_m2l_tc_ws<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
+                                 n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr,
+                                 P.tc_a_hi.ptr, P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        else
+            (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
+                                 n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr,
+                                 P.tc_a_hi.ptr, P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }
