@@ -111,6 +111,8 @@ static void check_config(const ibim_config &cfg) {
     IBIM_REQUIRE(cfg.kp.dE > 0 && cfg.kp.dI > 0, "solvent_dE and solvent_dI must be positive");
     IBIM_REQUIRE(cfg.kp.kappa >= 0 && cfg.kp.tau >= 0, "solvent_kappa and tau must be non-negative");
     IBIM_REQUIRE(cfg.precision == IBIM_PRECISION_FP64 || cfg.precision == IBIM_PRECISION_MIXED, "unknown precision");
+    IBIM_REQUIRE(cfg.jacobian == 0 || cfg.jacobian == 1, "jacobian must be 0 or 1");
+    IBIM_REQUIRE(cfg.kp.k3_scaled == 0 || cfg.kp.k3_scaled == 1, "k3_scaled must be 0 or 1");
 }
 
 static void fill_plan_stats(const Plan &P, ibim_result &res) {
@@ -161,7 +163,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     Timer t1(s);
     Tube *tube = nullptr;
     try {
-        tube = surface_extract(*g, cfg.thickness, &res.inclusion);
+        tube = surface_extract(*g, cfg.thickness, &res.inclusion, cfg.jacobian != 0);
     } catch (...) {
         delete g;
         throw;
@@ -183,7 +185,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         b_tube.alloc(2 * (size_t)tube->n, s);
         IBIM_CUDA(cudaEventRecord(c->ev_fork, s));
         IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
-        bie_rhs_tube(*tube, cfg.kp, atoms4, natoms, b_tube.ptr, c->aux);
+        bie_rhs_tube(*tube, cfg.kp, atoms4, natoms, b_tube.ptr, c->aux, cfg.precision);
         IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
         auto w0 = std::chrono::steady_clock::now();
         P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
@@ -527,11 +529,17 @@ int ibim_levelset_build(ibim_ctx ctx, const double *centers, const double *radii
 }
 
 int ibim_surface_extract(ibim_grid g, int thickness, ibim_tube *out, long *n_points, long *inclusion) {
+    return ibim_surface_extract_jacobian(g, thickness, 0, out, n_points, inclusion);
+}
+
+int ibim_surface_extract_jacobian(ibim_grid g, int thickness, int jacobian, ibim_tube *out, long *n_points,
+                                  long *inclusion) {
     return guard([&] {
         IBIM_REQUIRE(g && out, "null argument");
+        IBIM_REQUIRE(jacobian == 0 || jacobian == 1, "jacobian must be 0 or 1");
         bind(g->g->ctx);
         long inc = 0;
-        Tube *t = surface_extract(*g->g, thickness, &inc);
+        Tube *t = surface_extract(*g->g, thickness, &inc, jacobian != 0);
         IBIM_CUDA(cudaStreamSynchronize(g->g->ctx->stream));
         if (n_points) *n_points = t->n;
         if (inclusion) *inclusion = inc;

@@ -823,11 +823,11 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
 }
 
 void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision) {
-    const double key[4] = {kp.kappa, kp.dE, kp.dI, kp.tau};
+    const double key[5] = {kp.kappa, kp.dE, kp.dI, kp.tau, (double)kp.k3_scaled};
     const bool is64 = precision == IBIM_PRECISION_FP64;
     double *cache = is64 ? P.kp64 : P.kp32;
     bool same = is64 ? P.ops64_ready : P.ops32_ready;
-    for (int i = 0; i < 4; ++i) same = same && cache[i] == key[i];
+    for (int i = 0; i < 5; ++i) same = same && cache[i] == key[i];
     if (same || P.nops == 0) return;
     cudaStream_t s = P.ctx->stream;
     const int R = P.R, n4 = 4 * R;
@@ -838,9 +838,11 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
         { ProfScope ps_(PROF_OPS); (count_launch(), k_make_ops64<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops64.ptr)); }
         IBIM_CHECK_LAUNCH();
     } else {
-        fmm_prepare_operators_mixed(P, k);
+        bool have64 = P.ops64_ready;
+        for (int i = 0; i < 5; ++i) have64 = have64 && P.kp64[i] == key[i];
+        fmm_prepare_operators_mixed(P, k, have64 ? P.ops64.ptr : nullptr);
     }
-    for (int i = 0; i < 4; ++i) cache[i] = key[i];
+    for (int i = 0; i < 5; ++i) cache[i] = key[i];
     (is64 ? P.ops64_ready : P.ops32_ready) = true;
     if (is64) P.ops64_gen++;
 }

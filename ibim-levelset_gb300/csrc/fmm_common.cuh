@@ -28,6 +28,7 @@ struct ChebTables {
 // Kernel parameters, prepared once (electric.cpp:52-58, :96-97).
 struct KParams {
     double kappa, eps, ieps, vr, k2in, q4pi, vr2;
+    double k3f;  // factor on the K3 block: 1 (the reference) or 1 / (4 pi) (k3_scaled)
 };
 
 inline KParams make_kparams(const ibim_kernel_params &kp, double h) {
@@ -39,6 +40,7 @@ inline KParams make_kparams(const ibim_kernel_params &kp, double h) {
     k.k2in = kp.kappa == 0. ? 0. : (std::exp(-kp.kappa * k.vr) - 1.0 + kp.kappa * k.vr) / kp.kappa / 2.0 / M_PI / k.vr / k.vr;
     k.q4pi = 1.0 / (4.0 * M_PI);
     k.vr2 = k.vr * k.vr;
+    k.k3f = kp.k3_scaled ? k.q4pi : 1.0;
     return k;
 }
 
@@ -79,8 +81,8 @@ __device__ __forceinline__ void radial64(const KParams &k, double d2, double &c1
     c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
     c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
     k2 = (1.0 - e) * ir * k.q4pi;
-    hd = (1 - et1) * ir3;
-    ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 * ir2;
+    hd = (1 - et1) * ir3 * k.k3f;
+    ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 * ir2 * k.k3f;
 }
 
 // Fused 4x4 block of the 16 BIE kernels (electric.cpp:67-291) at d = source - target.
@@ -126,6 +128,7 @@ __device__ __forceinline__ void near_pair64(const KParams &k, double dx, double 
 }
 
 void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale);
-void fmm_prepare_operators_mixed(Plan &P, const KParams &k);
+// ops64: the FP64 operators for the same kernel parameters (rounded instead of re-evaluated), or null
+void fmm_prepare_operators_mixed(Plan &P, const KParams &k, const double *ops64);
 
 }  // namespace ibim

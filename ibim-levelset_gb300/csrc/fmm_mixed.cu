@@ -26,12 +26,12 @@ struct ChebTables32 {
 };
 
 struct KParams32 {
-    float kappa, eps, ieps, vr2, k2in, q4pi;
+    float kappa, eps, ieps, vr2, k2in, q4pi, k3f;
 };
 
 static KParams32 to32(const KParams &k) {
     return KParams32{(float)k.kappa, (float)k.eps, (float)k.ieps, (float)(k.vr * k.vr), (float)k.k2in,
-                     (float)k.q4pi};
+                     (float)k.q4pi, (float)k.k3f};
 }
 
 namespace {
@@ -68,6 +68,10 @@ __global__ void k_rel_coords(int nleaf, const int *__restrict__ leaves, const in
         yf[i] = (float)(y[i] - cy);
         zf[i] = (float)(z[i] - cz);
     }
+}
+
+__global__ void k_to_f32(long n, const double *__restrict__ a, float *b) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (float)a[i];
 }
 
 // Densities to FP32: [4][ns] for P2M, and per source the near-field record
@@ -334,8 +338,8 @@ __device__ __forceinline__ void kblock32(const KParams32 &k, float dx, float dy,
     const float c1 = (k.eps * et1 - 1.f) * ir3 * k.q4pi;
     const float c4 = -(k.ieps * et1 - 1.f) * ir3 * k.q4pi;
     const float k2 = (1.f - e) * ir * k.q4pi;
-    const float hd = (1.f - et1) * ir3;
-    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir;
+    const float hd = (1.f - et1) * ir3 * k.k3f;
+    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir * k.k3f;
     const float dd[3] = {dx, dy, dz};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -456,8 +460,8 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                     const float c1 = (kp.eps * et1 - 1.f) * ir3 * kp.q4pi;
                     const float c4 = -(kp.ieps * et1 - 1.f) * ir3 * kp.q4pi;
                     const float k2 = (1.f - e) * ir * kp.q4pi;
-                    const float hd = (1.f - et1) * ir3;
-                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir;
+                    const float hd = (1.f - et1) * ir3 * kp.k3f;
+                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir * kp.k3f;
                     const float dm = dx * m0 + dy * m1 + dz * m2;
                     a0 += c1 * dm - k2 * psi;
                     const float cm = ho * dm - c4 * psi;
@@ -645,12 +649,18 @@ void prepare_mixed(Plan &P, TargetSet &S) {
 
 }  // namespace
 
-void fmm_prepare_operators_mixed(Plan &P, const KParams &k) {
+void fmm_prepare_operators_mixed(Plan &P, const KParams &k, const double *ops64) {
     cudaStream_t s = P.ctx->stream;
     const int R = P.R, n4 = 4 * R;
-    P.ops32.alloc((size_t)P.nops * n4 * n4, s);
-    dim3 g(div_up((long)R * R, 256), P.nops);
-    { ProfScope ps_(PROF_OPS); (count_launch(), k_make_ops32<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops32.ptr)); }
+    const long n = (long)P.nops * n4 * n4;
+    P.ops32.alloc((size_t)n, s);
+    ProfScope ps_(PROF_OPS);
+    if (ops64) {  // the same kernel values rounded to FP32, as k_make_ops32 would compute them
+        (count_launch(), k_to_f32<<<ew(P.ctx, n), 256, 0, s>>>(n, ops64, P.ops32.ptr));
+    } else {
+        dim3 g(div_up((long)R * R, 256), P.nops);
+        (count_launch(), k_make_ops32<<<g, 256, 0, s>>>(P.tables.ptr, P.op_key.ptr, P.root_r.ptr, k, P.ops32.ptr));
+    }
     IBIM_CHECK_LAUNCH();
 }
 

@@ -256,7 +256,7 @@ struct Plan {
     int oz_kpad = 0, oz_mtiles = 0;
     DevBuf<uint16_t> oz_a, oz_b;
     DevBuf<double> oz_sig, oz_tau;
-    double kp64[4] = {-1, -1, -1, -1}, kp32[4] = {-1, -1, -1, -1};
+    double kp64[5] = {-1, -1, -1, -1, -1}, kp32[5] = {-1, -1, -1, -1, -1};  // kernel parameters of the cached operators
     bool ops64_ready = false, ops32_ready = false;
     ~Plan() { for (auto *t : targets) delete t; }
 };
@@ -302,7 +302,8 @@ int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel,
 void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc);
 void grid_scale(Grid &g, double s);
 void grid_copy(Grid &dst, const Grid &src);
-Tube *surface_extract(Grid &g, int thickness, long *inclusion);
+// jacobian: multiply the weights by the surface Jacobian (opt-in; the reference has none)
+Tube *surface_extract(Grid &g, int thickness, long *inclusion, bool jacobian = false);
 
 // Timing helper
 struct Timer {

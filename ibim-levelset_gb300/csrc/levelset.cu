@@ -339,12 +339,51 @@ __global__ void k_scan_counts(const int *counts, int nb, long *offsets) {
 }
 
 // Tube points in (i, j, k) order (levelset.cpp:540-583): normal = (D- + D+)/2 (not normalised),
-// projection P = x - n*phi, weight = (1 + cos(pi phi / tw)) / (2 tw); emitted in FP64.
+// projection P = x - n*phi, weight = (1 + cos(pi phi / tw)) / (2 tw), times the surface Jacobian
+// when asked (opt-in); emitted in FP64.
+// Surface Jacobian at grid point (i, j, k): J = 1 - phi (k1 + k2) + phi^2 k1 k2 with k1 + k2 and
+// k1 k2 the sum and product of the principal curvatures of the level set through the point,
+// from second-order central differences of phi (clamped at the grid edge):
+//   k1 + k2 = div(grad phi / |grad phi|),   k1 k2 = grad phi^T adj(Hess phi) grad phi / |grad phi|^4.
+// For a signed distance it is the area ratio of the zero level set to the level set through the
+// point (a sphere of radius R at distance phi: (R / (R + phi))^2), independent of the sign
+// convention of phi.
+template <class T>
+__device__ double surface_jacobian(const T *__restrict__ g, Dims dm, int i, int j, int k, double dx, double phi) {
+    auto at = [&](int a, int b, int c) -> double {
+        a = min(max(a, 0), dm.nx - 1);
+        b = min(max(b, 0), dm.ny - 1);
+        c = min(max(c, 0), dm.nz - 1);
+        return (double)g[((long)a * dm.ny + b) * dm.nz + c];
+    };
+    const double c0 = at(i, j, k), h2 = dx * dx;
+    const double fx = (at(i + 1, j, k) - at(i - 1, j, k)) / (2 * dx);
+    const double fy = (at(i, j + 1, k) - at(i, j - 1, k)) / (2 * dx);
+    const double fz = (at(i, j, k + 1) - at(i, j, k - 1)) / (2 * dx);
+    const double fxx = (at(i + 1, j, k) - 2 * c0 + at(i - 1, j, k)) / h2;
+    const double fyy = (at(i, j + 1, k) - 2 * c0 + at(i, j - 1, k)) / h2;
+    const double fzz = (at(i, j, k + 1) - 2 * c0 + at(i, j, k - 1)) / h2;
+    const double fxy = (at(i + 1, j + 1, k) - at(i + 1, j - 1, k) - at(i - 1, j + 1, k) + at(i - 1, j - 1, k)) / (4 * h2);
+    const double fxz = (at(i + 1, j, k + 1) - at(i + 1, j, k - 1) - at(i - 1, j, k + 1) + at(i - 1, j, k - 1)) / (4 * h2);
+    const double fyz = (at(i, j + 1, k + 1) - at(i, j + 1, k - 1) - at(i, j - 1, k + 1) + at(i, j - 1, k - 1)) / (4 * h2);
+    const double g2 = fx * fx + fy * fy + fz * fz;
+    if (!(g2 > 0.0)) return 1.0;
+    const double gn = sqrt(g2);
+    const double ksum = (fxx * (fy * fy + fz * fz) + fyy * (fx * fx + fz * fz) + fzz * (fx * fx + fy * fy) -
+                         2 * (fx * fy * fxy + fx * fz * fxz + fy * fz * fyz)) /
+                        (g2 * gn);
+    const double kprod = (fx * fx * (fyy * fzz - fyz * fyz) + fy * fy * (fxx * fzz - fxz * fxz) +
+                          fz * fz * (fxx * fyy - fxy * fxy) + 2 * fx * fy * (fxz * fyz - fxy * fzz) +
+                          2 * fy * fz * (fxy * fxz - fyz * fxx) + 2 * fx * fz * (fxy * fyz - fxz * fyy)) /
+                         (g2 * g2);
+    return 1.0 - phi * ksum + phi * phi * kprod;
+}
+
 template <class T>
 __global__ void __launch_bounds__(TUBE_BLOCK) k_tube_emit(Dims dm, double sx, double sy, double sz, double dx, T tw,
                                                           const T *__restrict__ g, const long *__restrict__ offsets,
                                                           double *px, double *py, double *pz, double *qx, double *qy,
-                                                          double *qz, double *w) {
+                                                          double *qz, double *w, int jacobian) {
     const long n = (long)dm.nx * dm.ny * dm.nz;
     const long I = blockIdx.x * (long)TUBE_BLOCK + threadIdx.x;
     const T v = I < n ? g[I] : (T)0;
@@ -377,7 +416,9 @@ __global__ void __launch_bounds__(TUBE_BLOCK) k_tube_emit(Dims dm, double sx, do
     qx[pos] = nxv;
     qy[pos] = nyv;
     qz[pos] = nzv;
-    w[pos] = 0.5 * (1.0 + cos(M_PI * vd / twd)) / twd;
+    double wv = 0.5 * (1.0 + cos(M_PI * vd / twd)) / twd;
+    if (jacobian) wv *= surface_jacobian(g, dm, i, j, k, dx, vd);
+    w[pos] = wv;
 }
 
 inline dim3 stencil_block() { return dim3(32, 4, 2); }
@@ -488,7 +529,7 @@ int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, 
 }
 
 template <class T>
-Tube *surface_t(Grid &g, int thickness, long *inclusion) {
+Tube *surface_t(Grid &g, int thickness, long *inclusion, bool jacobian) {
     Ctx *c = g.ctx;
     cudaStream_t s = c->stream;
     const double tw = thickness * g.dx;
@@ -557,7 +598,7 @@ Tube *surface_t(Grid &g, int thickness, long *inclusion) {
         ProfScope ps_(PROF_TUBE);
         (count_launch(), k_tube_emit<T><<<nb, TUBE_BLOCK, 0, s>>>(dm, g.sx, g.sy, g.sz, g.dx, (T)tw, G, offsets.ptr,
                                                                   t->x.ptr, t->y.ptr, t->z.ptr, t->nx.ptr, t->ny.ptr,
-                                                                  t->nz.ptr, t->w.ptr));
+                                                                  t->nz.ptr, t->w.ptr, jacobian ? 1 : 0));
         IBIM_CHECK_LAUNCH();
     } catch (...) {
         delete t;
@@ -660,10 +701,10 @@ void grid_copy(Grid &dst, const Grid &src) {
                               bytes, cudaMemcpyDeviceToDevice, dst.ctx->stream));
 }
 
-Tube *surface_extract(Grid &g, int thickness, long *inclusion) {
+Tube *surface_extract(Grid &g, int thickness, long *inclusion, bool jacobian) {
     IBIM_REQUIRE(thickness > 0, "thickness must be positive");
-    return g.prec == IBIM_PRECISION_FP64 ? surface_t<double>(g, thickness, inclusion)
-                                         : surface_t<float>(g, thickness, inclusion);
+    return g.prec == IBIM_PRECISION_FP64 ? surface_t<double>(g, thickness, inclusion, jacobian)
+                                         : surface_t<float>(g, thickness, inclusion, jacobian);
 }
 
 }  // namespace ibim

@@ -9,17 +9,16 @@
 //
 // One CTA takes one chunk of up to 128 pairs of an operator against up to four 128-row tiles of
 // the operator (four FP32 accumulators of 128 x 128 = all 512 TMEM columns), so each gathered
-// multipole is read once per chunk rather than once per row tile.  Operands are copied with
-// cp.async into shared memory in the canonical no-swizzle K-major layout (8-row x 16-byte core
-// matrices; K-direction core-matrix stride 128 B, row-group stride 256 B), 8 K-elements per
-// stage, five stage buffers.  One elected thread issues the MMAs of a stage and commits them to
-// that stage's mbarrier; two stages of MMAs may be queued while three stages of copies are in flight;
-// every wait is bounded and reports through an error flag instead of hanging.  The epilogue
-// reads the accumulators with tcgen05.ld (each warp its 32 TMEM lanes) and adds them into the
-// target nodes' local expansions.
+// multipole is read once per chunk rather than once per row tile.  Operands sit in shared memory
+// in the canonical no-swizzle K-major layout (8-row x 16-byte core matrices; K-direction
+// core-matrix stride 128 B, row-group stride 256 B), 8 K-elements per stage, five stage buffers.
+// The operator tiles are pre-packed in that layout and arrive by bulk asynchronous copies; the
+// multipole rows are gathered by cp.async.  Warp roles (copy issue, MMA issue, gather) meet only
+// on mbarriers; every wait is bounded and reports through an error flag instead of hanging.  The
+// epilogue reads the accumulators with tcgen05.ld (each warp its 32 TMEM lanes) and adds them
+// into the target nodes' local expansions.
 
 #include <cstdint>
-#include <cstdlib>
 
 #include "fmm_common.cuh"
 
@@ -29,7 +28,6 @@ namespace {
 
 constexpr int TC_M = 128, TC_N = 128, TC_KS = 8;   // rows per tile, pairs per chunk, K elements per stage
 constexpr int TC_NST = 5;                          // pipeline stages in shared memory
-constexpr int TC_QD = 2;                           // stages of MMAs allowed in flight
 constexpr int TC_RT = 4;                           // row tiles per CTA (4 x 128 TMEM columns)
 constexpr int TC_THREADS = 256;
 constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 4 KB per operand tile and stage
@@ -91,191 +89,10 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
 }
 
 // One CTA: one chunk of <= 128 V pairs of a single operator x up to TC_RT row tiles of 128
-// operator rows.  Stage st holds K elements [8 st, 8 st + 8) of A_hi, A_lo (per row tile) and of
-// B_hi, B_lo in buffer st % TC_NST.  The operator tiles are pre-packed as contiguous 4 KB blocks
-// in the shared-memory layout and arrive by bulk asynchronous copies that complete on the
-// stage's "full" mbarrier; the gathered multipole rows arrive by cp.async.  The MMAs of stage st
-// are committed to the stage's "done" mbarrier; while they run, the copies of stages st + 1 ..
-// st + 3 are in flight, and the buffer of stage st - 2 (whose MMAs are waited for) is refilled
-// with stage st + 3.
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
-             const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
-             const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
-    extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t done_bar[TC_NST], full_bar[TC_NST];
-    __shared__ uint32_t tmem_base;
-    __shared__ int src_s[TC_N], tgt_s[TC_N];
-    __shared__ int abort_s;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
-    const int tile0 = blockIdx.y * TC_RT;
-    const int rt = min(TC_RT, mtiles - tile0);
-    const int nstage = kpad / TC_KS;
-    constexpr int kStageBytes = (2 * TC_RT + 2) * TC_TILE_BYTES;
-    if (tid < TC_N) {
-        src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
-        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
-    }
-    if (tid == 0) {
-        abort_s = 0;
-        for (int i = 0; i < TC_NST; ++i) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done_bar[i])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[i])));
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(TC_RT * TC_N));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tmem_d = tmem_base;
-    // packed operator tiles: [op][row tile][stage][1024 floats]
-    const long atile0 = ((long)op * mtiles + tile0) * nstage;
-
-    auto load_stage = [&](int st) {
-        unsigned char *base = tc_smem + (st % TC_NST) * kStageBytes;
-        if (tid == 0) {
-            const uint32_t fb = smem_u32(&full_bar[st % TC_NST]);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
-                         "r"(2 * rt * TC_TILE_BYTES)
-                         : "memory");
-            for (int t = 0; t < rt; ++t) {
-                const long g = (atile0 + (long)t * nstage + st) * (TC_TILE_BYTES / 4);
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32(base + t * TC_TILE_BYTES)),
-                    "l"(a_hi + g), "r"(TC_TILE_BYTES), "r"(fb)
-                    : "memory");
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32(base + (rt + t) * TC_TILE_BYTES)),
-                    "l"(a_lo + g), "r"(TC_TILE_BYTES), "r"(fb)
-                    : "memory");
-            }
-        }
-        // multipole rows: 2 tiles x 128 rows x 2 pieces of 16 B
-        const int k0 = st * TC_KS;
-        for (int i = tid; i < 2 * 2 * TC_M; i += TC_THREADS) {
-            const int tile = i >> 8, row = (i >> 1) & (TC_M - 1), c = i & 1;
-            const uint32_t dst = smem_u32(base + (2 * rt + tile) * TC_TILE_BYTES + tile_off(row, c));
-            const int sn = src_s[row];
-            const float *B = tile == 0 ? b_hi : b_lo;
-            cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
-                       sn >= 0 ? 16u : 0u);
-        }
-        asm volatile("cp.async.commit_group;");
-    };
-
-    int issued = -1;       // last stage whose copies were issued
-    int full_waited = -1;  // last stage whose operator tiles thread 0 waited for
-    for (int s = 0; s < TC_NST - TC_QD; ++s) {
-        if (s < nstage) {
-            load_stage(s);
-            issued = s;
-        } else {
-            asm volatile("cp.async.commit_group;");
-        }
-    }
-    bool ok = true;
-    int last = -1;  // last stage whose MMAs were committed
-    for (int st = 0; st < nstage; ++st) {
-        const int ld = st + TC_NST - TC_QD;  // stage loaded now, into the buffer stage st - TC_QD used
-        bool w = true;
-        if (ld < nstage && st >= TC_QD)
-            w = mbar_wait(smem_u32(&done_bar[(st - TC_QD) % TC_NST]), (uint32_t)(((st - TC_QD) / TC_NST) & 1));
-        if (!__syncthreads_and((w && !abort_s) ? 1 : 0)) {
-            ok = false;
-            break;
-        }
-        if (ld < nstage) {
-            load_stage(ld);
-            issued = ld;
-        } else {
-            asm volatile("cp.async.commit_group;");
-        }
-        asm volatile("cp.async.wait_group %0;" ::"n"(TC_NST - TC_QD) : "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            const bool have = mbar_wait(smem_u32(&full_bar[st % TC_NST]), (uint32_t)((st / TC_NST) & 1));
-            if (have) {
-                full_waited = st;
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t base = smem_u32(tc_smem + (st % TC_NST) * kStageBytes);
-                const uint64_t bh = make_desc(base + (2 * rt) * TC_TILE_BYTES, 128, 256);
-                const uint64_t bl = make_desc(base + (2 * rt + 1) * TC_TILE_BYTES, 128, 256);
-                for (int t = 0; t < rt; ++t) {
-                    const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
-                    const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
-                    const uint32_t d = tmem_d + (uint32_t)(t * TC_N);
-                    mma_tf32(d, ah, bh, st > 0 ? 1u : 0u);
-                    mma_tf32(d, ah, bl, 1u);
-                    mma_tf32(d, al, bh, 1u);
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 smem_u32(&done_bar[st % TC_NST]))
-                             : "memory");
-                last = st;
-            } else {
-                abort_s = 1;
-            }
-        }
-    }
-    // drain: the multipole copies, then (thread 0) every operator-tile copy not yet waited for
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    if (tid == 0) {
-        for (int s = full_waited + 1; s <= issued; ++s)
-            if (!mbar_wait(smem_u32(&full_bar[s % TC_NST]), (uint32_t)((s / TC_NST) & 1))) ok = false;
-        if (last >= 0 && !mbar_wait(smem_u32(&done_bar[last % TC_NST]), (uint32_t)((last / TC_NST) & 1))) ok = false;
-        if (last != nstage - 1) ok = false;
-        if (!ok) {
-            abort_s = 1;
-            atomicExch(err, 1);
-        }
-    }
-    __syncthreads();
-    ok = !abort_s;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (ok) {
-        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (operator rows) of the row tiles t = w / 4, w / 4 + 2
-        const int lg = warp & 3;
-        for (int t = warp >> 2; t < rt; t += 2) {
-            const int row = (tile0 + t) * TC_M + 32 * lg + lane;
-            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(t * TC_N);
-#pragma unroll 1
-            for (int c0 = 0; c0 < TC_N; c0 += 16) {
-                uint32_t v[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-                    "%13, %14, %15}, [%16];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(taddr + (uint32_t)c0));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (row < n4) {
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int tg = tgt_s[c0 + q];
-                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]));
-                    }
-                }
-            }
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * TC_N));
-}
-
-// Warp-specialised form of the same contraction: warp 0 (one thread) issues the operator bulk
-// copies, warp 1 (one thread) issues the MMAs, warps 2-7 gather the multipole rows with cp.async.
+// operator rows.  Stage st holds K elements [8 st, 8 st + 8) of A_hi, A_lo (per row tile, pre-packed
+// as contiguous 4 KB blocks in the shared-memory layout) and of B_hi, B_lo in buffer st % TC_NST.
+// Warp-specialised: warp 0 (one thread) issues the operator bulk copies, warp 1 (one thread)
+// issues the MMAs, warps 2-7 gather the multipole rows with cp.async.
 // Per stage buffer: full_a (bulk copies, transaction count), full_b (the 192 gathering threads,
 // each after its own copies of the stage have landed and been fenced to the async proxy), empty
 // (tcgen05.commit of the stage's MMAs).  No CTA-wide barrier inside the K loop; every wait is
@@ -283,7 +100,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 constexpr int TC_BPROD = 192, TC_LAG = 2;
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_m2l_tc_ws(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+    k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
                 const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
                 const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -581,32 +398,55 @@ __device__ __forceinline__ int oz_scale_exp(double m) {
     return e;
 }
 
-// Operators (FP64, column-major n4 x n4 per op) -> digit tiles [op][row tile][stage][digit][4 KB]
-// in the shared-memory layout (tile_off with 16 K elements of 2 bytes per row) and the row scales
-// sig[op][mtiles * 128] = s_r 2^-48.  One thread per (op, row).
-__global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const double *__restrict__ ops, uint16_t *a,
-                              double *sig) {
-    const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M;
+// Row scales of the FP64 operators (column-major n4 x n4 per op): sig[op][mtiles * 128] =
+// s_r 2^-48 with s_r the power of two >= max_k |A_rk|, and the exponent of s_r.  One thread per
+// (op, row); neighbouring threads read neighbouring rows of a column.
+__global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const double *__restrict__ ops, double *sig, int *sexp) {
+    const int mpad = mtiles * OZ_M;
     const long total = (long)nops * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const int r = (int)(i % mpad), op = (int)(i / mpad);
-        const double *col0 = ops + (long)op * n4 * n4 + r;
         double m = 0.0;
-        if (r < n4)
+        if (r < n4) {
+            const double *col0 = ops + (long)op * n4 * n4 + r;
             for (int k = 0; k < n4; ++k) m = fmax(m, fabs(col0[(long)k * n4]));
+        }
         const int e = oz_scale_exp(m);
         sig[i] = ldexp(1.0, e - OZ_SCALE_EXP);
-        const int t = r / OZ_M, row = r % OZ_M;
-        for (int k = 0; k < kpad; ++k) {
-            const double x = (r < n4 && k < n4) ? ldexp(col0[(long)k * n4], -e) : 0.0;
+        sexp[i] = e;
+    }
+}
+
+// FP64 operators -> digit tiles [op][row tile][stage][digit][4 KB] in the shared-memory layout
+// (tile_off with 16 K elements of 2 bytes per row).  One thread per (op, row, group of 8 K
+// elements): 8 reads, then one 16-byte store per digit.
+__global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const double *__restrict__ ops,
+                              const int *__restrict__ sexp, uint4 *a) {
+    const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M, ngrp = kpad / 8;
+    const long total = (long)nops * ngrp * mpad;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(i % mpad);  // rows fastest: coalesced column reads
+        const long rest = i / mpad;
+        const int grp = (int)(rest % ngrp), op = (int)(rest / ngrp);
+        const int e = sexp[(long)op * mpad + r];
+        uint32_t w[OZ_S][4];
+        for (int q = 0; q < 8; ++q) {
+            const int k = grp * 8 + q;
+            const double x = (r < n4 && k < n4) ? ldexp(ops[(long)op * n4 * n4 + (long)k * n4 + r], -e) : 0.0;
             uint16_t dig[OZ_S];
             oz_digits(x, dig);
-            const int st = k / OZ_KS, kin = k % OZ_KS;
-            const long tbase = (((long)op * mtiles + t) * nstage + st) * OZ_S;
-            const uint32_t off = tile_off(row, kin >> 3) + 2 * (kin & 7);
 #pragma unroll
-            for (int d = 0; d < OZ_S; ++d) a[(tbase + d) * (OZ_ATILE / 2) + off / 2] = dig[d];
+            for (int d = 0; d < OZ_S; ++d) {
+                if (q & 1) w[d][q >> 1] |= (uint32_t)dig[d] << 16;
+                else w[d][q >> 1] = dig[d];
+            }
         }
+        const int t = r / OZ_M, row = r % OZ_M, st = grp / 2, half = grp & 1;
+        const long tbase = (((long)op * mtiles + t) * nstage + st) * OZ_S;
+        const uint32_t off = tile_off(row, half);  // byte offset of the 16-byte piece
+#pragma unroll
+        for (int d = 0; d < OZ_S; ++d)
+            a[((tbase + d) * OZ_ATILE + off) / 16] = make_uint4(w[d][0], w[d][1], w[d][2], w[d][3]);
     }
 }
 
@@ -831,7 +671,6 @@ void m2l_tc_prepare(Plan &P) {
     P.tc_err.zero();
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
     P.tc_ready = true;
 }
 
@@ -846,15 +685,9 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     {
         ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                       4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-        static const bool ws = std::getenv("IBIM_TC_NOWS") == nullptr;
-        if (ws)
-            (count_launch(), k_m2l_tc_ws<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
-                                 n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr,
-                                 P.tc_a_hi.ptr, P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
-        else
-            (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
-                                 n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr,
-                                 P.tc_a_hi.ptr, P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
+                             n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }
@@ -876,8 +709,14 @@ void m2l_oz_prepare(Plan &P) {
         P.tc_err.zero();
     }
     const long rows = (long)P.nops * P.oz_mtiles * OZ_M;
-    (count_launch(), k_pack_ops_oz<<<(int)std::min<long>((rows + 127) / 128, 64L * P.ctx->num_sms), 128, 0, s>>>(
-                         n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, P.oz_a.ptr, P.oz_sig.ptr));
+    DevBuf<int> sexp;
+    sexp.alloc((size_t)rows, s);
+    (count_launch(), k_scale_ops_oz<<<(int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms), 256, 0, s>>>(
+                         n4, P.oz_mtiles, P.nops, P.ops64.ptr, P.oz_sig.ptr, sexp.ptr));
+    const long pieces = rows * (P.oz_kpad / 8);
+    (count_launch(), k_pack_ops_oz<<<(int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms), 256, 0, s>>>(
+                         n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, sexp.ptr,
+                         reinterpret_cast<uint4 *>(P.oz_a.ptr)));
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmemBytes));
     P.oz_gen = P.ops64_gen;

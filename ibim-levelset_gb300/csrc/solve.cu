@@ -1,7 +1,7 @@
 // BIE operator, right-hand side, restarted GMRES, polarization energy and the whole solve.
 //
 //   bie_matvec     dmapping (electric.cpp:294-388): densities -> fused FMM -> combine
-//   k_rhs          load (electric.cpp:395-412), direct atom sums
+//   k_rhs          load (electric.cpp:395-412), direct atom sums (k_rhs32: FP32, mixed path)
 //   gmres          GMRES (gmres.cpp:50-164): modified Gram-Schmidt Arnoldi on the device with
 //                  fixed-order (deterministic) reductions; Givens rotations and the small
 //                  triangular solve on the host in FP64, as in the reference
@@ -80,6 +80,69 @@ __global__ void __launch_bounds__(256) k_rhs(long n, const double *__restrict__ 
     if (i < n) {
         b[i] = b1;
         b[n + i] = b2;
+    }
+}
+
+// load in FP32 for the mixed path: coordinates relative to the block's first point (differences
+// taken in FP64, so each point-atom offset carries FP32 rounding only), rsqrt in FP32, per-tile
+// partial sums added with Kahan compensation; the result is stored in FP64.
+__global__ void __launch_bounds__(256) k_rhs32(long n, const double *__restrict__ px, const double *__restrict__ py,
+                                               const double *__restrict__ pz, const double *__restrict__ nx,
+                                               const double *__restrict__ ny, const double *__restrict__ nz,
+                                               const double *__restrict__ atoms, int natoms, double c1, double c2,
+                                               double *b) {
+    __shared__ float A[4][256];
+    __shared__ double org[3];
+    const long i0 = blockIdx.x * (long)blockDim.x;
+    const long i = i0 + threadIdx.x;
+    if (threadIdx.x == 0) {
+        org[0] = px[i0];
+        org[1] = py[i0];
+        org[2] = pz[i0];
+    }
+    __syncthreads();
+    float X = 0.f, Y = 0.f, Z = 0.f, NX = 0.f, NY = 0.f, NZ = 0.f;
+    if (i < n) {
+        X = (float)(px[i] - org[0]);
+        Y = (float)(py[i] - org[1]);
+        Z = (float)(pz[i] - org[2]);
+        NX = (float)nx[i];
+        NY = (float)ny[i];
+        NZ = (float)nz[i];
+    }
+    float s1 = 0.f, k1 = 0.f, s2 = 0.f, k2 = 0.f;
+    for (int a0 = 0; a0 < natoms; a0 += 256) {
+        const int cnt = min(256, natoms - a0);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const double *at = atoms + 4 * (long)(a0 + threadIdx.x);
+            A[0][threadIdx.x] = (float)(at[0] - org[0]);
+            A[1][threadIdx.x] = (float)(at[1] - org[1]);
+            A[2][threadIdx.x] = (float)(at[2] - org[2]);
+            A[3][threadIdx.x] = (float)at[3];
+        }
+        __syncthreads();
+        if (i < n) {
+            float p1 = 0.f, p2 = 0.f;
+            for (int a = 0; a < cnt; ++a) {
+                const float dx = X - A[0][a], dy = Y - A[1][a], dz = Z - A[2][a];
+                const float ir = rsqrtf(dx * dx + dy * dy + dz * dz);
+                const float qi = A[3][a] * ir;
+                p1 += qi;
+                p2 += qi * ir * ir * (NX * dx + NY * dy + NZ * dz);
+            }
+            float y = p1 - k1, t = s1 + y;
+            k1 = (t - s1) - y;
+            s1 = t;
+            y = p2 - k2;
+            t = s2 + y;
+            k2 = (t - s2) - y;
+            s2 = t;
+        }
+    }
+    if (i < n) {
+        b[i] = c1 * (double)(s1 - k1);
+        b[n + i] = -c2 * (double)(s2 - k2);
     }
 }
 
@@ -200,22 +263,26 @@ void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *
 
 static void rhs_launch(Ctx *c, long n, const double *x, const double *y, const double *z, const double *nx,
                        const double *ny, const double *nz, const ibim_kernel_params &kp, const double *atoms4_dev,
-                       int natoms, double *b, cudaStream_t st) {
+                       int natoms, double *b, cudaStream_t st, bool fp32) {
     const double e1 = 0.5 * (1 + kp.dE / kp.dI), e2 = 0.5 * (1 + kp.dI / kp.dE);
     const double c1 = 1.0 / (kp.dI * 4.0 * M_PI * e1), c2 = 1.0 / (kp.dI * 4.0 * M_PI * e2);
     ProfScope ps_(PROF_RHS, 20.0 * n * (double)natoms, 0., st);
-    (count_launch(), k_rhs<<<div_up(n, 256), 256, 0, st>>>(n, x, y, z, nx, ny, nz, atoms4_dev, natoms, c1, c2, b));
+    if (fp32)
+        (count_launch(), k_rhs32<<<div_up(n, 256), 256, 0, st>>>(n, x, y, z, nx, ny, nz, atoms4_dev, natoms, c1, c2, b));
+    else
+        (count_launch(), k_rhs<<<div_up(n, 256), 256, 0, st>>>(n, x, y, z, nx, ny, nz, atoms4_dev, natoms, c1, c2, b));
     IBIM_CHECK_LAUNCH();
 }
 
 void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b) {
     rhs_launch(P.ctx, P.ns, P.sx.ptr, P.sy.ptr, P.sz.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, kp, atoms4_dev, natoms, b,
-               P.ctx->stream);
+               P.ctx->stream, P.precision == IBIM_PRECISION_MIXED);
 }
 
 void bie_rhs_tube(const Tube &t, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b,
-                  cudaStream_t st) {
-    rhs_launch(t.ctx, t.n, t.x.ptr, t.y.ptr, t.z.ptr, t.nx.ptr, t.ny.ptr, t.nz.ptr, kp, atoms4_dev, natoms, b, st);
+                  cudaStream_t st, int precision) {
+    rhs_launch(t.ctx, t.n, t.x.ptr, t.y.ptr, t.z.ptr, t.nx.ptr, t.ny.ptr, t.nz.ptr, kp, atoms4_dev, natoms, b, st,
+               precision == IBIM_PRECISION_MIXED);
 }
 
 // ---------------------------------------------------------------------------------------

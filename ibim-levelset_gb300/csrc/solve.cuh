@@ -30,14 +30,16 @@ struct Krylov {
 
 void permute(Ctx *c, long n, const int *perm, const double *in, double *out, bool scatter);
 void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision);
+// load (electric.cpp:395-412) in tree order; FP32 with compensated sums on a mixed plan.
 void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b);
 // b_tube: the right-hand side already computed in tube order (bie_rhs_tube), or null to compute
 // it here.
 void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, const double *charges_host,
                     int natoms, int restart, int maxiter, double tol, int precision, double *x_tree_out,
                     std::vector<double> *atom_pot, ibim_result &res, const double *b_tube = nullptr);
-// load (electric.cpp:395-412) on the tube points in tube order, on stream st.
+// load (electric.cpp:395-412) on the tube points in tube order, on stream st; FP32 with
+// compensated sums when precision is IBIM_PRECISION_MIXED.
 void bie_rhs_tube(const Tube &t, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b,
-                  cudaStream_t st);
+                  cudaStream_t st, int precision);
 
 }  // namespace ibim

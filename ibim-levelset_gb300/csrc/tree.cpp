@@ -34,24 +34,27 @@ struct BNode {
 
 struct Builder {
     const double *src, *tgt;
+    bool same = false;  // targets are the sources: one partition serves both
     int maxpoint, maxlevel;
     std::vector<BNode> nodes;
-    std::vector<int> sp, tp, tmp;
+    std::vector<int> *sp = nullptr, *tp = nullptr;
+    std::vector<int> tmp;
 
-    // assignChildren (bbfmm.cpp:67-138)
-    void split(int id) {
+    // assignChildren (bbfmm.cpp:67-138) for one node: leaf test, 8 children, partitions.
+    // Returns false when the node stays a leaf.
+    bool split_one(int id) {
         BNode &n0 = nodes[id];
         const int ns = n0.se - n0.sb;
         if (ns == 0) {
-            nodes[id].leaf = 1;
-            nodes[id].empty = 1;
-            return;
+            n0.leaf = 1;
+            n0.empty = 1;
+            return false;
         }
         if (ns <= maxpoint || n0.level == maxlevel) {
-            nodes[id].leaf = 1;
-            return;
+            n0.leaf = 1;
+            return false;
         }
-        int first = (int)nodes.size();
+        const int first = (int)nodes.size();
         for (int i = 0; i < 8; ++i) {
             BNode q;
             const BNode &p = nodes[id];
@@ -71,8 +74,20 @@ struct Builder {
             nodes.push_back(q);
         }
         for (int i = 0; i < 8; ++i) nodes[id].child[i] = first + i;
-        partition(nodes[id], first, sp, src, true);
-        partition(nodes[id], first, tp, tgt, false);
+        partition(nodes[id], first, *sp, src, true);
+        if (same) {
+            for (int i = 0; i < 8; ++i) {
+                nodes[first + i].tb = nodes[first + i].sb;
+                nodes[first + i].te = nodes[first + i].se;
+            }
+        } else {
+            partition(nodes[id], first, *tp, tgt, false);
+        }
+        return true;
+    }
+    void split(int id) {
+        if (!split_one(id)) return;
+        const int first = nodes[id].child[0];
         for (int i = 0; i < 8; ++i) split(first + i);
     }
 
@@ -97,6 +112,32 @@ struct Builder {
         std::copy(tmp.begin(), tmp.begin() + (e - b), perm.begin() + b);
     }
 };
+
+// The reference's node ids: creation order of its recursive assignChildren, which gives a
+// node's 8 children consecutive ids when the node is split and then recurses into child 0..7.
+void reference_ids(const std::vector<BNode> &nodes, std::vector<int> &ref) {
+    ref.assign(nodes.size(), 0);
+    int next = 1;
+    std::vector<std::pair<int, int>> stack{{0, 0}};  // (node, next child to descend into)
+    while (!stack.empty()) {
+        auto &top = stack.back();
+        const BNode &n = nodes[top.first];
+        if (n.child[0] < 0) {
+            stack.pop_back();
+            continue;
+        }
+        if (top.second == 0) {
+            for (int i = 0; i < 8; ++i) ref[n.child[i]] = next + i;
+            next += 8;
+        }
+        if (top.second == 8) {
+            stack.pop_back();
+            continue;
+        }
+        const int c = n.child[top.second++];
+        stack.push_back({c, 0});
+    }
+}
 
 }  // namespace
 
@@ -131,13 +172,57 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     root.se = (int)ns;
     root.tb = 0;
     root.te = (int)nt;
-    B.sp.resize(ns);
-    B.tp.resize(nt);
-    for (long i = 0; i < ns; ++i) B.sp[i] = (int)i;
-    for (long i = 0; i < nt; ++i) B.tp[i] = (int)i;
+    std::vector<int> sp(ns), tp;
+    for (long i = 0; i < ns; ++i) sp[i] = (int)i;
+    B.same = (tgt == src && nt == ns);
+    if (!B.same) {
+        tp.resize(nt);
+        for (long i = 0; i < nt; ++i) tp[i] = (int)i;
+    }
+    B.sp = &sp;
+    B.tp = B.same ? &sp : &tp;
     B.nodes.reserve(1024);
     B.nodes.push_back(root);
-    B.split(0);
+    // the top two levels serially, then the subtrees below them in parallel (disjoint point
+    // ranges), each into its own node list, appended in subtree order
+    std::vector<int> frontier{0};
+    for (int l = 0; l < 2; ++l) {
+        std::vector<int> next;
+        for (int id : frontier)
+            if (B.split_one(id))
+                for (int i = 0; i < 8; ++i) next.push_back(B.nodes[id].child[i]);
+        frontier.swap(next);
+    }
+    std::vector<Builder> sub(frontier.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)frontier.size(); ++k) {
+        Builder &S = sub[k];
+        S.src = B.src;
+        S.tgt = B.tgt;
+        S.same = B.same;
+        S.maxpoint = B.maxpoint;
+        S.maxlevel = B.maxlevel;
+        S.sp = B.sp;
+        S.tp = B.tp;
+        S.nodes.push_back(B.nodes[frontier[k]]);
+        S.nodes[0].parent = -1;
+        S.split(0);
+    }
+    for (size_t k = 0; k < frontier.size(); ++k) {
+        const int g = frontier[k];
+        const int base = (int)B.nodes.size() - 1;  // local j >= 1 -> base + j
+        auto map = [&](int j) { return j == 0 ? g : base + j; };
+        const std::vector<BNode> &L = sub[k].nodes;
+        B.nodes[g].leaf = L[0].leaf;
+        B.nodes[g].empty = L[0].empty;
+        for (int i = 0; i < 8; ++i) B.nodes[g].child[i] = L[0].child[i] < 0 ? -1 : map(L[0].child[i]);
+        for (size_t j = 1; j < L.size(); ++j) {
+            BNode q = L[j];
+            q.parent = map(q.parent);
+            for (int i = 0; i < 8; ++i) q.child[i] = q.child[i] < 0 ? -1 : map(q.child[i]);
+            B.nodes.push_back(q);
+        }
+    }
 
     const int nn = (int)B.nodes.size();
     int depth = 0;
@@ -165,29 +250,52 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         return (touch[0] && ot[1] && ot[2]) || (touch[1] && ot[0] && ot[2]) || (touch[2] && ot[0] && ot[1]);
     };
     std::vector<std::vector<int>> U(nn), V(nn), W(nn), X(nn);
-    // nodes are independent: build their lists in parallel
-#pragma omp parallel for schedule(dynamic, 64)
-    for (int id = 0; id < nn; ++id) {
+    // The candidates of a node are the 6 x 6 x 6 same-level cells around its parent, i.e. the
+    // children of the parent's 3 x 3 x 3 neighbourhood: findNode is resolved once per parent
+    // neighbour and shared by the 8 siblings.  A coarser leaf met by several candidates is
+    // listed once (the reference's lists are sets).
+    std::vector<int> parents;
+    for (int id = 0; id < nn; ++id)
+        if (B.nodes[id].child[0] >= 0) parents.push_back(id);
+    auto push_once = [](std::vector<int> &v, int x) {
+        if (std::find(v.begin(), v.end(), x) == v.end()) v.push_back(x);
+    };
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int k = 0; k < (int)parents.size(); ++k) {
+        const int pid = parents[k];
+        const BNode &pn = B.nodes[pid];
+        const int pside = 1 << pn.level;
+        int nb[27];
+        for (int d = 0; d < 27; ++d) {
+            const int c[3] = {pn.coord[0] + d % 3 - 1, pn.coord[1] + (d / 3) % 3 - 1, pn.coord[2] + d / 9 - 1};
+            nb[d] = (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= pside || c[1] >= pside || c[2] >= pside)
+                        ? -1
+                        : find_node(pn.level, c);
+        }
         std::vector<int> queue;
-        const BNode &n = B.nodes[id];
-        V[id].reserve(64);
-        if (n.parent != -1) {
-            const BNode &pn = B.nodes[n.parent];
-            const int side = 1 << n.level;
+        for (int ci = 0; ci < 8; ++ci) {
+            const int id = pn.child[ci];
+            const BNode &n = B.nodes[id];
+            V[id].reserve(64);
             for (int xi = -2; xi < 4; ++xi)
                 for (int yi = -2; yi < 4; ++yi)
                     for (int zi = -2; zi < 4; ++zi) {
+                        const int m = nb[(xi >= 0 ? xi / 2 : -1) + 1 + 3 * ((yi >= 0 ? yi / 2 : -1) + 1) +
+                                         9 * ((zi >= 0 ? zi / 2 : -1) + 1)];
+                        if (m < 0) continue;
                         const int c[3] = {2 * pn.coord[0] + xi, 2 * pn.coord[1] + yi, 2 * pn.coord[2] + zi};
-                        if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= side || c[1] >= side || c[2] >= side) continue;
                         if (c[0] == n.coord[0] && c[1] == n.coord[1] && c[2] == n.coord[2]) continue;
-                        const int cid = find_node(n.level, c);
+                        const BNode &mn = B.nodes[m];
+                        const int cid = (mn.level == pn.level && mn.child[0] >= 0)
+                                            ? mn.child[((c[2] & 1) << 2) | ((c[1] & 1) << 1) | (c[0] & 1)]
+                                            : m;
                         const bool adj = adjacent(id, cid);
                         const BNode &cn = B.nodes[cid];
                         if (cn.level < n.level) {
                             if (adj) {
-                                if (cn.leaf) U[id].push_back(cid);
+                                if (cn.leaf) push_once(U[id], cid);
                             } else {
-                                X[id].push_back(cid);
+                                push_once(X[id], cid);
                             }
                         }
                         if (cn.level == n.level) {
@@ -209,13 +317,19 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
                             }
                         }
                     }
+            if (n.leaf) U[id].push_back(id);
         }
-        if (n.leaf) U[id].push_back(id);
     }
+    if (B.nodes[0].leaf) U[0].push_back(0);
+    std::vector<int> ref_of;
+    reference_ids(B.nodes, ref_of);
     // level-ordered renumbering
     std::vector<int> order(nn);
     for (int i = 0; i < nn; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return B.nodes[a].level < B.nodes[b].level; });
+    // by level, then by the reference's id (its creation order)
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return B.nodes[a].level != B.nodes[b].level ? B.nodes[a].level < B.nodes[b].level : ref_of[a] < ref_of[b];
+    });
     std::vector<int> newid(nn);
     for (int i = 0; i < nn; ++i) newid[order[i]] = i;
 
@@ -256,12 +370,10 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         T.src_end[i] = n.se;
         T.tgt_begin[i] = n.tb;
         T.tgt_end[i] = n.te;
-        T.ref_id[i] = order[i];
+        T.ref_id[i] = ref_of[order[i]];
         auto remap = [&](const std::vector<int> &in, std::vector<int> &out) {
-            out.reserve(in.size());
-            for (int v : in) out.push_back(newid[v]);
-            std::sort(out.begin(), out.end());
-            out.erase(std::unique(out.begin(), out.end()), out.end());
+            out.resize(in.size());
+            for (size_t q = 0; q < in.size(); ++q) out[q] = newid[in[q]];
         };
         remap(U[order[i]], T.U[i]);
         remap(V[order[i]], T.V[i]);
@@ -269,8 +381,8 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         remap(X[order[i]], T.X[i]);
     }
     for (int l = 0; l < T.nlevels; ++l) T.level_begin[l + 1] += T.level_begin[l];
-    T.src_perm = std::move(B.sp);
-    T.tgt_perm = std::move(B.tp);
+    T.tgt_perm = B.same ? sp : std::move(tp);
+    T.src_perm = std::move(sp);
     return T;
 }
 

@@ -41,7 +41,8 @@ EXPORTS = [
     "ibim_ctx_create", "ibim_ctx_destroy", "ibim_last_error", "ibim_status_string", "ibim_config_default",
     "ibim_grid_create", "ibim_grid_destroy", "ibim_grid_upload", "ibim_grid_download", "ibim_grid_scale",
     "ibim_grid_copy", "ibim_levelset_expand", "ibim_levelset_evolve", "ibim_levelset_reinitialize",
-    "ibim_levelset_count_gradient", "ibim_levelset_build", "ibim_surface_extract", "ibim_tube_create",
+    "ibim_levelset_count_gradient", "ibim_levelset_build", "ibim_surface_extract", "ibim_surface_extract_jacobian",
+    "ibim_tube_create",
     "ibim_tube_destroy", "ibim_tube_size", "ibim_tube_download", "ibim_fmm_plan", "ibim_plan_destroy",
     "ibim_plan_stats", "ibim_plan_lists", "ibim_fmm_apply", "ibim_bie_matvec", "ibim_bie_rhs", "ibim_gmres_solve",
     "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host", "ibim_ctx_stream",
@@ -60,7 +61,8 @@ class IbimError(RuntimeError):
 
 
 class KernelParams(C.Structure):
-    _fields_ = [("kappa", C.c_double), ("dE", C.c_double), ("dI", C.c_double), ("tau", C.c_double)]
+    _fields_ = [("kappa", C.c_double), ("dE", C.c_double), ("dI", C.c_double), ("tau", C.c_double),
+                ("k3_scaled", C.c_int)]
 
 
 class Config(C.Structure):
@@ -68,7 +70,7 @@ class Config(C.Structure):
                 ("init", C.c_double), ("probe", C.c_double), ("reinit_t", C.c_double), ("thickness", C.c_int),
                 ("thres", C.c_double), ("np", C.c_int), ("maxpoint", C.c_int), ("maxlevel", C.c_int),
                 ("kp", KernelParams), ("restart", C.c_int), ("maxiter", C.c_int), ("tol", C.c_double),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("jacobian", C.c_int)]
 
 
 class Result(C.Structure):
@@ -122,6 +124,7 @@ def lib():
         "ibim_levelset_count_gradient": ([_vp, C.c_double, C.c_double, _lp, _lp, _dp], C.c_int),
         "ibim_levelset_build": ([_vp, _dp, _dp, C.c_int, C.POINTER(Config), C.POINTER(_vp), _ip], C.c_int),
         "ibim_surface_extract": ([_vp, C.c_int, C.POINTER(_vp), _lp, _lp], C.c_int),
+        "ibim_surface_extract_jacobian": ([_vp, C.c_int, C.c_int, C.POINTER(_vp), _lp, _lp], C.c_int),
         "ibim_tube_create": ([_vp, _dp, _dp, _dp, C.c_long, C.c_double, C.POINTER(_vp)], C.c_int),
         "ibim_tube_destroy": ([_vp], C.c_int),
         "ibim_tube_size": ([_vp], C.c_long),
@@ -183,15 +186,16 @@ def default_config(**kw) -> Config:
             cfg.lo = (C.c_double * 3)(*v)
         elif k == "n":
             cfg.n = (C.c_int * 3)(*v)
-        elif k in ("kappa", "dE", "dI", "tau"):
+        elif k in ("kappa", "dE", "dI", "tau", "k3_scaled"):
             setattr(cfg.kp, k, v)
         else:
             setattr(cfg, k, v)
     return cfg
 
 
-def kernel_params(kappa=0.0, dE=80.0, dI=1.0, tau=1.0) -> KernelParams:
-    return KernelParams(kappa, dE, dI, tau)
+def kernel_params(kappa=0.0, dE=80.0, dI=1.0, tau=1.0, k3_scaled=0) -> KernelParams:
+    """k3_scaled = 1 selects the opt-in K3 / (4 pi); 0 is the reference."""
+    return KernelParams(kappa, dE, dI, tau, k3_scaled)
 
 
 class Context:
@@ -331,10 +335,14 @@ class Grid:
                                                   C.byref(acc)))
         return bad.value, tot.value, acc.value
 
-    def surface(self, thickness) -> "Tube":
+    def surface(self, thickness, jacobian=False) -> "Tube":
+        """Tube quadrature (Surface); jacobian=True multiplies the weights by the surface Jacobian."""
         t = _vp()
         n, inc = C.c_long(0), C.c_long(0)
-        _check(lib().ibim_surface_extract(self.h, thickness, C.byref(t), C.byref(n), C.byref(inc)))
+        if jacobian:
+            _check(lib().ibim_surface_extract_jacobian(self.h, thickness, 1, C.byref(t), C.byref(n), C.byref(inc)))
+        else:
+            _check(lib().ibim_surface_extract(self.h, thickness, C.byref(t), C.byref(n), C.byref(inc)))
         tb = Tube(self.ctx, t)
         tb.inclusion = inc.value
         return tb

@@ -68,9 +68,12 @@ typedef struct ibim_grid_s *ibim_grid;
 typedef struct ibim_tube_s *ibim_tube;
 typedef struct ibim_plan_s *ibim_plan;
 
-/* Solvent / kernel parameters (electric.cpp:52-58: solvent_kappa, solvent_dE, solvent_dI, tau). */
+/* Solvent / kernel parameters (electric.cpp:52-58: solvent_kappa, solvent_dE, solvent_dI, tau).
+ * k3_scaled (opt-in, 0 = the reference): 1 divides the K3 kernels by 4 pi like K1, K2 and K4
+ * (electric.cpp:103-268 writes K3 without the factor; the difference vanishes at kappa = 0). */
 typedef struct {
     double kappa, dE, dI, tau;
+    int k3_scaled;
 } ibim_kernel_params;
 
 /* Everything input.cfg carries for this path, with the geometry explicit. */
@@ -92,6 +95,9 @@ typedef struct {
     int maxiter;       /* gmres_maxiter */
     double tol;        /* gmres_tol */
     int precision;     /* IBIM_PRECISION_* */
+    int jacobian;      /* opt-in, 0 = the reference: 1 multiplies each tube weight by the surface
+                          Jacobian 1 - phi (k1 + k2) + phi^2 k1 k2 of the level set through the
+                          grid point (levelset.cpp:576 has no Jacobian) */
 } ibim_config;
 
 typedef struct {
@@ -173,6 +179,10 @@ int ibim_levelset_evolve_static(double *grid_dev, int nx, int ny, int nz, double
 
 /* ---- tube quadrature: replaces Surface (levelset.h:62-72, levelset.cpp:437-586) ---- */
 int ibim_surface_extract(ibim_grid g, int thickness, ibim_tube *out, long *n_points, long *inclusion);
+/* Surface extraction with the opt-in surface Jacobian (jacobian = 1, see ibim_config.jacobian;
+ * no counterpart in the reference: its weights stop at levelset.cpp:576). */
+int ibim_surface_extract_jacobian(ibim_grid g, int thickness, int jacobian, ibim_tube *out, long *n_points,
+                                  long *inclusion);
 /* A tube from host arrays (points (n,3), normals (n,3), raw cosine weights (n)) on spacing h. */
 int ibim_tube_create(ibim_ctx ctx, const double *points, const double *normals, const double *weights, long n,
                      double h, ibim_tube *out);

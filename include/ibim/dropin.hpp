@@ -165,10 +165,12 @@ class levelset {
     double dx, sx, sy, sz;
     int Nx, Ny, Nz, bandwidth, thickness;
     double thres;
+    int jacobian = 0;  // opt-in key `jacobian`: surface Jacobian in the tube weights
     levelset(int nx, int ny, int nz, int band, double sx_, double sy_, double sz_, double dx_, Config &cfg)
         : dx(dx_), sx(sx_), sy(sy_), sz(sz_), Nx(nx), Ny(ny), Nz(nz), bandwidth(band) {
         thickness = (int)cfg.num("lvlset_thickness");
         thres = cfg.num("lvlset_thres");
+        if (cfg.options.count("jacobian")) jacobian = (int)cfg.num("jacobian");
     }
     Grid *make_grid(double val) const { return new Grid(val, Nx, Ny, Nz, sx, sy, sz, dx); }
     void expand(Molecule &mol, Grid &g, double probe) {
@@ -198,7 +200,7 @@ class Surface {
     double dx;
     Surface(Grid &g, levelset &ls, double /*s*/) : dx(ls.dx) {
         long n = 0;
-        check(ibim_surface_extract(g.h, ls.thickness, &tube, &n, &inclusion));
+        check(ibim_surface_extract_jacobian(g.h, ls.thickness, ls.jacobian, &tube, &n, &inclusion));
         std::vector<double> p(3 * (size_t)n), q(3 * (size_t)n);
         weight.resize(n);
         check(ibim_tube_download(tube, p.data(), q.data(), weight.data()));
@@ -229,7 +231,7 @@ typedef std::vector<double> Vector;
 class kernel {
   public:
     int eval = -1;
-    ibim_kernel_params kp{0.0, 80.0, 1.0, 1.0};
+    ibim_kernel_params kp{0.0, 80.0, 1.0, 1.0, 0};
     double h = 1.0;
     kernel() = default;
     kernel(const kernel &) = delete;
@@ -277,6 +279,9 @@ inline ibim_config config_from(const Config &cfg, const levelset &ls) {
     c.kp.dE = cfg.num("solvent_dE");
     c.kp.dI = cfg.num("solvent_dI");
     c.kp.tau = cfg.num("tau");
+    // opt-in modes with no counterpart in the reference (absent keys keep its behaviour)
+    if (cfg.options.count("k3_scaled")) c.kp.k3_scaled = (int)cfg.num("k3_scaled");
+    c.jacobian = ls.jacobian;
     c.restart = (int)cfg.num("gmres_restart");
     c.maxiter = (int)cfg.num("gmres_maxiter");
     c.tol = cfg.num("gmres_tol");

@@ -86,3 +86,18 @@ def test_mixed_levelset_close_to_fp64(ctx, golden, case):
     t32 = g32.surface(P["thickness"])
     assert abs(len(t64) - len(t32)) <= max(2, 0.002 * len(t64))
     assert abs(t64.inclusion - t32.inclusion) <= max(2, 0.01 * max(1, t64.inclusion))
+
+
+@pytest.mark.parametrize("case", ["synth30", "p1hje"])
+def test_mixed_rhs_close_to_fp64(ctx, golden, case):
+    """FP32 load (electric.cpp:395-412) with compensated sums: ~1e-7 of the FP64 right-hand side."""
+    G = golden(case)
+    P = G["params"]
+    t = tube_of(ctx, G)
+    kp = ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"])
+    b64 = t.plan(P["np"], P["maxpoint"], P["maxlevel"]).rhs(kp, G["centers"], G["charges"])
+    b32 = t.plan(P["np"], P["maxpoint"], P["maxlevel"], precision=ibim.PRECISION_MIXED).rhs(kp, G["centers"],
+                                                                                            G["charges"])
+    n = len(b64) // 2
+    for part in (slice(0, n), slice(n, 2 * n)):
+        assert np.abs(b32[part] - b64[part]).max() <= 2e-6 * np.abs(b64[part]).max()

@@ -1,0 +1,114 @@
+"""Opt-in modes with no counterpart in the reference (defaults keep its behaviour):
+
+* surface Jacobian in the tube weights (ibim_config.jacobian, ibim_surface_extract_jacobian): the
+  reference weights stop at the smoothed delta (levelset.cpp:576), which overstates the area of
+  a curved surface by O(tube width x curvature);
+* K3 divided by 4 pi (ibim_kernel_params.k3_scaled) like K1, K2 and K4 (electric.cpp:103-268
+  writes K3 without the factor; K3 vanishes at kappa = 0).
+
+Pins: the sphere's area 4 pi R^2, the Born energy -(q^2 / 8 pi R)(1/eps_I - 1/eps_E) and the
+Kirkwood (Debye-Hueckel) energy -(q^2 / 8 pi R)(1/eps_I - 1/(eps_E (1 + kappa R))) of one ion."""
+
+import math
+
+import numpy as np
+import pytest
+
+import ibim
+from conftest import config_for
+from test_oracle_golden import bie_densities, probe_vector
+
+pytestmark = pytest.mark.gpu
+
+R_ION = 2.0
+
+
+def born_config(G, **kw):
+    P = dict(G["params"])
+    P.update(kw)
+    cfg = config_for(P)
+    for k, v in kw.items():
+        if k in ("jacobian",):
+            setattr(cfg, k, v)
+        if k in ("k3_scaled",):
+            cfg.kp.k3_scaled = v
+    return cfg
+
+
+def analytic(kappa, dI, dE, q=1.0, R=R_ION):
+    return -(q * q / (8 * math.pi * R)) * (1.0 / dI - 1.0 / (dE * (1.0 + kappa * R)))
+
+
+def test_jacobian_area_of_the_sphere(ctx, golden):
+    G = golden("born")
+    P = G["params"]
+    g, _ = ctx.levelset(G["centers"], G["radii"], config_for(P))
+    exact = 4 * math.pi * R_ION ** 2
+    areas = {}
+    for jac in (False, True):
+        _, _, w = g.surface(P["thickness"], jacobian=jac).download()
+        areas[jac] = w.sum() * P["h"] ** 3
+    g.close()
+    err_plain = abs(areas[False] - exact) / exact
+    err_jac = abs(areas[True] - exact) / exact
+    assert err_jac < 0.2 * err_plain, (areas, exact)
+    assert err_jac < 2e-3, (areas, exact)
+
+
+def test_jacobian_improves_born_energy(ctx, golden):
+    G = golden("born")
+    E0 = analytic(0.0, G["params"]["dI"], G["params"]["dE"])
+    e = {}
+    for jac in (0, 1):
+        r = ctx.solve(G["centers"], G["charges"], G["radii"], born_config(G, jacobian=jac))
+        assert r["gmres_status"] == 0
+        e[jac] = r["energy"]
+    err0, err1 = abs(e[0] - E0) / abs(E0), abs(e[1] - E0) / abs(E0)
+    print("born", e, E0, err0, err1)
+    assert err1 < err0, (e, E0)
+
+
+@pytest.mark.parametrize("kernel", ["K3xx", "K3yy", "K3zz", "K3xy", "K3yz", "K3zx", "K3yx", "K3zy", "K3xz"])
+def test_k3_scaled_is_the_reference_over_4pi(ctx, golden, kernel):
+    G = golden("p1hje")
+    P = G["params"]
+    s = G["surface"]
+    t = ctx.tube(s[:, :3], s[:, 3:6], s[:, 6], P["h"])
+    plan = t.plan(P["np"], P["maxpoint"], P["maxlevel"])
+    q = np.sin(0.37 * np.arange(len(s))) * s[:, 6]
+    k = ibim.KERNELS.index(kernel)
+    a = plan.apply(k, ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"]), q)
+    b = plan.apply(k, ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"], k3_scaled=1), q)
+    assert np.abs(b * 4 * math.pi - a).max() <= 1e-12 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("kernel", ["K1x", "K2", "K4z"])
+def test_k3_scaled_leaves_other_kernels(ctx, golden, kernel):
+    G = golden("p1hje")
+    P = G["params"]
+    s = G["surface"]
+    t = ctx.tube(s[:, :3], s[:, 3:6], s[:, 6], P["h"])
+    plan = t.plan(P["np"], P["maxpoint"], P["maxlevel"])
+    q = np.sin(0.37 * np.arange(len(s))) * s[:, 6]
+    k = ibim.KERNELS.index(kernel)
+    a = plan.apply(k, ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"]), q)
+    b = plan.apply(k, ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"], k3_scaled=1), q)
+    assert np.abs(b - a).max() <= 1e-14 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("kappa", [0.1, 0.5])
+def test_kirkwood_sphere(ctx, golden, kappa):
+    """One ion in salt: the energies of both K3 forms against the analytic Kirkwood energy."""
+    G = golden("born")
+    P = G["params"]
+    E0 = analytic(kappa, P["dI"], P["dE"])
+    e = {}
+    for k3 in (0, 1):
+        for jac in (0, 1):
+            r = ctx.solve(G["centers"], G["charges"], G["radii"], born_config(G, kappa=kappa, k3_scaled=k3,
+                                                                              jacobian=jac))
+            assert r["gmres_status"] == 0
+            e[(k3, jac)] = r["energy"]
+    errs = {k: abs(v - E0) / abs(E0) for k, v in e.items()}
+    print("kirkwood", kappa, E0, e, errs)
+    assert errs[(1, 1)] < 0.02, errs
