@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libibim_gb300.so")
-SOURCES = ["levelset.cu", "tree.cpp", "fmm.cu", "fmm_mixed.cu", "m2l_tc.cu", "solve.cu", "capi.cu"]
+SOURCES = ["levelset.cu", "tree.cpp", "fmm.cu", "fmm_mixed.cu", "m2l_tc.cu", "solve.cu", "capi.cu", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xcompiler", "-Wno-unused-function", "--expt-relaxed-constexpr"]
@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         for s, log in zip(SOURCES, logs):
             print(f"== {s}\n{log}")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *[_obj(s) for s in SOURCES], "-lcudart", "-lgomp"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *[_obj(s) for s in SOURCES], "-lcudart", "-lgomp", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

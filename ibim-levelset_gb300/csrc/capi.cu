@@ -110,7 +110,9 @@ static void check_config(const ibim_config &cfg) {
     IBIM_REQUIRE(cfg.restart > 0 && cfg.maxiter > 0, "gmres_restart and gmres_maxiter must be positive");
     IBIM_REQUIRE(cfg.kp.dE > 0 && cfg.kp.dI > 0, "solvent_dE and solvent_dI must be positive");
     IBIM_REQUIRE(cfg.kp.kappa >= 0 && cfg.kp.tau >= 0, "solvent_kappa and tau must be non-negative");
-    IBIM_REQUIRE(cfg.precision == IBIM_PRECISION_FP64 || cfg.precision == IBIM_PRECISION_MIXED, "unknown precision");
+    IBIM_REQUIRE(cfg.precision == IBIM_PRECISION_FP64 || cfg.precision == IBIM_PRECISION_MIXED ||
+                     cfg.precision == IBIM_PRECISION_FP64_TC,
+                 "unknown precision");
     IBIM_REQUIRE(cfg.jacobian == 0 || cfg.jacobian == 1, "jacobian must be 0 or 1");
     IBIM_REQUIRE(cfg.kp.k3_scaled == 0 || cfg.kp.k3_scaled == 1, "k3_scaled must be 0 or 1");
 }
@@ -127,14 +129,15 @@ static void fill_plan_stats(const Plan &P, ibim_result &res) {
 // main.cpp:45-60 with s = 1
 static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *radii_dev, int natoms,
                                const ibim_config &cfg, int steps[2]) {
-    Grid *g = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, cfg.init,
-                          cfg.precision);
+    // FP32 grids on the mixed path only
+    const int gprec = cfg.precision == IBIM_PRECISION_MIXED ? IBIM_PRECISION_MIXED : IBIM_PRECISION_FP64;
+    Grid *g = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, cfg.init, gprec);
     Grid *phi0 = nullptr;
     try {
         levelset_expand(*g, centers_dev, radii_dev, natoms, cfg.probe, cfg.band);
         levelset_evolve(*g, cfg.probe, 1.0, 0.2);
         grid_scale(*g, -1.0);
-        phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0., cfg.precision);
+        phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0., gprec);
         grid_copy(*phi0, *g);
         steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
         grid_copy(*phi0, *g);
@@ -189,8 +192,20 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
         auto w0 = std::chrono::steady_clock::now();
         P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
-        fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
-        if (cfg.precision != IBIM_PRECISION_FP64) fmm_prepare_operators(*P, cfg.kp, cfg.precision);
+        if (cfg.precision == IBIM_PRECISION_FP64 || !m2l_tc_supported()) {
+            fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
+            if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
+        } else {
+            // digit images for the FP64-class operator (the mixed path's residual), then the
+            // TF32 images from FP32 operators rounded from the FP64 ones; afterwards only the
+            // images are used, so the FP64 operators are released
+            // (order keeps the peak at 26 bytes per operator entry: FP64 8 + digits 14 + FP32 4,
+            // then digits + FP32 + TF32 images 8 once the FP64 operators are gone)
+            fmm_ensure_oz_images(*P, cfg.kp);
+            if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
+            fmm_release_fp64_operators(*P);
+            if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);
+        }
         IBIM_CUDA(cudaStreamSynchronize(s));
         res.t_plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
         IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
@@ -299,6 +314,13 @@ int ibim_ctx_create(int device, ibim_ctx *out) {
             IBIM_CUDA(cudaDeviceGetAttribute(&h->c.num_sms, cudaDevAttrMultiProcessorCount, device));
             IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
             IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.aux, cudaStreamNonBlocking));
+            // device memory freed by a solve stays in the stream-ordered pool for the next one
+            // instead of going back to the driver at every synchronisation (a solve allocates
+            // several GB of operator images); ibim_ctx_trim hands it back
+            cudaMemPool_t pool;
+            IBIM_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+            uint64_t keep = UINT64_MAX;
+            IBIM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
             IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_fork, cudaEventDisableTiming));
             IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_join, cudaEventDisableTiming));
         } catch (...) {
@@ -326,6 +348,18 @@ int ibim_ctx_destroy(ibim_ctx ctx) {
 }
 
 void *ibim_ctx_stream(ibim_ctx ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+int ibim_ctx_trim(ibim_ctx ctx) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx, "null context");
+        bind(&ctx->c);
+        IBIM_CUDA(cudaStreamSynchronize(ctx->c.stream));
+        IBIM_CUDA(cudaStreamSynchronize(ctx->c.aux));
+        cudaMemPool_t pool;
+        IBIM_CUDA(cudaDeviceGetDefaultMemPool(&pool, ctx->c.device));
+        IBIM_CUDA(cudaMemPoolTrimTo(pool, 0));
+    });
+}
 
 long ibim_launch_count(void) { return launch_count(); }
 

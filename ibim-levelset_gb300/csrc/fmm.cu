@@ -844,13 +844,58 @@ void fmm_prepare_operators(Plan &P, const ibim_kernel_params &kp, int precision)
     }
     for (int i = 0; i < 5; ++i) cache[i] = key[i];
     (is64 ? P.ops64_ready : P.ops32_ready) = true;
-    if (is64) P.ops64_gen++;
+}
+
+static void kp_key(const ibim_kernel_params &kp, double key[5]) {
+    key[0] = kp.kappa;
+    key[1] = kp.dE;
+    key[2] = kp.dI;
+    key[3] = kp.tau;
+    key[4] = (double)kp.k3_scaled;
+}
+
+static bool same_key(const double a[5], const double b[5]) {
+    for (int i = 0; i < 5; ++i)
+        if (a[i] != b[i]) return false;
+    return true;
+}
+
+void fmm_ensure_tc_images(Plan &P, const ibim_kernel_params &kp) {
+    double key[5];
+    kp_key(kp, key);
+    if (P.tc_ready && same_key(P.tc_key, key)) return;
+    fmm_prepare_operators(P, kp, IBIM_PRECISION_MIXED);
+    m2l_tc_pack(P);
+    // the images replace the FP32 operators on this path
+    P.ops32.release();
+    P.ops32_ready = false;
+    for (int i = 0; i < 5; ++i) P.tc_key[i] = key[i];
+    P.tc_ready = true;
+}
+
+void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp) {
+    double key[5];
+    kp_key(kp, key);
+    if (P.oz_ready && same_key(P.oz_key, key)) return;
+    fmm_prepare_operators(P, kp, IBIM_PRECISION_FP64);
+    m2l_oz_pack(P);
+    for (int i = 0; i < 5; ++i) P.oz_key[i] = key[i];
+    P.oz_ready = true;
+}
+
+void fmm_release_fp64_operators(Plan &P) {
+    P.ops64.release();
+    P.ops64_ready = false;
 }
 
 // One FP64 FMM: dens (4 x ns, tree order) -> out (4 x nt of target set ts, tree order).
 void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out, bool m2l_sliced) {
     IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
-    fmm_prepare_operators(P, kpp, IBIM_PRECISION_FP64);
+    const bool use_oz = m2l_sliced && (4 * P.R + 15) / 16 * 16 <= M2L_OZ_MAXK;
+    if (use_oz)
+        fmm_ensure_oz_images(P, kpp);
+    else
+        fmm_prepare_operators(P, kpp, IBIM_PRECISION_FP64);
     const TargetSet &S = *P.targets[ts];
     cudaStream_t s = P.ctx->stream;
     const TreeHost &T = P.tree;
@@ -868,8 +913,7 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
                                                P.mult.ptr)); }
     }
     P.local.zero();
-    if (m2l_sliced && S.nchunks_oz > 0 && (n4 + 15) / 16 * 16 <= M2L_OZ_MAXK) {
-        m2l_oz_prepare(P);
+    if (use_oz) {
         m2l_oz_run(P, S);
     } else if (S.nchunks > 0)
         { ProfScope ps_(PROF_M2L_V64, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,

@@ -664,11 +664,20 @@ void fmm_prepare_operators_mixed(Plan &P, const KParams &k, const double *ops64)
     IBIM_CHECK_LAUNCH();
 }
 
+bool mixed_uses_tc() {
+    static const bool simt_m2l = std::getenv("IBIM_M2L_SIMT") != nullptr;  // SIMT FP32 M2L for comparison
+    return !simt_m2l && m2l_tc_supported();
+}
+
 void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out) {
     IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
     TargetSet &S = *P.targets[ts];
     prepare_mixed(P, S);
-    fmm_prepare_operators(P, kpp, IBIM_PRECISION_MIXED);
+    const bool tc = mixed_uses_tc();
+    if (tc)
+        fmm_ensure_tc_images(P, kpp);
+    else
+        fmm_prepare_operators(P, kpp, IBIM_PRECISION_MIXED);
     Ctx *c = P.ctx;
     cudaStream_t s = c->stream;
     const TreeHost &T = P.tree;
@@ -694,9 +703,7 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
         }
     }
     P.local32.zero();
-    static const bool simt_m2l = std::getenv("IBIM_M2L_SIMT") != nullptr;
-    if (!simt_m2l && m2l_tc_supported()) {
-        m2l_tc_prepare(P);
+    if (tc) {
         m2l_tc_run(P, S);
     } else if (S.nchunks32 > 0) {
         ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 4.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));

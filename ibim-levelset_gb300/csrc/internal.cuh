@@ -245,14 +245,16 @@ struct Plan {
     DevBuf<float> nrad32;          // per node radius (mixed)
     DevBuf<unsigned char> tables32;  // ChebTables32
     bool mixed_ready = false;
-    // tensor-core V-list M2L (m2l_tc.cu): 3xTF32 operands, padded
+    // tensor-core V-list M2L (m2l_tc.cu): 3xTF32 operand images, padded, for kernel parameters tc_key
     bool tc_ready = false;
+    double tc_key[5] = {-1, -1, -1, -1, -1};
     int tc_kpad = 0, tc_mpad = 0;
     DevBuf<float> tc_a_hi, tc_a_lo, tc_b_hi, tc_b_lo;
     DevBuf<int> tc_err;
     // FP64-class V-list M2L of the refinement residual (m2l_tc.cu): operators and multipoles as
     // exact BF16 integer slices under power-of-two row / column scales
-    int ops64_gen = 0, oz_gen = -1;  // generation of ops64, and the one the slices were cut from
+    bool oz_ready = false;           // digit images valid for kernel parameters oz_key
+    double oz_key[5] = {-1, -1, -1, -1, -1};
     int oz_kpad = 0, oz_mtiles = 0;
     DevBuf<uint16_t> oz_a, oz_b;
     DevBuf<double> oz_sig, oz_tau;
@@ -272,11 +274,19 @@ void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, 
 
 // Tensor-core V-list M2L (m2l_tc.cu)
 bool m2l_tc_supported();
-void m2l_tc_prepare(Plan &P);
+void m2l_tc_pack(Plan &P);  // TF32 hi/lo images from P.ops32
 void m2l_tc_run(Plan &P, TargetSet &S);
 int m2l_tc_error(Plan &P);
-void m2l_oz_prepare(Plan &P);
+void m2l_oz_pack(Plan &P);  // BF16 digit images and row scales from P.ops64
 void m2l_oz_run(Plan &P, const TargetSet &S);
+// Operator images for kernel parameters kp, built when missing or stale: the TF32 images (from
+// FP32 operators, which are then released) and the digit images (from the FP64 operators).
+void fmm_ensure_tc_images(Plan &P, const ibim_kernel_params &kp);
+void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp);
+// Release the FP64 operators (rebuilt on demand) once only their digit images are needed.
+void fmm_release_fp64_operators(Plan &P);
+// Whether the mixed path's V-list M2L runs on the tensor cores on this device.
+bool mixed_uses_tc();
 
 // Near-field work segments.  Target leaf k (node tl[k], nt[k] targets) owns source ranges
 // ptr[k] .. ptr[k+1] of `rng` (begin, end pairs); consecutive ranges are grouped into segments of

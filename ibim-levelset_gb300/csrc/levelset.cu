@@ -102,13 +102,31 @@ __global__ void k_expand(typename OrdT<T>::type *g, Dims d, double sx, double sy
     }
 }
 
+// Divisions of the WENO5 and RK3 formulas.  FP64 (the reference path) keeps IEEE divisions as
+// written in levelset.cpp; FP32 (mixed path) multiplies by reciprocal constants and uses the fast
+// hardware reciprocal (about 1 ulp), which the FP32 tolerance absorbs.
+struct Div64 {
+    __device__ static double q(double x, double c) { return x / c; }
+    __device__ static double rcp(double x) { return 1.0 / x; }
+    __device__ static double over_sqrt(double x, double y) { return x / sqrt(y); }
+};
+struct Div32 {
+    __device__ static float q(float x, float c) { return x * __fdividef(1.0f, c); }
+    __device__ static float rcp(float x) { return __fdividef(1.0f, x); }
+    __device__ static float over_sqrt(float x, float y) { return x * rsqrtf(y); }
+};
+template <class T> struct DivOf;
+template <> struct DivOf<double> { using type = Div64; };
+template <> struct DivOf<float> { using type = Div32; };
+
 // WENO5 one-sided derivatives along one axis from the 7 values w[0..6] centred on w[3]
 // (levelset::setGradient, levelset.cpp:330-388; Jiang-Peng smoothness indicators, eps 1e-6).
 template <class T>
 __device__ __forceinline__ void weno5(const T w[7], T h, T &up, T &un) {
+    using D = typename DivOf<T>::type;
     const T EPS_LS = (T)1e-6;
     T a = w[1] - w[0], b = w[2] - w[1], c = w[3] - w[2], d = w[4] - w[3], e = w[5] - w[4], f = w[6] - w[5];
-    const T df = (-b + (T)7.0 * (c + d) - e) / (T)12.0;
+    const T df = D::q(-b + (T)7.0 * (c + d) - e, (T)12.0);
     a = b - a;
     b = c - b;
     c = d - c;
@@ -117,20 +135,20 @@ __device__ __forceinline__ void weno5(const T w[7], T h, T &up, T &un) {
     T s0 = (T)13.0 * (e - d) * (e - d) + (T)3.0 * (e - (T)3.0 * d) * (e - (T)3.0 * d);
     T s1 = (T)13.0 * (d - c) * (d - c) + (T)3.0 * (d + c) * (d + c);
     T s2 = (T)13.0 * (c - b) * (c - b) + (T)3.0 * ((T)3.0 * c - b) * ((T)3.0 * c - b);
-    T a0 = (T)1.0 / ((EPS_LS + s0) * (EPS_LS + s0)), a1 = (T)6.0 / ((EPS_LS + s1) * (EPS_LS + s1)),
-      a2 = (T)3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
-    T w1 = (T)1.0 / (a0 + a1 + a2), w0 = a0 * w1, w2 = a2 * w1;
-    up = (df + w0 * (e - 2 * d + c) / (T)3.0 + (w2 - (T)0.5) * (d - (T)2.0 * c + b) / (T)6.0) / h;
+    T a0 = D::rcp((EPS_LS + s0) * (EPS_LS + s0)), a1 = D::q((T)6.0, (EPS_LS + s1) * (EPS_LS + s1)),
+      a2 = D::q((T)3.0, (EPS_LS + s2) * (EPS_LS + s2));
+    T w1 = D::rcp(a0 + a1 + a2), w0 = a0 * w1, w2 = a2 * w1;
+    up = D::q(df + D::q(w0 * (e - 2 * d + c), (T)3.0) + D::q((w2 - (T)0.5) * (d - (T)2.0 * c + b), (T)6.0), h);
     s0 = (T)13.0 * (a - b) * (a - b) + (T)3.0 * (a - (T)3.0 * b) * (a - (T)3.0 * b);
     s1 = (T)13.0 * (b - c) * (b - c) + (T)3.0 * (b + c) * (b + c);
     s2 = (T)13.0 * (c - d) * (c - d) + (T)3.0 * ((T)3.0 * c - d) * ((T)3.0 * c - d);
-    a0 = (T)1.0 / ((EPS_LS + s0) * (EPS_LS + s0));
-    a1 = (T)6.0 / ((EPS_LS + s1) * (EPS_LS + s1));
-    a2 = (T)3.0 / ((EPS_LS + s2) * (EPS_LS + s2));
-    w1 = (T)1.0 / (a0 + a1 + a2);
+    a0 = D::rcp((EPS_LS + s0) * (EPS_LS + s0));
+    a1 = D::q((T)6.0, (EPS_LS + s1) * (EPS_LS + s1));
+    a2 = D::q((T)3.0, (EPS_LS + s2) * (EPS_LS + s2));
+    w1 = D::rcp(a0 + a1 + a2);
     w0 = a0 * w1;
     w2 = a2 * w1;
-    un = (df - w0 * (a - 2 * b + c) / (T)3.0 - (w2 - (T)0.5) * (b - 2 * c + d) / (T)6.0) / h;
+    un = D::q(df - D::q(w0 * (a - 2 * b + c), (T)3.0) - D::q((w2 - (T)0.5) * (b - 2 * c + d), (T)6.0), h);
 }
 
 template <class T>
@@ -178,16 +196,17 @@ __global__ void __launch_bounds__(256) k_weno_stage(Dims dm, T h, T dtv, T eps, 
         L = dtv * godunov(un, up);
     } else {
         const T p0 = phi0[I];
-        const T sign = p0 / sqrt(p0 * p0 + eps);
+        const T sign = DivOf<T>::type::over_sqrt(p0, p0 * p0 + eps);
         const T nd = sign > (T)0 ? godunov(un, up) : godunov(up, un);
         L = dtv * sign * (nd - (T)1.0);
     }
+    using D = typename DivOf<T>::type;
     if (STAGE == 0)
         u1[I] = g[I] - L;
     else if (STAGE == 1)
-        u2[I] = (3 * g[I] + u1[I] - L) / (T)4.0;
+        u2[I] = (3 * g[I] + u1[I] - L) * (T)0.25;
     else
-        g[I] = (g[I] + 2 * (u2[I] - L)) / (T)3.0;
+        g[I] = D::q(g[I] + 2 * (u2[I] - L), (T)3.0);
 }
 
 // levelset::countGradient: among cells with |g| < thickness*dx, count | |grad g| - 1 | > thres.

@@ -337,7 +337,7 @@ __global__ void k_split_mult_tc(long nnodes, int n4, int kpad, const float *__re
 // multiplication by using fast routines of matrix multiplication", Numer. Algorithms 59, 2012),
 // in its fixed-point form: each operator row r is scaled by a power of two s_r >= max |A_r.|,
 // each multipole column j by t_j >= max |B_.j|, and the scaled values (in [-1, 1]) are cut into
-// OZ_S signed 6-bit digits by repeated round-to-nearest,
+// OZ_S signed 6-bit digits (balanced base-64 digits of rint(A_rk / s_r 2^42)),
 //     A_rk / s_r = sum_i a_i(r,k) 2^(-6(i+1)) + e,   |a_0| <= 64, |a_i>0| <= 32, |e| <= 2^-43.
 // Digits are small integers, exact in BF16; a digit product is an integer below 2^12 and a
 // K-term dot product of one digit pair below 2^21 (K <= 1024), so the FP32 tensor-core
@@ -350,11 +350,12 @@ __global__ void k_split_mult_tc(long nnodes, int n4, int kpad, const float *__re
 // One CTA: one chunk of <= 64 pairs x one 128-row tile; accumulator k (k = 0..6) in TMEM
 // columns [64 k, 64 k + 64).  Stage st holds K elements [16 st, 16 st + 16): the 7 operator digit
 // tiles (128 x 16 BF16, 4 KB each, pre-packed contiguously: one bulk copy) and the 7 multipole
-// digit tiles (64 x 16 BF16, gathered by cp.async).
+// digit tiles (64 x 16 BF16, gathered by cp.async).  Warp-specialised like k_m2l_tc: one thread
+// issues the bulk copies, one the MMAs, six warps gather; they meet on mbarriers only.
 // ---------------------------------------------------------------------------------------------
 
 constexpr int OZ_S = 7, OZ_M = 128, OZ_N = 64, OZ_KS = 16;
-constexpr int OZ_NST = 5, OZ_QD = 2, OZ_THREADS = 256;
+constexpr int OZ_NST = 5, OZ_THREADS = 256, OZ_BPROD = 192, OZ_LAG = 2;
 constexpr int OZ_ATILE = OZ_M * OZ_KS * 2;                 // 4 KB
 constexpr int OZ_BTILE = OZ_N * OZ_KS * 2;                 // 2 KB
 constexpr int OZ_STAGE = OZ_S * (OZ_ATILE + OZ_BTILE);      // 42 KB
@@ -379,15 +380,18 @@ __device__ __forceinline__ uint16_t bf16_bits_exact(float v) {
     return (uint16_t)(__float_as_uint(v) >> 16);
 }
 
-// Cut x (|x| <= 1) into OZ_S digits.
+// Cut x (|x| < 1) into OZ_S signed digits: m = rint(x 2^42) (one FP64 multiply and one
+// conversion), then balanced base-64 digits by integer arithmetic, least significant first
+// (a_i in [-32, 31] for i >= 1, |a_0| <= 64); x = sum_i a_i 2^-6(i+1) up to 2^-43.
 __device__ __forceinline__ void oz_digits(double x, uint16_t *dig) {
+    long long m = __double2ll_rn(x * 4398046511104.0);  // 2^42
 #pragma unroll
-    for (int i = 0; i < OZ_S; ++i) {
-        const double v = x * 64.0;
-        const double a = rint(v);
-        dig[i] = bf16_bits_exact((float)a);
-        x = v - a;
+    for (int i = OZ_S - 1; i > 0; --i) {
+        const long long a = ((m + 32) & 63) - 32;
+        dig[i] = bf16_bits_exact((float)(int)a);
+        m = (m - a) / 64;  // exact
     }
+    dig[0] = bf16_bits_exact((float)(int)m);
 }
 
 // Power-of-two scale >= m (1 for m == 0), returned as its exponent.
@@ -482,11 +486,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
              const int *__restrict__ vtgt, const uint16_t *__restrict__ a, const double *__restrict__ sig,
              const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err) {
     extern __shared__ __align__(1024) unsigned char oz_smem[];
-    __shared__ __align__(8) uint64_t done_bar[OZ_NST], full_bar[OZ_NST];
+    __shared__ __align__(8) uint64_t full_a[OZ_NST], full_b[OZ_NST], empty_bar[OZ_NST], acc_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int src_s[OZ_N], tgt_s[OZ_N];
     __shared__ double tau_s[OZ_N];
-    __shared__ int abort_s;
+    __shared__ volatile int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
     const int t = blockIdx.y;
@@ -500,9 +504,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (tid == 0) {
         abort_s = 0;
         for (int i = 0; i < OZ_NST; ++i) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done_bar[i])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_bar[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(OZ_BPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
         }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_bar)));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (warp == 0) {
@@ -516,62 +522,42 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t tmem_d = tmem_base;
     const long atile0 = ((long)op * mtiles + t) * nstage;
 
-    auto load_stage = [&](int st) {
-        unsigned char *base = oz_smem + (st % OZ_NST) * OZ_STAGE;
-        if (tid == 0) {
-            const uint32_t fb = smem_u32(&full_bar[st % OZ_NST]);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(OZ_S * OZ_ATILE)
-                         : "memory");
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    smem_u32(base)),
-                "l"(a + (atile0 + st) * (long)(OZ_S * OZ_ATILE / 2)), "r"(OZ_S * OZ_ATILE), "r"(fb)
-                : "memory");
+    if (warp == 0) {
+        if (lane == 0) {  // operator digit tiles: one bulk copy per stage
+            int issued = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % OZ_NST;
+                if (st >= OZ_NST &&
+                    !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / OZ_NST) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                if (abort_s) break;
+                const uint32_t fb = smem_u32(&full_a[buf]);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(OZ_S * OZ_ATILE)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(oz_smem + buf * OZ_STAGE)),
+                    "l"(a + (atile0 + st) * (long)(OZ_S * OZ_ATILE / 2)), "r"(OZ_S * OZ_ATILE), "r"(fb)
+                    : "memory");
+                issued = st;
+            }
+            for (int s2 = max(0, issued - OZ_NST + 1); s2 <= issued; ++s2)
+                if (!mbar_wait(smem_u32(&full_a[s2 % OZ_NST]), (uint32_t)((s2 / OZ_NST) & 1))) abort_s = 1;
         }
-        // multipole digits: 64 rows x 7 digits x 2 pieces of 16 B (224 contiguous bytes per row)
-        for (int i = tid; i < OZ_N * OZ_S * 2; i += OZ_THREADS) {
-            const int row = i / (OZ_S * 2), rem = i % (OZ_S * 2), d = rem >> 1, c = rem & 1;
-            const uint32_t dst = smem_u32(base + OZ_S * OZ_ATILE + d * OZ_BTILE + tile_off(row, c));
-            const int sn = src_s[row];
-            const uint16_t *g = sn >= 0 ? bdig + (((long)sn * nstage + st) * OZ_S + d) * OZ_KS + 8 * c : bdig;
-            cp_async16(dst, g, sn >= 0 ? 16u : 0u);
-        }
-        asm volatile("cp.async.commit_group;");
-    };
-
-    int issued = -1, full_waited = -1, last = -1;
-    for (int s = 0; s < OZ_NST - OZ_QD; ++s) {
-        if (s < nstage) {
-            load_stage(s);
-            issued = s;
-        } else {
-            asm volatile("cp.async.commit_group;");
-        }
-    }
-    bool ok = true;
-    for (int st = 0; st < nstage; ++st) {
-        const int ld = st + OZ_NST - OZ_QD;
-        bool w = true;
-        if (ld < nstage && st >= OZ_QD)
-            w = mbar_wait(smem_u32(&done_bar[(st - OZ_QD) % OZ_NST]), (uint32_t)(((st - OZ_QD) / OZ_NST) & 1));
-        if (!__syncthreads_and((w && !abort_s) ? 1 : 0)) {
-            ok = false;
-            break;
-        }
-        if (ld < nstage) {
-            load_stage(ld);
-            issued = ld;
-        } else {
-            asm volatile("cp.async.commit_group;");
-        }
-        asm volatile("cp.async.wait_group %0;" ::"n"(OZ_NST - OZ_QD) : "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            if (mbar_wait(smem_u32(&full_bar[st % OZ_NST]), (uint32_t)((st / OZ_NST) & 1))) {
-                full_waited = st;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issue: 28 digit-pair MMAs per stage into 7 group accumulators
+            int last = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % OZ_NST;
+                const uint32_t par = (uint32_t)((st / OZ_NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t base = smem_u32(oz_smem + (st % OZ_NST) * OZ_STAGE);
+                const uint32_t base = smem_u32(oz_smem + buf * OZ_STAGE);
 #pragma unroll
                 for (int k = 0; k < OZ_S; ++k) {
 #pragma unroll
@@ -582,27 +568,56 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 smem_u32(&done_bar[st % OZ_NST]))
+                                 smem_u32(&empty_bar[buf]))
                              : "memory");
                 last = st;
+            }
+            if (last == nstage - 1) {
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&acc_bar))
+                             : "memory");
             } else {
                 abort_s = 1;
+                if (last >= 0) mbar_wait(smem_u32(&empty_bar[last % OZ_NST]), (uint32_t)((last / OZ_NST) & 1));
             }
         }
-    }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    if (tid == 0) {
-        for (int s = full_waited + 1; s <= issued; ++s)
-            if (!mbar_wait(smem_u32(&full_bar[s % OZ_NST]), (uint32_t)((s / OZ_NST) & 1))) ok = false;
-        if (last >= 0 && !mbar_wait(smem_u32(&done_bar[last % OZ_NST]), (uint32_t)((last / OZ_NST) & 1))) ok = false;
-        if (last != nstage - 1) ok = false;
-        if (!ok) {
-            abort_s = 1;
-            atomicExch(err, 1);
+    } else {  // multipole digits: 64 rows x 7 digits x 2 pieces of 16 B per stage, 192 threads
+        const int tq = tid - 64;
+        int issued = -1;
+        for (int st = 0; st < nstage; ++st) {
+            const int buf = st % OZ_NST;
+            if (st >= OZ_NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / OZ_NST) - 1) & 1))) {
+                abort_s = 1;
+                break;
+            }
+            if (abort_s) break;
+            unsigned char *base = oz_smem + buf * OZ_STAGE;
+            for (int i = tq; i < OZ_N * OZ_S * 2; i += OZ_BPROD) {
+                const int row = i / (OZ_S * 2), rem = i % (OZ_S * 2), d = rem >> 1, c = rem & 1;
+                const uint32_t dst = smem_u32(base + OZ_S * OZ_ATILE + d * OZ_BTILE + tile_off(row, c));
+                const int sn = src_s[row];
+                const uint16_t *g = sn >= 0 ? bdig + (((long)sn * nstage + st) * OZ_S + d) * OZ_KS + 8 * c : bdig;
+                cp_async16(dst, g, sn >= 0 ? 16u : 0u);
+            }
+            asm volatile("cp.async.commit_group;");
+            issued = st;
+            if (st >= OZ_LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(OZ_LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - OZ_LAG) % OZ_NST]))
+                             : "memory");
+            }
         }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s2 = max(0, issued - OZ_LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % OZ_NST])) : "memory");
     }
     __syncthreads();
-    ok = !abort_s;
+    bool ok = !abort_s;
+    if (ok) ok = mbar_wait(smem_u32(&acc_bar), 0u);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (!ok && tid == 0) atomicExch(err, 1);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ok) {
         // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [32 (w / 4), + 32)
@@ -653,8 +668,8 @@ bool m2l_tc_supported() {
     return major == 10 && minor == 3;
 }
 
-void m2l_tc_prepare(Plan &P) {
-    if (P.tc_ready) return;
+void m2l_tc_pack(Plan &P) {
+    IBIM_REQUIRE(P.ops32.ptr || P.nops == 0, "tensor-core images need the FP32 operators");
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     P.tc_kpad = (n4 + TC_KS - 1) / TC_KS * TC_KS;
@@ -667,11 +682,12 @@ void m2l_tc_prepare(Plan &P) {
                                                                       P.tc_a_hi.ptr, P.tc_a_lo.ptr));
     P.tc_b_hi.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
     P.tc_b_lo.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
-    P.tc_err.alloc(1, s);
-    P.tc_err.zero();
+    if (!P.tc_err.ptr) {
+        P.tc_err.alloc(1, s);
+        P.tc_err.zero();
+    }
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
-    P.tc_ready = true;
 }
 
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating).
@@ -692,9 +708,10 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     IBIM_CHECK_LAUNCH();
 }
 
-// Digit tiles of the FP64 operators, rebuilt whenever the FP64 operators are.
-void m2l_oz_prepare(Plan &P) {
-    if (P.oz_gen == P.ops64_gen || P.nops == 0) return;
+// Digit tiles of the FP64 operators.
+void m2l_oz_pack(Plan &P) {
+    if (P.nops == 0) return;
+    IBIM_REQUIRE(P.ops64.ptr, "digit images need the FP64 operators");
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     P.oz_kpad = (n4 + OZ_KS - 1) / OZ_KS * OZ_KS;
@@ -719,7 +736,6 @@ void m2l_oz_prepare(Plan &P) {
                          reinterpret_cast<uint4 *>(P.oz_a.ptr)));
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmemBytes));
-    P.oz_gen = P.ops64_gen;
 }
 
 // V-list M2L of the FP64 operator by exact digit products on the tensor cores; mult -> local.
@@ -742,7 +758,7 @@ void m2l_oz_run(Plan &P, const TargetSet &S) {
 }
 
 int m2l_tc_error(Plan &P) {
-    if (!P.tc_err.ptr) return 0;
+    if (!P.tc_err.ptr) return 0;  // allocated by the first image pack of either kind
     int e = 0;
     P.tc_err.download(&e, 1);
     IBIM_CUDA(cudaStreamSynchronize(P.ctx->stream));

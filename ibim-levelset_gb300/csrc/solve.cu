@@ -459,8 +459,9 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
     Krylov K(c, n2, std::max(1, std::min(restart, 250)));
     GmresStats st;
     int status = 1;
-    if (precision == IBIM_PRECISION_FP64) {
-        auto A = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, IBIM_PRECISION_FP64); };
+    const bool plain = precision != IBIM_PRECISION_MIXED;  // FP64, or FP64 with tensor-core M2L
+    if (plain) {
+        auto A = [&](const double *in, double *out) { bie_matvec(P, kp, in, out, precision); };
         status = K.solve(A, x.ptr, b.ptr, maxiter, tol, true, st);
         res.matvecs_fp64 = st.matvecs;
         res.refinements = 0;
@@ -503,7 +504,7 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
         res.refinements = outer + (outer < 8 ? 1 : 0);
     }
     res.gmres_iters = st.iters;
-    res.matvecs = st.matvecs + (precision == IBIM_PRECISION_FP64 ? 0 : res.matvecs_fp64);
+    res.matvecs = st.matvecs + (plain ? 0 : res.matvecs_fp64);
     res.gmres_status = status;
     res.residual = st.residual;
     res.t_solve_ms = tm.ms();

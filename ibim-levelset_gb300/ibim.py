@@ -46,8 +46,10 @@ EXPORTS = [
     "ibim_tube_destroy", "ibim_tube_size", "ibim_tube_download", "ibim_fmm_plan", "ibim_plan_destroy",
     "ibim_plan_stats", "ibim_plan_lists", "ibim_fmm_apply", "ibim_bie_matvec", "ibim_bie_rhs", "ibim_gmres_solve",
     "ibim_electric", "ibim_solve", "ibim_solve_dev", "ibim_solve_pqr", "ibim_tree_lists_host", "ibim_ctx_stream",
+    "ibim_ctx_trim",
     "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
-    "ibim_levelset_evolve_static",
+    "ibim_levelset_evolve_static", "ibim_server_create", "ibim_server_destroy", "ibim_server_submit",
+    "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
@@ -144,6 +146,7 @@ def lib():
         "ibim_solve_pqr": ([_vp, C.c_char_p, C.POINTER(Config), C.POINTER(Result)], C.c_int),
         "ibim_tree_lists_host": ([_dp, C.c_long, C.c_int, C.c_int, _ip, C.c_long, _lp], C.c_int),
         "ibim_ctx_stream": ([_vp], _vp),
+        "ibim_ctx_trim": ([_vp], C.c_int),
         "ibim_launch_count": ([], C.c_long),
         "ibim_profile_enable": ([_vp, C.c_uint], C.c_int),
         "ibim_profile_read": ([_vp, _dp, _lp, C.c_int], C.c_int),
@@ -151,6 +154,13 @@ def lib():
         "ibim_measure_peak": ([_vp, C.c_int, _dp], C.c_int),
         "ibim_levelset_evolve_static": ([_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                          C.c_double, _vp], C.c_int),
+        "ibim_server_create": ([C.c_int, C.c_int, C.c_double, C.POINTER(_vp)], C.c_int),
+        "ibim_server_destroy": ([_vp], C.c_int),
+        "ibim_server_submit": ([_vp, _dp, _dp, _dp, C.c_int, C.POINTER(Config), _lp], C.c_int),
+        "ibim_server_poll": ([_vp, C.c_long, _ip, _ip, C.POINTER(Result), _dp, _dp], C.c_int),
+        "ibim_server_wait": ([_vp, C.c_long, _ip, C.POINTER(Result), _dp, _dp], C.c_int),
+        "ibim_server_stats": ([_vp, _dp], C.c_int),
+        "ibim_request_bytes_estimate": ([C.POINTER(Config)], C.c_double),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -218,6 +228,10 @@ class Context:
     def stream(self) -> int:
         """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
         return int(lib().ibim_ctx_stream(self.h) or 0)
+
+    def trim(self):
+        """Return the device memory cached by finished solves to the driver."""
+        _check(lib().ibim_ctx_trim(self.h))
 
     def profile(self, categories):
         """Enable CUDA-event timing of the named kernel categories (PROFILE_CATEGORIES)."""
@@ -502,3 +516,58 @@ class Workload:
     charges: np.ndarray
     radii: np.ndarray
     cfg: Config
+
+
+class Server:
+    """Request loop on one GPU (ibim_server): concurrent solves admitted by an HBM budget."""
+
+    STAT_KEYS = ["submitted", "completed", "in_flight", "queued", "bytes_in_flight", "peak_bytes", "budget"]
+
+    def __init__(self, device: int = 0, slots: int = 4, hbm_budget_bytes: float = 150e9):
+        h = _vp()
+        _check(lib().ibim_server_create(device, slots, float(hbm_budget_bytes), C.byref(h)))
+        self.h = h
+
+    def submit(self, centers, charges, radii, cfg: Config) -> int:
+        c = _c(centers).reshape(-1, 3)
+        q = _c(charges)
+        r = _c(radii)
+        rid = C.c_long(0)
+        _check(lib().ibim_server_submit(self.h, _p(c), _p(q), _p(r), len(q), C.byref(cfg), C.byref(rid)))
+        return rid.value
+
+    def _out(self, st, res, lat, run):
+        if st.value != OK:
+            raise IbimError(st.value, lib().ibim_last_error().decode())
+        d = res.as_dict()
+        d.update(latency_ms=lat.value, run_ms=run.value)
+        return d
+
+    def poll(self, rid: int):
+        """The result dict once the request has finished (collecting it), else None."""
+        done, st, res, lat, run = C.c_int(0), C.c_int(0), Result(), C.c_double(0), C.c_double(0)
+        _check(lib().ibim_server_poll(self.h, rid, C.byref(done), C.byref(st), C.byref(res), C.byref(lat),
+                                      C.byref(run)))
+        return self._out(st, res, lat, run) if done.value else None
+
+    def wait(self, rid: int) -> dict:
+        st, res, lat, run = C.c_int(0), Result(), C.c_double(0), C.c_double(0)
+        _check(lib().ibim_server_wait(self.h, rid, C.byref(st), C.byref(res), C.byref(lat), C.byref(run)))
+        return self._out(st, res, lat, run)
+
+    def stats(self) -> dict:
+        s = (C.c_double * 7)()
+        _check(lib().ibim_server_stats(self.h, s))
+        return dict(zip(self.STAT_KEYS, list(s)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibim_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def request_bytes_estimate(cfg: Config) -> float:
+    return float(lib().ibim_request_bytes_estimate(C.byref(cfg)))

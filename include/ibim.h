@@ -59,8 +59,8 @@ extern "C" {
 /* FP64 operator whose V-list M2L runs on the tensor cores as exact products of BF16 integer
  * digits (Ozaki scheme, 7 digits of 6 bits under power-of-two row/column scales; ~1e-11 of the
  * FP64 product): the operator of the mixed path's refinement residual.  Accepted by
- * ibim_fmm_plan (hence ibim_fmm_apply / ibim_bie_matvec) and ibim_gmres_solve; not a whole-solve
- * mode (ibim_config.precision is FP64 or MIXED). */
+ * ibim_fmm_plan (hence ibim_fmm_apply / ibim_bie_matvec), ibim_gmres_solve, and as a whole-solve
+ * mode (ibim_config.precision: FP64 level set, plain FP64 GMRES on this operator). */
 #define IBIM_PRECISION_FP64_TC 2
 
 typedef struct ibim_ctx_s *ibim_ctx;
@@ -127,6 +127,9 @@ const char *ibim_status_string(int status);
 void ibim_config_default(ibim_config *cfg);
 /* The context's CUDA stream (cudaStream_t), for callers that record events on it. */
 void *ibim_ctx_stream(ibim_ctx ctx);
+/* Device memory freed by finished solves stays reserved in the device's stream-ordered pool
+ * for the next solve; this returns it to the driver (no counterpart in the reference). */
+int ibim_ctx_trim(ibim_ctx ctx);
 /* Kernels this library has launched since load (all contexts). */
 long ibim_launch_count(void);
 /* Per-category kernel timing with CUDA events on the context stream.  mask bit k enables
@@ -234,6 +237,29 @@ int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charge
                    int natoms, const ibim_config *cfg, ibim_result *res);
 /* PQR file (molecule.h:21-50: ATOM lines, tokens 5..9 = x y z q r). */
 int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, ibim_result *res);
+
+/* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
+ * Solve requests queue in arrival order; `slots` worker threads, each with its own context and
+ * stream, take the head of the queue while the estimated device footprints of the requests in
+ * flight plus the head's stay within hbm_budget_bytes (a request is always admitted when none
+ * is in flight).  Requests run concurrently on the device and each keeps its level set, tree,
+ * operators and Krylov basis resident until it finishes. */
+typedef struct ibim_server_s *ibim_server;
+int ibim_server_create(int device, int slots, double hbm_budget_bytes, ibim_server *out);
+/* Waits for every queued and running request, then stops the workers. */
+int ibim_server_destroy(ibim_server s);
+/* Queue one whole solve (as ibim_solve; inputs are copied); *id identifies it. */
+int ibim_server_submit(ibim_server s, const double *centers, const double *charges, const double *radii, int natoms,
+                       const ibim_config *cfg, long *id);
+/* *done = 1 once finished, with the solve's status, result, latency (submit to finish) and run
+ * time (start to finish) in ms; a finished request is collected by the call that reports it. */
+int ibim_server_poll(ibim_server s, long id, int *done, int *status, ibim_result *res, double *latency_ms,
+                     double *run_ms);
+int ibim_server_wait(ibim_server s, long id, int *status, ibim_result *res, double *latency_ms, double *run_ms);
+/* submitted, completed, in flight, queued, bytes admitted in flight, peak bytes admitted, budget */
+int ibim_server_stats(ibim_server s, double stats[7]);
+/* The device footprint the server budgets for one solve of this configuration. */
+double ibim_request_bytes_estimate(const ibim_config *cfg);
 
 #ifdef __cplusplus
 }

@@ -75,3 +75,28 @@ def test_no_gpu_means_an_error_not_a_fallback():
     with pytest.raises(ibim.IbimError) as e:
         ibim.Context(0)
     assert e.value.status == ibim.ERR_CUDA
+
+
+def test_server_without_gpu_and_bad_arguments():
+    lib = ibim.lib()
+    import ctypes as C
+
+    h = C.c_void_p()
+    assert lib.ibim_server_create(0, 0, 1e9, C.byref(h)) == ibim.ERR_INVALID_ARGUMENT
+    assert lib.ibim_server_create(0, 2, -1.0, C.byref(h)) == ibim.ERR_INVALID_ARGUMENT
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    assert lib.ibim_server_create(0, 2, 1e9, C.byref(h)) == ibim.ERR_CUDA
+
+
+def test_request_footprint_estimate_grows_with_the_problem():
+    small = ibim.default_config(n=[64, 64, 64], np=4, maxpoint=64)
+    big = ibim.default_config(n=[256, 256, 256], np=6, maxpoint=64)
+    mixed = ibim.default_config(n=[64, 64, 64], np=4, maxpoint=64, precision=ibim.PRECISION_MIXED)
+    a, b, c = (ibim.request_bytes_estimate(x) for x in (small, big, mixed))
+    assert 0 < a < b and c > a

@@ -101,3 +101,41 @@ def test_mixed_rhs_close_to_fp64(ctx, golden, case):
     n = len(b64) // 2
     for part in (slice(0, n), slice(n, 2 * n)):
         assert np.abs(b32[part] - b64[part]).max() <= 2e-6 * np.abs(b64[part]).max()
+
+
+@pytest.mark.parametrize("order", [3, 6])
+def test_mixed_fmm_other_orders(ctx, golden, order):
+    """The tensor-core contraction at other operator sizes (4p^3 = 108: one row tile; 864: seven
+    row tiles in two CTA row groups of 4 and 3)."""
+    G = golden("p1hje")
+    P = G["params"]
+    s = G["surface"]
+    t = tube_of(ctx, G)
+    kp = ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"])
+    dens = bie_densities(s, P["h"], probe_vector(len(s)))
+    a = t.plan(order, P["maxpoint"], P["maxlevel"]).apply(ibim.KERNEL_BIE_FUSED, kp, dens)
+    b = t.plan(order, P["maxpoint"], P["maxlevel"], precision=ibim.PRECISION_MIXED).apply(ibim.KERNEL_BIE_FUSED, kp,
+                                                                                          dens)
+    for o in range(4):
+        assert np.abs(a[o] - b[o]).max() / np.abs(a[o]).max() < 2e-5, o
+
+
+def test_mixed_plan_follows_kernel_parameter_changes(ctx, golden):
+    """The tensor-core operator images are keyed on the kernel parameters: a second kappa on the
+    same plan re-cuts them (FP32 and digit images alike)."""
+    G = golden("p1hje")
+    P = G["params"]
+    s = G["surface"]
+    t = tube_of(ctx, G)
+    dens = bie_densities(s, P["h"], probe_vector(len(s)))
+    p64 = t.plan(P["np"], P["maxpoint"], P["maxlevel"])
+    p32 = t.plan(P["np"], P["maxpoint"], P["maxlevel"], precision=ibim.PRECISION_MIXED)
+    ptc = t.plan(P["np"], P["maxpoint"], P["maxlevel"], precision=ibim.PRECISION_FP64_TC)
+    for kappa in (P["kappa"], 0.4, P["kappa"]):
+        kp = ibim.kernel_params(kappa, P["dE"], P["dI"], P["tau"])
+        a = p64.apply(ibim.KERNEL_BIE_FUSED, kp, dens)
+        b = p32.apply(ibim.KERNEL_BIE_FUSED, kp, dens)
+        c = ptc.apply(ibim.KERNEL_BIE_FUSED, kp, dens)
+        for o in range(4):
+            assert np.abs(a[o] - b[o]).max() / np.abs(a[o]).max() < 2e-5, (kappa, o)
+            assert np.abs(a[o] - c[o]).max() / np.abs(a[o]).max() < 1e-10, (kappa, o)

@@ -82,3 +82,18 @@ def test_unknown_precision_rejected(ctx, golden):
     with pytest.raises(ibim.IbimError) as e:
         t.plan(P["np"], P["maxpoint"], P["maxlevel"], precision=7)
     assert e.value.status == ibim.ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("case", ["synth30", "p1hje"])
+def test_whole_solve_with_sliced_m2l(ctx, golden, case):
+    """ibim_config.precision = FP64_TC: FP64 level set and GMRES on the sliced operator reproduce
+    the FP64 solve (same iterations, energy to 1e-9)."""
+    from conftest import config_for
+
+    G = golden(case)
+    P = G["params"]
+    r64 = ctx.solve(G["centers"], G["charges"], G["radii"], config_for(P, ibim.PRECISION_FP64))
+    rtc = ctx.solve(G["centers"], G["charges"], G["radii"], config_for(P, ibim.PRECISION_FP64_TC))
+    assert rtc["n_points"] == r64["n_points"]
+    assert rtc["gmres_iters"] == r64["gmres_iters"]
+    assert abs(rtc["energy"] - r64["energy"]) <= 1e-9 * abs(r64["energy"])
