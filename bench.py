@@ -59,12 +59,15 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
-    ap.add_argument("--workload", choices=["protein2000", "born", "serve"], default="protein2000",
-                    help="serve: a bounded sample of the Poisson request stream through the request loop")
-    ap.add_argument("--requests", type=int, default=40, help="serve: number of requests")
+    ap.add_argument("--workload", choices=["protein2000", "born", "serve", "batch"], default="protein2000",
+                    help="serve: a bounded sample of the Poisson request stream through the request loop; "
+                         "batch: many molecules submitted at once (atoms log-uniform, default 50-5000)")
+    ap.add_argument("--requests", type=int, default=None, help="serve/batch: number of requests (40 / 256)")
     ap.add_argument("--rate", type=float, default=4.0, help="serve: offered rate, requests/s")
-    ap.add_argument("--slots", type=int, default=4, help="serve: solves in flight")
-    ap.add_argument("--atoms", type=str, default="100,2000", help="serve: log-uniform atom-count range")
+    ap.add_argument("--slots", type=int, default=4, help="serve/batch: solves in flight")
+    ap.add_argument("--atoms", type=str, default=None, help="serve/batch: log-uniform atom-count range")
+    ap.add_argument("--accuracy-sample", type=int, default=2,
+                    help="serve/batch: requests (smallest first) re-solved alone in FP64 to state the error")
     ap.add_argument("--hs", type=str, default="0.5", help="serve: grid spacings to draw from, e.g. 0.25,0.5")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -72,11 +75,16 @@ def parse():
                     help="skip the untimed FP64 solve that states the mixed path's energy error")
     ap.add_argument("--order", type=int, default=None,
                     help="override the workload's Chebyshev order (smaller operator storage for profiler captures)")
+    ap.add_argument("--protein-atoms", type=int, default=None,
+                    help="protein workload with this many atoms instead of 2,000 (smaller profiler captures)")
     return ap.parse_args()
 
 
-def get_workload(name, order=None):
-    W = workloads.protein2000() if name == "protein2000" else workloads.born()
+def get_workload(name, order=None, atoms=None):
+    if name == "protein2000":
+        W = workloads.protein(atoms, 1_000_000, 0.5, 5) if atoms else workloads.protein2000()
+    else:
+        W = workloads.born()
     if order is not None:
         W.np_ = order
         W.name = f"{W.name}_p{order}"
@@ -162,7 +170,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    W = get_workload(args.workload, args.order)
+    W = get_workload(args.workload, args.order, args.protein_atoms)
     import oracle as O
 
     O.build()
@@ -272,7 +280,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    W = get_workload(args.workload, args.order)
+    W = get_workload(args.workload, args.order, args.protein_atoms)
     precision = ibim.PRECISION_FP64 if args.precision == "fp64" else ibim.PRECISION_MIXED
     cfg = W.config(precision)
     ctx = ibim.Context(local)
@@ -452,21 +460,24 @@ def run_ours(args):
 def run_serve(args):
     """Serving sample: Poisson arrivals of whole-solve requests (atom counts log-uniform, kappa
     uniform in [0, 0.15], eps_out 80, h drawn from --hs) through ibim_server; throughput and p50/p99
-    latency.  The FP64 energy is computed alone for the two smallest requests to state the mixed
-    path's error."""
+    latency.  Batch: the same with every request submitted at once (default 256 molecules of
+    50-5000 atoms).  The FP64 energy is computed alone for the smallest requests to state the
+    mixed path's error."""
     import ibim
 
-    rng = np.random.default_rng(5_000_000)
-    lo, hi = (float(v) for v in args.atoms.split(","))
+    batch = args.workload == "batch"
+    nreq = args.requests or (256 if batch else 40)
+    rng = np.random.default_rng(3_000_000 if batch else 5_000_000)
+    lo, hi = (float(v) for v in (args.atoms or ("50,5000" if batch else "100,2000")).split(","))
     hs = [float(v) for v in args.hs.split(",")]
     reqs = []
-    for k in range(args.requests):
+    for k in range(nreq):
         n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
         h = float(rng.choice(hs))
         kappa = float(rng.uniform(0.0, 0.15))
-        W = workloads.protein(n, 4_000_000 + k, h=h, order=5, kappa=kappa)
+        W = workloads.protein(n, (3_000_000 if batch else 4_000_000) + k, h=h, order=5, kappa=kappa)
         reqs.append(W)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
+    arrivals = np.zeros(nreq) if batch else np.cumsum(rng.exponential(1.0 / args.rate, size=nreq))
     srv = ibim.Server(0, slots=args.slots, hbm_budget_bytes=150e9)
     ids, t0 = [], time.perf_counter()
     for W, ta in zip(reqs, arrivals):
@@ -480,7 +491,7 @@ def run_serve(args):
     srv.close()
     lat = np.array([r["latency_ms"] for r in res])
     run = np.array([r["run_ms"] for r in res])
-    small = sorted(range(len(reqs)), key=lambda k: reqs[k].mol.n)[:2]
+    small = sorted(range(len(reqs)), key=lambda k: reqs[k].mol.n)[:args.accuracy_sample]
     ctx = ibim.Context(0)
     errs = []
     for k in small:
@@ -488,10 +499,12 @@ def run_serve(args):
         e64 = ctx.solve(W.mol.centers, W.mol.charges, W.mol.radii, W.config(ibim.PRECISION_FP64))["energy"]
         errs.append(abs(res[k]["energy"] - e64) / abs(e64))
     ctx.close()
-    out = {"metric": "serving: solves/s with p50/p99 latency (Poisson arrivals, request loop)",
+    out = {"metric": ("batched: solves/s, all molecules submitted at once (request loop)" if batch else
+                      "serving: solves/s with p50/p99 latency (Poisson arrivals, request loop)"),
            "value": len(res) / t_end, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
            "dtype": "f32+f64", "data": "synthetic (seeded generator)",
-           "config": {"workload": "serve_sample", "requests": args.requests, "offered_rate_per_s": args.rate,
+           "config": {"workload": "batch" if batch else "serve_sample", "requests": nreq,
+                      "offered_rate_per_s": None if batch else args.rate,
                       "slots": args.slots, "atoms_range": [lo, hi], "h_choices": hs, "kappa_range": [0.0, 0.15],
                       "eps_out": 80.0, "chebyshev_order": 5, "precision": "mixed", "hbm_budget_gb": 150},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -500,7 +513,7 @@ def run_serve(args):
            "wall_s": t_end, "atoms_total": int(sum(W.mol.n for W in reqs)),
            "tube_points_total": int(sum(r["n_points"] for r in res)),
            "all_converged": all(r["gmres_status"] == 0 for r in res),
-           "rel_err_vs_fp64_two_smallest": errs, "server": st}
+           "rel_err_vs_fp64_smallest": errs, "server": st}
     print(json.dumps(out))
     return 0
 
@@ -509,7 +522,7 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "serve":
+    if args.workload in ("serve", "batch"):
         return run_serve(args)
     return run_ours(args)
 

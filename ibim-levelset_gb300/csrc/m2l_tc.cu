@@ -19,6 +19,8 @@
 // into the target nodes' local expansions.
 
 #include <cstdint>
+#include <cstdlib>
+#include <string>
 
 #include "fmm_common.cuh"
 
@@ -26,13 +28,25 @@ namespace ibim {
 
 namespace {
 
-constexpr int TC_M = 128, TC_N = 128, TC_KS = 8;   // rows per tile, pairs per chunk, K elements per stage
-constexpr int TC_NST = 5;                          // pipeline stages in shared memory
-constexpr int TC_RT = 4;                           // row tiles per CTA (4 x 128 TMEM columns)
+constexpr int TC_M = 128, TC_KS = 8;               // rows per tile, K elements per stage
 constexpr int TC_THREADS = 256;
-constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 4 KB per operand tile and stage
+constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 4 KB per operator tile and stage
 constexpr long TC_WAIT_LIMIT = 1L << 20;           // bounded mbarrier polling
-constexpr int kTcSmemBytes = TC_NST * (2 * TC_RT + 2) * TC_TILE_BYTES;  // 200 KB
+
+// Shape of the contraction for N pairs per chunk (MMA N): RT = 512 / N row tiles fill the 512
+// TMEM columns; a stage holds RT operator tiles (hi, lo) and the N multipole rows (hi, lo).
+template <int N> struct TcShape {
+    static constexpr int RT = 512 / N;
+    static constexpr int BT = N * TC_KS * 4;                           // multipole tile bytes
+    static constexpr int STAGE = 2 * RT * TC_TILE_BYTES + 2 * BT;       // 40 KB (N 128), 32 KB (N 256)
+    static constexpr int NST = (200 * 1024) / STAGE;                   // 5 or 6 stage buffers
+    static constexpr int SMEM = NST * STAGE;
+    // stages of multipole copies a gathering thread keeps in flight before it signals the oldest
+    static constexpr int LAG = NST - 2;
+    // D FP32, A and B TF32, both K-major, M = 128, N.
+    static constexpr uint32_t IDESC =
+        (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -48,17 +62,14 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// Instruction descriptor: D FP32, A and B TF32, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
-                            ((uint32_t)(TC_M >> 4) << 24);
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
         :
-        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, uint32_t src_bytes) {
@@ -88,7 +99,7 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
     return (uint32_t)((((row >> 3) << 1) + kchunk) * 128 + (row & 7) * 16);
 }
 
-// One CTA: one chunk of <= 128 V pairs of a single operator x up to TC_RT row tiles of 128
+// One CTA: one chunk of <= N V pairs of a single operator x up to RT = 512 / N row tiles of 128
 // operator rows.  Stage st holds K elements [8 st, 8 st + 8) of A_hi, A_lo (per row tile, pre-packed
 // as contiguous 4 KB blocks in the shared-memory layout) and of B_hi, B_lo in buffer st % TC_NST.
 // Warp-specialised: warp 0 (one thread) issues the operator bulk copies, warp 1 (one thread)
@@ -97,26 +108,29 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
 // each after its own copies of the stage have landed and been fenced to the async proxy), empty
 // (tcgen05.commit of the stage's MMAs).  No CTA-wide barrier inside the K loop; every wait is
 // bounded and an expired wait aborts the CTA through a shared flag and the error word.
-constexpr int TC_BPROD = 192, TC_LAG = 2;
+constexpr int TC_BPROD = 192;
 
+template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
                 const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
                 const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
+    using SH = TcShape<N>;
+    constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t full_a[TC_NST], full_b[TC_NST], empty_bar[TC_NST], acc_bar;
     __shared__ uint32_t tmem_base;
-    __shared__ int src_s[TC_N], tgt_s[TC_N];
+    __shared__ int src_s[N], tgt_s[N];
     __shared__ volatile int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
     const int tile0 = blockIdx.y * TC_RT;
     const int rt = min(TC_RT, mtiles - tile0);
     const int nstage = kpad / TC_KS;
-    constexpr int kStageBytes = (2 * TC_RT + 2) * TC_TILE_BYTES;
-    if (tid < TC_N) {
-        src_s[tid] = tid < cnt ? vsrc[b + tid] : -1;
-        tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
+    constexpr int kStageBytes = SH::STAGE;
+    for (int i = tid; i < N; i += TC_THREADS) {
+        src_s[i] = i < cnt ? vsrc[b + i] : -1;
+        tgt_s[i] = i < cnt ? vtgt[b + i] : -1;
     }
     if (tid == 0) {
         abort_s = 0;
@@ -130,7 +144,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(TC_RT * TC_N));
+                     "r"(TC_RT * N));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -187,14 +201,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t base = smem_u32(tc_smem + buf * kStageBytes);
                 const uint64_t bh = make_desc(base + (2 * rt) * TC_TILE_BYTES, 128, 256);
-                const uint64_t bl = make_desc(base + (2 * rt + 1) * TC_TILE_BYTES, 128, 256);
+                const uint64_t bl = make_desc(base + (2 * rt) * TC_TILE_BYTES + SH::BT, 128, 256);
                 for (int t = 0; t < rt; ++t) {
                     const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
                     const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
-                    const uint32_t d = tmem_d + (uint32_t)(t * TC_N);
-                    mma_tf32(d, ah, bh, st > 0 ? 1u : 0u);
-                    mma_tf32(d, ah, bl, 1u);
-                    mma_tf32(d, al, bh, 1u);
+                    const uint32_t d = tmem_d + (uint32_t)(t * N);
+                    mma_tf32(d, ah, bh, SH::IDESC, st > 0 ? 1u : 0u);
+                    mma_tf32(d, ah, bl, SH::IDESC, 1u);
+                    mma_tf32(d, al, bh, SH::IDESC, 1u);
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                  smem_u32(&empty_bar[buf]))
@@ -222,9 +236,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (abort_s) break;
             unsigned char *base = tc_smem + buf * kStageBytes;
             const int k0 = st * TC_KS;
-            for (int i = t; i < 2 * 2 * TC_M; i += TC_BPROD) {
-                const int tile = i >> 8, row = (i >> 1) & (TC_M - 1), c = i & 1;
-                const uint32_t dst = smem_u32(base + (2 * rt + tile) * TC_TILE_BYTES + tile_off(row, c));
+            for (int i = t; i < 4 * N; i += TC_BPROD) {  // 2 tiles x N rows x 2 pieces of 16 B
+                const int tile = i / (2 * N), row = (i >> 1) % N, c = i & 1;
+                const uint32_t dst = smem_u32(base + 2 * rt * TC_TILE_BYTES + tile * SH::BT + tile_off(row, c));
                 const int sn = src_s[row];
                 const float *B = tile == 0 ? b_hi : b_lo;
                 cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
@@ -254,9 +268,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int lg = warp & 3;
         for (int tt = warp >> 2; tt < rt; tt += 2) {
             const int row = (tile0 + tt) * TC_M + 32 * lg + lane;
-            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * TC_N);
+            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * N);
 #pragma unroll 1
-            for (int c0 = 0; c0 < TC_N; c0 += 16) {
+            for (int c0 = 0; c0 < N; c0 += 16) {
                 uint32_t v[16];
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
@@ -279,7 +293,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * TC_N));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * N));
 }
 
 // hi = x rounded to TF32 (10 explicit mantissa bits, to nearest even), lo = x - hi.
@@ -355,7 +369,7 @@ __global__ void k_split_mult_tc(long nnodes, int n4, int kpad, const float *__re
 // ---------------------------------------------------------------------------------------------
 
 constexpr int OZ_S = 7, OZ_M = 128, OZ_N = 64, OZ_KS = 16;
-constexpr int OZ_NST = 5, OZ_THREADS = 256, OZ_BPROD = 192, OZ_LAG = 2;
+constexpr int OZ_NST = 5, OZ_THREADS = 256, OZ_BPROD = 192, OZ_LAG = OZ_NST - 2;
 constexpr int OZ_ATILE = OZ_M * OZ_KS * 2;                 // 4 KB
 constexpr int OZ_BTILE = OZ_N * OZ_KS * 2;                 // 2 KB
 constexpr int OZ_STAGE = OZ_S * (OZ_ATILE + OZ_BTILE);      // 42 KB
@@ -687,22 +701,35 @@ void m2l_tc_pack(Plan &P) {
         P.tc_err.zero();
     }
     IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<128>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<256>::SMEM));
 }
 
-// V-list M2L on the tensor cores; mult32 -> local32 (accumulating).
+// V-list M2L on the tensor cores; mult32 -> local32 (accumulating).  Chunks of 128 pairs against
+// four row tiles, or (IBIM_TC_N=256) chunks of 256 pairs against two.
 void m2l_tc_run(Plan &P, TargetSet &S) {
-    if (S.nchunks_tc == 0) return;
+    static const bool wide = [] {
+        const char *e = std::getenv("IBIM_TC_N");
+        return e && std::string(e) == "256";
+    }();
+    const int nch = wide ? S.nchunks_tc256 : S.nchunks_tc;
+    if (nch == 0) return;
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     (count_launch(), k_split_mult_tc<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr,
                                                                         P.tc_b_hi.ptr, P.tc_b_lo.ptr));
-    const dim3 grid(S.nchunks_tc, (P.tc_mpad / TC_M + TC_RT - 1) / TC_RT);
-    {
-        ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
-                      4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-        (count_launch(), k_m2l_tc<<<grid, TC_THREADS, kTcSmemBytes, s>>>(
-                             n4, P.tc_kpad, P.tc_mpad / TC_M, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+    const int mt = P.tc_mpad / TC_M;
+    ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
+                  4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
+    if (wide) {
+        const dim3 grid(nch, (mt + TcShape<256>::RT - 1) / TcShape<256>::RT);
+        (count_launch(), k_m2l_tc<256><<<grid, TC_THREADS, TcShape<256>::SMEM, s>>>(
+                             n4, P.tc_kpad, mt, S.v_chunk_tc256.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+    } else {
+        const dim3 grid(nch, (mt + TcShape<128>::RT - 1) / TcShape<128>::RT);
+        (count_launch(), k_m2l_tc<128><<<grid, TC_THREADS, TcShape<128>::SMEM, s>>>(
+                             n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
     }
     IBIM_CHECK_LAUNCH();

@@ -105,7 +105,7 @@ void worker(ibim_server_s *S) {
         {
             std::lock_guard<std::mutex> lk(S->mu);
             S->in_flight--;
-            S->in_flight_bytes -= r->bytes;
+            S->in_flight_bytes = S->in_flight == 0 ? 0.0 : S->in_flight_bytes - r->bytes;
             S->completed++;
             r->done = true;
         }
