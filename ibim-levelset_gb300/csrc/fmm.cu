@@ -543,7 +543,7 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
                 }
             }
         }
-    std::vector<int> vs, vt, chunks, chunks32, chunks_tc, chunks_tc256, chunks_oz;
+    std::vector<int> vs, vt, chunks, chunks32, chunks_tc, chunks_oz;
     for (int op = 0; op < (int)byop.size(); ++op) {
         const int b = (int)vs.size();
         for (auto &pr : byop[op]) {
@@ -565,11 +565,6 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             chunks_tc.push_back(b + q);
             chunks_tc.push_back(std::min<int>(M2L_CHTC, (int)byop[op].size() - q));
         }
-        for (int q = 0; q < (int)byop[op].size(); q += 256) {
-            chunks_tc256.push_back(op);
-            chunks_tc256.push_back(b + q);
-            chunks_tc256.push_back(std::min<int>(256, (int)byop[op].size() - q));
-        }
         for (int q = 0; q < (int)byop[op].size(); q += M2L_CHOZ) {
             chunks_oz.push_back(op);
             chunks_oz.push_back(b + q);
@@ -584,8 +579,6 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     up_int(S.v_chunk_tc, chunks_tc, s);
     S.nchunks_oz = (int)chunks_oz.size() / 3;
     up_int(S.v_chunk_oz, chunks_oz, s);
-    S.nchunks_tc256 = (int)chunks_tc256.size() / 3;
-    up_int(S.v_chunk_tc256, chunks_tc256, s);
     up_int(S.v_src, vs, s);
     up_int(S.v_tgt, vt, s);
     up_int(S.v_chunk, chunks, s);
