@@ -459,7 +459,8 @@ def run_ours(args):
                          for k, v in rooflines.items()},
            "solve": {k: r0[k] for k in ("energy", "area", "n_points", "gmres_iters", "matvecs", "matvecs_fp64",
                                         "refinements", "residual", "gmres_status", "reinit_steps", "t_levelset_ms",
-                                        "t_surface_ms", "t_plan_ms", "t_solve_ms", "t_energy_ms", "fmm_nodes",
+                                        "t_surface_ms", "t_plan_ms", "t_tree_ms", "t_operators_ms", "t_solve_ms",
+                                        "t_energy_ms", "fmm_nodes",
                                         "fmm_v_pairs", "fmm_x_pairs", "fmm_near_pairs", "fmm_operators")},
            "kernels_ms_per_step": {k: round(v["ms"] / args.steps, 3) for k, v in prof.items()},
            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak,

@@ -192,6 +192,9 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
         auto w0 = std::chrono::steady_clock::now();
         P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        const auto w1 = std::chrono::steady_clock::now();
+        res.t_tree_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
         if (cfg.precision == IBIM_PRECISION_FP64 || !m2l_tc_supported()) {
             fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
             if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
@@ -207,7 +210,9 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
             if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);
         }
         IBIM_CUDA(cudaStreamSynchronize(s));
-        res.t_plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+        const auto w2 = std::chrono::steady_clock::now();
+        res.t_operators_ms = std::chrono::duration<double, std::milli>(w2 - w1).count();
+        res.t_plan_ms = std::chrono::duration<double, std::milli>(w2 - w0).count();
         IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
         // area = sum of quadrature weights (electric.cpp:60)
         std::vector<double> w(tube->n);

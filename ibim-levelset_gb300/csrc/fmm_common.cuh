@@ -78,11 +78,12 @@ __device__ __forceinline__ void radial64(const KParams &k, double d2, double &c1
     const double t = k.kappa * r;
     const double e = k.kappa == 0.0 ? 1.0 : exp(-t);
     const double et1 = e * (t + 1);
-    c1 = (k.eps * et1 - 1.) * ir3 * k.q4pi;
-    c4 = -(k.ieps * et1 - 1.) * ir3 * k.q4pi;
+    const double q3 = ir3 * k.q4pi, h3 = ir3 * k.k3f;  // shared factors of K1, K4 and of K3
+    c1 = (k.eps * et1 - 1.) * q3;
+    c4 = (1. - k.ieps * et1) * q3;
     k2 = (1.0 - e) * ir * k.q4pi;
-    hd = (1 - et1) * ir3 * k.k3f;
-    ho = (e * ((t + 3) * t + 3) - 3.0) * ir3 * ir2 * k.k3f;
+    hd = (1 - et1) * h3;
+    ho = (e * ((t + 3) * t + 3) - 3.0) * h3 * ir2;
 }
 
 // Fused 4x4 block of the 16 BIE kernels (electric.cpp:67-291) at d = source - target.

@@ -161,29 +161,57 @@ __device__ void kron_apply32(const ChebTables32 &T, int id, bool up, float *buf,
     }
 }
 
-__global__ void __launch_bounds__(128) k_m2m32(const ChebTables32 *__restrict__ tab, const int *__restrict__ nodes,
-                                               const int *__restrict__ child_first, const int *__restrict__ empty,
-                                               float *mult) {
-    extern __shared__ float smf[];
+// One warp's separable transfer (the 3 passes of kron_apply32) on its own buffers.
+__device__ void kron_apply32_warp(const ChebTables32 &T, int id, bool up, float *buf, float *tmp) {
+    const int p = T.p, R = T.R, lane = threadIdx.x & 31;
+    const int b[3] = {id & 1, (id >> 1) & 1, (id >> 2) & 1};
+    for (int ax = 0; ax < 3; ++ax) {
+        const int stride = ax == 0 ? 1 : (ax == 1 ? p : p * p);
+        float *src = (ax & 1) ? tmp : buf;
+        float *dst = (ax & 1) ? buf : tmp;
+        for (int o = lane; o < 4 * R; o += 32) {
+            const int d = o / R, cc = o % R;
+            const int idx = (cc / stride) % p;
+            const int base = d * R + cc - idx * stride;
+            float s = 0.f;
+            for (int k = 0; k < p; ++k) s = fmaf(up ? T.S[b[ax]][k][idx] : T.S[b[ax]][idx][k], src[base + k * stride], s);
+            dst[o] = s;
+        }
+        __syncwarp();
+    }
+}
+
+// M2M in FP32 (bbfmm.h:521-533): one parent per block, warp c transfers child c (its three
+// separable passes need no block barrier), then the block sums the eight results.
+constexpr int M2M32_THREADS = 256;
+__global__ void __launch_bounds__(M2M32_THREADS) k_m2m32(const ChebTables32 *__restrict__ tab,
+                                                         const int *__restrict__ nodes,
+                                                         const int *__restrict__ child_first,
+                                                         const int *__restrict__ empty, float *mult) {
+    extern __shared__ float smf[];  // [8 children][2][4R]
     __shared__ ChebTables32 T;
     load_tables(T, tab);
     __syncthreads();
     const int n4 = 4 * T.R;
-    float *buf = smf, *tmp = smf + n4, *acc = smf + 2 * n4;
     const int node = nodes[blockIdx.x];
-    for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] = 0.f;
-    const int c0 = child_first[node];
-    for (int c8 = 0; c8 < 8; ++c8) {
-        const int ch = c0 + c8;
-        if (empty[ch]) continue;
-        __syncthreads();
-        for (int o = threadIdx.x; o < n4; o += blockDim.x) buf[o] = mult[(long)ch * n4 + o];
-        __syncthreads();
-        kron_apply32(T, c8, true, buf, tmp);
-        for (int o = threadIdx.x; o < n4; o += blockDim.x) acc[o] += tmp[o];
+    const int c8 = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ch = child_first[node] + c8;
+    float *buf = smf + (size_t)c8 * 2 * n4, *tmp = buf + n4;
+    // after three passes the result is in tmp (odd pass count)
+    if (empty[ch]) {
+        for (int o = lane; o < n4; o += 32) tmp[o] = 0.f;
+    } else {
+        for (int o = lane; o < n4; o += 32) buf[o] = mult[(long)ch * n4 + o];
+        __syncwarp();
+        kron_apply32_warp(T, c8, true, buf, tmp);
     }
     __syncthreads();
-    for (int o = threadIdx.x; o < n4; o += blockDim.x) mult[(long)node * n4 + o] = acc[o];
+    for (int o = threadIdx.x; o < n4; o += blockDim.x) {
+        float a = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) a += smf[(size_t)c * 2 * n4 + n4 + o];
+        mult[(long)node * n4 + o] = a;
+    }
 }
 
 __global__ void __launch_bounds__(128) k_l2l32(const ChebTables32 *__restrict__ tab, const int *__restrict__ nodes,
@@ -333,13 +361,14 @@ __device__ __forceinline__ void kblock32(const KParams32 &k, float dx, float dy,
         b[3] = -k.k2in;
         return;
     }
-    const float ir = rsqrtf(d2), r = d2 * ir, ir3 = ir * ir * ir;
+    const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
     const float t = k.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
-    const float c1 = (k.eps * et1 - 1.f) * ir3 * k.q4pi;
-    const float c4 = -(k.ieps * et1 - 1.f) * ir3 * k.q4pi;
+    const float q3 = ir3 * k.q4pi, h3 = ir3 * k.k3f;
+    const float c1 = (k.eps * et1 - 1.f) * q3;
+    const float c4 = (1.f - k.ieps * et1) * q3;
     const float k2 = (1.f - e) * ir * k.q4pi;
-    const float hd = (1.f - et1) * ir3 * k.k3f;
-    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir * k.k3f;
+    const float hd = (1.f - et1) * h3;
+    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * h3 * ir2;
     const float dd[3] = {dx, dy, dz};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -455,13 +484,14 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                         a0 -= kp.k2in * psi;
                         continue;
                     }
-                    const float ir = rsqrtf(d2), r = d2 * ir, ir3 = ir * ir * ir;
+                    const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
                     const float t = kp.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
-                    const float c1 = (kp.eps * et1 - 1.f) * ir3 * kp.q4pi;
-                    const float c4 = -(kp.ieps * et1 - 1.f) * ir3 * kp.q4pi;
+                    const float q3 = ir3 * kp.q4pi, h3 = ir3 * kp.k3f;
+                    const float c1 = (kp.eps * et1 - 1.f) * q3;
+                    const float c4 = (1.f - kp.ieps * et1) * q3;
                     const float k2 = (1.f - e) * ir * kp.q4pi;
-                    const float hd = (1.f - et1) * ir3 * kp.k3f;
-                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * ir3 * ir * ir * kp.k3f;
+                    const float hd = (1.f - et1) * h3;
+                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * h3 * ir2;
                     const float dm = dx * m0 + dy * m1 + dz * m2;
                     a0 += c1 * dm - k2 * psi;
                     const float cm = ho * dm - c4 * psi;
@@ -563,11 +593,11 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         P.local32.alloc((size_t)nn * n4, s);
         P.dens32.alloc((size_t)4 * P.ns, s);
         P.src8.alloc((size_t)2 * P.ns, s);
-        const size_t smk = sizeof(float) * 3 * n4;
-        if (smk > 48 * 1024) {
-            IBIM_CUDA(cudaFuncSetAttribute(k_m2m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk));
+        const size_t smk = sizeof(float) * 3 * n4, smk_m2m = sizeof(float) * 16 * n4;
+        if (smk_m2m > 48 * 1024)
+            IBIM_CUDA(cudaFuncSetAttribute(k_m2m32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk_m2m));
+        if (smk > 48 * 1024)
             IBIM_CUDA(cudaFuncSetAttribute(k_l2l32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smk));
-        }
         IBIM_CUDA(cudaStreamSynchronize(s));
         P.mixed_ready = true;
     }
@@ -693,13 +723,13 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
                                                         P.nrad32.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr,
                                                         P.ns, P.mult32.ptr));
     }
-    const size_t smk = sizeof(float) * 3 * n4;
+    const size_t smk = sizeof(float) * 3 * n4, smk_m2m = sizeof(float) * 16 * n4;
     for (int l = T.nlevels - 1; l >= 0; --l) {
         const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
         if (e > b) {
             ProfScope ps_(PROF_M2M);
-            (count_launch(), k_m2m32<<<e - b, 128, smk, s>>>(tab, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
-                                                             P.mult32.ptr));
+            (count_launch(), k_m2m32<<<e - b, M2M32_THREADS, smk_m2m, s>>>(tab, P.m2m_nodes.ptr + b, P.nchild_first.ptr,
+                                                                            P.nempty.ptr, P.mult32.ptr));
         }
     }
     P.local32.zero();

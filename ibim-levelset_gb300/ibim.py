@@ -83,7 +83,7 @@ class Result(C.Structure):
                 ("t_plan_ms", C.c_double), ("t_solve_ms", C.c_double), ("t_energy_ms", C.c_double),
                 ("grid_cells", C.c_long), ("levelset_stages", C.c_int), ("fmm_nodes", C.c_long),
                 ("fmm_v_pairs", C.c_long), ("fmm_x_pairs", C.c_long), ("fmm_near_pairs", C.c_long),
-                ("fmm_operators", C.c_long)]
+                ("fmm_operators", C.c_long), ("t_tree_ms", C.c_double), ("t_operators_ms", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -116,6 +116,8 @@ typedef struct {
     long grid_cells;      /* level-set grid cells */
     int levelset_stages;  /* TVD-RK3 stage sweeps (evolve + both reinitialisations) */
     long fmm_nodes, fmm_v_pairs, fmm_x_pairs, fmm_near_pairs, fmm_operators; /* tree work counts */
+    double t_tree_ms;      /* part of t_plan_ms: octree, lists and work lists (host) with their uploads */
+    double t_operators_ms; /* part of t_plan_ms: M2L operators and their tensor-core images (device) */
 } ibim_result;
 
 /* ---- context ---- */
