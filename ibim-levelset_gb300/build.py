@@ -13,6 +13,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libibim_gb300.so")
 SOURCES = ["levelset.cu", "tree.cpp", "fmm.cu", "fmm_mixed.cu", "m2l_tc.cu", "solve.cu", "capi.cu", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+OPENMP_CU = {"fmm.cu", "fmm_mixed.cu"}  # CUDA files whose host code (plan building) uses OpenMP
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xcompiler", "-Wno-unused-function", "--expt-relaxed-constexpr"]
 
@@ -33,6 +34,8 @@ def _compile(src: str, verbose: bool) -> str:
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu", "-Xcompiler", "-fopenmp"]
+    elif src in OPENMP_CU:
+        cmd += ["-Xcompiler", "-fopenmp"]
     cmd += ["-c", path, "-o", _obj(src)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

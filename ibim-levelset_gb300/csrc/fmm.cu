@@ -510,67 +510,152 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     lb[T.nlevels] = (int)l2l.size();
     S.l2l_level_begin = lb;
     up_int(S.l2l_nodes, l2l, s);
-    std::vector<std::vector<std::pair<int, int>>> byop;
+    // V and X pairs grouped by operator with counting sorts: pairs are generated per target node
+    // in parallel, new operator keys get ids in key order (V: dense index, X: sorted keys), and
+    // each thread scatters its own contiguous node range, so the grouping is deterministic
     std::vector<int> xs, xt;
+    std::vector<long> poff(nn + 1, 0);
+    std::vector<long> vcount(nn, 0), xcount(nn, 0);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nn; ++i) {
+        if (!has_t(i)) continue;
+        long v = 0, x = 0;
+        for (int sidx : T.V[i]) v += has_s(sidx);
+        for (int sidx : T.X[i]) x += has_s(sidx);
+        vcount[i] = v;
+        xcount[i] = x;
+    }
+    for (int i = 0; i < nn; ++i) {
+        S.nv_list += vcount[i];
+        S.nx_list += xcount[i];
+        poff[i + 1] = poff[i] + vcount[i] + (P.x_as_ops ? xcount[i] : 0);
+    }
+    const long npair = poff[nn];
+    std::vector<int> pkey(npair), psrc(npair), ptgt(npair);  // pkey: V dense index, or -1 - X slot
+    std::vector<std::array<int, 5>> xkey;
+    std::vector<long> xslot_of_pair;
+    std::vector<long> xoff(nn + 1, 0);
+    if (P.x_as_ops) {
+        for (int i = 0; i < nn; ++i) xoff[i + 1] = xoff[i] + xcount[i];
+        xkey.resize(xoff[nn]);
+    }
+    std::vector<int> level_of(nn);
     for (int l = 0; l < T.nlevels; ++l)
-        for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i) {
+        for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i) level_of[i] = l;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < nn; ++i) {
+        if (!has_t(i)) continue;
+        const int l = level_of[i];
+        long q = poff[i];
+        for (int sidx : T.V[i]) {
+            if (!has_s(sidx)) continue;
+            const int ox = T.coord[3 * sidx] - T.coord[3 * i], oy = T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
+                      oz = T.coord[3 * sidx + 2] - T.coord[3 * i + 2];
+            pkey[q] = l * 343 + (ox + 3) * 49 + (oy + 3) * 7 + (oz + 3);
+            psrc[q] = sidx;
+            ptgt[q] = i;
+            ++q;
+        }
+        if (!P.x_as_ops) continue;
+        long xq = xoff[i];
+        for (int sidx : T.X[i]) {
+            if (!has_s(sidx)) continue;
+            // centre offset in target half-widths: (2 c_s + 1) 2^(lt - ls) - (2 c_t + 1)
+            const int ls = level_of[sidx], sh = l - ls;
+            std::array<int, 5> k{l, ls, 0, 0, 0};
+            for (int a = 0; a < 3; ++a)
+                k[2 + a] = (2 * T.coord[3 * sidx + a] + 1) * (1 << sh) - (2 * T.coord[3 * i + a] + 1);
+            xkey[xq] = k;
+            pkey[q] = -1 - (int)xq;
+            psrc[q] = sidx;
+            ptgt[q] = i;
+            ++q;
+            ++xq;
+        }
+    }
+    if (!P.x_as_ops) {
+        for (int i = 0; i < nn; ++i) {
             if (!has_t(i)) continue;
-            for (int sidx : T.V[i]) {
-                if (!has_s(sidx)) continue;
-                ++S.nv_list;
-                const int id = opid.get(l, T.coord[3 * sidx] - T.coord[3 * i], T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
-                                        T.coord[3 * sidx + 2] - T.coord[3 * i + 2]);
-                if ((int)byop.size() <= id) byop.resize(id + 1);
-                byop[id].push_back({sidx, i});
-            }
-            for (int sidx : T.X[i]) {
-                if (!has_s(sidx)) continue;
-                ++S.nx_list;
-                if (P.x_as_ops) {
-                    // centre offset in target half-widths: (2 c_s + 1) 2^(lt - ls) - (2 c_t + 1)
-                    const int ls = (int)(std::upper_bound(T.level_begin.begin(), T.level_begin.end(), sidx) -
-                                         T.level_begin.begin()) - 1;
-                    const int sh = l - ls;
-                    int d[3];
-                    for (int a = 0; a < 3; ++a)
-                        d[a] = (2 * T.coord[3 * sidx + a] + 1) * (1 << sh) - (2 * T.coord[3 * i + a] + 1);
-                    const int id = opid.get_x(l, ls, d[0], d[1], d[2]);
-                    if ((int)byop.size() <= id) byop.resize(id + 1);
-                    byop[id].push_back({sidx, i});
-                } else {
+            for (int sidx : T.X[i])
+                if (has_s(sidx)) {
                     xs.push_back(sidx);
                     xt.push_back(i);
                 }
-            }
-        }
-    std::vector<int> vs, vt, chunks, chunks32, chunks_tc, chunks_oz;
-    for (int op = 0; op < (int)byop.size(); ++op) {
-        const int b = (int)vs.size();
-        for (auto &pr : byop[op]) {
-            vs.push_back(pr.first);
-            vt.push_back(pr.second);
-        }
-        for (int q = 0; q < (int)byop[op].size(); q += M2L_CH) {
-            chunks.push_back(op);
-            chunks.push_back(b + q);
-            chunks.push_back(std::min<int>(M2L_CH, (int)byop[op].size() - q));
-        }
-        for (int q = 0; q < (int)byop[op].size(); q += M2L_CH32) {
-            chunks32.push_back(op);
-            chunks32.push_back(b + q);
-            chunks32.push_back(std::min<int>(M2L_CH32, (int)byop[op].size() - q));
-        }
-        for (int q = 0; q < (int)byop[op].size(); q += M2L_CHTC) {
-            chunks_tc.push_back(op);
-            chunks_tc.push_back(b + q);
-            chunks_tc.push_back(std::min<int>(M2L_CHTC, (int)byop[op].size() - q));
-        }
-        for (int q = 0; q < (int)byop[op].size(); q += M2L_CHOZ) {
-            chunks_oz.push_back(op);
-            chunks_oz.push_back(b + q);
-            chunks_oz.push_back(std::min<int>(M2L_CHOZ, (int)byop[op].size() - q));
         }
     }
+    // operator ids: V keys in dense-index order, then X keys in sorted order
+    {
+        std::vector<char> used(opid.dense.size(), 0);
+        for (long q = 0; q < npair; ++q)
+            if (pkey[q] >= 0) used[pkey[q]] = 1;
+        for (size_t d = 0; d < used.size(); ++d)
+            if (used[d]) {
+                const int l = (int)(d / 343), c = (int)(d % 343);
+                opid.get(l, c / 49 - 3, (c / 7) % 7 - 3, c % 7 - 3);
+            }
+    }
+    std::vector<int> xid(xkey.size());
+    if (!xkey.empty()) {
+        std::vector<std::array<int, 5>> u = xkey;
+        std::sort(u.begin(), u.end());
+        u.erase(std::unique(u.begin(), u.end()), u.end());
+        std::vector<int> uid(u.size());
+        for (size_t k = 0; k < u.size(); ++k) uid[k] = opid.get_x(u[k][0], u[k][1], u[k][2], u[k][3], u[k][4]);
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < (long)xkey.size(); ++k)
+            xid[k] = uid[std::lower_bound(u.begin(), u.end(), xkey[k]) - u.begin()];
+    }
+    const int nop = (int)opid.keys.size() / 5;
+    std::vector<int> pop(npair);
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < npair; ++q) pop[q] = pkey[q] >= 0 ? opid.dense[pkey[q]] : xid[-1 - pkey[q]];
+    // counting sort by operator; thread t owns pairs [t0, t1) and scatters them in order
+    std::vector<long> opbeg(nop + 1, 0);
+    std::vector<int> gs(npair), gt(npair);
+    {
+        const int nthr = std::max(1, std::min(64, (int)(npair / 65536) + 1));
+        std::vector<std::vector<long>> hist(nthr, std::vector<long>(nop, 0));
+#pragma omp parallel for schedule(static) num_threads(nthr)
+        for (int t = 0; t < nthr; ++t) {
+            const long t0 = npair * t / nthr, t1 = npair * (t + 1) / nthr;
+            for (long q = t0; q < t1; ++q) hist[t][pop[q]]++;
+        }
+        long run = 0;
+        for (int op = 0; op < nop; ++op) {
+            opbeg[op] = run;
+            for (int t = 0; t < nthr; ++t) {
+                const long c = hist[t][op];
+                hist[t][op] = run;
+                run += c;
+            }
+        }
+        opbeg[nop] = run;
+#pragma omp parallel for schedule(static) num_threads(nthr)
+        for (int t = 0; t < nthr; ++t) {
+            const long t0 = npair * t / nthr, t1 = npair * (t + 1) / nthr;
+            for (long q = t0; q < t1; ++q) {
+                const long d = hist[t][pop[q]]++;
+                gs[d] = psrc[q];
+                gt[d] = ptgt[q];
+            }
+        }
+    }
+    std::vector<int> chunks, chunks32, chunks_tc, chunks_oz;
+    auto cut = [&](std::vector<int> &out, int op, long b, long n, int width) {
+        for (long q = 0; q < n; q += width) {
+            out.push_back(op);
+            out.push_back((int)(b + q));
+            out.push_back((int)std::min<long>(width, n - q));
+        }
+    };
+    for (int op = 0; op < nop; ++op) {
+        const long b = opbeg[op], n = opbeg[op + 1] - opbeg[op];
+        cut(chunks, op, b, n, M2L_CH);
+        cut(chunks32, op, b, n, M2L_CH32);
+        cut(chunks_tc, op, b, n, M2L_CHTC);
+        cut(chunks_oz, op, b, n, M2L_CHOZ);
+    }
+    std::vector<int> &vs = gs, &vt = gt;
     S.nvpairs = (long)vs.size();
     S.nchunks = (int)chunks.size() / 3;
     S.nchunks32 = (int)chunks32.size() / 3;
@@ -585,32 +670,41 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     S.nxpairs = (long)xs.size();
     up_int(S.x_src, xs, s);
     up_int(S.x_tgt, xt, s);
-    std::vector<int> tl, nptr{0}, nr;
-    long npairs = 0;
-    for (int i = 0; i < nn; ++i) {
-        if (!T.leaf[i] || !has_t(i)) continue;
+    // near lists: per target leaf its U and W source ranges, sorted and merged (leaves in
+    // parallel, concatenated in leaf order)
+    std::vector<int> tl;
+    for (int i = 0; i < nn; ++i)
+        if (T.leaf[i] && has_t(i)) tl.push_back(i);
+    std::vector<std::vector<int>> per(tl.size());
+    std::vector<long> npair_leaf(tl.size(), 0);
+#pragma omp parallel for schedule(dynamic, 32)
+    for (long k = 0; k < (long)tl.size(); ++k) {
+        const int i = tl[k];
         std::vector<std::pair<int, int>> rg;
         for (int sidx : T.U[i])
             if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
         for (int sidx : T.W[i])
             if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
         std::sort(rg.begin(), rg.end());
-        std::vector<std::pair<int, int>> mg;
-        for (auto &r : rg) {
-            if (!mg.empty() && mg.back().second == r.first)
-                mg.back().second = r.second;
-            else
-                mg.push_back(r);
-        }
-        tl.push_back(i);
+        std::vector<int> &mg = per[k];
         long nsrc = 0;
-        for (auto &r : mg) {
-            nr.push_back(r.first);
-            nr.push_back(r.second);
-            nsrc += r.second - r.first;
+        for (auto &r : rg) {
+            if (!mg.empty() && mg.back() == r.first)
+                mg.back() = r.second;
+            else {
+                mg.push_back(r.first);
+                mg.push_back(r.second);
+            }
         }
-        npairs += nsrc * (S.end[i] - S.begin[i]);
+        for (size_t q = 0; q < mg.size(); q += 2) nsrc += mg[q + 1] - mg[q];
+        npair_leaf[k] = nsrc * (S.end[i] - S.begin[i]);
+    }
+    std::vector<int> nptr{0}, nr;
+    long npairs = 0;
+    for (size_t k = 0; k < tl.size(); ++k) {
+        nr.insert(nr.end(), per[k].begin(), per[k].end());
         nptr.push_back((int)nr.size() / 2);
+        npairs += npair_leaf[k];
     }
     S.ntleaves = (int)tl.size();
     S.near_pairs = npairs;
