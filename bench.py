@@ -362,9 +362,10 @@ def run_ours(args):
     fp32_peak = ctx.measure_peak("fp32")
     mixed = precision == ibim.PRECISION_MIXED
     fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
-                "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if mixed else "fp64", "rhs": "fp64",
+                "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if mixed else "fp64", "rhs": "fp32" if mixed else "fp64",
                 "weno_stage": "fp32" if mixed else "fp64", "p2m": "fp32" if mixed else "fp64",
-                "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": "bf16x28 tensor"}
+                "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": "bf16x28 tensor",
+                "near_ff": "fp32", "l2p": "fp32", "l2p_fp64": "fp64"}
 
     def roofline_of(name, d):
         bound = fp_bound.get(name, "hbm")

@@ -317,8 +317,12 @@ int ibim_ctx_create(int device, ibim_ctx *out) {
         try {
             IBIM_CUDA(cudaSetDevice(device));
             IBIM_CUDA(cudaDeviceGetAttribute(&h->c.num_sms, cudaDevAttrMultiProcessorCount, device));
-            IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
-            IBIM_CUDA(cudaStreamCreateWithFlags(&h->c.aux, cudaStreamNonBlocking));
+            // the far-field chain on the main stream is the critical path of a matvec; the near
+            // field on the auxiliary stream fills the resources it leaves free
+            int least = 0, greatest = 0;
+            IBIM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            IBIM_CUDA(cudaStreamCreateWithPriority(&h->c.stream, cudaStreamNonBlocking, greatest));
+            IBIM_CUDA(cudaStreamCreateWithPriority(&h->c.aux, cudaStreamNonBlocking, least));
             // device memory freed by a solve stays in the stream-ordered pool for the next one
             // instead of going back to the driver at every synchronisation (a solve allocates
             // several GB of operator images); ibim_ctx_trim hands it back
@@ -328,6 +332,8 @@ int ibim_ctx_create(int device, ibim_ctx *out) {
             IBIM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
             IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_fork, cudaEventDisableTiming));
             IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_join, cudaEventDisableTiming));
+            IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_near_fork, cudaEventDisableTiming));
+            IBIM_CUDA(cudaEventCreateWithFlags(&h->c.ev_near_join, cudaEventDisableTiming));
         } catch (...) {
             delete h;
             throw;
@@ -347,6 +353,8 @@ int ibim_ctx_destroy(ibim_ctx ctx) {
         }
         if (ctx->c.ev_fork) cudaEventDestroy(ctx->c.ev_fork);
         if (ctx->c.ev_join) cudaEventDestroy(ctx->c.ev_join);
+        if (ctx->c.ev_near_fork) cudaEventDestroy(ctx->c.ev_near_fork);
+        if (ctx->c.ev_near_join) cudaEventDestroy(ctx->c.ev_near_join);
         cudaStreamDestroy(ctx->c.stream);
         delete ctx;
     });

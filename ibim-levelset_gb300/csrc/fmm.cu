@@ -320,71 +320,129 @@ __global__ void __launch_bounds__(NEAR_T) k_near64(const ChebTables *__restrict_
                                                    const double *__restrict__ dens, long ns,
                                                    const double *__restrict__ tx, const double *__restrict__ ty,
                                                    const double *__restrict__ tz, long nt,
-                                                   const double *__restrict__ local, double *out) {
+                                                   const double *__restrict__ local, double *out, int l2p_mask,
+                                                   int nseg, int *next) {
     __shared__ ChebTables T;
     __shared__ double S[7][NEAR_TILE];
     __shared__ double red[NEAR_T][4];
+    __shared__ int cur;
     for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
         reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
-    const int4 sg = segs[blockIdx.x];
-    const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
+    // with a work counter the CTA takes segments until none is left (several launches may drain
+    // the same counter); without one it does segment blockIdx.x
+    for (int it = 0;; ++it) {
+        int si;
+        if (next) {
+            __syncthreads();  // every thread has read the previous segment number
+            if (threadIdx.x == 0) cur = atomicAdd(next, 1);
+            __syncthreads();
+            si = cur;
+            if (si >= nseg) break;
+        } else {
+            if (it > 0) break;
+            si = blockIdx.x;
+        }
+        const int4 sg = segs[si];
+        const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
+        const int tb = tb_[leaf], te = te_[leaf];
+        __syncthreads();
+        for (int t0 = tb; t0 < te; t0 += NEAR_T) {
+            const int nT = min(NEAR_T, te - t0);
+            const int nph = NEAR_T / nT;
+            const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
+            const bool active = ph < nph;
+            double X = 0, Y = 0, Z = 0;
+            if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
+            double acc[4] = {0., 0., 0., 0.};
+            for (int rr = r0; rr < r1; ++rr) {
+                const int b = near_range[2 * rr], e = near_range[2 * rr + 1];
+                for (int s0 = b; s0 < e; s0 += NEAR_TILE) {
+                    const int cnt = min(NEAR_TILE, e - s0);
+                    __syncthreads();
+                    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+                        S[0][q] = sx[s0 + q];
+                        S[1][q] = sy[s0 + q];
+                        S[2][q] = sz[s0 + q];
+                        S[3][q] = dens[s0 + q];
+                        S[4][q] = dens[ns + s0 + q];
+                        S[5][q] = dens[2 * ns + s0 + q];
+                        S[6][q] = dens[3 * ns + s0 + q];
+                    }
+                    __syncthreads();
+                    if (active)
+                        for (int q = ph; q < cnt; q += nph)
+                            near_pair64(kp, S[0][q] - X, S[1][q] - Y, S[2][q] - Z, S[3][q], S[4][q], S[5][q], S[6][q],
+                                        acc);
+                }
+            }
+            for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = acc[o];
+            __syncthreads();
+            if (threadIdx.x < nT) {
+                double f[4] = {0., 0., 0., 0.};
+                for (int q = 0; q < nph; ++q)
+                    for (int o = 0; o < 4; ++o) f[o] += red[threadIdx.x + q * nT][o];
+                // L2P (bbfmm.h:600): local expansion at the target, by the leaf's first segment
+                double l2p[4] = {0., 0., 0., 0.};
+                if (mode & l2p_mask & 1) {
+                    double Sp[3][MAXP];
+                    const double xyz[3] = {X, Y, Z};
+                    for (int a = 0; a < 3; ++a) interp1(T, (xyz[a] - ctr[3 * leaf + a]) / rad[3 * leaf + a], Sp[a]);
+                    const int p = T.p, R = T.R;
+                    const double *L = local + (long)leaf * 4 * R;
+                    for (int c = 0; c < R; ++c) {
+                        const double w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                        for (int o = 0; o < 4; ++o) l2p[o] += w * L[o * R + c];
+                    }
+                }
+                for (int o = 0; o < 4; ++o) {
+                    double *dst = out + o * nt + t0 + threadIdx.x;
+                    if (mode & 2) atomicAdd(dst, f[o] + l2p[o]);
+                    else *dst = f[o] + l2p[o];
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// L2P alone (bbfmm.h:600), one target leaf per block, added to the near-field sums already in
+// `out`: the form used when the near field runs beside the far field.
+__global__ void __launch_bounds__(NEAR_T) k_l2p64(const ChebTables *__restrict__ tab, const int *__restrict__ tleaf,
+                                                  const int *__restrict__ tb_, const int *__restrict__ te_,
+                                                  const double *__restrict__ ctr, const double *__restrict__ rad,
+                                                  const double *__restrict__ tx, const double *__restrict__ ty,
+                                                  const double *__restrict__ tz, long nt,
+                                                  const double *__restrict__ local, double *out) {
+    __shared__ ChebTables T;
+    __shared__ double Ls[4 * MAXR];                // the leaf's local expansion
+    __shared__ double W[3][NEAR_T][MAXP + 1];      // per-thread interpolation weights (odd stride)
+    for (int t = threadIdx.x; t < (int)(sizeof(ChebTables) / 8); t += blockDim.x)
+        reinterpret_cast<double *>(&T)[t] = reinterpret_cast<const double *>(tab)[t];
+    const int leaf = tleaf[blockIdx.x];
     const int tb = tb_[leaf], te = te_[leaf];
     __syncthreads();
-    for (int t0 = tb; t0 < te; t0 += NEAR_T) {
-        const int nT = min(NEAR_T, te - t0);
-        const int nph = NEAR_T / nT;
-        const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
-        const bool active = ph < nph;
-        double X = 0, Y = 0, Z = 0;
-        if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
-        double acc[4] = {0., 0., 0., 0.};
-        for (int rr = r0; rr < r1; ++rr) {
-            const int b = near_range[2 * rr], e = near_range[2 * rr + 1];
-            for (int s0 = b; s0 < e; s0 += NEAR_TILE) {
-                const int cnt = min(NEAR_TILE, e - s0);
-                __syncthreads();
-                for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-                    S[0][q] = sx[s0 + q];
-                    S[1][q] = sy[s0 + q];
-                    S[2][q] = sz[s0 + q];
-                    S[3][q] = dens[s0 + q];
-                    S[4][q] = dens[ns + s0 + q];
-                    S[5][q] = dens[2 * ns + s0 + q];
-                    S[6][q] = dens[3 * ns + s0 + q];
-                }
-                __syncthreads();
-                if (active)
-                    for (int q = ph; q < cnt; q += nph)
-                        near_pair64(kp, S[0][q] - X, S[1][q] - Y, S[2][q] - Z, S[3][q], S[4][q], S[5][q], S[6][q],
-                                    acc);
-            }
-        }
-        for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = acc[o];
-        __syncthreads();
-        if (threadIdx.x < nT) {
-            double f[4] = {0., 0., 0., 0.};
-            for (int q = 0; q < nph; ++q)
-                for (int o = 0; o < 4; ++o) f[o] += red[threadIdx.x + q * nT][o];
-            // L2P (bbfmm.h:600): local expansion at the target, by the leaf's first segment
-            double l2p[4] = {0., 0., 0., 0.};
-            if (mode & 1) {
-                double Sp[3][MAXP];
-                const double xyz[3] = {X, Y, Z};
-                for (int a = 0; a < 3; ++a) interp1(T, (xyz[a] - ctr[3 * leaf + a]) / rad[3 * leaf + a], Sp[a]);
-                const int p = T.p, R = T.R;
-                const double *L = local + (long)leaf * 4 * R;
-                for (int c = 0; c < R; ++c) {
-                    const double w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
-                    for (int o = 0; o < 4; ++o) l2p[o] += w * L[o * R + c];
+    const int p = T.p, R = p * p * p;
+    for (int i = threadIdx.x; i < 4 * R; i += blockDim.x) Ls[i] = local[(long)leaf * 4 * R + i];
+    __syncthreads();
+    double *w0 = W[0][threadIdx.x], *w1 = W[1][threadIdx.x], *w2 = W[2][threadIdx.x];
+    for (int t = tb + threadIdx.x; t < te; t += blockDim.x) {
+        interp1(T, (tx[t] - ctr[3 * leaf]) / rad[3 * leaf], w0);
+        interp1(T, (ty[t] - ctr[3 * leaf + 1]) / rad[3 * leaf + 1], w1);
+        interp1(T, (tz[t] - ctr[3 * leaf + 2]) / rad[3 * leaf + 2], w2);
+        double l2p[4] = {0., 0., 0., 0.};
+        int c = 0;
+        for (int c2 = 0; c2 < p; ++c2) {
+            const double s2 = w2[c2];
+            for (int c1 = 0; c1 < p; ++c1) {
+                const double s1 = w1[c1];
+                for (int c0 = 0; c0 < p; ++c0, ++c) {
+                    const double w = w0[c0] * s1 * s2;
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) l2p[o] += w * Ls[o * R + c];
                 }
             }
-            for (int o = 0; o < 4; ++o) {
-                double *dst = out + o * nt + t0 + threadIdx.x;
-                if (mode & 2) atomicAdd(dst, f[o] + l2p[o]);
-                else *dst = f[o] + l2p[o];
-            }
         }
-        __syncthreads();
+        for (int o = 0; o < 4; ++o) out[o * nt + t] += l2p[o];
     }
 }
 
@@ -991,44 +1049,116 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
     else
         fmm_prepare_operators(P, kpp, IBIM_PRECISION_FP64);
     const TargetSet &S = *P.targets[ts];
-    cudaStream_t s = P.ctx->stream;
+    Ctx *c = P.ctx;
+    cudaStream_t s = c->stream;
     const TreeHost &T = P.tree;
     const int R = P.R, n4 = 4 * R;
     const KParams kp = make_kparams(kpp, P.tube->h);
     const size_t smem_k = sizeof(double) * 3 * n4;
-    if (P.np2m > 0)
-        { ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 56.0 * P.ns); (count_launch(), k_p2m64<<<P.np2m, 128, 0, s>>>(P.tables.ptr, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
-                                       P.ncenter.ptr, P.nradius.ptr, P.sx.ptr, P.sy.ptr, P.sz.ptr, dens, P.ns,
-                                       P.mult.ptr)); }
-    for (int l = T.nlevels - 1; l >= 0; --l) {
-        const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
-        if (e > b)
-            { ProfScope ps_(PROF_M2M); (count_launch(), k_m2m64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, P.m2m_nodes.ptr + b, P.nchild_first.ptr, P.nempty.ptr,
-                                               P.mult.ptr)); }
-    }
-    P.local.zero();
-    if (use_oz) {
-        m2l_oz_run(P, S);
-    } else if (S.nchunks > 0)
-        { ProfScope ps_(PROF_M2L_V64, 2.0 * n4 * (double)n4 * S.nvpairs, 8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops)); (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr,
-                                                                       P.ops64.ptr, P.mult.ptr, P.local.ptr)); }
-    if (S.nxpairs > 0)
-        { ProfScope ps_(PROF_M2L_X64, 102.0 * R * (double)R * S.nxpairs, 16.0 * n4 * S.nxpairs); (count_launch(), k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr, P.ncenter.ptr,
-                                                 P.nradius.ptr, P.mult.ptr, P.local.ptr)); }
-    for (int l = 3; l < T.nlevels; ++l) {
-        const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
-        if (e > b)
-            { ProfScope ps_(PROF_L2L); (count_launch(), k_l2l64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
-                                               P.local.ptr)); }
-    }
     const double *tx = S.self ? P.sx.ptr : S.tx.ptr;
     const double *ty = S.self ? P.sy.ptr : S.ty.ptr;
     const double *tz = S.self ? P.sz.ptr : S.tz.ptr;
-    if (S.ntleaves > 0 && S.near_atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
-    if (S.ntleaves > 0)
-        { ProfScope ps_(PROF_NEAR64, 70.0 * S.near_pairs, 56.0 * P.ns + 40.0 * S.nt); (count_launch(), k_near64<<<S.nnear_seg, NEAR_T, 0, s>>>(P.tables.ptr, kp, reinterpret_cast<const int4 *>(S.near_seg.ptr), S.near_range.ptr,
-                                               S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
-                                               P.sy.ptr, P.sz.ptr, dens, P.ns, tx, ty, tz, S.nt, P.local.ptr, out)); }
+    // near field (U and W lists, bbfmm.h:571-609): depends only on the densities.  With the
+    // overlap on it starts on the auxiliary stream at full occupancy, CTAs taking work segments
+    // from a counter, beside the far field; the L2P follows the join (see fmm_run_mixed).  The
+    // FP64-class path evaluates it in float-float on the FP32 pipes over the FP32 near lists.
+    const bool ff = m2l_sliced && near_ff_enabled() && S.ntleaves > 0;
+    KParamsFF kff{};
+    if (ff) {
+        prepare_mixed(P, *P.targets[ts]);
+        kff = make_kparams_ff(kp);
+        near_ff_pack(P, dens, s);
+    }
+    const int nseg = ff ? S.nnear32_seg : S.nnear_seg;
+    const bool atomic = ff ? S.near32_atomic : S.near_atomic;
+    auto near = [&](cudaStream_t st, int l2p_mask, int grid, int *next, bool count_work) {
+        if (ff) {
+            ProfScope ps_(PROF_NEARFF, count_work ? NEAR_FF_FLOPS * S.near_pairs : 0.,
+                          count_work ? 64.0 * P.ns + 40.0 * S.nt : 0., st);
+            near_ff_run(P, S, kff, out, st, grid, next);
+            return;
+        }
+        ProfScope ps_(PROF_NEAR64, count_work ? 70.0 * S.near_pairs : 0., count_work ? 56.0 * P.ns + 40.0 * S.nt : 0.,
+                      st);
+        (count_launch(), k_near64<<<grid, NEAR_T, 0, st>>>(P.tables.ptr, kp, reinterpret_cast<const int4 *>(S.near_seg.ptr),
+                                                         S.near_range.ptr, S.tbeg.ptr, S.tend.ptr, P.ncenter.ptr,
+                                                         P.nradius.ptr, P.sx.ptr, P.sy.ptr, P.sz.ptr, dens, P.ns, tx,
+                                                         ty, tz, S.nt, P.local.ptr, out, l2p_mask, S.nnear_seg, next));
+    };
+    const bool overlap = near_overlap() && S.ntleaves > 0;
+    static const int occ64 = [] {
+        int b = 0;
+        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near64, NEAR_T, 0));
+        return std::max(1, b);
+    }();
+    const int full = (ff ? near_ff_occupancy() : occ64) * c->num_sms;
+    const int side = near_side_ctas() > 0 ? near_side_ctas() * c->num_sms : full;
+    if (overlap) {
+        if (!P.near_next.ptr) P.near_next.alloc(1, s);
+        IBIM_CUDA(cudaMemsetAsync(P.near_next.ptr, 0, sizeof(int), s));
+        if (atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
+        IBIM_CUDA(cudaEventRecord(c->ev_near_fork, s));
+        IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_near_fork, 0));
+        near(c->aux, 0, std::min(nseg, side), P.near_next.ptr, true);
+        IBIM_CUDA(cudaEventRecord(c->ev_near_join, c->aux));
+    }
+    try {
+        if (P.np2m > 0) {
+            ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 56.0 * P.ns);
+            (count_launch(), k_p2m64<<<P.np2m, 128, 0, s>>>(P.tables.ptr, P.p2m_nodes.ptr, P.nsrc_begin.ptr,
+                                                            P.nsrc_end.ptr, P.ncenter.ptr, P.nradius.ptr, P.sx.ptr,
+                                                            P.sy.ptr, P.sz.ptr, dens, P.ns, P.mult.ptr));
+        }
+        for (int l = T.nlevels - 1; l >= 0; --l) {
+            const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
+            if (e > b) {
+                ProfScope ps_(PROF_M2M);
+                (count_launch(), k_m2m64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, P.m2m_nodes.ptr + b,
+                                                                    P.nchild_first.ptr, P.nempty.ptr, P.mult.ptr));
+            }
+        }
+        P.local.zero();
+        if (use_oz) {
+            m2l_oz_run(P, S);
+        } else if (S.nchunks > 0) {
+            ProfScope ps_(PROF_M2L_V64, 2.0 * n4 * (double)n4 * S.nvpairs,
+                          8.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));
+            (count_launch(), k_m2l_v64<<<S.nchunks, 256, sizeof(double) * M2L_CH * n4, s>>>(
+                 n4, S.v_chunk.ptr, S.v_src.ptr, S.v_tgt.ptr, P.ops64.ptr, P.mult.ptr, P.local.ptr));
+        }
+        if (S.nxpairs > 0) {
+            ProfScope ps_(PROF_M2L_X64, 102.0 * R * (double)R * S.nxpairs, 16.0 * n4 * S.nxpairs);
+            (count_launch(), k_m2l_x64<<<(int)S.nxpairs, 128, 0, s>>>(P.tables.ptr, kp, S.x_src.ptr, S.x_tgt.ptr,
+                                                                      P.ncenter.ptr, P.nradius.ptr, P.mult.ptr,
+                                                                      P.local.ptr));
+        }
+        for (int l = 3; l < T.nlevels; ++l) {
+            const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
+            if (e > b) {
+                ProfScope ps_(PROF_L2L);
+                (count_launch(), k_l2l64<<<e - b, 128, smem_k, s>>>(P.tables.ptr, S.l2l_nodes.ptr + b, P.nparent.ptr,
+                                                                    P.nindex8.ptr, P.local.ptr));
+            }
+        }
+    } catch (...) {
+        if (overlap) cudaStreamSynchronize(c->aux);  // the near field still reads dens and writes out
+        throw;
+    }
+    if (S.ntleaves > 0) {
+        if (overlap) {
+            if (side < std::min(nseg, full)) near(s, 0, std::min(nseg, full), P.near_next.ptr, false);
+            IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_near_join, 0));
+        } else {
+            if (atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
+            near(s, 1, nseg, nullptr, true);
+        }
+        if (overlap || ff) {  // the L2P runs on its own after the near field
+            ProfScope ps_(PROF_L2P64, (10.0 * R + 6.0 * P.p * P.p) * S.nt, 32.0 * n4 * S.ntleaves + 88.0 * S.nt);
+            (count_launch(), k_l2p64<<<S.ntleaves, NEAR_T, 0, s>>>(P.tables.ptr, S.tleaf.ptr, S.tbeg.ptr, S.tend.ptr,
+                                                                   P.ncenter.ptr, P.nradius.ptr, tx, ty, tz, S.nt,
+                                                                   P.local.ptr, out));
+        }
+    }
     IBIM_CHECK_LAUNCH();
 }
 

@@ -128,6 +128,29 @@ __device__ __forceinline__ void near_pair64(const KParams &k, double dx, double 
     acc[3] += hd * m2 + dz * cm;
 }
 
+// Kernel parameters of the float-float near field (hi, lo word pairs) with the tables of its
+// exponential: e0[j] = e^{-j/64}, e1[j] = e^{-j}.
+struct KParamsFF {
+    float2 kappa, eps, ieps, k2in, q4pi, vr2, k3f;
+    int yukawa;
+    float2 e0[64], e1[64];
+};
+KParamsFF make_kparams_ff(const KParams &k);
+// FP32 flops (an FMA counts 2) of one float-float pair update outside the cutoff
+constexpr double NEAR_FF_FLOPS = 690.0;
+// Whether the FP64-class matvec evaluates its near field in float-float (default; IBIM_NEAR_FF=0
+// keeps native FP64).
+bool near_ff_enabled();
+int near_ff_occupancy();
+// Leaf-relative coordinates, FP32 near lists and segments of a target set (shared by the mixed
+// path and the float-float near field).
+void prepare_mixed(Plan &P, TargetSet &S);
+// Pack one matvec's densities (4 x ns, FP64) into the float-float source records.
+void near_ff_pack(Plan &P, const double *dens, cudaStream_t st);
+// Near field without the L2P into out (4 x nt), over the FP32 near segments: grid CTAs, taking
+// segments from *next when next is not null (else one segment per CTA).
+void near_ff_run(Plan &P, const TargetSet &S, const KParamsFF &kp, double *out, cudaStream_t st, int grid, int *next);
+
 void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale);
 // ops64: the FP64 operators for the same kernel parameters (rounded instead of re-evaluated), or null
 void fmm_prepare_operators_mixed(Plan &P, const KParams &k, const double *ops64);

@@ -56,17 +56,23 @@ __device__ __forceinline__ void load_tables(TT &T, const TT *__restrict__ g) {
     for (int t = threadIdx.x; t < n; t += blockDim.x) reinterpret_cast<int *>(&T)[t] = reinterpret_cast<const int *>(g)[t];
 }
 
+// Coordinates relative to the leaf centre, rounded to FP32 (xf) with the rounding error as a
+// second FP32 word (xl: the float-float low word).
 __global__ void k_rel_coords(int nleaf, const int *__restrict__ leaves, const int *__restrict__ b_,
                              const int *__restrict__ e_, const double *__restrict__ ctr, const double *__restrict__ x,
                              const double *__restrict__ y, const double *__restrict__ z, float *xf, float *yf,
-                             float *zf) {
+                             float *zf, float *xl, float *yl, float *zl) {
     const int L = blockIdx.x < nleaf ? leaves[blockIdx.x] : -1;
     if (L < 0) return;
     const double cx = ctr[3 * L], cy = ctr[3 * L + 1], cz = ctr[3 * L + 2];
     for (int i = b_[L] + threadIdx.x; i < e_[L]; i += blockDim.x) {
-        xf[i] = (float)(x[i] - cx);
-        yf[i] = (float)(y[i] - cy);
-        zf[i] = (float)(z[i] - cz);
+        const double dx = x[i] - cx, dy = y[i] - cy, dz = z[i] - cz;
+        xf[i] = (float)dx;
+        yf[i] = (float)dy;
+        zf[i] = (float)dz;
+        xl[i] = (float)(dx - (double)xf[i]);
+        yl[i] = (float)(dy - (double)yf[i]);
+        zl[i] = (float)(dz - (double)zf[i]);
     }
 }
 
@@ -425,116 +431,171 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                                                  const float *__restrict__ rad, const float4 *__restrict__ src8,
                                                  const float *__restrict__ tx, const float *__restrict__ ty,
                                                  const float *__restrict__ tz, long nt,
-                                                 const float *__restrict__ local, double *out) {
+                                                 const float *__restrict__ local, double *out, int l2p_mask,
+                                                 int nseg, int *next) {
     __shared__ ChebTables32 T;
     __shared__ float S[7][TILE32];
     __shared__ float red[NT32][4];
+    __shared__ int cur;
     load_tables(T, tab);
-    const int4 sg = segs[blockIdx.x];
-    const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
-    const int tb = tb_[leaf], te = te_[leaf];
-    __syncthreads();
-    for (int t0 = tb; t0 < te; t0 += NT32) {
-        const int nT = min(NT32, te - t0);
-        const int nph = NT32 / nT;
-        const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
-        const bool active = ph < nph;
-        float X = 0.f, Y = 0.f, Z = 0.f;
-        if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
-        float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
-        // fill tiles across consecutive source leaves
-        int rr = r0, pos = r1 > r0 ? nrange[2 * r0] : 0;
-        while (rr < r1) {
+    // with a work counter the CTA takes segments until none is left (several launches may drain
+    // the same counter); without one it does segment blockIdx.x
+    for (int it = 0;; ++it) {
+        int si;
+        if (next) {
+            __syncthreads();  // every thread has read the previous segment number
+            if (threadIdx.x == 0) cur = atomicAdd(next, 1);
             __syncthreads();
-            int filled = 0;
-            // sequentially pack up to TILE32 sources; each thread copies its slots
-            int lrr = rr, lpos = pos;
-            while (lrr < r1 && filled < TILE32) {
-                const int e = nrange[2 * lrr + 1];
-                const int take = min(TILE32 - filled, e - lpos);
-                const float ox = noff[3 * lrr], oy = noff[3 * lrr + 1], oz = noff[3 * lrr + 2];
-                for (int q = threadIdx.x; q < take; q += blockDim.x) {
-                    const int si = lpos + q;
-                    const float4 A = __ldg(src8 + 2 * si), B = __ldg(src8 + 2 * si + 1);
-                    S[0][filled + q] = A.x + ox;
-                    S[1][filled + q] = A.y + oy;
-                    S[2][filled + q] = A.z + oz;
-                    S[3][filled + q] = A.w;
-                    S[4][filled + q] = B.x;
-                    S[5][filled + q] = B.y;
-                    S[6][filled + q] = B.z;
-                }
-                filled += take;
-                lpos += take;
-                if (lpos >= e) {
-                    ++lrr;
-                    if (lrr < r1) lpos = nrange[2 * lrr];
-                }
-            }
-            rr = lrr;
-            pos = lpos;
-            __syncthreads();
-            if (active) {
-                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-                for (int q = ph; q < filled; q += nph) {
-                    const float dx = S[0][q] - X, dy = S[1][q] - Y, dz = S[2][q] - Z;
-                    const float m0 = S[3][q], m1 = S[4][q], m2 = S[5][q], psi = S[6][q];
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if (d2 < kp.vr2) {
-                        a0 -= kp.k2in * psi;
-                        continue;
+            si = cur;
+            if (si >= nseg) break;
+        } else {
+            if (it > 0) break;
+            si = blockIdx.x;
+        }
+        const int4 sg = segs[si];
+        const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
+        const int tb = tb_[leaf], te = te_[leaf];
+        __syncthreads();
+        for (int t0 = tb; t0 < te; t0 += NT32) {
+            const int nT = min(NT32, te - t0);
+            const int nph = NT32 / nT;
+            const int my_t = threadIdx.x % nT, ph = threadIdx.x / nT;
+            const bool active = ph < nph;
+            float X = 0.f, Y = 0.f, Z = 0.f;
+            if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
+            float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+            // fill tiles across consecutive source leaves
+            int rr = r0, pos = r1 > r0 ? nrange[2 * r0] : 0;
+            while (rr < r1) {
+                __syncthreads();
+                int filled = 0;
+                // sequentially pack up to TILE32 sources; each thread copies its slots
+                int lrr = rr, lpos = pos;
+                while (lrr < r1 && filled < TILE32) {
+                    const int e = nrange[2 * lrr + 1];
+                    const int take = min(TILE32 - filled, e - lpos);
+                    const float ox = noff[3 * lrr], oy = noff[3 * lrr + 1], oz = noff[3 * lrr + 2];
+                    for (int q = threadIdx.x; q < take; q += blockDim.x) {
+                        const int si = lpos + q;
+                        const float4 A = __ldg(src8 + 2 * si), B = __ldg(src8 + 2 * si + 1);
+                        S[0][filled + q] = A.x + ox;
+                        S[1][filled + q] = A.y + oy;
+                        S[2][filled + q] = A.z + oz;
+                        S[3][filled + q] = A.w;
+                        S[4][filled + q] = B.x;
+                        S[5][filled + q] = B.y;
+                        S[6][filled + q] = B.z;
                     }
-                    const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
-                    const float t = kp.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
-                    const float q3 = ir3 * kp.q4pi, h3 = ir3 * kp.k3f;
-                    const float c1 = (kp.eps * et1 - 1.f) * q3;
-                    const float c4 = (1.f - kp.ieps * et1) * q3;
-                    const float k2 = (1.f - e) * ir * kp.q4pi;
-                    const float hd = (1.f - et1) * h3;
-                    const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * h3 * ir2;
-                    const float dm = dx * m0 + dy * m1 + dz * m2;
-                    a0 += c1 * dm - k2 * psi;
-                    const float cm = ho * dm - c4 * psi;
-                    a1 += hd * m0 + dx * cm;
-                    a2 += hd * m1 + dy * cm;
-                    a3 += hd * m2 + dz * cm;
+                    filled += take;
+                    lpos += take;
+                    if (lpos >= e) {
+                        ++lrr;
+                        if (lrr < r1) lpos = nrange[2 * lrr];
+                    }
                 }
-                const float part[4] = {a0, a1, a2, a3};
+                rr = lrr;
+                pos = lpos;
+                __syncthreads();
+                if (active) {
+                    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+                    for (int q = ph; q < filled; q += nph) {
+                        const float dx = S[0][q] - X, dy = S[1][q] - Y, dz = S[2][q] - Z;
+                        const float m0 = S[3][q], m1 = S[4][q], m2 = S[5][q], psi = S[6][q];
+                        const float d2 = dx * dx + dy * dy + dz * dz;
+                        if (d2 < kp.vr2) {
+                            a0 -= kp.k2in * psi;
+                            continue;
+                        }
+                        const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
+                        const float t = kp.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
+                        const float q3 = ir3 * kp.q4pi, h3 = ir3 * kp.k3f;
+                        const float c1 = (kp.eps * et1 - 1.f) * q3;
+                        const float c4 = (1.f - kp.ieps * et1) * q3;
+                        const float k2 = (1.f - e) * ir * kp.q4pi;
+                        const float hd = (1.f - et1) * h3;
+                        const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * h3 * ir2;
+                        const float dm = dx * m0 + dy * m1 + dz * m2;
+                        a0 += c1 * dm - k2 * psi;
+                        const float cm = ho * dm - c4 * psi;
+                        a1 += hd * m0 + dx * cm;
+                        a2 += hd * m1 + dy * cm;
+                        a3 += hd * m2 + dz * cm;
+                    }
+                    const float part[4] = {a0, a1, a2, a3};
+    #pragma unroll
+                    for (int o = 0; o < 4; ++o) {  // Kahan: sum += part
+                        const float yk = part[o] - cmp[o];
+                        const float tk = sum[o] + yk;
+                        cmp[o] = (tk - sum[o]) - yk;
+                        sum[o] = tk;
+                    }
+                }
+            }
+            __syncthreads();
+            for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = sum[o] - cmp[o];
+            __syncthreads();
+            if (threadIdx.x < nT) {
+                double f[4] = {0., 0., 0., 0.};
+                for (int q = 0; q < nph; ++q)
+                    for (int o = 0; o < 4; ++o) f[o] += (double)red[threadIdx.x + q * nT][o];
+                float l2p[4] = {0.f, 0.f, 0.f, 0.f};
+                if (mode & l2p_mask & 1) {  // L2P by the leaf's first segment
+                    float Sp[3][MAXP];
+                    const float xyz[3] = {X, Y, Z};
+                    for (int a = 0; a < 3; ++a) interp1f(T, xyz[a] / rad[3 * leaf + a], Sp[a]);
+                    const int p = T.p, R = T.R;
+                    const float *L = local + (long)leaf * 4 * R;
+                    for (int c = 0; c < R; ++c) {
+                        const float w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
+                        for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, L[o * R + c], l2p[o]);
+                    }
+                }
+                for (int o = 0; o < 4; ++o) {
+                    double *dst = out + o * nt + t0 + threadIdx.x;
+                    if (mode & 2) atomicAdd(dst, f[o] + (double)l2p[o]);
+                    else *dst = f[o] + (double)l2p[o];
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// L2P alone (downPass leaf, bbfmm.h:600), one target leaf per block, added to the near-field
+// sums already in `out`: the form used when the near field runs beside the far field.
+__global__ void __launch_bounds__(NT32) k_l2p32(const ChebTables32 *__restrict__ tab, const int *__restrict__ tleaf,
+                                                const int *__restrict__ tb_, const int *__restrict__ te_,
+                                                const float *__restrict__ rad, const float *__restrict__ tx,
+                                                const float *__restrict__ ty, const float *__restrict__ tz, long nt,
+                                                const float *__restrict__ local, double *out) {
+    __shared__ ChebTables32 T;
+    __shared__ float Ls[4 * MAXR];                 // the leaf's local expansion
+    __shared__ float W[3][NT32][MAXP + 1];         // per-thread interpolation weights (odd stride)
+    load_tables(T, tab);
+    const int leaf = tleaf[blockIdx.x];
+    const int tb = tb_[leaf], te = te_[leaf];
+    const int p = T.p, R = p * p * p;
+    for (int i = threadIdx.x; i < 4 * R; i += blockDim.x) Ls[i] = local[(long)leaf * 4 * R + i];
+    __syncthreads();
+    float *w0 = W[0][threadIdx.x], *w1 = W[1][threadIdx.x], *w2 = W[2][threadIdx.x];
+    for (int t = tb + threadIdx.x; t < te; t += blockDim.x) {
+        interp1f(T, tx[t] / rad[3 * leaf], w0);
+        interp1f(T, ty[t] / rad[3 * leaf + 1], w1);
+        interp1f(T, tz[t] / rad[3 * leaf + 2], w2);
+        float l2p[4] = {0.f, 0.f, 0.f, 0.f};
+        int c = 0;
+        for (int c2 = 0; c2 < p; ++c2) {
+            const float s2 = w2[c2];
+            for (int c1 = 0; c1 < p; ++c1) {
+                const float s1 = w1[c1];
+                for (int c0 = 0; c0 < p; ++c0, ++c) {
+                    const float w = w0[c0] * s1 * s2;
 #pragma unroll
-                for (int o = 0; o < 4; ++o) {  // Kahan: sum += part
-                    const float yk = part[o] - cmp[o];
-                    const float tk = sum[o] + yk;
-                    cmp[o] = (tk - sum[o]) - yk;
-                    sum[o] = tk;
+                    for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, Ls[o * R + c], l2p[o]);
                 }
             }
         }
-        __syncthreads();
-        for (int o = 0; o < 4; ++o) red[threadIdx.x][o] = sum[o] - cmp[o];
-        __syncthreads();
-        if (threadIdx.x < nT) {
-            double f[4] = {0., 0., 0., 0.};
-            for (int q = 0; q < nph; ++q)
-                for (int o = 0; o < 4; ++o) f[o] += (double)red[threadIdx.x + q * nT][o];
-            float l2p[4] = {0.f, 0.f, 0.f, 0.f};
-            if (mode & 1) {  // L2P by the leaf's first segment
-                float Sp[3][MAXP];
-                const float xyz[3] = {X, Y, Z};
-                for (int a = 0; a < 3; ++a) interp1f(T, xyz[a] / rad[3 * leaf + a], Sp[a]);
-                const int p = T.p, R = T.R;
-                const float *L = local + (long)leaf * 4 * R;
-                for (int c = 0; c < R; ++c) {
-                    const float w = Sp[0][c % p] * Sp[1][(c / p) % p] * Sp[2][c / (p * p)];
-                    for (int o = 0; o < 4; ++o) l2p[o] = fmaf(w, L[o * R + c], l2p[o]);
-                }
-            }
-            for (int o = 0; o < 4; ++o) {
-                double *dst = out + o * nt + t0 + threadIdx.x;
-                if (mode & 2) atomicAdd(dst, f[o] + (double)l2p[o]);
-                else *dst = f[o] + (double)l2p[o];
-            }
-        }
-        __syncthreads();
+        for (int o = 0; o < 4; ++o) out[o * nt + t] += (double)l2p[o];
     }
 }
 
@@ -549,7 +610,10 @@ void up_f(DevBuf<float> &b, const std::vector<float> &v, cudaStream_t s) {
     b.upload(v.data(), v.size());
 }
 
-// Leaf-relative FP32 coordinates, FP32 tables, and the FP32 near and X lists of a target set.
+}  // namespace
+
+// Leaf-relative FP32 coordinates (high and low words), FP32 tables, and the FP32 near and X
+// lists of a target set.
 void prepare_mixed(Plan &P, TargetSet &S) {
     cudaStream_t s = P.ctx->stream;
     const TreeHost &T = P.tree;
@@ -578,6 +642,9 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         P.sxf.alloc(P.ns, s);
         P.syf.alloc(P.ns, s);
         P.szf.alloc(P.ns, s);
+        P.sxl.alloc(P.ns, s);
+        P.syl.alloc(P.ns, s);
+        P.szl.alloc(P.ns, s);
         std::vector<int> leaves;
         for (int i = 0; i < nn; ++i)
             if (T.leaf[i] && T.src_end[i] > T.src_begin[i]) leaves.push_back(i);
@@ -586,7 +653,8 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         if (!leaves.empty())
             (count_launch(), k_rel_coords<<<(int)leaves.size(), 128, 0, s>>>((int)leaves.size(), dl.ptr, P.nsrc_begin.ptr,
                                                                        P.nsrc_end.ptr, P.ncenter.ptr, P.sx.ptr, P.sy.ptr,
-                                                                       P.sz.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr));
+                                                                       P.sz.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr,
+                                                                       P.sxl.ptr, P.syl.ptr, P.szl.ptr));
         IBIM_CHECK_LAUNCH();
         const int n4 = 4 * P.R;
         P.mult32.alloc((size_t)nn * n4, s);
@@ -612,18 +680,22 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         S.txf.alloc(std::max<long>(1, S.nt), s);
         S.tyf.alloc(std::max<long>(1, S.nt), s);
         S.tzf.alloc(std::max<long>(1, S.nt), s);
+        S.txl.alloc(std::max<long>(1, S.nt), s);
+        S.tyl.alloc(std::max<long>(1, S.nt), s);
+        S.tzl.alloc(std::max<long>(1, S.nt), s);
         DevBuf<int> dl;
         up_i(dl, leaves, s);
         if (!leaves.empty())
             (count_launch(), k_rel_coords<<<(int)leaves.size(), 128, 0, s>>>((int)leaves.size(), dl.ptr, S.tbeg.ptr,
                                                                        S.tend.ptr, P.ncenter.ptr, S.tx.ptr, S.ty.ptr,
-                                                                       S.tz.ptr, S.txf.ptr, S.tyf.ptr, S.tzf.ptr));
+                                                                       S.tz.ptr, S.txf.ptr, S.tyf.ptr, S.tzf.ptr,
+                                                                       S.txl.ptr, S.tyl.ptr, S.tzl.ptr));
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaStreamSynchronize(s));
     }
     // near lists: U and W nodes expanded into their non-empty leaves, with centre offsets
     std::vector<int> ptr{0}, rng;
-    std::vector<float> off;
+    std::vector<float> off, offl;
     std::vector<int> child_first(nn, -1);
     for (int i = nn - 1; i >= 0; --i)
         if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
@@ -642,7 +714,11 @@ void prepare_mixed(Plan &P, TargetSet &S) {
                 if (T.leaf[n]) {
                     rng.push_back(T.src_begin[n]);
                     rng.push_back(T.src_end[n]);
-                    for (int a = 0; a < 3; ++a) off.push_back((float)(T.center[3 * n + a] - T.center[3 * i + a]));
+                    for (int a = 0; a < 3; ++a) {
+                        const double d = T.center[3 * n + a] - T.center[3 * i + a];
+                        off.push_back((float)d);
+                        offl.push_back((float)(d - (double)(float)d));
+                    }
                 } else {
                     for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
                 }
@@ -661,6 +737,7 @@ void prepare_mixed(Plan &P, TargetSet &S) {
     up_i(S.near32_ptr, ptr, s);
     up_i(S.near32_range, rng, s);
     up_f(S.near32_off, off, s);
+    up_f(S.near32_offl, offl, s);
     S.near32_entries = (int)rng.size() / 2;
     // X pair centre offsets (FP64 difference, rounded)
     std::vector<int> xs(std::max<long>(1, S.nxpairs)), xt(std::max<long>(1, S.nxpairs));
@@ -677,7 +754,6 @@ void prepare_mixed(Plan &P, TargetSet &S) {
     S.mixed_ready = true;
 }
 
-}  // namespace
 
 void fmm_prepare_operators_mixed(Plan &P, const KParams &k, const double *ops64) {
     cudaStream_t s = P.ctx->stream;
@@ -699,6 +775,22 @@ bool mixed_uses_tc() {
     return !simt_m2l && m2l_tc_supported();
 }
 
+bool near_overlap() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_NEAR_OVERLAP");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+int near_side_ctas() {
+    static const int n = [] {
+        const char *v = std::getenv("IBIM_NEAR_SIDE");
+        return v ? std::max(0, std::atoi(v)) : 0;
+    }();
+    return n;
+}
+
 void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out) {
     IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
     TargetSet &S = *P.targets[ts];
@@ -717,52 +809,89 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     const ChebTables32 *tab = reinterpret_cast<const ChebTables32 *>(P.tables32.ptr);
     (count_launch(), k_pack_src32<<<ew(c, P.ns), 256, 0, s>>>(P.ns, dens, P.sxf.ptr, P.syf.ptr, P.szf.ptr,
                                                                P.dens32.ptr, P.src8.ptr));
-    if (P.np2m > 0) {
-        ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 28.0 * P.ns);
-        (count_launch(), k_p2m32<<<P.np2m, 128, 0, s>>>(tab, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
-                                                        P.nrad32.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr,
-                                                        P.ns, P.mult32.ptr));
-    }
-    const size_t smk = sizeof(float) * 3 * n4, smk_m2m = sizeof(float) * 16 * n4;
-    for (int l = T.nlevels - 1; l >= 0; --l) {
-        const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
-        if (e > b) {
-            ProfScope ps_(PROF_M2M);
-            (count_launch(), k_m2m32<<<e - b, M2M32_THREADS, smk_m2m, s>>>(tab, P.m2m_nodes.ptr + b, P.nchild_first.ptr,
-                                                                            P.nempty.ptr, P.mult32.ptr));
-        }
-    }
-    P.local32.zero();
-    if (tc) {
-        m2l_tc_run(P, S);
-    } else if (S.nchunks32 > 0) {
-        ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 4.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));
-        const dim3 grid(S.nchunks32, div_up(n4, GM_BM));
-        (count_launch(), k_m2l_v32<<<grid, 256, 0, s>>>(n4, S.v_chunk32.ptr, S.v_src.ptr, S.v_tgt.ptr, P.ops32.ptr,
-                                                        P.mult32.ptr, P.local32.ptr));
-    }
-    if (S.nxpairs > 0) {
-        ProfScope ps_(PROF_M2L_X, 102.0 * R * (double)R * S.nxpairs, 8.0 * n4 * S.nxpairs);
-        (count_launch(), k_m2l_x32<<<(int)S.nxpairs, 128, 0, s>>>(tab, k32, S.x_src.ptr, S.x_tgt.ptr, S.x_off32.ptr,
-                                                                  P.nrad32.ptr, P.mult32.ptr, P.local32.ptr));
-    }
-    for (int l = 3; l < T.nlevels; ++l) {
-        const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
-        if (e > b) {
-            ProfScope ps_(PROF_L2L);
-            (count_launch(), k_l2l32<<<e - b, 128, smk, s>>>(tab, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
-                                                             P.local32.ptr));
-        }
-    }
     const float *tx = S.self ? P.sxf.ptr : S.txf.ptr;
     const float *ty = S.self ? P.syf.ptr : S.tyf.ptr;
     const float *tz = S.self ? P.szf.ptr : S.tzf.ptr;
-    if (S.ntleaves > 0) {
-        ProfScope ps_(PROF_NEAR, 70.0 * S.near_pairs, 28.0 * P.ns + 40.0 * S.nt);
+    // near field (U and W lists): needs only the packed sources.  With the overlap on it starts on
+    // the auxiliary stream at full occupancy, CTAs taking work segments from a counter, and fills
+    // the SMs the latency-bound far-field launches (P2M, M2M levels) leave idle; the L2P follows
+    // the join.  A smaller side launch (IBIM_NEAR_SIDE CTAs per SM) leaves the rest to a drain
+    // launch after the far field
+    auto near = [&](cudaStream_t st, int l2p_mask, int grid, int *next, double flops) {
+        ProfScope ps_(PROF_NEAR, flops, flops > 0 ? 28.0 * P.ns + 40.0 * S.nt : 0., st);
+        (count_launch(), k_near32<<<grid, NT32, 0, st>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr),
+                                                      S.near32_range.ptr, S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr,
+                                                      P.nrad32.ptr, P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out,
+                                                      l2p_mask, S.nnear32_seg, next));
+    };
+    const bool overlap = near_overlap() && S.ntleaves > 0;
+    static const int occ = [] {
+        int b = 0;
+        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near32, NT32, 0));
+        return std::max(1, b);
+    }();
+    const int full = occ * c->num_sms, side = near_side_ctas() > 0 ? near_side_ctas() * c->num_sms : full;
+    if (overlap) {
+        if (!P.near_next.ptr) P.near_next.alloc(1, s);
+        IBIM_CUDA(cudaMemsetAsync(P.near_next.ptr, 0, sizeof(int), s));
         if (S.near32_atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
-        (count_launch(), k_near32<<<S.nnear32_seg, NT32, 0, s>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr), S.near32_range.ptr,
-                                                              S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr, P.nrad32.ptr,
-                                                              P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out));
+        IBIM_CUDA(cudaEventRecord(c->ev_near_fork, s));
+        IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_near_fork, 0));
+        near(c->aux, 0, std::min(S.nnear32_seg, side), P.near_next.ptr,
+             70.0 * S.near_pairs);
+        IBIM_CUDA(cudaEventRecord(c->ev_near_join, c->aux));
+    }
+    try {
+        if (P.np2m > 0) {
+            ProfScope ps_(PROF_P2M, (8.0 * R + 6.0 * P.p * P.p) * P.ns, 28.0 * P.ns);
+            (count_launch(), k_p2m32<<<P.np2m, 128, 0, s>>>(tab, P.p2m_nodes.ptr, P.nsrc_begin.ptr, P.nsrc_end.ptr,
+                                                            P.nrad32.ptr, P.sxf.ptr, P.syf.ptr, P.szf.ptr, P.dens32.ptr,
+                                                            P.ns, P.mult32.ptr));
+        }
+        const size_t smk = sizeof(float) * 3 * n4, smk_m2m = sizeof(float) * 16 * n4;
+        for (int l = T.nlevels - 1; l >= 0; --l) {
+            const int b = P.m2m_level_begin[l], e = P.m2m_level_begin[l + 1];
+            if (e > b) {
+                ProfScope ps_(PROF_M2M);
+                (count_launch(), k_m2m32<<<e - b, M2M32_THREADS, smk_m2m, s>>>(tab, P.m2m_nodes.ptr + b, P.nchild_first.ptr,
+                                                                                P.nempty.ptr, P.mult32.ptr));
+            }
+        }
+        P.local32.zero();
+        if (tc) {
+            m2l_tc_run(P, S);
+        } else if (S.nchunks32 > 0) {
+            ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs, 4.0 * n4 * (2.0 * S.nvpairs + (double)n4 * P.nops));
+            const dim3 grid(S.nchunks32, div_up(n4, GM_BM));
+            (count_launch(), k_m2l_v32<<<grid, 256, 0, s>>>(n4, S.v_chunk32.ptr, S.v_src.ptr, S.v_tgt.ptr, P.ops32.ptr,
+                                                            P.mult32.ptr, P.local32.ptr));
+        }
+        if (S.nxpairs > 0) {
+            ProfScope ps_(PROF_M2L_X, 102.0 * R * (double)R * S.nxpairs, 8.0 * n4 * S.nxpairs);
+            (count_launch(), k_m2l_x32<<<(int)S.nxpairs, 128, 0, s>>>(tab, k32, S.x_src.ptr, S.x_tgt.ptr, S.x_off32.ptr,
+                                                                      P.nrad32.ptr, P.mult32.ptr, P.local32.ptr));
+        }
+        for (int l = 3; l < T.nlevels; ++l) {
+            const int b = S.l2l_level_begin[l], e = S.l2l_level_begin[l + 1];
+            if (e > b) {
+                ProfScope ps_(PROF_L2L);
+                (count_launch(), k_l2l32<<<e - b, 128, smk, s>>>(tab, S.l2l_nodes.ptr + b, P.nparent.ptr, P.nindex8.ptr,
+                                                                 P.local32.ptr));
+            }
+        }
+    } catch (...) {
+        if (overlap) cudaStreamSynchronize(c->aux);  // the near field still reads dens and writes out
+        throw;
+    }
+    if (overlap) {
+        if (side < std::min(S.nnear32_seg, full)) near(s, 0, std::min(S.nnear32_seg, full), P.near_next.ptr, 0.);
+        IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_near_join, 0));
+        ProfScope ps_(PROF_L2P, (10.0 * R + 6.0 * P.p * P.p) * S.nt, 16.0 * n4 * S.ntleaves + 44.0 * S.nt);
+        (count_launch(), k_l2p32<<<S.ntleaves, NT32, 0, s>>>(tab, S.tleaf.ptr, S.tbeg.ptr, S.tend.ptr, P.nrad32.ptr,
+                                                             tx, ty, tz, S.nt, P.local32.ptr, out));
+    } else if (S.ntleaves > 0) {
+        if (S.near32_atomic) IBIM_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * 4 * S.nt, s));
+        near(s, 1, S.nnear32_seg, nullptr, 70.0 * S.near_pairs);
     }
     IBIM_CHECK_LAUNCH();
 }

@@ -78,6 +78,7 @@ struct DevBuf {
 enum ProfCat {
     PROF_EXPAND = 0, PROF_WENO, PROF_COUNT, PROF_FLOOD, PROF_TUBE, PROF_OPS, PROF_P2M, PROF_M2M, PROF_M2L_V,
     PROF_M2L_X, PROF_L2L, PROF_NEAR, PROF_RHS, PROF_GMRES, PROF_M2L_V64, PROF_M2L_X64, PROF_NEAR64, PROF_M2L_VOZ,
+    PROF_L2P, PROF_L2P64, PROF_NEARFF,
     PROF_NCAT
 };
 
@@ -92,6 +93,8 @@ struct Ctx {
     // forked from and joined back to `stream` by the two events
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the near field of a matvec runs on `aux` while the far field runs on `stream`
+    cudaEvent_t ev_near_fork = nullptr, ev_near_join = nullptr;
     int num_sms = 0;
     unsigned prof_mask = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[PROF_NCAT];
@@ -202,6 +205,8 @@ struct TargetSet {
     DevBuf<float> txf, tyf, tzf;       // target coordinates relative to their leaf centre
     DevBuf<int> near32_ptr, near32_range;  // per target leaf: source leaves (begin, end)
     DevBuf<float> near32_off;          // per source leaf entry: source leaf centre - target leaf centre
+    DevBuf<float> near32_offl;         // its FP32 rounding error (float-float low word)
+    DevBuf<float> txl, tyl, tzl;       // low words of the leaf-relative target coordinates
     int near32_entries = 0;
     DevBuf<int> near32_seg;            // work segments over the near32 ranges (as near_seg)
     int nnear32_seg = 0;
@@ -226,6 +231,7 @@ struct Plan {
     DevBuf<int> p2m_nodes;
     std::vector<int> m2m_level_begin;
     DevBuf<int> m2m_nodes;
+    DevBuf<int> near_next;      // work counter shared by the near-field launches of one matvec
     // M2L operators keyed by (target level, source level, centre offset), union over target sets:
     // the V list's, and (x_as_ops) the X list's, whose pairs then join the V contraction
     bool x_as_ops = true;
@@ -242,6 +248,8 @@ struct Plan {
     DevBuf<float> mult32, local32, dens32;
     DevBuf<float4> src8;           // near-field source records (mixed): {x, y, z, m_x}, {m_y, m_z, psi, 0}
     DevBuf<float> sxf, syf, szf;   // source coordinates relative to their leaf centre (mixed)
+    DevBuf<float> sxl, syl, szl;   // their FP32 rounding errors (float-float low words)
+    DevBuf<float4> src16;          // float-float near-field source records (FP64-class matvec)
     DevBuf<float> nrad32;          // per node radius (mixed)
     DevBuf<unsigned char> tables32;  // ChebTables32
     bool mixed_ready = false;
@@ -287,6 +295,12 @@ void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp);
 void fmm_release_fp64_operators(Plan &P);
 // Whether the mixed path's V-list M2L runs on the tensor cores on this device.
 bool mixed_uses_tc();
+// Whether a matvec's near field runs on the auxiliary stream beside its far field (default on;
+// IBIM_NEAR_OVERLAP=0 runs it after the far field with the L2P fused in).
+bool near_overlap();
+// CTAs per SM of the near-field launch that runs beside the far field (IBIM_NEAR_SIDE; 0, the
+// default, is full occupancy); a drain launch after the far field takes the segments it leaves.
+int near_side_ctas();
 
 // Near-field work segments.  Target leaf k (node tl[k], nt[k] targets) owns source ranges
 // ptr[k] .. ptr[k+1] of `rng` (begin, end pairs); consecutive ranges are grouped into segments of

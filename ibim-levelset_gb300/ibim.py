@@ -53,7 +53,7 @@ EXPORTS = [
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
-                      "near_l2p_fp64", "m2l_v_sliced"]
+                      "near_l2p_fp64", "m2l_v_sliced", "l2p", "l2p_fp64", "near_ff"]
 
 
 class IbimError(RuntimeError):

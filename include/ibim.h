@@ -134,12 +134,17 @@ void *ibim_ctx_stream(ibim_ctx ctx);
 int ibim_ctx_trim(ibim_ctx ctx);
 /* Kernels this library has launched since load (all contexts). */
 long ibim_launch_count(void);
-/* Per-category kernel timing with CUDA events on the context stream.  mask bit k enables
- * category k: 0 expand, 1 WENO stage, 2 gradient count, 3 flood fill, 4 tube extraction,
- * 5 M2L operators, 6 P2M, 7 M2M, 8 M2L (V list), 9 M2L (X list), 10 L2L, 11 near field + L2P,
- * 12 right-hand side, 13 GMRES vector kernels; FP64 versions of 8, 9 and 11 are categories 14, 15
- * and 16 (categories 6-11 then count the mixed-precision kernels); 17 is the V-list M2L of the
- * mixed path's refinement residual (BF16 integer slices on the tensor cores, FP64-class).
+/* Per-category kernel timing with CUDA events on the stream each launch runs on.  mask bit k
+ * enables category k: 0 expand, 1 WENO stage, 2 gradient count, 3 flood fill, 4 tube extraction,
+ * 5 M2L operators, 6 P2M, 7 M2M, 8 M2L (V list), 9 M2L (X list), 10 L2L, 11 near field (+ L2P
+ * when it runs after the far field), 12 right-hand side, 13 GMRES vector kernels; FP64 versions of
+ * 8, 9 and 11 are categories 14, 15 and 16 (categories 6-11 then count the mixed-precision
+ * kernels); 17 is the V-list M2L of the mixed path's refinement residual (BF16 integer slices on
+ * the tensor cores, FP64-class); 18 and 19 are the separate L2P of the mixed and FP64 paths when
+ * the near field runs beside the far field (the default; IBIM_NEAR_OVERLAP=0 fuses them again),
+ * in which case the near-field times overlap the far-field ones; 20 is the FP64-class near field
+ * in float-float arithmetic on the FP32 pipes (IBIM_PRECISION_FP64_TC; IBIM_NEAR_FF=0 keeps the
+ * native FP64 near field, category 16).
  * ibim_profile_read returns (and clears) the summed milliseconds and launch counts of the first
  * ncat categories. */
 int ibim_profile_enable(ibim_ctx ctx, unsigned mask);
