@@ -22,6 +22,15 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(); }
 Ctx *current_ctx() { return g_current; }
+
+void trace_mark(const char *phase) {
+    static const bool on = std::getenv("IBIM_TRACE") != nullptr;
+    if (!on) return;
+    thread_local auto last = std::chrono::steady_clock::now();
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[ibim] %-30s %9.3f ms\n", phase, std::chrono::duration<double, std::milli>(now - last).count());
+    last = now;
+}
 void set_current_ctx(Ctx *c) { g_current = c; }
 
 cudaEvent_t Ctx::take_event() {
@@ -158,6 +167,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     IBIM_REQUIRE(natoms > 0, "need at least one atom");
     std::memset(&res, 0, sizeof(res));
     cudaStream_t s = c->stream;
+    trace_mark("solve: start");
     Timer t0(s);
     Grid *g = levelset_pipeline(c, centers_dev, radii_dev, natoms, cfg, res.reinit_steps);
     res.t_levelset_ms = t0.ms();
@@ -174,6 +184,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     delete g;
     res.n_points = tube->n;
     res.t_surface_ms = t1.ms();
+    trace_mark("solve: level set + surface");
     IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
     Plan *P = nullptr;
     DevBuf<double> a4, b_tube;
@@ -190,11 +201,13 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
         bie_rhs_tube(*tube, cfg.kp, atoms4, natoms, b_tube.ptr, c->aux, cfg.precision);
         IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
+        trace_mark("solve: atoms, rhs enqueued");
         auto w0 = std::chrono::steady_clock::now();
         P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
         IBIM_CUDA(cudaStreamSynchronize(s));
         const auto w1 = std::chrono::steady_clock::now();
         res.t_tree_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
+        trace_mark("solve: plan synced");
         if (cfg.precision == IBIM_PRECISION_FP64 || !m2l_tc_supported()) {
             fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
             if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
@@ -209,10 +222,17 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
             fmm_release_fp64_operators(*P);
             if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);
         }
+        trace_mark("solve: operators enqueued");
+        // the FP32 / float-float near lists of the target sets are built on the host while the
+        // device computes the operators
+        if (cfg.precision == IBIM_PRECISION_MIXED ||
+            (cfg.precision == IBIM_PRECISION_FP64_TC && m2l_tc_supported() && near_ff_enabled()))
+            for (TargetSet *ts : P->targets) mixed_lists_host(*P, *ts);
         IBIM_CUDA(cudaStreamSynchronize(s));
         const auto w2 = std::chrono::steady_clock::now();
         res.t_operators_ms = std::chrono::duration<double, std::milli>(w2 - w1).count();
         res.t_plan_ms = std::chrono::duration<double, std::milli>(w2 - w0).count();
+        trace_mark("solve: operators synced");
         IBIM_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
         // area = sum of quadrature weights (electric.cpp:60)
         std::vector<double> w(tube->n);
@@ -224,6 +244,7 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         electric_solve(*P, cfg.kp, atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol, cfg.precision,
                        nullptr, nullptr, res, b_tube.ptr);
         fill_plan_stats(*P, res);
+        trace_mark("solve: electric done");
     } catch (...) {
         cudaStreamSynchronize(c->aux);  // the right-hand side may still read the tube and atoms
         delete P;

@@ -33,7 +33,7 @@ namespace ibim {
 // Tables
 // ----------------------------------------------------------------------------------------
 
-static void cheb_tables_host(int p, ChebTables &T) {
+void cheb_tables_host(int p, ChebTables &T) {
     std::memset(&T, 0, sizeof(T));
     T.p = p;
     T.R = p * p * p;
@@ -215,9 +215,11 @@ __global__ void k_make_ops64(const ChebTables *__restrict__ tab, const int *__re
     double rt[3], rs[3];
     int D[3];
     op_geometry(keys, op, root_r, rt, rs, D);
+    // consecutive threads take consecutive target nodes ct, so each output row is written by
+    // contiguous 8-byte stores
     const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (pair >= (long)R * R) return;
-    const int ct = (int)(pair / R), cs = (int)(pair % R);
+    const int cs = (int)(pair / R), ct = (int)(pair % R);
     const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
     const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
     double d[3];
@@ -470,15 +472,14 @@ void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, do
     IBIM_CHECK_LAUNCH();
 }
 
-constexpr long NEAR_SEG_PAIRS = 1L << 17;
 
 bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::vector<int> &ptr,
-                   std::vector<int> &rng, bool split_long, std::vector<int> &seg) {
+                   std::vector<int> &rng, bool split_long, std::vector<int> &seg, long max_pairs, long min_sources) {
     const int nl = (int)tl.size();
     if (split_long) {
         std::vector<int> p2{0}, r2;
         for (int k = 0; k < nl; ++k) {
-            const long cap = std::max<long>(256, NEAR_SEG_PAIRS / std::max(1, nt[k]));
+            const long cap = std::max<long>(min_sources, max_pairs / std::max(1, nt[k]));
             for (int r = ptr[k]; r < ptr[k + 1]; ++r)
                 for (long b = rng[2 * r]; b < rng[2 * r + 1]; b += cap) {
                     r2.push_back((int)b);
@@ -496,7 +497,7 @@ bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::
     std::vector<Seg> out;
     bool atomic = false;
     for (int k = 0; k < nl; ++k) {
-        const long cap = std::max<long>(256, NEAR_SEG_PAIRS / std::max(1, nt[k]));
+        const long cap = std::max<long>(min_sources, max_pairs / std::max(1, nt[k]));
         const size_t first = out.size();
         int r0 = ptr[k];
         long acc = 0;
@@ -728,54 +729,25 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     S.nxpairs = (long)xs.size();
     up_int(S.x_src, xs, s);
     up_int(S.x_tgt, xt, s);
-    // near lists: per target leaf its U and W source ranges, sorted and merged (leaves in
-    // parallel, concatenated in leaf order)
+    trace_mark("lists: V and X pairs by operator");
+    // target leaves and the near-field pair count (U and W lists); the FP64 kernel's merged
+    // source ranges are built on first use (near64_lists)
     std::vector<int> tl;
     for (int i = 0; i < nn; ++i)
         if (T.leaf[i] && has_t(i)) tl.push_back(i);
-    std::vector<std::vector<int>> per(tl.size());
-    std::vector<long> npair_leaf(tl.size(), 0);
-#pragma omp parallel for schedule(dynamic, 32)
+    long npairs = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : npairs)
     for (long k = 0; k < (long)tl.size(); ++k) {
         const int i = tl[k];
-        std::vector<std::pair<int, int>> rg;
-        for (int sidx : T.U[i])
-            if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
-        for (int sidx : T.W[i])
-            if (has_s(sidx)) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
-        std::sort(rg.begin(), rg.end());
-        std::vector<int> &mg = per[k];
         long nsrc = 0;
-        for (auto &r : rg) {
-            if (!mg.empty() && mg.back() == r.first)
-                mg.back() = r.second;
-            else {
-                mg.push_back(r.first);
-                mg.push_back(r.second);
-            }
-        }
-        for (size_t q = 0; q < mg.size(); q += 2) nsrc += mg[q + 1] - mg[q];
-        npair_leaf[k] = nsrc * (S.end[i] - S.begin[i]);
-    }
-    std::vector<int> nptr{0}, nr;
-    long npairs = 0;
-    for (size_t k = 0; k < tl.size(); ++k) {
-        nr.insert(nr.end(), per[k].begin(), per[k].end());
-        nptr.push_back((int)nr.size() / 2);
-        npairs += npair_leaf[k];
+        for (int sidx : T.U[i]) nsrc += T.src_end[sidx] - T.src_begin[sidx];
+        for (int sidx : T.W[i]) nsrc += T.src_end[sidx] - T.src_begin[sidx];
+        npairs += nsrc * (S.end[i] - S.begin[i]);
     }
     S.ntleaves = (int)tl.size();
     S.near_pairs = npairs;
-    {
-        std::vector<int> ntk(tl.size()), seg;
-        for (size_t k = 0; k < tl.size(); ++k) ntk[k] = (int)(S.end[tl[k]] - S.begin[tl[k]]);
-        S.near_atomic = near_segments(tl, ntk, nptr, nr, true, seg);
-        S.nnear_seg = tl.empty() ? 0 : (int)seg.size() / 4;
-        up_int(S.near_seg, seg, s);
-    }
+    S.tl_h = tl;
     up_int(S.tleaf, tl, s);
-    up_int(S.near_ptr, nptr, s);
-    up_int(S.near_range, nr, s);
     up_int(S.tbeg, S.begin, s);
     up_int(S.tend, S.end, s);
     S.out4.alloc((size_t)4 * std::max<long>(1, S.nt), s);
@@ -872,7 +844,9 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
     P->maxlevel = maxlevel;
     P->precision = precision;
     try {
+        trace_mark("plan: coordinates downloaded");
         P->tree = build_tree(pts.data(), ns, pts.data(), ns, maxpoint, maxlevel);
+        trace_mark("plan: tree and lists");
         TreeHost &T = P->tree;
         const int nn = T.nnodes, R = P->R, n4 = 4 * R;
         T.p = order;
@@ -915,6 +889,7 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
         P->m2m_level_begin = m2m_lb;
         P->np2m = (int)p2m.size();
         OpIndex opid(T.nlevels);
+        trace_mark("plan: node arrays enqueued");
         if (with_self) {
             TargetSet *S = new TargetSet();
             P->targets.push_back(S);
@@ -925,6 +900,7 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
             S->perm = T.src_perm;
             up_int(S->perm_d, S->perm, s);
             build_target_lists(*P, *S, opid);
+            trace_mark("plan: self target lists");
         }
         if (extra && n_extra > 0) {
             TargetSet *S = new TargetSet();
@@ -944,6 +920,7 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
             S->tz.upload(tq[2].data(), n_extra);
             up_int(S->perm_d, S->perm, s);
             build_target_lists(*P, *S, opid);
+            trace_mark("plan: extra target lists");
         }
         P->nops = (int)opid.keys.size() / 5;
         P->op_key_h = opid.keys;
@@ -1040,6 +1017,48 @@ void fmm_release_fp64_operators(Plan &P) {
     P.ops64_ready = false;
 }
 
+// Merged U and W source ranges per target leaf and their work segments, for the FP64 near-field
+// kernel (leaves in parallel, concatenated in leaf order).
+void near64_lists(Plan &P, TargetSet &S) {
+    if (S.near64_ready) return;
+    const TreeHost &T = P.tree;
+    cudaStream_t s = P.ctx->stream;
+    const std::vector<int> &tl = S.tl_h;
+    std::vector<std::vector<int>> per(tl.size());
+#pragma omp parallel for schedule(dynamic, 32)
+    for (long k = 0; k < (long)tl.size(); ++k) {
+        const int i = tl[k];
+        std::vector<std::pair<int, int>> rg;
+        for (int sidx : T.U[i])
+            if (T.src_end[sidx] > T.src_begin[sidx]) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
+        for (int sidx : T.W[i])
+            if (T.src_end[sidx] > T.src_begin[sidx]) rg.push_back({T.src_begin[sidx], T.src_end[sidx]});
+        std::sort(rg.begin(), rg.end());
+        std::vector<int> &mg = per[k];
+        for (auto &r : rg) {
+            if (!mg.empty() && mg.back() == r.first)
+                mg.back() = r.second;
+            else {
+                mg.push_back(r.first);
+                mg.push_back(r.second);
+            }
+        }
+    }
+    std::vector<int> nptr{0}, nr;
+    for (size_t k = 0; k < tl.size(); ++k) {
+        nr.insert(nr.end(), per[k].begin(), per[k].end());
+        nptr.push_back((int)nr.size() / 2);
+    }
+    std::vector<int> ntk(tl.size()), seg;
+    for (size_t k = 0; k < tl.size(); ++k) ntk[k] = (int)(S.end[tl[k]] - S.begin[tl[k]]);
+    S.near_atomic = near_segments(tl, ntk, nptr, nr, true, seg);
+    S.nnear_seg = tl.empty() ? 0 : (int)seg.size() / 4;
+    up_int(S.near_seg, seg, s);
+    up_int(S.near_ptr, nptr, s);
+    up_int(S.near_range, nr, s);
+    S.near64_ready = true;
+}
+
 // One FP64 FMM: dens (4 x ns, tree order) -> out (4 x nt of target set ts, tree order).
 void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *dens, double *out, bool m2l_sliced) {
     IBIM_REQUIRE(ts >= 0 && ts < (int)P.targets.size(), "no such target set");
@@ -1069,8 +1088,9 @@ void fmm_run_fp64(Plan &P, int ts, const ibim_kernel_params &kpp, const double *
         kff = make_kparams_ff(kp);
         near_ff_pack(P, dens, s);
     }
-    const int nseg = ff ? S.nnear32_seg : S.nnear_seg;
-    const bool atomic = ff ? S.near32_atomic : S.near_atomic;
+    if (!ff && S.ntleaves > 0) near64_lists(P, *P.targets[ts]);
+    const int nseg = ff ? S.nnearff_seg : S.nnear_seg;
+    const bool atomic = ff ? S.nearff_atomic : S.near_atomic;
     auto near = [&](cudaStream_t st, int l2p_mask, int grid, int *next, bool count_work) {
         if (ff) {
             ProfScope ps_(PROF_NEARFF, count_work ? NEAR_FF_FLOPS * S.near_pairs : 0.,

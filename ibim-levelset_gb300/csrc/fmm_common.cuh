@@ -138,18 +138,18 @@ struct KParamsFF {
 KParamsFF make_kparams_ff(const KParams &k);
 // FP32 flops (an FMA counts 2) of one float-float pair update outside the cutoff
 constexpr double NEAR_FF_FLOPS = 690.0;
-// Whether the FP64-class matvec evaluates its near field in float-float (default; IBIM_NEAR_FF=0
-// keeps native FP64).
-bool near_ff_enabled();
 int near_ff_occupancy();
 // Leaf-relative coordinates, FP32 near lists and segments of a target set (shared by the mixed
 // path and the float-float near field).
 void prepare_mixed(Plan &P, TargetSet &S);
 // Pack one matvec's densities (4 x ns, FP64) into the float-float source records.
 void near_ff_pack(Plan &P, const double *dens, cudaStream_t st);
-// Near field without the L2P into out (4 x nt), over the FP32 near segments: grid CTAs, taking
+// Near field without the L2P into out (4 x nt), over the float-float segments: grid CTAs, taking
 // segments from *next when next is not null (else one segment per CTA).
 void near_ff_run(Plan &P, const TargetSet &S, const KParamsFF &kp, double *out, cudaStream_t st, int grid, int *next);
+
+// Chebyshev nodes and interpolation tables of order p (bbfmm.h:409-419), computed on the host.
+void cheb_tables_host(int p, ChebTables &T);
 
 void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, double scale);
 // ops64: the FP64 operators for the same kernel parameters (rounded instead of re-evaluated), or null

@@ -253,9 +253,10 @@ __global__ void k_make_ops32(const ChebTables *__restrict__ tab, const int *__re
         rt[a] = vt;
         rs[a] = vs;
     }
+    // consecutive threads take consecutive target nodes ct: contiguous stores along a row
     const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (pair >= (long)R * R) return;
-    const int ct = (int)(pair / R), cs = (int)(pair % R);
+    const int cs = (int)(pair / R), ct = (int)(pair % R);
     const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
     const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
     double d[3];
@@ -574,6 +575,7 @@ __global__ void __launch_bounds__(NT32) k_l2p32(const ChebTables32 *__restrict__
     load_tables(T, tab);
     const int leaf = tleaf[blockIdx.x];
     const int tb = tb_[leaf], te = te_[leaf];
+    __syncthreads();  // the tables are loaded
     const int p = T.p, R = p * p * p;
     for (int i = threadIdx.x; i < 4 * R; i += blockDim.x) Ls[i] = local[(long)leaf * 4 * R + i];
     __syncthreads();
@@ -612,6 +614,72 @@ void up_f(DevBuf<float> &b, const std::vector<float> &v, cudaStream_t s) {
 
 }  // namespace
 
+// Host half of the FP32 near lists (no CUDA calls; safe while device work is queued).
+void mixed_lists_host(const Plan &P, TargetSet &S) {
+    if (S.mixed_host_ready || S.mixed_ready) return;
+    const TreeHost &T = P.tree;
+    const int nn = T.nnodes;
+    // near lists: U and W nodes expanded into their non-empty leaves, with centre offsets
+    std::vector<int> ptr{0}, rng;
+    std::vector<float> off, offl;
+    std::vector<int> child_first(nn, -1);
+    for (int i = nn - 1; i >= 0; --i)
+        if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
+    // target leaves in node order, expanded in parallel into per-leaf lists, then concatenated
+    std::vector<int> tl32, nt32;
+    for (int i = 0; i < nn; ++i)
+        if (T.leaf[i] && S.end[i] > S.begin[i]) {
+            tl32.push_back(i);
+            nt32.push_back((int)(S.end[i] - S.begin[i]));
+        }
+    const long ntl = (long)tl32.size();
+    std::vector<std::vector<int>> prng(ntl);
+    std::vector<std::vector<float>> poff(ntl), poffl(ntl);
+#pragma omp parallel for schedule(dynamic, 32)
+    for (long k = 0; k < ntl; ++k) {
+        const int i = tl32[k];
+        std::vector<int> stack;
+        auto add_leaves = [&](int root) {
+            stack.clear();
+            stack.push_back(root);
+            while (!stack.empty()) {
+                const int n = stack.back();
+                stack.pop_back();
+                if (T.src_end[n] <= T.src_begin[n]) continue;
+                if (T.leaf[n]) {
+                    prng[k].push_back(T.src_begin[n]);
+                    prng[k].push_back(T.src_end[n]);
+                    for (int a = 0; a < 3; ++a) {
+                        const double d = T.center[3 * n + a] - T.center[3 * i + a];
+                        poff[k].push_back((float)d);
+                        poffl[k].push_back((float)(d - (double)(float)d));
+                    }
+                } else {
+                    for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
+                }
+            }
+        };
+        for (int u : T.U[i]) add_leaves(u);
+        for (int w : T.W[i]) add_leaves(w);
+    }
+    for (long k = 0; k < ntl; ++k) {
+        rng.insert(rng.end(), prng[k].begin(), prng[k].end());
+        off.insert(off.end(), poff[k].begin(), poff[k].end());
+        offl.insert(offl.end(), poffl[k].begin(), poffl[k].end());
+        ptr.push_back((int)rng.size() / 2);
+    }
+    S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_seg32);
+    S.nnear32_seg = tl32.empty() ? 0 : (int)S.h_seg32.size() / 4;
+    S.nearff_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_segff, NEAR_FF_SEG_PAIRS, 128);
+    S.nnearff_seg = tl32.empty() ? 0 : (int)S.h_segff.size() / 4;
+    S.h_ptr32.swap(ptr);
+    S.h_rng32.swap(rng);
+    S.h_off32.swap(off);
+    S.h_offl32.swap(offl);
+    S.mixed_host_ready = true;
+    trace_mark("mixed: near lists");
+}
+
 // Leaf-relative FP32 coordinates (high and low words), FP32 tables, and the FP32 near and X
 // lists of a target set.
 void prepare_mixed(Plan &P, TargetSet &S) {
@@ -620,8 +688,7 @@ void prepare_mixed(Plan &P, TargetSet &S) {
     const int nn = T.nnodes;
     if (!P.mixed_ready) {
         ChebTables h64;
-        P.tables.download(&h64, 1);
-        IBIM_CUDA(cudaStreamSynchronize(s));
+        cheb_tables_host(P.p, h64);
         ChebTables32 h;
         std::memset(&h, 0, sizeof(h));
         h.p = h64.p;
@@ -670,6 +737,7 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         P.mixed_ready = true;
     }
     if (S.mixed_ready) return;
+    trace_mark("mixed: plan data");
     // target coordinates relative to their leaf
     if (S.self) {
         // the source arrays are used
@@ -693,52 +761,14 @@ void prepare_mixed(Plan &P, TargetSet &S) {
         IBIM_CHECK_LAUNCH();
         IBIM_CUDA(cudaStreamSynchronize(s));
     }
-    // near lists: U and W nodes expanded into their non-empty leaves, with centre offsets
-    std::vector<int> ptr{0}, rng;
-    std::vector<float> off, offl;
-    std::vector<int> child_first(nn, -1);
-    for (int i = nn - 1; i >= 0; --i)
-        if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
-    std::vector<int> stack, tl32, nt32;
-    for (int i = 0; i < nn; ++i) {
-        if (!T.leaf[i] || S.end[i] <= S.begin[i]) continue;
-        tl32.push_back(i);
-        nt32.push_back((int)(S.end[i] - S.begin[i]));
-        auto add_leaves = [&](int root) {
-            stack.clear();
-            stack.push_back(root);
-            while (!stack.empty()) {
-                const int n = stack.back();
-                stack.pop_back();
-                if (T.src_end[n] <= T.src_begin[n]) continue;
-                if (T.leaf[n]) {
-                    rng.push_back(T.src_begin[n]);
-                    rng.push_back(T.src_end[n]);
-                    for (int a = 0; a < 3; ++a) {
-                        const double d = T.center[3 * n + a] - T.center[3 * i + a];
-                        off.push_back((float)d);
-                        offl.push_back((float)(d - (double)(float)d));
-                    }
-                } else {
-                    for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
-                }
-            }
-        };
-        for (int u : T.U[i]) add_leaves(u);
-        for (int w : T.W[i]) add_leaves(w);
-        ptr.push_back((int)rng.size() / 2);
-    }
-    {
-        std::vector<int> seg;
-        S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, seg);
-        S.nnear32_seg = tl32.empty() ? 0 : (int)seg.size() / 4;
-        up_i(S.near32_seg, seg, s);
-    }
-    up_i(S.near32_ptr, ptr, s);
-    up_i(S.near32_range, rng, s);
-    up_f(S.near32_off, off, s);
-    up_f(S.near32_offl, offl, s);
-    S.near32_entries = (int)rng.size() / 2;
+    if (!S.mixed_host_ready) mixed_lists_host(P, S);
+    up_i(S.near32_seg, S.h_seg32, s);
+    up_i(S.nearff_seg, S.h_segff, s);
+    up_i(S.near32_ptr, S.h_ptr32, s);
+    up_i(S.near32_range, S.h_rng32, s);
+    up_f(S.near32_off, S.h_off32, s);
+    up_f(S.near32_offl, S.h_offl32, s);
+    S.near32_entries = (int)S.h_rng32.size() / 2;
     // X pair centre offsets (FP64 difference, rounded)
     std::vector<int> xs(std::max<long>(1, S.nxpairs)), xt(std::max<long>(1, S.nxpairs));
     if (S.nxpairs > 0) {
@@ -752,6 +782,14 @@ void prepare_mixed(Plan &P, TargetSet &S) {
     up_f(S.x_off32, xo, s);
     IBIM_CUDA(cudaStreamSynchronize(s));
     S.mixed_ready = true;
+    // the host copies are no longer needed
+    std::vector<int>().swap(S.h_ptr32);
+    std::vector<int>().swap(S.h_rng32);
+    std::vector<int>().swap(S.h_seg32);
+    std::vector<int>().swap(S.h_segff);
+    std::vector<float>().swap(S.h_off32);
+    std::vector<float>().swap(S.h_offl32);
+    trace_mark("mixed: segments, uploads");
 }
 
 

@@ -103,6 +103,10 @@ struct Ctx {
     cudaEvent_t take_event();
 };
 
+// Host phase trace for tuning: with IBIM_TRACE set, each mark prints to stderr the wall time
+// since the previous mark on this thread.
+void trace_mark(const char *phase);
+
 // The context bound by the current C-ABI call on this thread.
 Ctx *current_ctx();
 void set_current_ctx(Ctx *c);
@@ -191,8 +195,10 @@ struct TargetSet {
     long nxpairs = 0;
     long nv_list = 0, nx_list = 0;     // V and X list sizes (bbfmm.cpp lists, pairs with sources)
     DevBuf<int> tleaf, near_ptr, near_range;
+    std::vector<int> tl_h;             // target leaves (nodes with targets), node order
     int ntleaves = 0;
     long near_pairs = 0;
+    bool near64_ready = false;         // near_ptr / near_range / near_seg built (FP64 kernel)
     // near-field work segments (one CTA each): {target leaf node, first range, end range, mode},
     // mode bit 0 = this segment adds the L2P term, bit 1 = the leaf has several segments (atomic
     // accumulation into a zeroed output); heaviest first
@@ -211,6 +217,13 @@ struct TargetSet {
     DevBuf<int> near32_seg;            // work segments over the near32 ranges (as near_seg)
     int nnear32_seg = 0;
     bool near32_atomic = false;
+    DevBuf<int> nearff_seg;            // finer segments over the same ranges for the float-float kernel
+    int nnearff_seg = 0;
+    bool nearff_atomic = false;
+    // host copies of the near32 lists between mixed_lists_host and their upload
+    bool mixed_host_ready = false;
+    std::vector<int> h_ptr32, h_rng32, h_seg32, h_segff;
+    std::vector<float> h_off32, h_offl32;
     DevBuf<float> x_off32;             // per X pair: source centre - target centre
 };
 
@@ -295,6 +308,13 @@ void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp);
 void fmm_release_fp64_operators(Plan &P);
 // Whether the mixed path's V-list M2L runs on the tensor cores on this device.
 bool mixed_uses_tc();
+// Whether the FP64-class matvec evaluates its near field in float-float (default; IBIM_NEAR_FF=0
+// keeps native FP64).
+bool near_ff_enabled();
+// Host half of prepare_mixed for one target set (no CUDA calls): the FP32 / float-float near
+// lists and their work segments, kept in the target set until prepare_mixed uploads them, so a
+// solve can build them while the device computes the M2L operators.
+void mixed_lists_host(const Plan &P, TargetSet &S);
 // Whether a matvec's near field runs on the auxiliary stream beside its far field (default on;
 // IBIM_NEAR_OVERLAP=0 runs it after the far field with the L2P fused in).
 bool near_overlap();
@@ -304,12 +324,15 @@ int near_side_ctas();
 
 // Near-field work segments.  Target leaf k (node tl[k], nt[k] targets) owns source ranges
 // ptr[k] .. ptr[k+1] of `rng` (begin, end pairs); consecutive ranges are grouped into segments of
-// at most max(256, NEAR_SEG_PAIRS / nt[k]) sources, so no CTA carries more than about
-// NEAR_SEG_PAIRS pairs; ranges longer than that are split first (split_long).  Output: 4 ints per
+// at most max(min_sources, max_pairs / nt[k]) sources, so no CTA carries much more than max_pairs
+// source-target pairs; ranges longer than that are split first (split_long).  Output: 4 ints per
 // segment (see TargetSet::near_seg), sorted by descending work; returns whether any leaf has
 // several segments.
+constexpr long NEAR_SEG_PAIRS = 1L << 17;   // FP64 and FP32 near fields
+constexpr long NEAR_FF_SEG_PAIRS = 1L << 14;  // float-float near field (about 8 times the work a pair)
 bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::vector<int> &ptr,
-                   std::vector<int> &rng, bool split_long, std::vector<int> &seg);
+                   std::vector<int> &rng, bool split_long, std::vector<int> &seg, long max_pairs = NEAR_SEG_PAIRS,
+                   long min_sources = 256);
 
 // Plan creation (fmm.cu): target set 0 = the tube points when with_self, then `extra` (host
 // (n, 3)) when n_extra > 0.

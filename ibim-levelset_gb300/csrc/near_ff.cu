@@ -135,8 +135,8 @@ __global__ void k_pack_src_ff(long ns, const double *__restrict__ dens, const fl
 }
 
 // Near field (U and W lists, source leaves in the target leaf's frame) of the FP64-class
-// matvec, without the L2P.  Work segments over the per-source-leaf ranges of the FP32 near
-// lists; with a work counter the CTA takes segments until none is left, else it does segment
+// matvec, without the L2P.  Work segments (at most about 2^14 pairs) over the per-source-leaf
+// ranges of the FP32 near lists; with a work counter the CTA takes segments until none is left, else it does segment
 // blockIdx.x.  Threads = targets x source phases as in the FP32 kernel.
 constexpr int NTF = 128, TILEF = 128;
 __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__restrict__ segs, int nseg, int *next,
@@ -298,13 +298,13 @@ void near_ff_pack(Plan &P, const double *dens, cudaStream_t st) {
 }
 
 void near_ff_run(Plan &P, const TargetSet &S, const KParamsFF &kp, double *out, cudaStream_t st, int grid, int *next) {
-    if (S.nnear32_seg == 0) return;
+    if (S.nnearff_seg == 0) return;
     const float *xh = S.self ? P.sxf.ptr : S.txf.ptr, *yh = S.self ? P.syf.ptr : S.tyf.ptr,
                 *zh = S.self ? P.szf.ptr : S.tzf.ptr;
     const float *xl = S.self ? P.sxl.ptr : S.txl.ptr, *yl = S.self ? P.syl.ptr : S.tyl.ptr,
                 *zl = S.self ? P.szl.ptr : S.tzl.ptr;
-    (count_launch(), k_near_ff<<<grid, NTF, 0, st>>>(kp, reinterpret_cast<const int4 *>(S.near32_seg.ptr),
-                                                     S.nnear32_seg, next, S.near32_range.ptr, S.near32_off.ptr,
+    (count_launch(), k_near_ff<<<grid, NTF, 0, st>>>(kp, reinterpret_cast<const int4 *>(S.nearff_seg.ptr),
+                                                     S.nnearff_seg, next, S.near32_range.ptr, S.near32_off.ptr,
                                                      S.near32_offl.ptr, S.tbeg.ptr, S.tend.ptr, P.src16.ptr, xh, yh, zh,
                                                      xl, yl, zl, S.nt, out));
     IBIM_CHECK_LAUNCH();

@@ -486,6 +486,7 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
             // inner tolerance relative to ||r||: enough for the outer target, above the FP32 noise
             const double inner = std::min(0.5, std::max(0.3 * tol / rel, 3e-7));
             K.solve(A32, d.ptr, r.ptr, left, inner, true, si);
+            trace_mark("electric: inner gmres");
             st.iters += si.iters;
             st.matvecs += si.matvecs;
             left -= si.iters;
@@ -495,6 +496,7 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
             (count_launch(), k_sub<<<ew_grid(c, n2), 256, 0, s>>>(n2, b.ptr, K.w.ptr, r.ptr));
             IBIM_CHECK_LAUNCH();
             rel = K.norm(r.ptr) / (normb == 0 ? 1 : normb);
+            trace_mark("electric: fp64-class residual");
             st.history.push_back(rel);
             if (rel < tol) break;
         }
@@ -527,6 +529,7 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
         if (atom_pot) *atom_pot = pot;
     }
     res.t_energy_ms = te.ms();
+    trace_mark("electric: energy");
     if (m2l_tc_error(P)) throw Error(IBIM_ERR_LIMIT, "tensor-core M2L: an MMA completion wait exceeded its bound");
     if (x_tree_out) IBIM_CUDA(cudaMemcpyAsync(x_tree_out, x.ptr, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
     IBIM_CUDA(cudaStreamSynchronize(s));

@@ -227,6 +227,7 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     const int nn = (int)B.nodes.size();
     int depth = 0;
     for (auto &n : B.nodes) depth = std::max(depth, n.level);
+    trace_mark("tree: nodes");
     // findNode: the node at the candidate's level if it exists, else the leaf that contains it
     auto find_node = [&](int level, const int c[3]) {
         int id = 0;
@@ -321,6 +322,7 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         }
     }
     if (B.nodes[0].leaf) U[0].push_back(0);
+    trace_mark("tree: U V W X lists");
     std::vector<int> ref_of;
     reference_ids(B.nodes, ref_of);
     // level-ordered renumbering
