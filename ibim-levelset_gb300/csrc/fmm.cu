@@ -699,7 +699,7 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             }
         }
     }
-    std::vector<int> chunks, chunks32, chunks_tc, chunks_oz;
+    std::vector<int> chunks, chunks32, chunks_tc, chunks_tc2, chunks_oz;
     auto cut = [&](std::vector<int> &out, int op, long b, long n, int width) {
         for (long q = 0; q < n; q += width) {
             out.push_back(op);
@@ -712,6 +712,7 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
         cut(chunks, op, b, n, M2L_CH);
         cut(chunks32, op, b, n, M2L_CH32);
         cut(chunks_tc, op, b, n, M2L_CHTC);
+        cut(chunks_tc2, op, b, n, 2 * M2L_CHTC);
         cut(chunks_oz, op, b, n, M2L_CHOZ);
     }
     std::vector<int> &vs = gs, &vt = gt;
@@ -721,6 +722,8 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     up_int(S.v_chunk32, chunks32, s);
     S.nchunks_tc = (int)chunks_tc.size() / 3;
     up_int(S.v_chunk_tc, chunks_tc, s);
+    S.nchunks_tc2 = (int)chunks_tc2.size() / 3;
+    up_int(S.v_chunk_tc2, chunks_tc2, s);
     S.nchunks_oz = (int)chunks_oz.size() / 3;
     up_int(S.v_chunk_oz, chunks_oz, s);
     up_int(S.v_src, vs, s);

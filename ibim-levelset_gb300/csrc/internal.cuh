@@ -188,6 +188,8 @@ struct TargetSet {
     int nchunks32 = 0;
     DevBuf<int> v_chunk_tc;            // chunks of the tensor-core contraction (<= 128 pairs)
     int nchunks_tc = 0;
+    DevBuf<int> v_chunk_tc2;           // chunks of the CTA-pair tensor-core contraction (<= 256 pairs)
+    int nchunks_tc2 = 0;
     DevBuf<int> v_chunk_oz;            // chunks of the sliced FP64-class contraction (<= 64 pairs)
     int nchunks_oz = 0;
     long nvpairs = 0;                  // pairs of the operator contraction (V, plus X when x_as_ops)

@@ -19,6 +19,7 @@
 // into the target nodes' local expansions.
 
 #include <cstdint>
+#include <cstdlib>
 
 #include "fmm_common.cuh"
 
@@ -292,6 +293,271 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * N));
+}
+
+// ---------------------------------------------------------------------------------------------
+// CTA-pair form (tcgen05 cta_group::2).  A cluster of two CTAs on two SMs takes one chunk of up to
+// 256 pairs of an operator against four operator row tiles.  Each MMA is M = 256 (128 operator
+// rows from each CTA's shared memory) x N = 256 pairs (the multipole rows of 128 pairs from each
+// CTA) x K = 8, issued by the even CTA; each CTA's TMEM receives its own 128 rows for all 256
+// pairs, two row tiles filling its 512 columns.  Per SM and stage this moves 16 KB of operator
+// tiles and 8 KB of multipole rows for the MMA work that the one-CTA form feeds with 32 KB + 8 KB.
+// The even CTA holds operator row tiles 0 and 2 of its group of four, the odd CTA tiles 1 and 3.
+// Barriers: each CTA keeps the one-CTA form's full_a / full_b / empty; the odd CTA's relay thread
+// waits on its own full barriers and arrives remotely on the even CTA's peer_full; the even CTA's
+// MMA thread waits on all three and multicasts its commits to both CTAs' empty and accumulator
+// barriers.  Every wait is bounded; an abort in either CTA is written into the other's flag
+// before the epilogue, and both CTAs meet at cluster barriers only on paths every thread takes.
+// ---------------------------------------------------------------------------------------------
+constexpr int TC2_N = 256, TC2_HALF = 128, TC2_PT = 2;  // pairs per chunk, per CTA; row tiles per CTA
+constexpr int TC2_STAGE = 2 * TC2_PT * TC_TILE_BYTES + 2 * TC_TILE_BYTES;  // 16 KB operator + 8 KB multipoles
+constexpr int TC2_NST = 8, TC2_LAG = 2;  // (copy lag 2, 4 and 6 measured 5.35, 5.39 and 6.13 ms)
+constexpr int TC2_SMEM = TC2_NST * TC2_STAGE;  // 192 KB
+// D FP32, A and B TF32, K-major, N = 256, M = 256 (the pair)
+constexpr uint32_t TC2_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC2_N >> 3) << 17) | ((256u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_tf32_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(TC2_IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit_pair(uint32_t mbar) {
+    const uint16_t both = 3;
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(mbar),
+        "h"(both)
+        : "memory");
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1)
+    k_m2l_tc2(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+              const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
+              const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full_a[TC2_NST], full_b[TC2_NST], empty_bar[TC2_NST], peer_full[TC2_NST], acc_bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int src_s[TC2_HALF], tgt_s[TC2_N];
+    __shared__ volatile int abort_s;
+    uint32_t rank;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int chunk = blockIdx.x >> 1;
+    const int op = chunks[3 * chunk], b = chunks[3 * chunk + 1], cnt = chunks[3 * chunk + 2];
+    const int tile_base = blockIdx.y * 2 * TC2_PT;               // first operator row tile of the group
+    const int pt = min(TC2_PT, (mtiles - tile_base + 1) / 2);    // row tiles of the pair in use
+    const int nstage = kpad / TC_KS;
+    for (int i = tid; i < TC2_N; i += TC_THREADS) tgt_s[i] = i < cnt ? vtgt[b + i] : -1;
+    for (int i = tid; i < TC2_HALF; i += TC_THREADS) {
+        const int j = (int)rank * TC2_HALF + i;
+        src_s[i] = j < cnt ? vsrc[b + j] : -1;
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        for (int i = 0; i < TC2_NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(TC_BPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&peer_full[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {  // collective over the pair: both CTAs allocate, and receive the same columns
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TC2_PT * TC2_N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // both CTAs' barriers initialised and TMEM allocated
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem_d = tmem_base;
+    auto has_tile = [&](int T) { return tile_base + 2 * T + (int)rank < mtiles; };
+
+    if (warp == 0) {
+        if (lane == 0) {  // this CTA's operator tiles: bulk copies
+            int issued = -1;
+            int nbytes = 0;
+            for (int T = 0; T < pt; ++T)
+                if (has_tile(T)) nbytes += 2 * TC_TILE_BYTES;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % TC2_NST;
+                if (st >= TC2_NST &&
+                    !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / TC2_NST) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                if (abort_s) break;
+                unsigned char *base = tc_smem + buf * TC2_STAGE;
+                const uint32_t fb = smem_u32(&full_a[buf]);
+                if (nbytes == 0) {
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(fb) : "memory");
+                } else {
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(nbytes)
+                                 : "memory");
+                    for (int T = 0; T < pt; ++T) {
+                        if (!has_tile(T)) continue;
+                        const int tile = tile_base + 2 * T + (int)rank;
+                        const long g = (((long)op * mtiles + tile) * nstage + st) * (TC_TILE_BYTES / 4);
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                smem_u32(base + T * TC_TILE_BYTES)),
+                            "l"(a_hi + g), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                smem_u32(base + (TC2_PT + T) * TC_TILE_BYTES)),
+                            "l"(a_lo + g), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                    }
+                }
+                issued = st;
+            }
+            for (int s2 = max(0, issued - TC2_NST + 1); s2 <= issued; ++s2)
+                if (!mbar_wait(smem_u32(&full_a[s2 % TC2_NST]), (uint32_t)((s2 / TC2_NST) & 1))) abort_s = 1;
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {  // MMA issue for the pair
+            int last = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % TC2_NST;
+                const uint32_t par = (uint32_t)((st / TC2_NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) ||
+                    !mbar_wait(smem_u32(&peer_full[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(tc_smem + buf * TC2_STAGE);
+                const uint64_t bh = make_desc(base + (2 * TC2_PT) * TC_TILE_BYTES, 128, 256);
+                const uint64_t bl = make_desc(base + (2 * TC2_PT + 1) * TC_TILE_BYTES, 128, 256);
+                for (int T = 0; T < pt; ++T) {
+                    const uint64_t ah = make_desc(base + T * TC_TILE_BYTES, 128, 256);
+                    const uint64_t al = make_desc(base + (TC2_PT + T) * TC_TILE_BYTES, 128, 256);
+                    const uint32_t d = tmem_d + (uint32_t)(T * TC2_N);
+                    mma_tf32_pair(d, ah, bh, st > 0 ? 1u : 0u);
+                    mma_tf32_pair(d, ah, bl, 1u);
+                    mma_tf32_pair(d, al, bh, 1u);
+                }
+                commit_pair(smem_u32(&empty_bar[buf]));
+                last = st;
+            }
+            // the accumulator barriers of both CTAs always receive a commit: it tracks every MMA
+            // issued above, so after it neither CTA's shared memory is read any more
+            commit_pair(smem_u32(&acc_bar));
+            if (last != nstage - 1) abort_s = 1;
+        } else if (lane == 0) {  // odd CTA: relay its full stages to the even CTA
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % TC2_NST;
+                const uint32_t par = (uint32_t)((st / TC2_NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(
+                                 cluster_addr(smem_u32(&peer_full[buf]), 0))
+                             : "memory");
+            }
+        }
+    } else {  // this CTA's 128 multipole rows: cp.async by 192 threads
+        const int t = tid - 64;
+        int issued = -1;
+        for (int st = 0; st < nstage; ++st) {
+            const int buf = st % TC2_NST;
+            if (st >= TC2_NST &&
+                !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / TC2_NST) - 1) & 1))) {
+                abort_s = 1;
+                break;
+            }
+            if (abort_s) break;
+            unsigned char *base = tc_smem + buf * TC2_STAGE + 2 * TC2_PT * TC_TILE_BYTES;
+            const int k0 = st * TC_KS;
+            for (int i = t; i < 4 * TC2_HALF; i += TC_BPROD) {  // 2 tiles x 128 rows x 2 pieces of 16 B
+                const int tile = i / (2 * TC2_HALF), row = (i >> 1) % TC2_HALF, c = i & 1;
+                const uint32_t dst = smem_u32(base + tile * TC_TILE_BYTES + tile_off(row, c));
+                const int sn = src_s[row];
+                const float *B = tile == 0 ? b_hi : b_lo;
+                cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
+                           sn >= 0 ? 16u : 0u);
+            }
+            asm volatile("cp.async.commit_group;");
+            issued = st;
+            if (st >= TC2_LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(TC2_LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                 smem_u32(&full_b[(st - TC2_LAG) % TC2_NST]))
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s2 = max(0, issued - TC2_LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % TC2_NST])) : "memory");
+    }
+    __syncthreads();
+    // every MMA of the pair is complete once the accumulator barrier flips (the even CTA commits
+    // to it on every path); an abort on either side is copied into the other CTA's flag
+    if (tid == 0) {
+        const bool acc = mbar_wait(smem_u32(&acc_bar), 0u);
+        if (!acc || abort_s) {
+            abort_s = 1;
+            asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr(smem_u32((const void *)&abort_s), rank ^ 1u)),
+                         "r"(1u)
+                         : "memory");
+        }
+    }
+    cluster_sync_all();
+    const bool ok = !abort_s;
+    if (!ok && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+        const int lg = warp & 3;
+        for (int T = warp >> 2; T < pt; T += 2) {
+            if (!has_tile(T)) continue;
+            const int row = (tile_base + 2 * T + (int)rank) * TC_M + 32 * lg + lane;
+            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(T * TC2_N);
+#pragma unroll 1
+            for (int c0 = 0; c0 < TC2_N; c0 += 16) {
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr + (uint32_t)c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < n4) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int tg = tgt_s[c0 + q];
+                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]));
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // neither CTA leaves while the other may still use the pair's TMEM
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC2_PT * TC2_N));
 }
 
 // hi = x rounded to TF32 (10 explicit mantissa bits, to nearest even), lo = x - hi.
@@ -701,6 +967,19 @@ void m2l_tc_pack(Plan &P) {
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
+}
+
+// The CTA-pair kernel is opt-in (IBIM_TC_PAIR=1): on the 2,000-atom protein it takes 5.35 ms a
+// launch against the one-CTA kernel's 3.9 ms.  Its 256-pair chunks fill 71 % of their slots
+// against 83 %; the rest of the gap is not explained yet (ncu, 150-atom protein: tensor pipe
+// active 30 %, 5 long-scoreboard stalls per issued instruction).
+bool m2l_tc_pair() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_TC_PAIR");
+        return v && v[0] == '1';
+    }();
+    return on;
 }
 
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating): chunks of 128 pairs against
@@ -716,6 +995,15 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     const int mt = P.tc_mpad / TC_M;
     ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                   4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
+    if (m2l_tc_pair()) {
+        if (S.nchunks_tc2 == 0) return;
+        const dim3 grid2(2 * S.nchunks_tc2, (mt + 2 * TC2_PT - 1) / (2 * TC2_PT));
+        (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
+                             n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        IBIM_CHECK_LAUNCH();
+        return;
+    }
     const dim3 grid(S.nchunks_tc, (mt + TcShape<N>::RT - 1) / TcShape<N>::RT);
     (count_launch(), k_m2l_tc<N><<<grid, TC_THREADS, TcShape<N>::SMEM, s>>>(
                          n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr, P.tc_a_lo.ptr,
