@@ -361,8 +361,11 @@ def run_ours(args):
     fp64_peak = ctx.measure_peak("fp64")
     fp32_peak = ctx.measure_peak("fp32")
     mixed = precision == ibim.PRECISION_MIXED
+    # operand form of the mixed path's tensor-core M2L (the library's default: scaled FP16 splits)
+    tc_form = ("tf32x3 tensor" if os.environ.get("IBIM_TC_FP16") == "0" or os.environ.get("IBIM_TC_PAIR") == "1"
+               else "fp16x3 tensor")
     fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
-                "m2l_x": "fp32", "m2l_v": "tf32x3 tensor" if mixed else "fp64", "rhs": "fp32" if mixed else "fp64",
+                "m2l_x": "fp32", "m2l_v": tc_form if mixed else "fp64", "rhs": "fp32" if mixed else "fp64",
                 "weno_stage": "fp32" if mixed else "fp64", "p2m": "fp32" if mixed else "fp64",
                 "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": "bf16x28 tensor",
                 "near_ff": "fp32", "l2p": "fp32", "l2p_fp64": "fp64"}
@@ -386,6 +389,13 @@ def run_ours(args):
                 peak = 0.5 * peaks.get("bf16_tflops", 1909.5)
                 unit = "TFLOP/s"
                 src = "TF32 = 1/2 of MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 3 MMAs"
+            elif bound.startswith("fp16"):
+                # 3 FP16 MMAs per algorithmic multiply-add (scaled hi / lo splits); peak: the measured
+                # dense BF16 rate (FP16 runs at the same rate)
+                ach = 3 * alg / (per_launch_ms * 1e-3) / 1e12
+                peak = peaks.get("bf16_tflops", 1909.5)
+                unit = "TFLOP/s"
+                src = "MEASURED_PEAKS.json bf16_tflops (FP16 rate, of measured); achieved counts the 3 MMAs"
             elif bound.startswith("bf16"):
                 # 28 BF16 digit-pair MMAs per algorithmic multiply-add (7 digits, pairs i + l <= 6)
                 ach = 28 * alg / (per_launch_ms * 1e-3) / 1e12

@@ -272,7 +272,9 @@ struct Plan {
     bool tc_ready = false;
     double tc_key[5] = {-1, -1, -1, -1, -1};
     int tc_kpad = 0, tc_mpad = 0;
-    DevBuf<float> tc_a_hi, tc_a_lo, tc_b_hi, tc_b_lo;
+    bool tc_h16 = false;               // images in the scaled FP16 form (else TF32)
+    DevBuf<float> tc_a_hi, tc_a_lo, tc_b_hi, tc_b_lo;  // raw image words
+    DevBuf<float> tc_rsc, tc_csc;      // FP16 form: operator row scales, multipole column scales
     DevBuf<int> tc_err;
     // FP64-class V-list M2L of the refinement residual (m2l_tc.cu): operators and multipoles as
     // exact BF16 integer slices under power-of-two row / column scales

@@ -2,10 +2,11 @@
 //
 // Per operator o (level, lattice offset) the V-list pairs form a dense contraction
 //     L[tgt_j] += K_o . M[src_j]        K_o: 4p^3 x 4p^3,  j = pairs of the operator
-// computed as D[128 rows x 128 pairs] (FP32, in TMEM) += A[128 x K] . B[K x 128 pairs] with
-// kind::tf32 MMAs (M = 128, N = 128, K = 8 per instruction).  FP32 accuracy comes from the
-// 3xTF32 split: A = A_hi + A_lo, B = B_hi + B_lo with hi = x rounded to TF32 and lo = x - hi, and
-// D accumulates A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the dropped A_lo.B_lo is below FP32 rounding).
+// computed as D[128 rows x 128 pairs] (FP32, in TMEM) += A[128 x K] . B[K x 128 pairs].  FP32
+// accuracy comes from a three-product split, A = A_hi + A_lo, B = B_hi + B_lo, D accumulating
+// A_hi.B_hi + A_hi.B_lo + A_lo.B_hi (the dropped A_lo.B_lo is below FP32 rounding), in one of two
+// operand forms: scaled FP16 (the default: operator rows and multipole columns scaled by powers
+// of two, kind::f16 MMAs with K = 16) or TF32 (IBIM_TC_FP16=0: kind::tf32, K = 8).
 //
 // One CTA takes one chunk of up to 128 pairs of an operator against up to four 128-row tiles of
 // the operator (four FP32 accumulators of 128 x 128 = all 512 TMEM columns), so each gathered
@@ -21,6 +22,8 @@
 #include <cstdint>
 #include <cstdlib>
 
+#include <cuda_fp16.h>
+
 #include "fmm_common.cuh"
 
 namespace ibim {
@@ -31,6 +34,9 @@ constexpr int TC_M = 128, TC_KS = 8;               // rows per tile, K elements 
 constexpr int TC_THREADS = 256;
 constexpr int TC_TILE_BYTES = TC_M * TC_KS * 4;    // 4 KB per operator tile and stage
 constexpr long TC_WAIT_LIMIT = 1L << 20;           // bounded mbarrier polling
+
+// FP16 operand form: K elements per stage (a stage row is 32 bytes in both forms)
+constexpr int TC_KS16 = 16;
 
 // Shape of the contraction for N pairs per chunk (MMA N): RT = 512 / N row tiles fill the 512
 // TMEM columns; a stage holds RT operator tiles (hi, lo) and the N multipole rows (hi, lo).
@@ -45,6 +51,9 @@ template <int N> struct TcShape {
     // D FP32, A and B TF32, both K-major, M = 128, N.
     static constexpr uint32_t IDESC =
         (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+    // D FP32, A and B FP16 (kind::f16), both K-major, M = 128, N.
+    static constexpr uint32_t IDESC16 =
+        (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -67,6 +76,16 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         :
         : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
@@ -109,27 +128,33 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
 // bounded and an expired wait aborts the CTA through a shared flag and the error word.
 constexpr int TC_BPROD = 192;
 
-template <int N>
+template <int N, bool H16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
-                const int *__restrict__ vtgt, const float *__restrict__ a_hi, const float *__restrict__ a_lo,
-                const float *__restrict__ b_hi, const float *__restrict__ b_lo, float *local, int *err) {
+                const int *__restrict__ vtgt, const void *__restrict__ a_hi_, const void *__restrict__ a_lo_,
+                const void *__restrict__ b_hi_, const void *__restrict__ b_lo_, const float *__restrict__ rscale,
+                const float *__restrict__ cscale, float *local, int *err) {
     using SH = TcShape<N>;
     constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
+    constexpr int KS = H16 ? TC_KS16 : TC_KS, ES = H16 ? 2 : 4;  // K elements per stage, bytes per element
+    const char *a_hi = static_cast<const char *>(a_hi_), *a_lo = static_cast<const char *>(a_lo_);
+    const char *b_hi = static_cast<const char *>(b_hi_), *b_lo = static_cast<const char *>(b_lo_);
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t full_a[TC_NST], full_b[TC_NST], empty_bar[TC_NST], acc_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int src_s[N], tgt_s[N];
+    __shared__ float csc_s[N];
     __shared__ volatile int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
     const int tile0 = blockIdx.y * TC_RT;
     const int rt = min(TC_RT, mtiles - tile0);
-    const int nstage = kpad / TC_KS;
+    const int nstage = kpad / KS;
     constexpr int kStageBytes = SH::STAGE;
     for (int i = tid; i < N; i += TC_THREADS) {
         src_s[i] = i < cnt ? vsrc[b + i] : -1;
         tgt_s[i] = i < cnt ? vtgt[b + i] : -1;
+        if (H16) csc_s[i] = i < cnt ? cscale[src_s[i]] : 0.f;
     }
     if (tid == 0) {
         abort_s = 0;
@@ -169,7 +194,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                              "r"(2 * rt * TC_TILE_BYTES)
                              : "memory");
                 for (int t = 0; t < rt; ++t) {
-                    const long g = (atile0 + (long)t * nstage + st) * (TC_TILE_BYTES / 4);
+                    const long g = (atile0 + (long)t * nstage + st) * TC_TILE_BYTES;
                     asm volatile(
                         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                             smem_u32(base + t * TC_TILE_BYTES)),
@@ -205,9 +230,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
                     const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
                     const uint32_t d = tmem_d + (uint32_t)(t * N);
-                    mma_tf32(d, ah, bh, SH::IDESC, st > 0 ? 1u : 0u);
-                    mma_tf32(d, ah, bl, SH::IDESC, 1u);
-                    mma_tf32(d, al, bh, SH::IDESC, 1u);
+                    if (H16) {
+                        mma_f16(d, ah, bh, SH::IDESC16, st > 0 ? 1u : 0u);
+                        mma_f16(d, ah, bl, SH::IDESC16, 1u);
+                        mma_f16(d, al, bh, SH::IDESC16, 1u);
+                    } else {
+                        mma_tf32(d, ah, bh, SH::IDESC, st > 0 ? 1u : 0u);
+                        mma_tf32(d, ah, bl, SH::IDESC, 1u);
+                        mma_tf32(d, al, bh, SH::IDESC, 1u);
+                    }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                  smem_u32(&empty_bar[buf]))
@@ -234,13 +265,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (abort_s) break;
             unsigned char *base = tc_smem + buf * kStageBytes;
-            const int k0 = st * TC_KS;
+            const int k0 = st * KS;
             for (int i = t; i < 4 * N; i += TC_BPROD) {  // 2 tiles x N rows x 2 pieces of 16 B
                 const int tile = i / (2 * N), row = (i >> 1) % N, c = i & 1;
                 const uint32_t dst = smem_u32(base + 2 * rt * TC_TILE_BYTES + tile * SH::BT + tile_off(row, c));
                 const int sn = src_s[row];
-                const float *B = tile == 0 ? b_hi : b_lo;
-                cp_async16(dst, sn >= 0 ? (const void *)(B + (long)sn * kpad + k0 + 4 * c) : (const void *)B,
+                const char *B = tile == 0 ? b_hi : b_lo;
+                cp_async16(dst, sn >= 0 ? (const void *)(B + ((long)sn * kpad + k0) * ES + 16 * c) : (const void *)B,
                            sn >= 0 ? 16u : 0u);
             }
             asm volatile("cp.async.commit_group;");
@@ -267,6 +298,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int lg = warp & 3;
         for (int tt = warp >> 2; tt < rt; tt += 2) {
             const int row = (tile0 + tt) * TC_M + 32 * lg + lane;
+            const float rs = H16 ? rscale[(long)op * mtiles * TC_M + row] : 1.f;  // row < mtiles * 128
             const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * N);
 #pragma unroll 1
             for (int c0 = 0; c0 < N; c0 += 16) {
@@ -283,7 +315,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
                         const int tg = tgt_s[c0 + q];
-                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]));
+                        const float x = H16 ? __uint_as_float(v[q]) * rs * csc_s[c0 + q] : __uint_as_float(v[q]);
+                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, x);
                     }
                 }
             }
@@ -607,6 +640,99 @@ __global__ void k_split_mult_tc(long nnodes, int n4, int kpad, const float *__re
     }
 }
 
+
+// Scaled FP16 operand form.  Each operator row r is divided by a power of two s_r with
+// max_k |A_rk| / s_r in [2^13, 2^14), each multipole column (source node) j likewise by t_j, and
+// a scaled value x is split into hi = fp16(x) and lo = fp16(x - hi), 11 significant bits each;
+// D accumulates A_hi.B_hi + A_hi.B_lo + A_lo.B_hi in FP32 (kind::f16, K = 16 per MMA; products
+// below 2^28, sums below 2^37) and the epilogue multiplies by s_r t_j.  Placing the maximum at
+// 2^14 keeps lo in the FP16 normal range down to 2^-17 of the row or column maximum, so a split
+// value carries about 22 bits, as the TF32 split does, while a stage of 32 bytes per row holds
+// 16 K elements instead of 8: half the operand bytes per flop.
+
+// Power-of-two scale s with m / s in [2^13, 2^14) (2^-14 for m == 0).
+__device__ __forceinline__ float h16_scale(float m) {
+    if (!(m > 0.f)) return ldexpf(1.f, -14);
+    int e;
+    frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return ldexpf(1.f, e - 14);
+}
+
+// Row scales s_r of the FP32 operators (column-major n4 x n4 per op): rscale[op][mtiles * 128].
+__global__ void k_scale_ops_h16(int n4, int mtiles, int nops, const float *__restrict__ ops, float *rscale) {
+    const int mpad = mtiles * TC_M;
+    const long total = (long)nops * mpad;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(i % mpad), op = (int)(i / mpad);
+        float m = 0.f;
+        if (r < n4) {
+            const float *col0 = ops + (long)op * n4 * n4 + r;
+            for (int k = 0; k < n4; ++k) m = fmaxf(m, fabsf(col0[(long)k * n4]));
+        }
+        rscale[i] = h16_scale(m);
+    }
+}
+
+__device__ __forceinline__ void split_h16(float x, uint16_t &hi, uint16_t &lo) {
+    const __half h = __float2half_rn(x);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn(x - __half2float(h)));
+}
+
+// FP32 operators -> scaled FP16 hi / lo tiles [op][row tile][stage of 16 K][4 KB] in the
+// shared-memory layout (tile_off with 8 K elements of 2 bytes per 16-byte row piece).  One thread
+// per (op, row, group of 8 K elements): 8 coalesced column reads, one 16-byte store per word.
+__global__ void k_pack_ops_h16(int n4, int mtiles, int kpad, int nops, const float *__restrict__ ops,
+                               const float *__restrict__ rscale, uint4 *a_hi, uint4 *a_lo) {
+    const int nstage = kpad / TC_KS16, mpad = mtiles * TC_M, ngrp = kpad / 8;
+    const long total = (long)nops * ngrp * mpad;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(i % mpad);
+        const long rest = i / mpad;
+        const int grp = (int)(rest % ngrp), op = (int)(rest / ngrp);
+        const float inv = 1.f / rscale[(long)op * mpad + r];  // a power of two: exact
+        uint32_t wh[4], wl[4];
+        for (int q = 0; q < 8; q += 2) {
+            uint16_t h0, l0, h1, l1;
+            const int k = grp * 8 + q;
+            const float x0 = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] * inv : 0.f;
+            const float x1 = (r < n4 && k + 1 < n4) ? ops[(long)op * n4 * n4 + (long)(k + 1) * n4 + r] * inv : 0.f;
+            split_h16(x0, h0, l0);
+            split_h16(x1, h1, l1);
+            wh[q >> 1] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            wl[q >> 1] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        }
+        const int t = r / TC_M, row = r % TC_M, st = grp / 2, half = grp & 1;
+        const long tile = ((long)op * mtiles + t) * nstage + st;
+        const long idx = (tile * TC_TILE_BYTES + tile_off(row, half)) / 16;
+        a_hi[idx] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+        a_lo[idx] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+    }
+}
+
+// Multipoles [node][n4] (FP32) -> scaled FP16 hi / lo [node][kpad] and the column scales t_j.
+// One warp per node.
+__global__ void k_split_mult_h16(long nnodes, int n4, int kpad, const float *__restrict__ m, uint16_t *hi,
+                                 uint16_t *lo, float *cscale) {
+    const int lane = threadIdx.x & 31;
+    const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+    for (long node = warp; node < nnodes; node += nwarps) {
+        const float *x = m + node * n4;
+        float mx = 0.f;
+        for (int k = lane; k < n4; k += 32) mx = fmaxf(mx, fabsf(x[k]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const float sc = h16_scale(mx), inv = 1.f / sc;
+        if (lane == 0) cscale[node] = sc;
+        for (int k = lane; k < kpad; k += 32) {
+            uint16_t h, l;
+            split_h16(k < n4 ? x[k] * inv : 0.f, h, l);
+            hi[node * kpad + k] = h;
+            lo[node * kpad + k] = l;
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------------------------
 // FP64-class V-list M2L for the refinement residual: exact integer slices on the tensor cores.
@@ -946,30 +1072,6 @@ bool m2l_tc_supported() {
     return major == 10 && minor == 3;
 }
 
-void m2l_tc_pack(Plan &P) {
-    IBIM_REQUIRE(P.ops32.ptr || P.nops == 0, "tensor-core images need the FP32 operators");
-    cudaStream_t s = P.ctx->stream;
-    const int n4 = 4 * P.R;
-    P.tc_kpad = (n4 + TC_KS - 1) / TC_KS * TC_KS;
-    P.tc_mpad = (n4 + TC_M - 1) / TC_M * TC_M;
-    const size_t na = (size_t)std::max(1, P.nops) * P.tc_mpad * P.tc_kpad;
-    P.tc_a_hi.alloc(na, s);
-    P.tc_a_lo.alloc(na, s);
-    if (P.nops > 0)
-        (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, P.tc_mpad / TC_M, P.tc_kpad, P.nops, P.ops32.ptr,
-                                                                      P.tc_a_hi.ptr, P.tc_a_lo.ptr));
-    P.tc_b_hi.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
-    P.tc_b_lo.alloc((size_t)P.tree.nnodes * P.tc_kpad, s);
-    if (!P.tc_err.ptr) {
-        P.tc_err.alloc(1, s);
-        P.tc_err.zero();
-    }
-    IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TcShape<M2L_CHTC>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
-}
-
 // The CTA-pair kernel is opt-in (IBIM_TC_PAIR=1): on the 2,000-atom protein it takes 5.35 ms a
 // launch against the one-CTA kernel's 3.9 ms.  Its 256-pair chunks fill 71 % of their slots
 // against 83 %; the rest of the gap is not explained yet (ncu, 150-atom protein: tensor pipe
@@ -982,6 +1084,60 @@ bool m2l_tc_pair() {
     return on;
 }
 
+// Operand form of the mixed path's tensor-core M2L: scaled FP16 hi / lo (default) or TF32 hi / lo
+// (IBIM_TC_FP16=0, or the CTA-pair kernel).
+static bool tc_fp16() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_TC_FP16");
+        return !(v && v[0] == '0');
+    }();
+    return on && !m2l_tc_pair();
+}
+
+void m2l_tc_pack(Plan &P) {
+    IBIM_REQUIRE(P.ops32.ptr || P.nops == 0, "tensor-core images need the FP32 operators");
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R;
+    P.tc_h16 = tc_fp16();
+    const int ks = P.tc_h16 ? TC_KS16 : TC_KS;
+    P.tc_kpad = (n4 + ks - 1) / ks * ks;
+    P.tc_mpad = (n4 + TC_M - 1) / TC_M * TC_M;
+    const int mt = P.tc_mpad / TC_M;
+    // image sizes in floats (an FP16 image takes half the words)
+    const size_t na = (size_t)std::max(1, P.nops) * P.tc_mpad * P.tc_kpad / (P.tc_h16 ? 2 : 1);
+    const size_t nb = (size_t)P.tree.nnodes * P.tc_kpad / (P.tc_h16 ? 2 : 1);
+    P.tc_a_hi.alloc(na, s);
+    P.tc_a_lo.alloc(na, s);
+    if (P.tc_h16) {
+        P.tc_rsc.alloc((size_t)std::max(1, P.nops) * P.tc_mpad, s);
+        P.tc_csc.alloc((size_t)P.tree.nnodes, s);
+        if (P.nops > 0) {
+            const long rows = (long)P.nops * P.tc_mpad;
+            (count_launch(), k_scale_ops_h16<<<(int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms), 256, 0, s>>>(
+                                 n4, mt, P.nops, P.ops32.ptr, P.tc_rsc.ptr));
+            const long pieces = rows * (P.tc_kpad / 8);
+            (count_launch(), k_pack_ops_h16<<<(int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms), 256, 0, s>>>(
+                                 n4, mt, P.tc_kpad, P.nops, P.ops32.ptr, P.tc_rsc.ptr,
+                                 reinterpret_cast<uint4 *>(P.tc_a_hi.ptr), reinterpret_cast<uint4 *>(P.tc_a_lo.ptr)));
+        }
+    } else if (P.nops > 0) {
+        (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, mt, P.tc_kpad, P.nops, P.ops32.ptr,
+                                                                      P.tc_a_hi.ptr, P.tc_a_lo.ptr));
+    }
+    P.tc_b_hi.alloc(nb, s);
+    P.tc_b_lo.alloc(nb, s);
+    if (!P.tc_err.ptr) {
+        P.tc_err.alloc(1, s);
+        P.tc_err.zero();
+    }
+    IBIM_CHECK_LAUNCH();
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
+}
+
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating): chunks of 128 pairs against
 // four row tiles.  (Chunks of 256 pairs against two row tiles, k_m2l_tc<256>, measured 5.0 ms
 // against 3.9 ms on the 2,000-atom protein: the operator traffic falls but the chunks fill worse.)
@@ -990,12 +1146,17 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     if (S.nchunks_tc == 0) return;
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
-    (count_launch(), k_split_mult_tc<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr,
-                                                                        P.tc_b_hi.ptr, P.tc_b_lo.ptr));
+    if (P.tc_h16)
+        (count_launch(), k_split_mult_h16<<<4 * P.ctx->num_sms, 256, 0, s>>>(
+                             P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr, reinterpret_cast<uint16_t *>(P.tc_b_hi.ptr),
+                             reinterpret_cast<uint16_t *>(P.tc_b_lo.ptr), P.tc_csc.ptr));
+    else
+        (count_launch(), k_split_mult_tc<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr,
+                                                                            P.tc_b_hi.ptr, P.tc_b_lo.ptr));
     const int mt = P.tc_mpad / TC_M;
     ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                   4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-    if (m2l_tc_pair()) {
+    if (!P.tc_h16 && m2l_tc_pair()) {
         if (S.nchunks_tc2 == 0) return;
         const dim3 grid2(2 * S.nchunks_tc2, (mt + 2 * TC2_PT - 1) / (2 * TC2_PT));
         (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
@@ -1005,9 +1166,10 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         return;
     }
     const dim3 grid(S.nchunks_tc, (mt + TcShape<N>::RT - 1) / TcShape<N>::RT);
-    (count_launch(), k_m2l_tc<N><<<grid, TC_THREADS, TcShape<N>::SMEM, s>>>(
+    auto kern = P.tc_h16 ? k_m2l_tc<N, true> : k_m2l_tc<N, false>;
+    (count_launch(), kern<<<grid, TC_THREADS, TcShape<N>::SMEM, s>>>(
                          n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr, P.tc_a_lo.ptr,
-                         P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+                         P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr));
     IBIM_CHECK_LAUNCH();
 }
 

@@ -1,6 +1,9 @@
-"""The CTA-pair tensor-core M2L (tcgen05 cta_group::2, opt-in with IBIM_TC_PAIR=1) against the
-default one-CTA kernel: the same 3xTF32 products, accumulated in other chunks (256 pairs per CTA
-pair instead of 128 per CTA), so the mixed FMM outputs agree to FP32 summation order."""
+"""Operand forms of the mixed path's tensor-core M2L against each other, each in its own process
+(the form is fixed per process by the environment): the CTA-pair kernel (tcgen05 cta_group::2,
+IBIM_TC_PAIR=1, TF32 splits) and the one-CTA kernel with TF32 splits (IBIM_TC_FP16=0) compute the
+same 3xTF32 products in other chunks, so they agree to FP32 summation order; the default scaled
+FP16 splits carry as many bits (each form is 1e-6..3e-6 from the FP64 operator, the FP16 one
+the closer)."""
 
 import json
 import os
@@ -36,23 +39,30 @@ print(json.dumps(pl.stats()))
 """
 
 
+def run_child(tmp_path, case, order, env_extra, tag):
+    path = str(tmp_path / f"{tag}.npy")
+    code = CHILD.format(root=ROOT, pkg=os.path.join(ROOT, "ibim-levelset_gb300"), tests=HERE, case=case,
+                        order=order, path=path)
+    env = dict(os.environ, **env_extra)
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert json.loads(r.stdout.strip().splitlines()[-1])["v_pairs"] > 0
+    return np.load(path)
+
+
 @pytest.mark.parametrize("case,order", [("cavity", None), ("p1hje", None), ("synth30", 5), ("p1hje", 3), ("synth30", 6)])
 def test_pair_kernel_matches_one_cta_kernel(ctx, golden, case, order, tmp_path):
     G = golden(case)
     P = G["params"]
     s = G["surface"]
     p = order or P["np"]
-    path = str(tmp_path / "pair.npy")
-    code = CHILD.format(root=ROOT, pkg=os.path.join(ROOT, "ibim-levelset_gb300"), tests=HERE, case=case,
-                        order=p, path=path)
-    env = dict(os.environ, IBIM_TC_PAIR="1")
-    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0, r.stderr[-2000:]
-    assert json.loads(r.stdout.strip().splitlines()[-1])["v_pairs"] > 0
-    b = np.load(path)
+    pair = run_child(tmp_path, case, p, {"IBIM_TC_PAIR": "1"}, "pair")
+    tf32 = run_child(tmp_path, case, p, {"IBIM_TC_FP16": "0"}, "tf32")
     t = ctx.tube(s[:, :3], s[:, 3:6], s[:, 6], P["h"])
     pl = t.plan(p, P["maxpoint"], P["maxlevel"], precision=ibim.PRECISION_MIXED)
     kp = ibim.kernel_params(P["kappa"], P["dE"], P["dI"], P["tau"])
-    a = pl.apply(ibim.KERNEL_BIE_FUSED, kp, bie_densities(s, P["h"], probe_vector(len(s))))
+    fp16 = pl.apply(ibim.KERNEL_BIE_FUSED, kp, bie_densities(s, P["h"], probe_vector(len(s))))
     for o in range(4):
-        assert np.abs(a[o] - b[o]).max() / np.abs(a[o]).max() < 1e-6, (o, case)
+        assert np.abs(pair[o] - tf32[o]).max() / np.abs(tf32[o]).max() < 1e-6, (o, case)
+        # each form is 1e-6..3e-6 (max-normalised) from the FP64 operator on these fixtures
+        assert np.abs(fp16[o] - tf32[o]).max() / np.abs(tf32[o]).max() < 4e-6, (o, case)
