@@ -27,11 +27,12 @@ struct ChebTables32 {
 
 struct KParams32 {
     float kappa, eps, ieps, vr2, k2in, q4pi, k3f;
+    float k2in_q, k3q;  // k2in / q4pi and k3f / q4pi: the near field's densities carry the 1 / (4 pi)
 };
 
 static KParams32 to32(const KParams &k) {
     return KParams32{(float)k.kappa, (float)k.eps, (float)k.ieps, (float)(k.vr * k.vr), (float)k.k2in,
-                     (float)k.q4pi, (float)k.k3f};
+                     (float)k.q4pi, (float)k.k3f, (float)(k.k2in / k.q4pi), (float)(k.k3f / k.q4pi)};
 }
 
 namespace {
@@ -82,17 +83,19 @@ __global__ void k_to_f32(long n, const double *__restrict__ a, float *b) {
 
 // Densities to FP32: [4][ns] for P2M, and per source the near-field record
 // {x, y, z, m_x | m_y, m_z, psi, 0} (leaf-relative coordinates) as two float4.
+// Densities to FP32 (for P2M) and the near field's source records, whose densities carry the
+// kernels' common factor q = 1 / (4 pi): {x, y, z, q m_x}, {q m_y, q m_z, q psi, 0}.
 __global__ void k_pack_src32(long ns, const double *__restrict__ dens, const float *__restrict__ sx,
-                             const float *__restrict__ sy, const float *__restrict__ sz, float *d32, float4 *src8) {
+                             const float *__restrict__ sy, const float *__restrict__ sz, float *d32, float4 *src8,
+                             double q) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ns; i += (long)gridDim.x * blockDim.x) {
-        const float m0 = (float)dens[i], m1 = (float)dens[ns + i], m2 = (float)dens[2 * ns + i],
-                    psi = (float)dens[3 * ns + i];
-        d32[i] = m0;
-        d32[ns + i] = m1;
-        d32[2 * ns + i] = m2;
-        d32[3 * ns + i] = psi;
-        src8[2 * i] = make_float4(sx[i], sy[i], sz[i], m0);
-        src8[2 * i + 1] = make_float4(m1, m2, psi, 0.f);
+        const double m0 = dens[i], m1 = dens[ns + i], m2 = dens[2 * ns + i], psi = dens[3 * ns + i];
+        d32[i] = (float)m0;
+        d32[ns + i] = (float)m1;
+        d32[2 * ns + i] = (float)m2;
+        d32[3 * ns + i] = (float)psi;
+        src8[2 * i] = make_float4(sx[i], sy[i], sz[i], (float)(q * m0));
+        src8[2 * i + 1] = make_float4((float)(q * m1), (float)(q * m2), (float)(q * psi), 0.f);
     }
 }
 
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                                                  const float *__restrict__ local, double *out, int l2p_mask,
                                                  int nseg, int *next) {
     __shared__ ChebTables32 T;
-    __shared__ float S[7][TILE32];
+    __shared__ float4 S4[TILE32][2];  // {x, y, z, q m_x}, {q m_y, q m_z, q psi, 0} in the target leaf's frame
     __shared__ float red[NT32][4];
     __shared__ int cur;
     load_tables(T, tab);
@@ -479,13 +482,8 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                     for (int q = threadIdx.x; q < take; q += blockDim.x) {
                         const int si = lpos + q;
                         const float4 A = __ldg(src8 + 2 * si), B = __ldg(src8 + 2 * si + 1);
-                        S[0][filled + q] = A.x + ox;
-                        S[1][filled + q] = A.y + oy;
-                        S[2][filled + q] = A.z + oz;
-                        S[3][filled + q] = A.w;
-                        S[4][filled + q] = B.x;
-                        S[5][filled + q] = B.y;
-                        S[6][filled + q] = B.z;
+                        S4[filled + q][0] = make_float4(A.x + ox, A.y + oy, A.z + oz, A.w);
+                        S4[filled + q][1] = B;
                     }
                     filled += take;
                     lpos += take;
@@ -499,28 +497,32 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                 __syncthreads();
                 if (active) {
                     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+                    // the densities carry 1 / (4 pi): the K1, K2, K4 factors lose it and the K3 ones
+                    // take k3f / q4pi (near_pair64 has the unscaled form)
                     for (int q = ph; q < filled; q += nph) {
-                        const float dx = S[0][q] - X, dy = S[1][q] - Y, dz = S[2][q] - Z;
-                        const float m0 = S[3][q], m1 = S[4][q], m2 = S[5][q], psi = S[6][q];
+                        const float4 P0 = S4[q][0], P1 = S4[q][1];
+                        const float dx = P0.x - X, dy = P0.y - Y, dz = P0.z - Z;
+                        // the cutoff test is a discontinuity: d2 in the FP64 kernel's evaluation order
+                        // (near_pair64), so points at exactly tau h decide alike in both precisions
                         const float d2 = dx * dx + dy * dy + dz * dz;
                         if (d2 < kp.vr2) {
-                            a0 -= kp.k2in * psi;
+                            a0 = fmaf(-kp.k2in_q, P1.z, a0);
                             continue;
                         }
                         const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
-                        const float t = kp.kappa * r, e = __expf(-t), et1 = e * (t + 1.f);
-                        const float q3 = ir3 * kp.q4pi, h3 = ir3 * kp.k3f;
-                        const float c1 = (kp.eps * et1 - 1.f) * q3;
-                        const float c4 = (1.f - kp.ieps * et1) * q3;
-                        const float k2 = (1.f - e) * ir * kp.q4pi;
+                        const float t = kp.kappa * r, e = __expf(-t), et1 = fmaf(e, t, e);
+                        const float h3 = ir3 * kp.k3q;
+                        const float c1 = fmaf(kp.eps, et1, -1.f) * ir3;
+                        const float c4 = fmaf(-kp.ieps, et1, 1.f) * ir3;
+                        const float k2 = (1.f - e) * ir;
                         const float hd = (1.f - et1) * h3;
-                        const float ho = (e * ((t + 3.f) * t + 3.f) - 3.f) * h3 * ir2;
-                        const float dm = dx * m0 + dy * m1 + dz * m2;
-                        a0 += c1 * dm - k2 * psi;
-                        const float cm = ho * dm - c4 * psi;
-                        a1 += hd * m0 + dx * cm;
-                        a2 += hd * m1 + dy * cm;
-                        a3 += hd * m2 + dz * cm;
+                        const float ho = fmaf(e, fmaf(t + 3.f, t, 3.f), -3.f) * h3 * ir2;
+                        const float dm = fmaf(dx, P0.w, fmaf(dy, P1.x, dz * P1.y));
+                        a0 = fmaf(c1, dm, fmaf(-k2, P1.z, a0));
+                        const float cm = fmaf(ho, dm, -c4 * P1.z);
+                        a1 = fmaf(hd, P0.w, fmaf(dx, cm, a1));
+                        a2 = fmaf(hd, P1.x, fmaf(dy, cm, a2));
+                        a3 = fmaf(hd, P1.y, fmaf(dz, cm, a3));
                     }
                     const float part[4] = {a0, a1, a2, a3};
     #pragma unroll
@@ -846,7 +848,7 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     const KParams32 k32 = to32(kp);
     const ChebTables32 *tab = reinterpret_cast<const ChebTables32 *>(P.tables32.ptr);
     (count_launch(), k_pack_src32<<<ew(c, P.ns), 256, 0, s>>>(P.ns, dens, P.sxf.ptr, P.syf.ptr, P.szf.ptr,
-                                                               P.dens32.ptr, P.src8.ptr));
+                                                               P.dens32.ptr, P.src8.ptr, kp.q4pi));
     const float *tx = S.self ? P.sxf.ptr : S.txf.ptr;
     const float *ty = S.self ? P.syf.ptr : S.tyf.ptr;
     const float *tz = S.self ? P.szf.ptr : S.tzf.ptr;
