@@ -3,8 +3,8 @@
 
 One step = one whole solve of the workload (level set -> tube quadrature -> octree plan ->
 GMRES on the fused BIE FMM -> polarization energy) through the C ABI.  The default precision is
-the mixed path (FP32 level set, TF32x3 tensor-core M2L, FP32 near field, FP64 iterative
-refinement); --precision fp64 times the reference-exact FP64 path.
+the mixed path (FP32 level set, tensor-core M2L on scaled FP16 splits, FP32 near field, FP64-class
+iterative refinement); --precision fp64 times the reference-exact FP64 path.
 
   value   solves/sec with the atoms already in HBM (ibim_solve_dev), device time from CUDA events
           on the library's stream, L2 flushed (256 MB write) between steps

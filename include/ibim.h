@@ -55,7 +55,7 @@ extern "C" {
 
 /* ---- precision modes ---- */
 #define IBIM_PRECISION_FP64 0  /* reference-exact FP64 path */
-#define IBIM_PRECISION_MIXED 1 /* FP32 far/near field inside FP64 iterative refinement */
+#define IBIM_PRECISION_MIXED 1 /* FP32-class far/near field inside FP64-class iterative refinement */
 /* FP64 operator whose V-list M2L runs on the tensor cores as exact products of BF16 integer
  * digits (Ozaki scheme, 7 digits of 6 bits under power-of-two row/column scales; ~1e-11 of the
  * FP64 product): the operator of the mixed path's refinement residual.  Accepted by
