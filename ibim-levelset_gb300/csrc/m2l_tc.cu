@@ -784,11 +784,32 @@ __device__ __forceinline__ uint16_t bf16_bits_exact(float v) {
     return (uint16_t)(__float_as_uint(v) >> 16);
 }
 
-// Cut x (|x| < 1) into OZ_S signed digits: m = rint(x 2^42) (one FP64 multiply and one
-// conversion), then balanced base-64 digits by integer arithmetic, least significant first
-// (a_i in [-32, 31] for i >= 1, |a_0| <= 64); x = sum_i a_i 2^-6(i+1) up to 2^-43.
-__device__ __forceinline__ void oz_digits(double x, uint16_t *dig) {
-    long long m = __double2ll_rn(x * 4398046511104.0);  // 2^42
+// rint(v 2^s), rounding half to even, from the bits of v by integer arithmetic (no FP64 pipe);
+// |v 2^s| < 2^62.  The same value as __double2ll_rn(ldexp(v, s)).
+__device__ __forceinline__ long long scaled_rint_bits(double v, int s) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((u >> 52) & 0x7ff);
+    unsigned long long M = u & 0xfffffffffffffULL;
+    if (E != 0) M |= 1ULL << 52;                       // v = M 2^(max(E, 1) - 1075)
+    const int sh = (E == 0 ? 1 : E) - 1075 + s;
+    long long m;
+    if (sh >= 0) {
+        m = (long long)(M << sh);
+    } else {
+        const int k = -sh;
+        if (k > 63) {
+            m = 0;
+        } else {
+            const unsigned long long q = M >> k, rem = M & ((1ULL << k) - 1), half = 1ULL << (k - 1);
+            m = (long long)(q + ((rem > half || (rem == half && (q & 1ULL))) ? 1ULL : 0ULL));
+        }
+    }
+    return (u >> 63) ? -m : m;
+}
+
+// Balanced base-64 digits of m = rint(x 2^42), |x| < 1, least significant first (a_i in
+// [-32, 31] for i >= 1, |a_0| <= 64); x = sum_i a_i 2^-6(i+1) up to 2^-43.
+__device__ __forceinline__ void oz_digits_of(long long m, uint16_t *dig) {
 #pragma unroll
     for (int i = OZ_S - 1; i > 0; --i) {
         const long long a = ((m + 32) & 63) - 32;
@@ -796,6 +817,12 @@ __device__ __forceinline__ void oz_digits(double x, uint16_t *dig) {
         m = (m - a) / 64;  // exact
     }
     dig[0] = bf16_bits_exact((float)(int)m);
+}
+
+// Digits of ldexp(v, -e) (|v| < 2^e): the cut of the operator or multipole value v under its
+// power-of-two scale 2^e.
+__device__ __forceinline__ void oz_digits(double v, int e, uint16_t *dig) {
+    oz_digits_of(scaled_rint_bits(v, 42 - e), dig);
 }
 
 // Power-of-two scale >= m (1 for m == 0), returned as its exponent.
@@ -814,12 +841,14 @@ __global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const double *__res
     const long total = (long)nops * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const int r = (int)(i % mpad), op = (int)(i / mpad);
-        double m = 0.0;
+        // max |A_rk| on the bit patterns: for non-negative doubles their order is the integer order
+        unsigned long long mb = 0;
         if (r < n4) {
             const double *col0 = ops + (long)op * n4 * n4 + r;
-            for (int k = 0; k < n4; ++k) m = fmax(m, fabs(col0[(long)k * n4]));
+            for (int k = 0; k < n4; ++k)
+                mb = max(mb, (unsigned long long)__double_as_longlong(col0[(long)k * n4]) & 0x7fffffffffffffffULL);
         }
-        const int e = oz_scale_exp(m);
+        const int e = oz_scale_exp(__longlong_as_double((long long)mb));
         sig[i] = ldexp(1.0, e - OZ_SCALE_EXP);
         sexp[i] = e;
     }
@@ -840,9 +869,9 @@ __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const doub
         uint32_t w[OZ_S][4];
         for (int q = 0; q < 8; ++q) {
             const int k = grp * 8 + q;
-            const double x = (r < n4 && k < n4) ? ldexp(ops[(long)op * n4 * n4 + (long)k * n4 + r], -e) : 0.0;
+            const double v = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] : 0.0;
             uint16_t dig[OZ_S];
-            oz_digits(x, dig);
+            oz_digits(v, e, dig);
 #pragma unroll
             for (int d = 0; d < OZ_S; ++d) {
                 if (q & 1) w[d][q >> 1] |= (uint32_t)dig[d] << 16;
@@ -875,9 +904,9 @@ __global__ void k_split_mult_oz(long nnodes, int n4, int kpad, const double *__r
         const int e = oz_scale_exp(mx);
         if (lane == 0) tau[node] = ldexp(1.0, e);
         for (int k = lane; k < kpad; k += 32) {
-            const double x = k < n4 ? ldexp(m[k], -e) : 0.0;
+            const double v = k < n4 ? m[k] : 0.0;
             uint16_t dig[OZ_S];
-            oz_digits(x, dig);
+            oz_digits(v, e, dig);
             const long base = ((node * nstage + k / OZ_KS) * OZ_S) * OZ_KS + (k % OZ_KS);
 #pragma unroll
             for (int d = 0; d < OZ_S; ++d) b[base + (long)d * OZ_KS] = dig[d];
