@@ -218,9 +218,14 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
             // (order keeps the peak at 26 bytes per operator entry: FP64 8 + digits 14 + FP32 4,
             // then digits + FP32 + TF32 images 8 once the FP64 operators are gone)
             fmm_ensure_oz_images(*P, cfg.kp);
-            if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
-            fmm_release_fp64_operators(*P);
-            if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);
+            if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc() && m2l_tc_fp16_form() && P->opsff_ready) {
+                fmm_ensure_tc_images(*P, cfg.kp);  // FP16 images from the float-float operators
+                fmm_release_fp64_operators(*P);
+            } else {
+                if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
+                fmm_release_fp64_operators(*P);
+                if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);
+            }
         }
         trace_mark("solve: operators enqueued");
         // the FP32 / float-float near lists of the target sets are built on the host while the

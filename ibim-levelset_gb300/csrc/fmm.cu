@@ -996,8 +996,12 @@ void fmm_ensure_tc_images(Plan &P, const ibim_kernel_params &kp) {
     double key[5];
     kp_key(kp, key);
     if (P.tc_ready && same_key(P.tc_key, key)) return;
-    fmm_prepare_operators(P, kp, IBIM_PRECISION_MIXED);
-    m2l_tc_pack(P);
+    if (m2l_tc_fp16_form() && P.opsff_ready && same_key(P.kpff, key)) {
+        m2l_tc_pack(P, P.opsff.ptr);  // FP16 images from the float-float operators of the digit images
+    } else {
+        fmm_prepare_operators(P, kp, IBIM_PRECISION_MIXED);
+        m2l_tc_pack(P);
+    }
     // the images replace the FP32 operators on this path
     P.ops32.release();
     P.ops32_ready = false;
@@ -1009,8 +1013,15 @@ void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp) {
     double key[5];
     kp_key(kp, key);
     if (P.oz_ready && same_key(P.oz_key, key)) return;
-    fmm_prepare_operators(P, kp, IBIM_PRECISION_FP64);
-    m2l_oz_pack(P);
+    if (P.precision != IBIM_PRECISION_FP64 && ops_ff_enabled()) {
+        // FP64-class plans: operators in float-float on the FP32 pipes (2^-44 a value, below the
+        // digit cut's 2^-43)
+        fmm_prepare_operators_ff(P, kp);
+        m2l_oz_pack(P, P.opsff.ptr);
+    } else {
+        fmm_prepare_operators(P, kp, IBIM_PRECISION_FP64);
+        m2l_oz_pack(P);
+    }
     for (int i = 0; i < 5; ++i) P.oz_key[i] = key[i];
     P.oz_ready = true;
 }
@@ -1018,6 +1029,8 @@ void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp) {
 void fmm_release_fp64_operators(Plan &P) {
     P.ops64.release();
     P.ops64_ready = false;
+    P.opsff.release();
+    P.opsff_ready = false;
 }
 
 // Merged U and W source ranges per target leaf and their work segments, for the FP64 near-field

@@ -265,6 +265,9 @@ struct Plan {
     DevBuf<float> sxf, syf, szf;   // source coordinates relative to their leaf centre (mixed)
     DevBuf<float> sxl, syl, szl;   // their FP32 rounding errors (float-float low words)
     DevBuf<float4> src16;          // float-float near-field source records (FP64-class matvec)
+    DevBuf<float2> opsff;          // M2L operators in float-float (hi, lo) for the FP64-class images
+    bool opsff_ready = false;
+    double kpff[5] = {0, 0, 0, 0, 0};
     DevBuf<float> nrad32;          // per node radius (mixed)
     DevBuf<unsigned char> tables32;  // ChebTables32
     bool mixed_ready = false;
@@ -299,10 +302,14 @@ void fmm_run(Plan &P, int ts, const ibim_kernel_params &kp, const double *dens, 
 
 // Tensor-core V-list M2L (m2l_tc.cu)
 bool m2l_tc_supported();
-void m2l_tc_pack(Plan &P);  // TF32 hi/lo images from P.ops32
+// Tensor-core images from P.ops32, or in the FP16 form from float-float operators when ff is given.
+void m2l_tc_pack(Plan &P, const float2 *ff = nullptr);
+// Whether the mixed path's tensor-core M2L uses the scaled FP16 operand form.
+bool m2l_tc_fp16_form();
 void m2l_tc_run(Plan &P, TargetSet &S);
 int m2l_tc_error(Plan &P);
-void m2l_oz_pack(Plan &P);  // BF16 digit images and row scales from P.ops64
+// BF16 digit images and row scales from P.ops64, or from float-float operators when ff is given.
+void m2l_oz_pack(Plan &P, const float2 *ff = nullptr);
 void m2l_oz_run(Plan &P, const TargetSet &S);
 // Operator images for kernel parameters kp, built when missing or stale: the TF32 images (from
 // FP32 operators, which are then released) and the digit images (from the FP64 operators).
@@ -315,6 +322,11 @@ bool mixed_uses_tc();
 // Whether the FP64-class matvec evaluates its near field in float-float (default; IBIM_NEAR_FF=0
 // keeps native FP64).
 bool near_ff_enabled();
+// Whether the FP64-class operator images (digit slices, and the mixed path's FP16 images made
+// beside them) come from float-float operators instead of FP64 ones (default; IBIM_OPS_FF=0).
+bool ops_ff_enabled();
+// The M2L operators in float-float into P.opsff (once per kernel-parameter set).
+void fmm_prepare_operators_ff(Plan &P, const ibim_kernel_params &kp);
 // Host half of prepare_mixed for one target set (no CUDA calls): the FP32 / float-float near
 // lists and their work segments, kept in the target set until prepare_mixed uploads them, so a
 // solve can build them while the device computes the M2L operators.

@@ -658,16 +658,25 @@ __device__ __forceinline__ float h16_scale(float m) {
     return ldexpf(1.f, e - 14);
 }
 
-// Row scales s_r of the FP32 operators (column-major n4 x n4 per op): rscale[op][mtiles * 128].
-__global__ void k_scale_ops_h16(int n4, int mtiles, int nops, const float *__restrict__ ops, float *rscale) {
+// An operator entry as (hi, lo): FP32 operators have lo = 0, float-float ones carry both words.
+__device__ __forceinline__ float2 op_word(const float *__restrict__ ops, long i) { return make_float2(ops[i], 0.f); }
+__device__ __forceinline__ float2 op_word(const float2 *__restrict__ ops, long i) { return ops[i]; }
+
+// Row scales s_r of the operators (FP32 or float-float, column-major n4 x n4 per op):
+// rscale[op][mtiles * 128].
+template <class OW>
+__global__ void k_scale_ops_h16(int n4, int mtiles, int nops, const OW *__restrict__ ops, float *rscale) {
     const int mpad = mtiles * TC_M;
     const long total = (long)nops * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const int r = (int)(i % mpad), op = (int)(i / mpad);
         float m = 0.f;
         if (r < n4) {
-            const float *col0 = ops + (long)op * n4 * n4 + r;
-            for (int k = 0; k < n4; ++k) m = fmaxf(m, fabsf(col0[(long)k * n4]));
+            const long c0 = (long)op * n4 * n4 + r;
+            for (int k = 0; k < n4; ++k) {
+                const float2 x = op_word(ops, c0 + (long)k * n4);
+                m = fmaxf(m, fabsf(x.x) + fabsf(x.y));
+            }
         }
         rscale[i] = h16_scale(m);
     }
@@ -679,10 +688,18 @@ __device__ __forceinline__ void split_h16(float x, uint16_t &hi, uint16_t &lo) {
     lo = __half_as_ushort(__float2half_rn(x - __half2float(h)));
 }
 
+// The same for a scaled (hi, lo) word pair: hi from the high word, lo from the rest.
+__device__ __forceinline__ void split_h16(float2 x, uint16_t &hi, uint16_t &lo) {
+    const __half h = __float2half_rn(x.x);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn((x.x - __half2float(h)) + x.y));
+}
+
 // FP32 operators -> scaled FP16 hi / lo tiles [op][row tile][stage of 16 K][4 KB] in the
 // shared-memory layout (tile_off with 8 K elements of 2 bytes per 16-byte row piece).  One thread
 // per (op, row, group of 8 K elements): 8 coalesced column reads, one 16-byte store per word.
-__global__ void k_pack_ops_h16(int n4, int mtiles, int kpad, int nops, const float *__restrict__ ops,
+template <class OW>
+__global__ void k_pack_ops_h16(int n4, int mtiles, int kpad, int nops, const OW *__restrict__ ops,
                                const float *__restrict__ rscale, uint4 *a_hi, uint4 *a_lo) {
     const int nstage = kpad / TC_KS16, mpad = mtiles * TC_M, ngrp = kpad / 8;
     const long total = (long)nops * ngrp * mpad;
@@ -695,8 +712,13 @@ __global__ void k_pack_ops_h16(int n4, int mtiles, int kpad, int nops, const flo
         for (int q = 0; q < 8; q += 2) {
             uint16_t h0, l0, h1, l1;
             const int k = grp * 8 + q;
-            const float x0 = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] * inv : 0.f;
-            const float x1 = (r < n4 && k + 1 < n4) ? ops[(long)op * n4 * n4 + (long)(k + 1) * n4 + r] * inv : 0.f;
+            float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
+            if (r < n4 && k < n4) x0 = op_word(ops, (long)op * n4 * n4 + (long)k * n4 + r);
+            if (r < n4 && k + 1 < n4) x1 = op_word(ops, (long)op * n4 * n4 + (long)(k + 1) * n4 + r);
+            x0.x *= inv;  // powers of two: exact
+            x0.y *= inv;
+            x1.x *= inv;
+            x1.y *= inv;
             split_h16(x0, h0, l0);
             split_h16(x1, h1, l1);
             wh[q >> 1] = (uint32_t)h0 | ((uint32_t)h1 << 16);
@@ -825,6 +847,29 @@ __device__ __forceinline__ void oz_digits(double v, int e, uint16_t *dig) {
     oz_digits_of(scaled_rint_bits(v, 42 - e), dig);
 }
 
+// trunc(v 2^s) toward zero from the bits of a float, |v 2^s| < 2^62.
+__device__ __forceinline__ long long scaled_trunc_bits_f32(float v, int s) {
+    const unsigned u = __float_as_uint(v);
+    const int E = (int)((u >> 23) & 0xff);
+    unsigned long long M = u & 0x7fffffu;
+    if (E != 0) M |= 0x800000u;  // v = M 2^(max(E, 1) - 150)
+    const int sh = (E == 0 ? 1 : E) - 150 + s;
+    long long m = 0;
+    if (sh >= 0)
+        m = (long long)(M << sh);
+    else if (sh > -24)
+        m = (long long)(M >> -sh);
+    return (u >> 31) ? -m : m;
+}
+
+// Digits of (h + l) 2^-e for a float-float value: rint from a 2^-16 fixed point of the exact sum
+// (only the rounding of a value within 2^-16 of a half-way point can differ from the exact rint,
+// by one unit of 2^-42, below the cut's own 2^-43).
+__device__ __forceinline__ void oz_digits(float2 v, int e, uint16_t *dig) {
+    const long long f = scaled_trunc_bits_f32(v.x, 58 - e) + scaled_trunc_bits_f32(v.y, 58 - e);
+    oz_digits_of((f + (1LL << 15)) >> 16, dig);
+}
+
 // Power-of-two scale >= m (1 for m == 0), returned as its exponent.
 __device__ __forceinline__ int oz_scale_exp(double m) {
     if (!(m > 0.0)) return 0;
@@ -836,28 +881,47 @@ __device__ __forceinline__ int oz_scale_exp(double m) {
 // Row scales of the FP64 operators (column-major n4 x n4 per op): sig[op][mtiles * 128] =
 // s_r 2^-48 with s_r the power of two >= max_k |A_rk|, and the exponent of s_r.  One thread per
 // (op, row); neighbouring threads read neighbouring rows of a column.
-__global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const double *__restrict__ ops, double *sig, int *sexp) {
+// Exponent of the power-of-two scale of one operator row (n4 entries, stride n4): FP64 entries
+// by the maximum of |x|'s bit patterns (for non-negative doubles their order is the integer
+// order), float-float entries by the maximum of |hi| + |lo|.
+__device__ __forceinline__ int row_scale_exp(const double *__restrict__ col0, int n4) {
+    unsigned long long mb = 0;
+    for (int k = 0; k < n4; ++k)
+        mb = max(mb, (unsigned long long)__double_as_longlong(col0[(long)k * n4]) & 0x7fffffffffffffffULL);
+    return oz_scale_exp(__longlong_as_double((long long)mb));
+}
+__device__ __forceinline__ int row_scale_exp(const float2 *__restrict__ col0, int n4) {
+    float m = 0.f;
+    for (int k = 0; k < n4; ++k) {
+        const float2 x = col0[(long)k * n4];
+        m = fmaxf(m, fabsf(x.x) + fabsf(x.y));
+    }
+    if (!(m > 0.f)) return 0;
+    int e;
+    frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return e;
+}
+
+// Row scales of the operators (FP64 or float-float, column-major n4 x n4 per op):
+// sig[op][mtiles * 128] = s_r 2^-48 with s_r the power of two >= max_k |A_rk|, and the exponent
+// of s_r.  One thread per (op, row); neighbouring threads read neighbouring rows of a column.
+template <class OW>
+__global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const OW *__restrict__ ops, double *sig, int *sexp) {
     const int mpad = mtiles * OZ_M;
     const long total = (long)nops * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const int r = (int)(i % mpad), op = (int)(i / mpad);
-        // max |A_rk| on the bit patterns: for non-negative doubles their order is the integer order
-        unsigned long long mb = 0;
-        if (r < n4) {
-            const double *col0 = ops + (long)op * n4 * n4 + r;
-            for (int k = 0; k < n4; ++k)
-                mb = max(mb, (unsigned long long)__double_as_longlong(col0[(long)k * n4]) & 0x7fffffffffffffffULL);
-        }
-        const int e = oz_scale_exp(__longlong_as_double((long long)mb));
+        const int e = r < n4 ? row_scale_exp(ops + (long)op * n4 * n4 + r, n4) : 0;
         sig[i] = ldexp(1.0, e - OZ_SCALE_EXP);
         sexp[i] = e;
     }
 }
 
-// FP64 operators -> digit tiles [op][row tile][stage][digit][4 KB] in the shared-memory layout
-// (tile_off with 16 K elements of 2 bytes per row).  One thread per (op, row, group of 8 K
-// elements): 8 reads, then one 16-byte store per digit.
-__global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const double *__restrict__ ops,
+// Operators (FP64 or float-float) -> digit tiles [op][row tile][stage][digit][4 KB] in the
+// shared-memory layout (tile_off with 16 K elements of 2 bytes per row).  One thread per (op, row,
+// group of 8 K elements): 8 reads, then one 16-byte store per digit.
+template <class OW>
+__global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *__restrict__ ops,
                               const int *__restrict__ sexp, uint4 *a) {
     const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M, ngrp = kpad / 8;
     const long total = (long)nops * ngrp * mpad;
@@ -869,7 +933,7 @@ __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const doub
         uint32_t w[OZ_S][4];
         for (int q = 0; q < 8; ++q) {
             const int k = grp * 8 + q;
-            const double v = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] : 0.0;
+            const OW v = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] : OW{};
             uint16_t dig[OZ_S];
             oz_digits(v, e, dig);
 #pragma unroll
@@ -1123,11 +1187,14 @@ static bool tc_fp16() {
     return on && !m2l_tc_pair();
 }
 
-void m2l_tc_pack(Plan &P) {
-    IBIM_REQUIRE(P.ops32.ptr || P.nops == 0, "tensor-core images need the FP32 operators");
+bool m2l_tc_fp16_form() { return tc_fp16(); }
+
+void m2l_tc_pack(Plan &P, const float2 *ff) {
+    P.tc_h16 = tc_fp16();
+    if (!P.tc_h16) ff = nullptr;
+    IBIM_REQUIRE(P.ops32.ptr || ff || P.nops == 0, "tensor-core images need the operators");
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
-    P.tc_h16 = tc_fp16();
     const int ks = P.tc_h16 ? TC_KS16 : TC_KS;
     P.tc_kpad = (n4 + ks - 1) / ks * ks;
     P.tc_mpad = (n4 + TC_M - 1) / TC_M * TC_M;
@@ -1141,13 +1208,19 @@ void m2l_tc_pack(Plan &P) {
         P.tc_rsc.alloc((size_t)std::max(1, P.nops) * P.tc_mpad, s);
         P.tc_csc.alloc((size_t)P.tree.nnodes, s);
         if (P.nops > 0) {
-            const long rows = (long)P.nops * P.tc_mpad;
-            (count_launch(), k_scale_ops_h16<<<(int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms), 256, 0, s>>>(
-                                 n4, mt, P.nops, P.ops32.ptr, P.tc_rsc.ptr));
-            const long pieces = rows * (P.tc_kpad / 8);
-            (count_launch(), k_pack_ops_h16<<<(int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms), 256, 0, s>>>(
-                                 n4, mt, P.tc_kpad, P.nops, P.ops32.ptr, P.tc_rsc.ptr,
-                                 reinterpret_cast<uint4 *>(P.tc_a_hi.ptr), reinterpret_cast<uint4 *>(P.tc_a_lo.ptr)));
+            const long rows = (long)P.nops * P.tc_mpad, pieces = rows * (P.tc_kpad / 8);
+            const int gs = (int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms);
+            const int gp = (int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms);
+            uint4 *ah = reinterpret_cast<uint4 *>(P.tc_a_hi.ptr), *al = reinterpret_cast<uint4 *>(P.tc_a_lo.ptr);
+            if (ff) {  // from the float-float operators of the FP64-class images
+                (count_launch(), k_scale_ops_h16<float2><<<gs, 256, 0, s>>>(n4, mt, P.nops, ff, P.tc_rsc.ptr));
+                (count_launch(), k_pack_ops_h16<float2><<<gp, 256, 0, s>>>(n4, mt, P.tc_kpad, P.nops, ff, P.tc_rsc.ptr,
+                                                                           ah, al));
+            } else {
+                (count_launch(), k_scale_ops_h16<float><<<gs, 256, 0, s>>>(n4, mt, P.nops, P.ops32.ptr, P.tc_rsc.ptr));
+                (count_launch(), k_pack_ops_h16<float><<<gp, 256, 0, s>>>(n4, mt, P.tc_kpad, P.nops, P.ops32.ptr,
+                                                                          P.tc_rsc.ptr, ah, al));
+            }
         }
     } else if (P.nops > 0) {
         (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, mt, P.tc_kpad, P.nops, P.ops32.ptr,
@@ -1202,10 +1275,10 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     IBIM_CHECK_LAUNCH();
 }
 
-// Digit tiles of the FP64 operators.
-void m2l_oz_pack(Plan &P) {
+// Digit tiles of the FP64 operators, or of the float-float ones when ff is given.
+void m2l_oz_pack(Plan &P, const float2 *ff) {
     if (P.nops == 0) return;
-    IBIM_REQUIRE(P.ops64.ptr, "digit images need the FP64 operators");
+    IBIM_REQUIRE(P.ops64.ptr || ff, "digit images need the FP64-class operators");
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     P.oz_kpad = (n4 + OZ_KS - 1) / OZ_KS * OZ_KS;
@@ -1222,12 +1295,19 @@ void m2l_oz_pack(Plan &P) {
     const long rows = (long)P.nops * P.oz_mtiles * OZ_M;
     DevBuf<int> sexp;
     sexp.alloc((size_t)rows, s);
-    (count_launch(), k_scale_ops_oz<<<(int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms), 256, 0, s>>>(
-                         n4, P.oz_mtiles, P.nops, P.ops64.ptr, P.oz_sig.ptr, sexp.ptr));
     const long pieces = rows * (P.oz_kpad / 8);
-    (count_launch(), k_pack_ops_oz<<<(int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms), 256, 0, s>>>(
-                         n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, sexp.ptr,
-                         reinterpret_cast<uint4 *>(P.oz_a.ptr)));
+    const int gs = (int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms);
+    const int gp = (int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms);
+    uint4 *a = reinterpret_cast<uint4 *>(P.oz_a.ptr);
+    if (ff) {
+        (count_launch(), k_scale_ops_oz<float2><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, ff, P.oz_sig.ptr, sexp.ptr));
+        (count_launch(), k_pack_ops_oz<float2><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff, sexp.ptr, a));
+    } else {
+        (count_launch(), k_scale_ops_oz<double><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, P.ops64.ptr, P.oz_sig.ptr,
+                                                                   sexp.ptr));
+        (count_launch(), k_pack_ops_oz<double><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr,
+                                                                  sexp.ptr, a));
+    }
     IBIM_CHECK_LAUNCH();
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmemBytes));
 }

@@ -76,15 +76,11 @@ __device__ __forceinline__ f2 exp_neg(f2 t, const float2 *E0, const float2 *E1) 
     return mul(mul(ld(E1[k >> 6]), ld(E0[k & 63])), a);
 }
 
-// One source -> target update of the fused 4x4 block, the formulas of near_pair64
-// (electric.cpp:67-291) in float-float; d = source - target.
-__device__ __forceinline__ void pair_ff(const KParamsFF &k, const float2 *E0, const float2 *E1, f2 dx, f2 dy, f2 dz,
-                                        f2 m0, f2 m1, f2 m2, f2 psi, f2 acc[4]) {
-    const f2 d2 = add(add(sqr(dx), sqr(dy)), sqr(dz));
-    if (d2.h < k.vr2.x || (d2.h == k.vr2.x && d2.l < k.vr2.y)) {
-        acc[0] = sub(acc[0], mul(ld(k.k2in), psi));
-        return;
-    }
+// Radial factors of the 16 kernels at squared distance d2 (radial64 in float-float): c1 (K1),
+// c4 (K4), k2 (K2), hd and ho (K3: hd delta_ab + ho d_a d_b); false inside the cutoff r < tau h.
+__device__ __forceinline__ bool radial_ff(const KParamsFF &k, const float2 *E0, const float2 *E1, f2 d2, f2 &c1,
+                                          f2 &c4, f2 &k2, f2 &hd, f2 &ho) {
+    if (d2.h < k.vr2.x || (d2.h == k.vr2.x && d2.l < k.vr2.y)) return false;
     // 1/sqrt(d2): FP32 estimate y, then y (1 + e/2 + 3e^2/8) with e = 1 - d2 y^2 from exact products
     const float y = rsqrtf(d2.h);
     const float p = __fmul_rn(y, y), pe = __fmaf_rn(y, y, -p);
@@ -100,11 +96,24 @@ __device__ __forceinline__ void pair_ff(const KParamsFF &k, const float2 *E0, co
     }
     const f2 et1 = mul(E, addf(t, 1.f));
     const f2 q3 = mul(ir3, ld(k.q4pi)), h3 = mul(ir3, ld(k.k3f));
-    const f2 c1 = mul(addf(mul(ld(k.eps), et1), -1.f), q3);
-    const f2 c4 = mul(addf(neg(mul(ld(k.ieps), et1)), 1.f), q3);
-    const f2 k2 = mul(mul(addf(neg(E), 1.f), ir), ld(k.q4pi));
-    const f2 hd = mul(addf(neg(et1), 1.f), h3);
-    const f2 ho = mul(mul(addf(mul(E, addf(mul(addf(t, 3.f), t), 3.f)), -3.f), h3), ir2);
+    c1 = mul(addf(mul(ld(k.eps), et1), -1.f), q3);
+    c4 = mul(addf(neg(mul(ld(k.ieps), et1)), 1.f), q3);
+    k2 = mul(mul(addf(neg(E), 1.f), ir), ld(k.q4pi));
+    hd = mul(addf(neg(et1), 1.f), h3);
+    ho = mul(mul(addf(mul(E, addf(mul(addf(t, 3.f), t), 3.f)), -3.f), h3), ir2);
+    return true;
+}
+
+// One source -> target update of the fused 4x4 block, the formulas of near_pair64
+// (electric.cpp:67-291) in float-float; d = source - target.
+__device__ __forceinline__ void pair_ff(const KParamsFF &k, const float2 *E0, const float2 *E1, f2 dx, f2 dy, f2 dz,
+                                        f2 m0, f2 m1, f2 m2, f2 psi, f2 acc[4]) {
+    const f2 d2 = add(add(sqr(dx), sqr(dy)), sqr(dz));
+    f2 c1, c4, k2, hd, ho;
+    if (!radial_ff(k, E0, E1, d2, c1, c4, k2, hd, ho)) {
+        acc[0] = sub(acc[0], mul(ld(k.k2in), psi));
+        return;
+    }
     const f2 dm = add(add(mul(dx, m0), mul(dy, m1)), mul(dz, m2));
     acc[0] = add(acc[0], sub(mul(c1, dm), mul(k2, psi)));
     const f2 cm = sub(mul(ho, dm), mul(c4, psi));
@@ -247,6 +256,68 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
     }
 }
 
+// M2L operators of the FP64-class paths in float-float (k_make_ops64's layout: column-major
+// n4 x n4 per op, entry (row o R + ct, column in R + cs) = block entry (o, in) between target node
+// ct and source node cs), written as (hi, lo) word pairs.  The per-op geometry (half-widths
+// root / 2^level, lattice offset, Chebyshev nodes) is split once per block from FP64.
+__global__ void __launch_bounds__(256) k_make_ops_ff(KParamsFF kp, const ChebTables *__restrict__ tab,
+                                                     const int *__restrict__ keys, const double *__restrict__ root_r,
+                                                     float2 *ops) {
+    __shared__ float2 E0[64], E1[64];
+    __shared__ f2 rt_s[3], rs_s[3], ch_s[MAXP];
+    __shared__ float D_s[3];
+    const int op = blockIdx.y;
+    if (threadIdx.x < 64) {
+        E0[threadIdx.x] = kp.e0[threadIdx.x];
+        E1[threadIdx.x] = kp.e1[threadIdx.x];
+    }
+    if (threadIdx.x == 0) {
+        const int lt = keys[5 * op], ls = keys[5 * op + 1];
+        for (int a = 0; a < 3; ++a) {
+            rt_s[a] = split_d(ldexp(root_r[a], -lt));
+            rs_s[a] = split_d(ldexp(root_r[a], -ls));
+            D_s[a] = (float)keys[5 * op + 2 + a];
+        }
+        for (int m = 0; m < tab->p; ++m) ch_s[m] = split_d(tab->cheb[m]);
+    }
+    __syncthreads();
+    const int p = tab->p, R = tab->R, n4 = 4 * R;
+    const long pair = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (pair >= (long)R * R) return;
+    const int cs = (int)(pair / R), ct = (int)(pair % R);  // consecutive threads: consecutive rows
+    const int ti[3] = {ct % p, (ct / p) % p, ct / (p * p)};
+    const int si[3] = {cs % p, (cs / p) % p, cs / (p * p)};
+    f2 d[3];
+    for (int a = 0; a < 3; ++a)  // (D rt + rs cheb_s) - rt cheb_t, as op_geometry / k_make_ops64
+        d[a] = sub(add(mul(rt_s[a], {D_s[a], 0.f}), mul(rs_s[a], ch_s[si[a]])), mul(rt_s[a], ch_s[ti[a]]));
+    f2 b[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) b[q] = {0.f, 0.f};
+    const f2 d2 = add(add(sqr(d[0]), sqr(d[1])), sqr(d[2]));
+    f2 c1, c4, k2, hd, ho;
+    if (radial_ff(kp, E0, E1, d2, c1, c4, k2, hd, ho)) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            b[a] = mul(d[a], c1);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const f2 v = mul(mul(ho, d[a]), d[c]);
+                b[4 * (a + 1) + c] = a == c ? add(v, hd) : v;
+            }
+            b[4 * (a + 1) + 3] = neg(mul(d[a], c4));
+        }
+        b[3] = neg(k2);
+    } else {
+        b[3] = neg(ld(kp.k2in));
+    }
+    float2 *K = ops + (long)op * n4 * n4;
+#pragma unroll
+    for (int o = 0; o < 4; ++o)
+#pragma unroll
+        for (int in = 0; in < 4; ++in)
+            K[(long)(in * R + cs) * n4 + (o * R + ct)] = make_float2(b[o * 4 + in].h, b[o * 4 + in].l);
+}
+
 float2 split_h(double x) {
     const float h = (float)x;
     return make_float2(h, (float)(x - (double)h));
@@ -287,6 +358,33 @@ int near_ff_occupancy() {
         return std::max(1, b);
     }();
     return occ;
+}
+
+void fmm_prepare_operators_ff(Plan &P, const ibim_kernel_params &kpp) {
+    double key[5] = {kpp.kappa, kpp.dE, kpp.dI, kpp.tau, (double)kpp.k3_scaled};
+    bool same = P.opsff_ready;
+    for (int i = 0; i < 5; ++i) same = same && P.kpff[i] == key[i];
+    if (same || P.nops == 0) return;
+    cudaStream_t s = P.ctx->stream;
+    const int R = P.R, n4 = 4 * R;
+    P.opsff.alloc((size_t)P.nops * n4 * n4, s);
+    const KParamsFF kff = make_kparams_ff(make_kparams(kpp, P.tube->h));
+    dim3 g((unsigned)div_up((long)R * R, 256), P.nops);
+    {
+        ProfScope ps_(PROF_OPS);
+        (count_launch(), k_make_ops_ff<<<g, 256, 0, s>>>(kff, P.tables.ptr, P.op_key.ptr, P.root_r.ptr, P.opsff.ptr));
+    }
+    IBIM_CHECK_LAUNCH();
+    for (int i = 0; i < 5; ++i) P.kpff[i] = key[i];
+    P.opsff_ready = true;
+}
+
+bool ops_ff_enabled() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_OPS_FF");
+        return !(v && v[0] == '0');
+    }();
+    return on;
 }
 
 void near_ff_pack(Plan &P, const double *dens, cudaStream_t st) {
