@@ -150,6 +150,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tile0 = blockIdx.y * TC_RT;
     const int rt = min(TC_RT, mtiles - tile0);
     const int nstage = kpad / KS;
+    // MMA width of this chunk: its pairs rounded up to 16 (the last chunk of an operator is
+    // partial), set in the instruction descriptor's N field; gathers and epilogue stop there too
+    const int neff = max(16, (cnt + 15) & ~15);
+    constexpr uint32_t NMASK = 0x3Fu << 17;
+    const uint32_t idesc16 = (SH::IDESC16 & ~NMASK) | ((uint32_t)(neff >> 3) << 17);
+    const uint32_t idesc32 = (SH::IDESC & ~NMASK) | ((uint32_t)(neff >> 3) << 17);
     constexpr int kStageBytes = SH::STAGE;
     for (int i = tid; i < N; i += TC_THREADS) {
         src_s[i] = i < cnt ? vsrc[b + i] : -1;
@@ -231,13 +237,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const uint64_t al = make_desc(base + (rt + t) * TC_TILE_BYTES, 128, 256);
                     const uint32_t d = tmem_d + (uint32_t)(t * N);
                     if (H16) {
-                        mma_f16(d, ah, bh, SH::IDESC16, st > 0 ? 1u : 0u);
-                        mma_f16(d, ah, bl, SH::IDESC16, 1u);
-                        mma_f16(d, al, bh, SH::IDESC16, 1u);
+                        mma_f16(d, ah, bh, idesc16, st > 0 ? 1u : 0u);
+                        mma_f16(d, ah, bl, idesc16, 1u);
+                        mma_f16(d, al, bh, idesc16, 1u);
                     } else {
-                        mma_tf32(d, ah, bh, SH::IDESC, st > 0 ? 1u : 0u);
-                        mma_tf32(d, ah, bl, SH::IDESC, 1u);
-                        mma_tf32(d, al, bh, SH::IDESC, 1u);
+                        mma_tf32(d, ah, bh, idesc32, st > 0 ? 1u : 0u);
+                        mma_tf32(d, ah, bl, idesc32, 1u);
+                        mma_tf32(d, al, bh, idesc32, 1u);
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -266,8 +272,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (abort_s) break;
             unsigned char *base = tc_smem + buf * kStageBytes;
             const int k0 = st * KS;
-            for (int i = t; i < 4 * N; i += TC_BPROD) {  // 2 tiles x N rows x 2 pieces of 16 B
-                const int tile = i / (2 * N), row = (i >> 1) % N, c = i & 1;
+            for (int i = t; i < 4 * neff; i += TC_BPROD) {  // 2 tiles x neff rows x 2 pieces of 16 B
+                const int tile = i / (2 * neff), row = (i >> 1) % neff, c = i & 1;
                 const uint32_t dst = smem_u32(base + 2 * rt * TC_TILE_BYTES + tile * SH::BT + tile_off(row, c));
                 const int sn = src_s[row];
                 const char *B = tile == 0 ? b_hi : b_lo;
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const float rs = H16 ? rscale[(long)op * mtiles * TC_M + row] : 1.f;  // row < mtiles * 128
             const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * N);
 #pragma unroll 1
-            for (int c0 = 0; c0 < N; c0 += 16) {
+            for (int c0 = 0; c0 < neff; c0 += 16) {
                 uint32_t v[16];
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
