@@ -644,9 +644,19 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     }
     // operator ids: V keys in dense-index order, then X keys in sorted order
     {
-        std::vector<char> used(opid.dense.size(), 0);
-        for (long q = 0; q < npair; ++q)
-            if (pkey[q] >= 0) used[pkey[q]] = 1;
+        // which dense V keys occur: per-thread flags over pair ranges, OR-ed afterwards
+        const size_t nd = opid.dense.size();
+        const int nthr = std::max(1, std::min(32, (int)(npair / 65536) + 1));
+        std::vector<std::vector<char>> part(nthr, std::vector<char>(nd, 0));
+#pragma omp parallel for schedule(static) num_threads(nthr)
+        for (int t = 0; t < nthr; ++t) {
+            const long q0 = npair * t / nthr, q1 = npair * (t + 1) / nthr;
+            for (long q = q0; q < q1; ++q)
+                if (pkey[q] >= 0) part[t][pkey[q]] = 1;
+        }
+        std::vector<char> used(nd, 0);
+        for (int t = 0; t < nthr; ++t)
+            for (size_t d = 0; d < nd; ++d) used[d] |= part[t][d];
         for (size_t d = 0; d < used.size(); ++d)
             if (used[d]) {
                 const int l = (int)(d / 343), c = (int)(d % 343);

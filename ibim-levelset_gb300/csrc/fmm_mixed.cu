@@ -621,13 +621,30 @@ void mixed_lists_host(const Plan &P, TargetSet &S) {
     if (S.mixed_host_ready || S.mixed_ready) return;
     const TreeHost &T = P.tree;
     const int nn = T.nnodes;
-    // near lists: U and W nodes expanded into their non-empty leaves, with centre offsets
-    std::vector<int> ptr{0}, rng;
-    std::vector<float> off, offl;
+    // near lists: U and W nodes expanded into their non-empty leaves (depth first, child 0
+    // first), with centre offsets.  The non-empty leaves below a node form one contiguous run of
+    // the tree's depth-first leaf order, so each target leaf's list is a concatenation of runs.
     std::vector<int> child_first(nn, -1);
     for (int i = nn - 1; i >= 0; --i)
         if (T.parent[i] >= 0) child_first[T.parent[i]] = i - T.index8[i];
-    // target leaves in node order, expanded in parallel into per-leaf lists, then concatenated
+    std::vector<int> cnt(nn, 0), first(nn, 0);
+    for (int i = nn - 1; i >= 0; --i) {  // nodes are level-ordered: children after parents
+        if (T.leaf[i])
+            cnt[i] = T.src_end[i] > T.src_begin[i] ? 1 : 0;
+        else if (child_first[i] >= 0)
+            for (int c = 0; c < 8; ++c) cnt[i] += cnt[child_first[i] + c];
+    }
+    for (int i = 0; i < nn; ++i) {
+        if (T.leaf[i] || child_first[i] < 0) continue;
+        int f = first[i];
+        for (int c = 0; c < 8; ++c) {
+            first[child_first[i] + c] = f;
+            f += cnt[child_first[i] + c];
+        }
+    }
+    std::vector<int> dfs_leaf(std::max(1, nn > 0 ? cnt[0] : 0));
+    for (int i = 0; i < nn; ++i)
+        if (T.leaf[i] && cnt[i]) dfs_leaf[first[i]] = i;
     std::vector<int> tl32, nt32;
     for (int i = 0; i < nn; ++i)
         if (T.leaf[i] && S.end[i] > S.begin[i]) {
@@ -635,40 +652,37 @@ void mixed_lists_host(const Plan &P, TargetSet &S) {
             nt32.push_back((int)(S.end[i] - S.begin[i]));
         }
     const long ntl = (long)tl32.size();
-    std::vector<std::vector<int>> prng(ntl);
-    std::vector<std::vector<float>> poff(ntl), poffl(ntl);
-#pragma omp parallel for schedule(dynamic, 32)
+    std::vector<int> ptr(ntl + 1, 0);
+#pragma omp parallel for schedule(static)
     for (long k = 0; k < ntl; ++k) {
         const int i = tl32[k];
-        std::vector<int> stack;
-        auto add_leaves = [&](int root) {
-            stack.clear();
-            stack.push_back(root);
-            while (!stack.empty()) {
-                const int n = stack.back();
-                stack.pop_back();
-                if (T.src_end[n] <= T.src_begin[n]) continue;
-                if (T.leaf[n]) {
-                    prng[k].push_back(T.src_begin[n]);
-                    prng[k].push_back(T.src_end[n]);
-                    for (int a = 0; a < 3; ++a) {
-                        const double d = T.center[3 * n + a] - T.center[3 * i + a];
-                        poff[k].push_back((float)d);
-                        poffl[k].push_back((float)(d - (double)(float)d));
-                    }
-                } else {
-                    for (int c = 7; c >= 0; --c) stack.push_back(child_first[n] + c);
+        int c = 0;
+        for (int u : T.U[i]) c += cnt[u];
+        for (int w : T.W[i]) c += cnt[w];
+        ptr[k + 1] = c;
+    }
+    for (long k = 0; k < ntl; ++k) ptr[k + 1] += ptr[k];
+    const long nent = ptr[ntl];
+    std::vector<int> rng(2 * nent);
+    std::vector<float> off(3 * nent), offl(3 * nent);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long k = 0; k < ntl; ++k) {
+        const int i = tl32[k];
+        long q = ptr[k];
+        auto add_run = [&](int root) {
+            for (int r = first[root]; r < first[root] + cnt[root]; ++r, ++q) {
+                const int n = dfs_leaf[r];
+                rng[2 * q] = T.src_begin[n];
+                rng[2 * q + 1] = T.src_end[n];
+                for (int a = 0; a < 3; ++a) {
+                    const double d = T.center[3 * n + a] - T.center[3 * i + a];
+                    off[3 * q + a] = (float)d;
+                    offl[3 * q + a] = (float)(d - (double)(float)d);
                 }
             }
         };
-        for (int u : T.U[i]) add_leaves(u);
-        for (int w : T.W[i]) add_leaves(w);
-    }
-    for (long k = 0; k < ntl; ++k) {
-        rng.insert(rng.end(), prng[k].begin(), prng[k].end());
-        off.insert(off.end(), poff[k].begin(), poff[k].end());
-        offl.insert(offl.end(), poffl[k].begin(), poffl[k].end());
-        ptr.push_back((int)rng.size() / 2);
+        for (int u : T.U[i]) add_run(u);
+        for (int w : T.W[i]) add_run(w);
     }
     S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_seg32);
     S.nnear32_seg = tl32.empty() ? 0 : (int)S.h_seg32.size() / 4;
