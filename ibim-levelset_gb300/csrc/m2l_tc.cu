@@ -38,13 +38,15 @@ constexpr long TC_WAIT_LIMIT = 1L << 20;           // bounded mbarrier polling
 // FP16 operand form: K elements per stage (a stage row is 32 bytes in both forms)
 constexpr int TC_KS16 = 16;
 
-// Shape of the contraction for N pairs per chunk (MMA N): RT = 512 / N row tiles fill the 512
-// TMEM columns; a stage holds RT operator tiles (hi, lo) and the N multipole rows (hi, lo).
-template <int N> struct TcShape {
-    static constexpr int RT = 512 / N;
+// Shape of the contraction for N pairs per chunk (MMA N) against RT row tiles of 128 operator
+// rows, CPS CTAs resident per SM: RT N TMEM columns per CTA (all 512 for CPS 1); a stage holds RT
+// operator tiles (hi, lo) and the N multipole rows (hi, lo).
+template <int N, int RT_ = 512 / N, int CPS = 1> struct TcShape {
+    static constexpr int RT = RT_;
+    static_assert(RT * N * CPS <= 512, "TMEM columns of the resident CTAs");
     static constexpr int BT = N * TC_KS * 4;                           // multipole tile bytes
-    static constexpr int STAGE = 2 * RT * TC_TILE_BYTES + 2 * BT;       // 40 KB (N 128), 32 KB (N 256)
-    static constexpr int NST = (200 * 1024) / STAGE;                   // 5 or 6 stage buffers
+    static constexpr int STAGE = 2 * RT * TC_TILE_BYTES + 2 * BT;       // 40 KB (N 128, RT 4)
+    static constexpr int NST = ((CPS == 1 ? 200 : 96) * 1024) / STAGE;  // 5 (RT 4) or 4 (RT 2, CPS 2)
     static constexpr int SMEM = NST * STAGE;
     // stages of multipole copies a gathering thread keeps in flight before it signals the oldest
     static constexpr int LAG = NST - 2;
@@ -117,7 +119,7 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
     return (uint32_t)((((row >> 3) << 1) + kchunk) * 128 + (row & 7) * 16);
 }
 
-// One CTA: one chunk of <= N V pairs of a single operator x up to RT = 512 / N row tiles of 128
+// One CTA: one chunk of <= N V pairs of a single operator x up to RT row tiles of 128
 // operator rows.  Stage st holds K elements [8 st, 8 st + 8) of A_hi, A_lo (per row tile, pre-packed
 // as contiguous 4 KB blocks in the shared-memory layout) and of B_hi, B_lo in buffer st % TC_NST.
 // Warp-specialised: warp 0 (one thread) issues the operator bulk copies, warp 1 (one thread)
@@ -128,13 +130,13 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
 // bounded and an expired wait aborts the CTA through a shared flag and the error word.
 constexpr int TC_BPROD = 192;
 
-template <int N, bool H16>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <int N, bool H16, int RT = 512 / N, int CPS = 1>
+__global__ void __launch_bounds__(TC_THREADS, CPS)
     k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
                 const int *__restrict__ vtgt, const void *__restrict__ a_hi_, const void *__restrict__ a_lo_,
                 const void *__restrict__ b_hi_, const void *__restrict__ b_lo_, const float *__restrict__ rscale,
                 const float *__restrict__ cscale, float *local, int *err) {
-    using SH = TcShape<N>;
+    using SH = TcShape<N, RT, CPS>;
     constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
     constexpr int KS = H16 ? TC_KS16 : TC_KS, ES = H16 ? 2 : 4;  // K elements per stage, bytes per element
     const char *a_hi = static_cast<const char *>(a_hi_), *a_lo = static_cast<const char *>(a_lo_);
@@ -1195,6 +1197,17 @@ static bool tc_fp16() {
 
 bool m2l_tc_fp16_form() { return tc_fp16(); }
 
+// Two CTAs per SM of two row tiles each (default) or one CTA of four (IBIM_TC_RT=4): with two,
+// one CTA's prologue and epilogue overlap the other's MMAs, at twice the multipole gathers
+// (2,000-atom protein: 2.32 against 2.50 ms a launch).
+static bool tc_two_per_sm() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_TC_RT");
+        return !(v && v[0] == '4');
+    }();
+    return on;
+}
+
 void m2l_tc_pack(Plan &P, const float2 *ff) {
     P.tc_h16 = tc_fp16();
     if (!P.tc_h16) ff = nullptr;
@@ -1243,11 +1256,15 @@ void m2l_tc_pack(Plan &P, const float2 *ff) {
                                    TcShape<M2L_CHTC>::SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
 }
 
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating): chunks of 128 pairs against
-// four row tiles.  (Chunks of 256 pairs against two row tiles, k_m2l_tc<256>, measured 5.0 ms
+// two row tiles per CTA, two CTAs per SM (or four row tiles, one CTA per SM).  (Chunks of 256 pairs against two row tiles, k_m2l_tc<256>, measured 5.0 ms
 // against 3.9 ms on the 2,000-atom protein: the operator traffic falls but the chunks fill worse.)
 void m2l_tc_run(Plan &P, TargetSet &S) {
     constexpr int N = M2L_CHTC;
@@ -1270,6 +1287,17 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
                              n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        IBIM_CHECK_LAUNCH();
+        return;
+    }
+    if (tc_two_per_sm()) {
+        using SH2 = TcShape<N, 2, 2>;
+        const dim3 grid(S.nchunks_tc, (mt + SH2::RT - 1) / SH2::RT);
+        auto kern = P.tc_h16 ? k_m2l_tc<N, true, 2, 2> : k_m2l_tc<N, false, 2, 2>;
+        (count_launch(), kern<<<grid, TC_THREADS, SH2::SMEM, s>>>(
+                             n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr,
+                             P.tc_err.ptr));
         IBIM_CHECK_LAUNCH();
         return;
     }
