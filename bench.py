@@ -364,10 +364,14 @@ def run_ours(args):
     # operand form of the mixed path's tensor-core M2L (the library's default: scaled FP16 splits)
     tc_form = ("tf32x3 tensor" if os.environ.get("IBIM_TC_FP16") == "0" or os.environ.get("IBIM_TC_PAIR") == "1"
                else "fp16x3 tensor")
+    # digit-pair MMAs per multiply-add of the sliced FP64-class M2L: 6 digits of 7 bits (21 pairs)
+    # while K = 4 p^3 padded to 16 is at most 800, else 7 digits of 6 bits (28 pairs)
+    oz_digits = 6 if (4 * W.np_ ** 3 + 15) // 16 * 16 <= 800 else 7
+    oz_mmas = oz_digits * (oz_digits + 1) // 2
     fp_bound = {"m2l_v_fp64": "fp64", "m2l_x_fp64": "fp64", "near_l2p_fp64": "fp64", "near_l2p": "fp32",
                 "m2l_x": "fp32", "m2l_v": tc_form if mixed else "fp64", "rhs": "fp32" if mixed else "fp64",
                 "weno_stage": "fp32" if mixed else "fp64", "p2m": "fp32" if mixed else "fp64",
-                "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": "bf16x28 tensor",
+                "count_gradient": "hbm", "gmres_vectors": "hbm", "m2l_v_sliced": f"bf16x{oz_mmas} tensor",
                 "near_ff": "fp32", "l2p": "fp32", "l2p_fp64": "fp64"}
 
     def roofline_of(name, d):
@@ -397,11 +401,11 @@ def run_ours(args):
                 unit = "TFLOP/s"
                 src = "MEASURED_PEAKS.json bf16_tflops (FP16 rate, of measured); achieved counts the 3 MMAs"
             elif bound.startswith("bf16"):
-                # 28 BF16 digit-pair MMAs per algorithmic multiply-add (7 digits, pairs i + l <= 6)
-                ach = 28 * alg / (per_launch_ms * 1e-3) / 1e12
+                # oz_mmas BF16 digit-pair MMAs per algorithmic multiply-add (pairs i + l < digits)
+                ach = oz_mmas * alg / (per_launch_ms * 1e-3) / 1e12
                 peak = peaks.get("bf16_tflops", 1909.5)
                 unit = "TFLOP/s"
-                src = "MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the 28 digit MMAs"
+                src = f"MEASURED_PEAKS.json bf16_tflops (of measured); achieved counts the {oz_mmas} digit MMAs"
             else:
                 ach = alg / (per_launch_ms * 1e-3) / 1e12
                 peak = fp64_peak if bound == "fp64" else fp32_peak

@@ -12,7 +12,7 @@ constexpr int MAXP = 8;
 constexpr int MAXR = MAXP * MAXP * MAXP;
 constexpr int M2L_CH32 = 32;  // V pairs per chunk of the FP32 contraction
 constexpr int M2L_CHTC = 128; // V pairs per chunk of the tensor-core contraction (MMA N)
-constexpr int M2L_CHOZ = 64;  // V pairs per chunk of the sliced FP64-class contraction (MMA N)
+constexpr int M2L_CHOZ = 128; // V pairs per chunk of the sliced FP64-class contraction (MMA N)
 // Largest padded contraction length whose digit-group sums stay below 2^24 (exact in FP32):
 // K * (2 * 64 * 32 + 5 * 32 * 32) < 2^24, i.e. orders p <= 7.
 constexpr int M2L_OZ_MAXK = 1792;

@@ -283,7 +283,7 @@ struct Plan {
     // exact BF16 integer slices under power-of-two row / column scales
     bool oz_ready = false;           // digit images valid for kernel parameters oz_key
     double oz_key[5] = {-1, -1, -1, -1, -1};
-    int oz_kpad = 0, oz_mtiles = 0;
+    int oz_kpad = 0, oz_mtiles = 0, oz_s = 7;  // digit images: K padded, row tiles, digits
     DevBuf<uint16_t> oz_a, oz_b;
     DevBuf<double> oz_sig, oz_tau;
     double kp64[5] = {-1, -1, -1, -1, -1}, kp32[5] = {-1, -1, -1, -1, -1};  // kernel parameters of the cached operators

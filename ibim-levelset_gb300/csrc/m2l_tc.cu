@@ -765,51 +765,63 @@ __global__ void k_split_mult_h16(long nnodes, int n4, int kpad, const float *__r
 }
 
 // ---------------------------------------------------------------------------------------------
-// FP64-class V-list M2L for the refinement residual: exact integer slices on the tensor cores.
+// FP64-class V-list M2L for the refinement residual: integer digit slices on the tensor cores.
 //
 // The Ozaki scheme (Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix
 // multiplication by using fast routines of matrix multiplication", Numer. Algorithms 59, 2012),
 // in its fixed-point form: each operator row r is scaled by a power of two s_r >= max |A_r.|,
 // each multipole column j by t_j >= max |B_.j|, and the scaled values (in [-1, 1]) are cut into
-// OZ_S signed 6-bit digits (balanced base-64 digits of rint(A_rk / s_r 2^42)),
-//     A_rk / s_r = sum_i a_i(r,k) 2^(-6(i+1)) + e,   |a_0| <= 64, |a_i>0| <= 32, |e| <= 2^-43.
-// Digits are small integers, exact in BF16; a digit product is an integer below 2^12 and a
-// K-term dot product of one digit pair below 2^21 (K <= 1024), so the FP32 tensor-core
-// accumulation of each group G_k = sum_{i+l=k} a_i b_l (at most 7 digit pairs, < 2^24) is exact.
-// The epilogue recombines sum_k G_k 2^(-6(k+2)) exactly in 64-bit integers, converts once to
-// FP64 and applies s_r t_j.  Digit pairs with i + l >= OZ_S are dropped: the result differs from
-// the FP64 product by about 2^-40 of s_r t_j per term (~1e-11 relative), far below the FP32
-// operator the refinement corrects.
+// S signed digits of D = 42 / S bits (balanced base-2^D digits of rint(A_rk / s_r 2^42)),
+//     A_rk / s_r = sum_i a_i(r,k) 2^(-D(i+1)) + e,   |a_0| <= 2^D, |a_i>0| <= 2^(D-1), |e| <= 2^-43.
+// Digit i is stored as a_i 2^(-D i) (a power-of-two multiple of a small integer: exact in BF16),
+// so the product of operator digit i and multipole digit l carries its weight 2^(-D(i+l))
+// and the MMAs of one group k = i + l accumulate G_k 2^(-D k), G_k = sum_{i+l=k} sum_K a_i b_l.
+// Groups 0, 1 and 2 get one TMEM accumulator each and stay exact in the FP32 accumulation:
+// |G_k| <= 1.25 2^(2D) K < 2^24 (S = 6, D = 7: K <= 800; S = 7, D = 6: K <= 3200).  Groups
+// 3 .. S-1 share a fourth accumulator, rounded at 2^-24 of a value 2^(-3D) below group 0
+// (~2^-45 of s_r t_j per step of 16 K elements).  The epilogue adds the four in FP64 (exact),
+// applies s_r t_j 2^(-2D) and adds into the FP64 locals.  Digit pairs with i + l >= S are
+// dropped: the result differs from the FP64 product by about 2^-40 of s_r t_j per term (~1e-11
+// relative), far below the FP32 operator the refinement corrects.  S = 6 (7-bit digits, 21
+// digit MMAs a step) where K allows it (orders up to 5), else S = 7 (6-bit digits, 28 MMAs).
 //
-// One CTA: one chunk of <= 64 pairs x one 128-row tile; accumulator k (k = 0..6) in TMEM
-// columns [64 k, 64 k + 64).  Stage st holds K elements [16 st, 16 st + 16): the 7 operator digit
-// tiles (128 x 16 BF16, 4 KB each, pre-packed contiguously: one bulk copy) and the 7 multipole
-// digit tiles (64 x 16 BF16, gathered by cp.async).  Warp-specialised like k_m2l_tc: one thread
-// issues the bulk copies, one the MMAs, six warps gather; they meet on mbarriers only.
+// One CTA: one chunk of <= 128 pairs x one 128-row tile; accumulator g (g = 0..3) in TMEM
+// columns [128 g, 128 g + 128).  Stage st holds K elements [16 st, 16 st + 16): the S operator
+// digit tiles (128 x 16 BF16, 4 KB each, pre-packed contiguously: one bulk copy) and the S
+// multipole digit tiles (128 x 16 BF16, gathered by cp.async).  Warp-specialised like k_m2l_tc:
+// one thread issues the bulk copies, one the MMAs, six warps gather; they meet on mbarriers only.
 // ---------------------------------------------------------------------------------------------
 
-constexpr int OZ_S = 7, OZ_M = 128, OZ_N = 64, OZ_KS = 16;
-constexpr int OZ_NST = 5, OZ_THREADS = 256, OZ_BPROD = 192, OZ_LAG = OZ_NST - 2;
+constexpr int OZ_M = 128, OZ_N = 128, OZ_KS = 16, OZ_ACC = 4;
+constexpr int OZ_THREADS = 256, OZ_BPROD = 192;
 constexpr int OZ_ATILE = OZ_M * OZ_KS * 2;                 // 4 KB
-constexpr int OZ_BTILE = OZ_N * OZ_KS * 2;                 // 2 KB
-constexpr int OZ_STAGE = OZ_S * (OZ_ATILE + OZ_BTILE);      // 42 KB
-constexpr int kOzSmemBytes = OZ_NST * OZ_STAGE;             // 210 KB
-constexpr int OZ_SCALE_EXP = 6 * (OZ_S + 1);                // 2^-48 folded into the row scale
+constexpr int OZ_BTILE = OZ_N * OZ_KS * 2;                 // 4 KB
+constexpr int OZ_K7 = 800;                                  // largest K for 7-bit digits (S = 6)
+static_assert(OZ_N * OZ_ACC <= 512, "TMEM columns");
 
-// D FP32, A and B BF16, both K-major, M = 128, N = 64.
-constexpr uint32_t kIdescOz = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_N >> 3) << 17) |
-                              ((uint32_t)(OZ_M >> 4) << 24);
+template <int S> struct OzShape {
+    static constexpr int D = 42 / S;                        // bits per digit
+    static_assert(S * D == 42, "42-bit cut");
+    static constexpr int STAGE = S * (OZ_ATILE + OZ_BTILE);  // 48 KB (S 6), 56 KB (S 7)
+    static constexpr int NST = (200 * 1024) / STAGE;        // 4 or 3 stage buffers
+    static constexpr int LAG = NST - 2;
+    static constexpr int SMEM = NST * STAGE;
+};
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+// D FP32, A and B BF16, both K-major, M = 128; N in bits 17-22 per chunk.
+constexpr uint32_t kIdescOz = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_M >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         :
-        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescOz), "r"(accumulate));
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-// BF16 bits of a small integer-valued float (exact: the low 16 bits are zero).
+// BF16 bits of a float whose significand has at most 8 bits (exact: the low 16 bits are zero).
 __device__ __forceinline__ uint16_t bf16_bits_exact(float v) {
     return (uint16_t)(__float_as_uint(v) >> 16);
 }
@@ -837,22 +849,27 @@ __device__ __forceinline__ long long scaled_rint_bits(double v, int s) {
     return (u >> 63) ? -m : m;
 }
 
-// Balanced base-64 digits of m = rint(x 2^42), |x| < 1, least significant first (a_i in
-// [-32, 31] for i >= 1, |a_0| <= 64); x = sum_i a_i 2^-6(i+1) up to 2^-43.
+// Balanced base-2^D digits of m = rint(x 2^42), |x| <= 1, stored scaled: dig[i] = a_i 2^(-D i)
+// with x = sum_i a_i 2^(-D(i+1)) up to 2^-43 (a_i in [-2^(D-1), 2^(D-1)) for i >= 1,
+// |a_0| <= 2^D).
+template <int S>
 __device__ __forceinline__ void oz_digits_of(long long m, uint16_t *dig) {
+    constexpr int D = OzShape<S>::D;
+    constexpr long long H = 1LL << (D - 1), MASK = (1LL << D) - 1;
 #pragma unroll
-    for (int i = OZ_S - 1; i > 0; --i) {
-        const long long a = ((m + 32) & 63) - 32;
-        dig[i] = bf16_bits_exact((float)(int)a);
-        m = (m - a) / 64;  // exact
+    for (int i = S - 1; i > 0; --i) {
+        const long long a = ((m + H) & MASK) - H;
+        dig[i] = bf16_bits_exact((float)(int)a * __int_as_float((127 - D * i) << 23));  // a 2^(-D i)
+        m = (m - a) >> D;  // exact: m - a is a multiple of 2^D
     }
     dig[0] = bf16_bits_exact((float)(int)m);
 }
 
 // Digits of ldexp(v, -e) (|v| < 2^e): the cut of the operator or multipole value v under its
 // power-of-two scale 2^e.
+template <int S>
 __device__ __forceinline__ void oz_digits(double v, int e, uint16_t *dig) {
-    oz_digits_of(scaled_rint_bits(v, 42 - e), dig);
+    oz_digits_of<S>(scaled_rint_bits(v, 42 - e), dig);
 }
 
 // trunc(v 2^s) toward zero from the bits of a float, |v 2^s| < 2^62.
@@ -873,9 +890,10 @@ __device__ __forceinline__ long long scaled_trunc_bits_f32(float v, int s) {
 // Digits of (h + l) 2^-e for a float-float value: rint from a 2^-16 fixed point of the exact sum
 // (only the rounding of a value within 2^-16 of a half-way point can differ from the exact rint,
 // by one unit of 2^-42, below the cut's own 2^-43).
+template <int S>
 __device__ __forceinline__ void oz_digits(float2 v, int e, uint16_t *dig) {
     const long long f = scaled_trunc_bits_f32(v.x, 58 - e) + scaled_trunc_bits_f32(v.y, 58 - e);
-    oz_digits_of((f + (1LL << 15)) >> 16, dig);
+    oz_digits_of<S>((f + (1LL << 15)) >> 16, dig);
 }
 
 // Power-of-two scale >= m (1 for m == 0), returned as its exponent.
@@ -886,9 +904,6 @@ __device__ __forceinline__ int oz_scale_exp(double m) {
     return e;
 }
 
-// Row scales of the FP64 operators (column-major n4 x n4 per op): sig[op][mtiles * 128] =
-// s_r 2^-48 with s_r the power of two >= max_k |A_rk|, and the exponent of s_r.  One thread per
-// (op, row); neighbouring threads read neighbouring rows of a column.
 // Exponent of the power-of-two scale of one operator row (n4 entries, stride n4): FP64 entries
 // by the maximum of |x|'s bit patterns (for non-negative doubles their order is the integer
 // order), float-float entries by the maximum of |hi| + |lo|.
@@ -911,16 +926,17 @@ __device__ __forceinline__ int row_scale_exp(const float2 *__restrict__ col0, in
 }
 
 // Row scales of the operators (FP64 or float-float, column-major n4 x n4 per op):
-// sig[op][mtiles * 128] = s_r 2^-48 with s_r the power of two >= max_k |A_rk|, and the exponent
+// sig[op][mtiles * 128] = s_r 2^(-2D) with s_r the power of two >= max_k |A_rk|, and the exponent
 // of s_r.  One thread per (op, row); neighbouring threads read neighbouring rows of a column.
 template <class OW>
-__global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const OW *__restrict__ ops, double *sig, int *sexp) {
+__global__ void k_scale_ops_oz(int n4, int mtiles, int nops, int scale_exp, const OW *__restrict__ ops, double *sig,
+                               int *sexp) {
     const int mpad = mtiles * OZ_M;
     const long total = (long)nops * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const int r = (int)(i % mpad), op = (int)(i / mpad);
         const int e = r < n4 ? row_scale_exp(ops + (long)op * n4 * n4 + r, n4) : 0;
-        sig[i] = ldexp(1.0, e - OZ_SCALE_EXP);
+        sig[i] = ldexp(1.0, e - scale_exp);
         sexp[i] = e;
     }
 }
@@ -928,7 +944,7 @@ __global__ void k_scale_ops_oz(int n4, int mtiles, int nops, const OW *__restric
 // Operators (FP64 or float-float) -> digit tiles [op][row tile][stage][digit][4 KB] in the
 // shared-memory layout (tile_off with 16 K elements of 2 bytes per row).  One thread per (op, row,
 // group of 8 K elements): 8 reads, then one 16-byte store per digit.
-template <class OW>
+template <int S, class OW>
 __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *__restrict__ ops,
                               const int *__restrict__ sexp, uint4 *a) {
     const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M, ngrp = kpad / 8;
@@ -938,29 +954,30 @@ __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *
         const long rest = i / mpad;
         const int grp = (int)(rest % ngrp), op = (int)(rest / ngrp);
         const int e = sexp[(long)op * mpad + r];
-        uint32_t w[OZ_S][4];
+        uint32_t w[S][4];
         for (int q = 0; q < 8; ++q) {
             const int k = grp * 8 + q;
             const OW v = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] : OW{};
-            uint16_t dig[OZ_S];
-            oz_digits(v, e, dig);
+            uint16_t dig[S];
+            oz_digits<S>(v, e, dig);
 #pragma unroll
-            for (int d = 0; d < OZ_S; ++d) {
+            for (int d = 0; d < S; ++d) {
                 if (q & 1) w[d][q >> 1] |= (uint32_t)dig[d] << 16;
                 else w[d][q >> 1] = dig[d];
             }
         }
         const int t = r / OZ_M, row = r % OZ_M, st = grp / 2, half = grp & 1;
-        const long tbase = (((long)op * mtiles + t) * nstage + st) * OZ_S;
+        const long tbase = (((long)op * mtiles + t) * nstage + st) * S;
         const uint32_t off = tile_off(row, half);  // byte offset of the 16-byte piece
 #pragma unroll
-        for (int d = 0; d < OZ_S; ++d)
+        for (int d = 0; d < S; ++d)
             a[((tbase + d) * OZ_ATILE + off) / 16] = make_uint4(w[d][0], w[d][1], w[d][2], w[d][3]);
     }
 }
 
 // Multipoles (FP64 [node][n4]) -> digits [node][stage][digit][16] and column scales tau = t_j.
 // One warp per node.
+template <int S>
 __global__ void k_split_mult_oz(long nnodes, int n4, int kpad, const double *__restrict__ mult, uint16_t *b,
                                 double *tau) {
     const int lane = threadIdx.x & 31;
@@ -977,21 +994,24 @@ __global__ void k_split_mult_oz(long nnodes, int n4, int kpad, const double *__r
         if (lane == 0) tau[node] = ldexp(1.0, e);
         for (int k = lane; k < kpad; k += 32) {
             const double v = k < n4 ? m[k] : 0.0;
-            uint16_t dig[OZ_S];
-            oz_digits(v, e, dig);
-            const long base = ((node * nstage + k / OZ_KS) * OZ_S) * OZ_KS + (k % OZ_KS);
+            uint16_t dig[S];
+            oz_digits<S>(v, e, dig);
+            const long base = ((node * nstage + k / OZ_KS) * S) * OZ_KS + (k % OZ_KS);
 #pragma unroll
-            for (int d = 0; d < OZ_S; ++d) b[base + (long)d * OZ_KS] = dig[d];
+            for (int d = 0; d < S; ++d) b[base + (long)d * OZ_KS] = dig[d];
         }
     }
 }
 
+template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_m2l_oz(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
              const int *__restrict__ vtgt, const uint16_t *__restrict__ a, const double *__restrict__ sig,
              const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err) {
+    using SH = OzShape<S>;
+    constexpr int NST = SH::NST, LAG = SH::LAG, STAGE = SH::STAGE;
     extern __shared__ __align__(1024) unsigned char oz_smem[];
-    __shared__ __align__(8) uint64_t full_a[OZ_NST], full_b[OZ_NST], empty_bar[OZ_NST], acc_bar;
+    __shared__ __align__(8) uint64_t full_a[NST], full_b[NST], empty_bar[NST], acc_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int src_s[OZ_N], tgt_s[OZ_N];
     __shared__ double tau_s[OZ_N];
@@ -1000,6 +1020,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
     const int t = blockIdx.y;
     const int nstage = kpad / OZ_KS;
+    // MMA width of this chunk: its pairs rounded up to 16; gathers and epilogue stop there too
+    const int neff = max(16, (cnt + 15) & ~15);
+    const uint32_t idesc = kIdescOz | ((uint32_t)(neff >> 3) << 17);
     if (tid < OZ_N) {
         const int sn = tid < cnt ? vsrc[b + tid] : -1;
         src_s[tid] = sn;
@@ -1008,7 +1031,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     if (tid == 0) {
         abort_s = 0;
-        for (int i = 0; i < OZ_NST; ++i) {
+        for (int i = 0; i < NST; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(OZ_BPROD));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
@@ -1031,45 +1054,47 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         if (lane == 0) {  // operator digit tiles: one bulk copy per stage
             int issued = -1;
             for (int st = 0; st < nstage; ++st) {
-                const int buf = st % OZ_NST;
-                if (st >= OZ_NST &&
-                    !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / OZ_NST) - 1) & 1))) {
+                const int buf = st % NST;
+                if (st >= NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / NST) - 1) & 1))) {
                     abort_s = 1;
                     break;
                 }
                 if (abort_s) break;
                 const uint32_t fb = smem_u32(&full_a[buf]);
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(OZ_S * OZ_ATILE)
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(S * OZ_ATILE)
                              : "memory");
                 asm volatile(
                     "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                        smem_u32(oz_smem + buf * OZ_STAGE)),
-                    "l"(a + (atile0 + st) * (long)(OZ_S * OZ_ATILE / 2)), "r"(OZ_S * OZ_ATILE), "r"(fb)
+                        smem_u32(oz_smem + buf * STAGE)),
+                    "l"(a + (atile0 + st) * (long)(S * OZ_ATILE / 2)), "r"(S * OZ_ATILE), "r"(fb)
                     : "memory");
                 issued = st;
             }
-            for (int s2 = max(0, issued - OZ_NST + 1); s2 <= issued; ++s2)
-                if (!mbar_wait(smem_u32(&full_a[s2 % OZ_NST]), (uint32_t)((s2 / OZ_NST) & 1))) abort_s = 1;
+            for (int s2 = max(0, issued - NST + 1); s2 <= issued; ++s2)
+                if (!mbar_wait(smem_u32(&full_a[s2 % NST]), (uint32_t)((s2 / NST) & 1))) abort_s = 1;
         }
     } else if (warp == 1) {
-        if (lane == 0) {  // MMA issue: 28 digit-pair MMAs per stage into 7 group accumulators
+        if (lane == 0) {  // MMA issue: S (S + 1) / 2 digit-pair MMAs per stage into 4 accumulators
             int last = -1;
             for (int st = 0; st < nstage; ++st) {
-                const int buf = st % OZ_NST;
-                const uint32_t par = (uint32_t)((st / OZ_NST) & 1);
+                const int buf = st % NST;
+                const uint32_t par = (uint32_t)((st / NST) & 1);
                 if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) || abort_s) {
                     abort_s = 1;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t base = smem_u32(oz_smem + buf * OZ_STAGE);
+                const uint32_t base = smem_u32(oz_smem + buf * STAGE);
 #pragma unroll
-                for (int k = 0; k < OZ_S; ++k) {
+                for (int k = 0; k < S; ++k) {
+                    const int g = min(k, OZ_ACC - 1);
 #pragma unroll
                     for (int i = 0; i <= k; ++i) {
                         const uint64_t ad = make_desc(base + i * OZ_ATILE, 128, 256);
-                        const uint64_t bd = make_desc(base + OZ_S * OZ_ATILE + (k - i) * OZ_BTILE, 128, 256);
-                        mma_bf16(tmem_d + (uint32_t)(k * OZ_N), ad, bd, (st > 0 || i > 0) ? 1u : 0u);
+                        const uint64_t bd = make_desc(base + S * OZ_ATILE + (k - i) * OZ_BTILE, 128, 256);
+                        // the first MMA into each accumulator overwrites it
+                        const bool first = st == 0 && i == 0 && k <= OZ_ACC - 1;
+                        mma_bf16(tmem_d + (uint32_t)(g * OZ_N), ad, bd, idesc, first ? 0u : 1u);
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -1083,40 +1108,40 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                              : "memory");
             } else {
                 abort_s = 1;
-                if (last >= 0) mbar_wait(smem_u32(&empty_bar[last % OZ_NST]), (uint32_t)((last / OZ_NST) & 1));
+                if (last >= 0) mbar_wait(smem_u32(&empty_bar[last % NST]), (uint32_t)((last / NST) & 1));
             }
         }
-    } else {  // multipole digits: 64 rows x 7 digits x 2 pieces of 16 B per stage, 192 threads
+    } else {  // multipole digits: neff rows x S digits x 2 pieces of 16 B per stage, 192 threads
         const int tq = tid - 64;
         int issued = -1;
         for (int st = 0; st < nstage; ++st) {
-            const int buf = st % OZ_NST;
-            if (st >= OZ_NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / OZ_NST) - 1) & 1))) {
+            const int buf = st % NST;
+            if (st >= NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / NST) - 1) & 1))) {
                 abort_s = 1;
                 break;
             }
             if (abort_s) break;
-            unsigned char *base = oz_smem + buf * OZ_STAGE;
-            for (int i = tq; i < OZ_N * OZ_S * 2; i += OZ_BPROD) {
-                const int row = i / (OZ_S * 2), rem = i % (OZ_S * 2), d = rem >> 1, c = rem & 1;
-                const uint32_t dst = smem_u32(base + OZ_S * OZ_ATILE + d * OZ_BTILE + tile_off(row, c));
+            unsigned char *base = oz_smem + buf * STAGE;
+            for (int i = tq; i < neff * S * 2; i += OZ_BPROD) {
+                const int row = i / (S * 2), rem = i % (S * 2), d = rem >> 1, c = rem & 1;
+                const uint32_t dst = smem_u32(base + S * OZ_ATILE + d * OZ_BTILE + tile_off(row, c));
                 const int sn = src_s[row];
-                const uint16_t *g = sn >= 0 ? bdig + (((long)sn * nstage + st) * OZ_S + d) * OZ_KS + 8 * c : bdig;
+                const uint16_t *g = sn >= 0 ? bdig + (((long)sn * nstage + st) * S + d) * OZ_KS + 8 * c : bdig;
                 cp_async16(dst, g, sn >= 0 ? 16u : 0u);
             }
             asm volatile("cp.async.commit_group;");
             issued = st;
-            if (st >= OZ_LAG) {
-                asm volatile("cp.async.wait_group %0;" ::"n"(OZ_LAG) : "memory");
+            if (st >= LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - OZ_LAG) % OZ_NST]))
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - LAG) % NST]))
                              : "memory");
             }
         }
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (int s2 = max(0, issued - OZ_LAG + 1); s2 <= issued; ++s2)
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % OZ_NST])) : "memory");
+        for (int s2 = max(0, issued - LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % NST])) : "memory");
     }
     __syncthreads();
     bool ok = !abort_s;
@@ -1125,17 +1150,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (!ok && tid == 0) atomicExch(err, 1);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ok) {
-        // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [32 (w / 4), + 32)
+        // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [64 (w / 4), + 64) below neff
         const int lg = warp & 3, h = warp >> 2;
         const int row = t * OZ_M + 32 * lg + lane;
         const double srow = row < n4 ? sig[(long)op * mtiles * OZ_M + row] : 0.0;
 #pragma unroll 1
-        for (int c0 = 32 * h; c0 < 32 * h + 32; c0 += 16) {
-            long long acc[16];
+        for (int c0 = 64 * h; c0 < min(64 * h + 64, neff); c0 += 16) {
+            double acc[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) acc[q] = 0;
+            for (int q = 0; q < 16; ++q) acc[q] = 0.0;
+            // smallest group first, in FP64
 #pragma unroll 1
-            for (int k = 0; k < OZ_S; ++k) {
+            for (int g = OZ_ACC - 1; g >= 0; --g) {
                 uint32_t v[16];
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
@@ -1143,17 +1169,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
                       "=r"(v[15])
-                    : "r"(tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(k * OZ_N + c0)));
+                    : "r"(tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(g * OZ_N + c0)));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                const long long wgt = 1LL << (6 * (OZ_S - 1 - k));
 #pragma unroll
-                for (int q = 0; q < 16; ++q) acc[q] += (long long)__float2int_rn(__uint_as_float(v[q])) * wgt;
+                for (int q = 0; q < 16; ++q) acc[q] += (double)__uint_as_float(v[q]);
             }
             if (row < n4) {
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int tg = tgt_s[c0 + q];
-                    if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, (double)acc[q] * srow * tau_s[c0 + q]);
+                    if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, acc[q] * srow * tau_s[c0 + q]);
                 }
             }
         }
@@ -1309,7 +1334,8 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     IBIM_CHECK_LAUNCH();
 }
 
-// Digit tiles of the FP64 operators, or of the float-float ones when ff is given.
+// Digit tiles of the FP64 operators, or of the float-float ones when ff is given: 6 digits of 7
+// bits where K <= 800 (orders up to 5), else 7 of 6 bits.
 void m2l_oz_pack(Plan &P, const float2 *ff) {
     if (P.nops == 0) return;
     IBIM_REQUIRE(P.ops64.ptr || ff, "digit images need the FP64-class operators");
@@ -1317,10 +1343,11 @@ void m2l_oz_pack(Plan &P, const float2 *ff) {
     const int n4 = 4 * P.R;
     P.oz_kpad = (n4 + OZ_KS - 1) / OZ_KS * OZ_KS;
     P.oz_mtiles = (n4 + OZ_M - 1) / OZ_M;
-    const int nstage = P.oz_kpad / OZ_KS;
-    P.oz_a.alloc((size_t)P.nops * P.oz_mtiles * nstage * OZ_S * (OZ_ATILE / 2), s);
+    P.oz_s = P.oz_kpad <= OZ_K7 ? 6 : 7;
+    const int S = P.oz_s, nstage = P.oz_kpad / OZ_KS;
+    P.oz_a.alloc((size_t)P.nops * P.oz_mtiles * nstage * S * (OZ_ATILE / 2), s);
     P.oz_sig.alloc((size_t)P.nops * P.oz_mtiles * OZ_M, s);
-    P.oz_b.alloc((size_t)P.tree.nnodes * nstage * OZ_S * OZ_KS, s);
+    P.oz_b.alloc((size_t)P.tree.nnodes * nstage * S * OZ_KS, s);
     P.oz_tau.alloc((size_t)P.tree.nnodes, s);
     if (!P.tc_err.ptr) {
         P.tc_err.alloc(1, s);
@@ -1332,35 +1359,51 @@ void m2l_oz_pack(Plan &P, const float2 *ff) {
     const long pieces = rows * (P.oz_kpad / 8);
     const int gs = (int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms);
     const int gp = (int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms);
+    const int sc = 2 * (42 / S);  // 2^(-2D) folded into the row scale
     uint4 *a = reinterpret_cast<uint4 *>(P.oz_a.ptr);
-    if (ff) {
-        (count_launch(), k_scale_ops_oz<float2><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, ff, P.oz_sig.ptr, sexp.ptr));
-        (count_launch(), k_pack_ops_oz<float2><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff, sexp.ptr, a));
-    } else {
-        (count_launch(), k_scale_ops_oz<double><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, P.ops64.ptr, P.oz_sig.ptr,
+    if (ff)
+        (count_launch(), k_scale_ops_oz<float2><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, sc, ff, P.oz_sig.ptr,
                                                                    sexp.ptr));
-        (count_launch(), k_pack_ops_oz<double><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr,
-                                                                  sexp.ptr, a));
-    }
+    else
+        (count_launch(), k_scale_ops_oz<double><<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, sc, P.ops64.ptr,
+                                                                   P.oz_sig.ptr, sexp.ptr));
+    auto pack = [&](auto kf, auto kd) {
+        if (ff)
+            (count_launch(), kf<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff, sexp.ptr, a));
+        else
+            (count_launch(), kd<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, sexp.ptr, a));
+    };
+    if (S == 6)
+        pack(k_pack_ops_oz<6, float2>, k_pack_ops_oz<6, double>);
+    else
+        pack(k_pack_ops_oz<7, float2>, k_pack_ops_oz<7, double>);
     IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmemBytes));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<6>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<7>::SMEM));
 }
 
-// V-list M2L of the FP64 operator by exact digit products on the tensor cores; mult -> local.
+// V-list M2L of the FP64 operator by digit products on the tensor cores; mult -> local.
 void m2l_oz_run(Plan &P, const TargetSet &S) {
     if (S.nchunks_oz == 0) return;
     cudaStream_t s = P.ctx->stream;
-    const int n4 = 4 * P.R;
-    (count_launch(), k_split_mult_oz<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.oz_kpad, P.mult.ptr,
-                                                                        P.oz_b.ptr, P.oz_tau.ptr));
+    const int n4 = 4 * P.R, ns = P.oz_s;
+    const int gsplit = 4 * P.ctx->num_sms;
+    if (ns == 6)
+        (count_launch(), k_split_mult_oz<6><<<gsplit, 256, 0, s>>>(P.tree.nnodes, n4, P.oz_kpad, P.mult.ptr,
+                                                                   P.oz_b.ptr, P.oz_tau.ptr));
+    else
+        (count_launch(), k_split_mult_oz<7><<<gsplit, 256, 0, s>>>(P.tree.nnodes, n4, P.oz_kpad, P.mult.ptr,
+                                                                   P.oz_b.ptr, P.oz_tau.ptr));
     const dim3 grid(S.nchunks_oz, P.oz_mtiles);
     {
         const double nst = P.oz_kpad / OZ_KS;
         ProfScope ps_(PROF_M2L_VOZ, 2.0 * n4 * (double)n4 * S.nvpairs,
-                      2.0 * OZ_S * nst * OZ_KS * ((double)P.oz_mtiles * OZ_M * P.nops + (double)S.nvpairs));
-        (count_launch(), k_m2l_oz<<<grid, OZ_THREADS, kOzSmemBytes, s>>>(
-                             n4, P.oz_kpad, P.oz_mtiles, S.v_chunk_oz.ptr, S.v_src.ptr, S.v_tgt.ptr, P.oz_a.ptr,
-                             P.oz_sig.ptr, P.oz_b.ptr, P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr));
+                      2.0 * ns * nst * OZ_KS * ((double)P.oz_mtiles * OZ_M * P.nops + (double)S.nvpairs));
+        auto kern = ns == 6 ? k_m2l_oz<6> : k_m2l_oz<7>;
+        const int smem = ns == 6 ? OzShape<6>::SMEM : OzShape<7>::SMEM;
+        (count_launch(), kern<<<grid, OZ_THREADS, smem, s>>>(n4, P.oz_kpad, P.oz_mtiles, S.v_chunk_oz.ptr, S.v_src.ptr,
+                                                            S.v_tgt.ptr, P.oz_a.ptr, P.oz_sig.ptr, P.oz_b.ptr,
+                                                            P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }

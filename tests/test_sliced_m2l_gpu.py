@@ -1,9 +1,10 @@
 """The FP64 operator with its V-list M2L as exact BF16 digit products on the tensor cores
 (IBIM_PRECISION_FP64_TC, the mixed path's refinement residual) against the plain FP64 operator.
 
-Only the V-list M2L differs between the two; its digit truncation (7 digits of 6 bits under
-power-of-two row and column scales) leaves about 2^-40 of the row-scale x column-scale product per
-term, so the FMM outputs agree to ~1e-11 of their magnitude."""
+Only the V-list M2L differs between the two; its digit truncation (a 42-bit cut into 6 digits of
+7 bits, or 7 of 6 bits from order 6 up, under power-of-two row and column scales) leaves about
+2^-40 of the row-scale x column-scale product per term, so the FMM outputs agree to ~1e-11 of
+their magnitude.  Orders 3, 5 (6 digits) and 6 (7 digits) are covered."""
 
 import numpy as np
 import pytest
