@@ -779,8 +779,9 @@ __global__ void k_split_mult_h16(long nnodes, int n4, int kpad, const float *__r
 // Groups 0, 1 and 2 get one TMEM accumulator each and stay exact in the FP32 accumulation:
 // |G_k| <= 1.25 2^(2D) K < 2^24 (S = 6, D = 7: K <= 800; S = 7, D = 6: K <= 3200).  Groups
 // 3 .. S-1 share a fourth accumulator, rounded at 2^-24 of a value 2^(-3D) below group 0
-// (~2^-45 of s_r t_j per step of 16 K elements).  The epilogue adds the four in FP64 (exact),
-// applies s_r t_j 2^(-2D) and adds into the FP64 locals.  Digit pairs with i + l >= S are
+// (~2^-45 of s_r t_j per step of 16 K elements).  The epilogue combines the four in int64 fixed
+// point, assembles the double times s_r t_j 2^(-2D) from its bits (integer instructions: the
+// FP64 pipe is narrow) and adds it into the FP64 locals.  Digit pairs with i + l >= S are
 // dropped: the result differs from the FP64 product by about 2^-40 of s_r t_j per term (~1e-11
 // relative), far below the FP32 operator the refinement corrects.  S = 6 (7-bit digits, 21
 // digit MMAs a step) where K allows it (orders up to 5), else S = 7 (6-bit digits, 28 MMAs).
@@ -1003,6 +1004,51 @@ __global__ void k_split_mult_oz(long nnodes, int n4, int kpad, const double *__r
     }
 }
 
+// Exponent e of a positive power of two 2^e (normal range), from its bits.
+__device__ __forceinline__ int exp_of_pow2(double p) {
+    return (int)((__double_as_longlong(p) >> 52) & 0x7ff) - 1023;
+}
+
+// The double nearest T 2^e (ties to even) for an integer 0 < |T| < 2^63, assembled from T's bits
+// by integer instructions while the result is a normal number, else by an FP64 multiply.
+__device__ __forceinline__ double pow2_scaled_ll(long long T, const int e0) {
+    unsigned long long a = (unsigned long long)(T < 0 ? -T : T);
+    int e = e0;
+    int msb = 63 - __clzll((long long)a);
+    if (msb > 52) {  // round the low bits away
+        const int sh = msb - 52;
+        const unsigned long long rem = a & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+        a >>= sh;
+        if (rem > half || (rem == half && (a & 1ULL))) ++a;
+        e += sh;
+        if (a >> 53) {  // the rounding carried into bit 53: a = 2^53
+            a >>= 1;
+            ++e;
+        }
+        msb = 52;
+    }
+    const int E = msb + e + 1023;  // biased exponent of the result
+    if (E < 1 || E > 2046) return ldexp((double)T, e0);  // subnormal or overflowing result
+    const unsigned long long mant = ((a << (63 - msb)) & 0x7fffffffffffffffULL) >> 11;
+    const unsigned long long bits = ((unsigned long long)(T < 0) << 63) | ((unsigned long long)E << 52) | mant;
+    return __longlong_as_double((long long)bits);
+}
+
+// rint(x 2^s) of an FP32 value, |x 2^s| < 2^62, from its bits (ties away from zero; subnormal
+// x, below 2^-126, count as zero).
+__device__ __forceinline__ long long f32_fixed(float x, int s) {
+    const unsigned u = __float_as_uint(x);
+    const int E = (int)((u >> 23) & 0xff);
+    if (E == 0) return 0;
+    const long long m = (long long)((u & 0x7fffffu) | 0x800000u);  // x = m 2^(E - 150)
+    const int sh = E - 150 + s;
+    long long r;
+    if (sh >= 0) r = m << sh;
+    else if (sh < -25) r = 0;
+    else r = (m + (1LL << (-sh - 1))) >> -sh;
+    return (u >> 31) ? -r : r;
+}
+
 template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_m2l_oz(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
@@ -1014,7 +1060,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     __shared__ __align__(8) uint64_t full_a[NST], full_b[NST], empty_bar[NST], acc_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int src_s[OZ_N], tgt_s[OZ_N];
-    __shared__ double tau_s[OZ_N];
+    __shared__ int tau_e[OZ_N];
     __shared__ volatile int abort_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int op = chunks[3 * blockIdx.x], b = chunks[3 * blockIdx.x + 1], cnt = chunks[3 * blockIdx.x + 2];
@@ -1027,7 +1073,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int sn = tid < cnt ? vsrc[b + tid] : -1;
         src_s[tid] = sn;
         tgt_s[tid] = tid < cnt ? vtgt[b + tid] : -1;
-        tau_s[tid] = sn >= 0 ? tau[sn] : 0.0;
+        tau_e[tid] = sn >= 0 ? exp_of_pow2(tau[sn]) : 0;
     }
     if (tid == 0) {
         abort_s = 0;
@@ -1150,35 +1196,41 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (!ok && tid == 0) atomicExch(err, 1);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ok) {
-        // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [64 (w / 4), + 64) below neff
+        // warp w: TMEM lanes 32 (w % 4) .. + 31 = rows, pair columns [64 (w / 4), + 64) below neff.
+        // Integer epilogue (the FP64 pipe is narrow): T = (G_0 2^(2D) + G_1 2^D + G_2) 2^F +
+        // rint(M 2^(2D+F)) in int64 with F = 24 (|G_0 2^(2D)| < 2^38, so |T| < 2^62; M kept to
+        // 2^-(2D+24) of a group-0 unit, far below the cut's own error), then the double nearest
+        // T 2^(e_r + e_j - 4D - F) is assembled from T's bits; s_r = 2^e_r and t_j = 2^e_j.
+        constexpr int D = SH::D;
         const int lg = warp & 3, h = warp >> 2;
         const int row = t * OZ_M + 32 * lg + lane;
-        const double srow = row < n4 ? sig[(long)op * mtiles * OZ_M + row] : 0.0;
+        const int erow = row < n4 ? exp_of_pow2(sig[(long)op * mtiles * OZ_M + row]) + 2 * D : 0;
 #pragma unroll 1
         for (int c0 = 64 * h; c0 < min(64 * h + 64, neff); c0 += 16) {
-            double acc[16];
+            uint32_t v[OZ_ACC][16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) acc[q] = 0.0;
-            // smallest group first, in FP64
-#pragma unroll 1
-            for (int g = OZ_ACC - 1; g >= 0; --g) {
-                uint32_t v[16];
+            for (int g = 0; g < OZ_ACC; ++g)
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
                     "%13, %14, %15}, [%16];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
+                    : "=r"(v[g][0]), "=r"(v[g][1]), "=r"(v[g][2]), "=r"(v[g][3]), "=r"(v[g][4]), "=r"(v[g][5]),
+                      "=r"(v[g][6]), "=r"(v[g][7]), "=r"(v[g][8]), "=r"(v[g][9]), "=r"(v[g][10]), "=r"(v[g][11]),
+                      "=r"(v[g][12]), "=r"(v[g][13]), "=r"(v[g][14]), "=r"(v[g][15])
                     : "r"(tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(g * OZ_N + c0)));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int q = 0; q < 16; ++q) acc[q] += (double)__uint_as_float(v[q]);
-            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row < n4) {
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int tg = tgt_s[c0 + q];
-                    if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, acc[q] * srow * tau_s[c0 + q]);
+                    constexpr int F = 24;
+                    const long long g0 = __float2int_rn(__uint_as_float(v[0][q]));
+                    const long long g1 = __float2int_rn(__uint_as_float(v[1][q]) * (float)(1 << D));
+                    const long long g2 = __float2int_rn(__uint_as_float(v[2][q]) * (float)(1 << (2 * D)));
+                    const long long T = (((g0 << (2 * D)) + (g1 << D) + g2) << F) +
+                                        f32_fixed(__uint_as_float(v[3][q]), 2 * D + F);
+                    if (tg >= 0 && T != 0)
+                        atomicAdd(local + (long)tg * n4 + row,
+                                  pow2_scaled_ll(T, erow + tau_e[c0 + q] - 4 * D - F));
                 }
             }
         }
