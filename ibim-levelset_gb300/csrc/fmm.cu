@@ -25,6 +25,8 @@
 #include <map>
 #include <tuple>
 
+#include <omp.h>
+
 #include "fmm_common.cuh"
 
 namespace ibim {
@@ -590,7 +592,7 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
         poff[i + 1] = poff[i] + vcount[i] + (P.x_as_ops ? xcount[i] : 0);
     }
     const long npair = poff[nn];
-    std::vector<int> pkey(npair), psrc(npair), ptgt(npair);  // pkey: V dense index, or -1 - X slot
+    HostArr<int> pkey(npair), psrc(npair), ptgt(npair);  // pkey: V dense index, or -1 - X slot
     std::vector<std::array<int, 5>> xkey;
     std::vector<long> xslot_of_pair;
     std::vector<long> xoff(nn + 1, 0);
@@ -642,11 +644,12 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
                 }
         }
     }
+    trace_mark("lists: pairs generated");
     // operator ids: V keys in dense-index order, then X keys in sorted order
     {
         // which dense V keys occur: per-thread flags over pair ranges, OR-ed afterwards
         const size_t nd = opid.dense.size();
-        const int nthr = std::max(1, std::min(32, (int)(npair / 65536) + 1));
+        const int nthr = std::max(1, std::min({32, omp_get_max_threads(), (int)(npair / 65536) + 1}));
         std::vector<std::vector<char>> part(nthr, std::vector<char>(nd, 0));
 #pragma omp parallel for schedule(static) num_threads(nthr)
         for (int t = 0; t < nthr; ++t) {
@@ -664,25 +667,65 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             }
     }
     std::vector<int> xid(xkey.size());
-    if (!xkey.empty()) {
-        std::vector<std::array<int, 5>> u = xkey;
+    const long nx = (long)xkey.size();
+    // X keys as 64-bit codes in the same order (levels 5 bits each, offsets 18 bits each biased
+    // by 2^17) while every key fits, else the keys themselves: per-thread sorted unique keys,
+    // merged; operator ids in sorted key order
+    auto fits = [](const std::array<int, 5> &k) {
+        return k[0] < 32 && k[1] < 32 && std::abs(k[2]) < (1 << 17) && std::abs(k[3]) < (1 << 17) &&
+               std::abs(k[4]) < (1 << 17);
+    };
+    int all_fit = 1;
+#pragma omp parallel for schedule(static) reduction(min : all_fit)
+    for (long k = 0; k < nx; ++k) all_fit = std::min(all_fit, fits(xkey[k]) ? 1 : 0);
+    auto ids_by_sorted_keys = [&](auto key_of, auto make_op) {
+        using K = decltype(key_of(xkey[0]));
+        std::vector<K> xc(nx);
+        const int nthr = std::max(1, std::min({32, omp_get_max_threads(), (int)(nx / 4096) + 1}));
+        std::vector<std::vector<K>> part(nthr);
+#pragma omp parallel for schedule(static) num_threads(nthr)
+        for (int t = 0; t < nthr; ++t) {
+            const long k0 = nx * t / nthr, k1 = nx * (t + 1) / nthr;
+            for (long k = k0; k < k1; ++k) xc[k] = key_of(xkey[k]);
+            std::vector<K> &u = part[t];
+            u.assign(xc.begin() + k0, xc.begin() + k1);
+            std::sort(u.begin(), u.end());
+            u.erase(std::unique(u.begin(), u.end()), u.end());
+        }
+        std::vector<K> u;
+        for (auto &v : part) u.insert(u.end(), v.begin(), v.end());
         std::sort(u.begin(), u.end());
         u.erase(std::unique(u.begin(), u.end()), u.end());
         std::vector<int> uid(u.size());
-        for (size_t k = 0; k < u.size(); ++k) uid[k] = opid.get_x(u[k][0], u[k][1], u[k][2], u[k][3], u[k][4]);
+        for (size_t k = 0; k < u.size(); ++k) uid[k] = make_op(u[k]);
 #pragma omp parallel for schedule(static)
-        for (long k = 0; k < (long)xkey.size(); ++k)
-            xid[k] = uid[std::lower_bound(u.begin(), u.end(), xkey[k]) - u.begin()];
+        for (long k = 0; k < nx; ++k) xid[k] = uid[std::lower_bound(u.begin(), u.end(), xc[k]) - u.begin()];
+    };
+    if (nx > 0 && all_fit) {
+        const uint64_t b17 = 1u << 17, m18 = (1u << 18) - 1;
+        ids_by_sorted_keys(
+            [&](const std::array<int, 5> &k) {
+                return ((uint64_t)k[0] << 59) | ((uint64_t)k[1] << 54) | ((uint64_t)(k[2] + b17) << 36) |
+                       ((uint64_t)(k[3] + b17) << 18) | (uint64_t)(k[4] + b17);
+            },
+            [&](uint64_t c) {
+                return opid.get_x((int)(c >> 59), (int)((c >> 54) & 31), (int)((c >> 36) & m18) - (int)b17,
+                                  (int)((c >> 18) & m18) - (int)b17, (int)(c & m18) - (int)b17);
+            });
+    } else if (nx > 0) {
+        ids_by_sorted_keys([](const std::array<int, 5> &k) { return k; },
+                           [&](const std::array<int, 5> &k) { return opid.get_x(k[0], k[1], k[2], k[3], k[4]); });
     }
+    trace_mark("lists: operator ids");
     const int nop = (int)opid.keys.size() / 5;
-    std::vector<int> pop(npair);
+    HostArr<int> pop(npair);
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < npair; ++q) pop[q] = pkey[q] >= 0 ? opid.dense[pkey[q]] : xid[-1 - pkey[q]];
     // counting sort by operator; thread t owns pairs [t0, t1) and scatters them in order
     std::vector<long> opbeg(nop + 1, 0);
-    std::vector<int> gs(npair), gt(npair);
+    HostArr<int> gs(npair), gt(npair);
     {
-        const int nthr = std::max(1, std::min(64, (int)(npair / 65536) + 1));
+        const int nthr = std::max(1, std::min({64, omp_get_max_threads(), (int)(npair / 65536) + 1}));
         std::vector<std::vector<long>> hist(nthr, std::vector<long>(nop, 0));
 #pragma omp parallel for schedule(static) num_threads(nthr)
         for (int t = 0; t < nthr; ++t) {
@@ -725,8 +768,8 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
         cut(chunks_tc2, op, b, n, 2 * M2L_CHTC);
         cut(chunks_oz, op, b, n, M2L_CHOZ);
     }
-    std::vector<int> &vs = gs, &vt = gt;
-    S.nvpairs = (long)vs.size();
+    trace_mark("lists: pairs grouped");
+    S.nvpairs = npair;
     S.nchunks = (int)chunks.size() / 3;
     S.nchunks32 = (int)chunks32.size() / 3;
     up_int(S.v_chunk32, chunks32, s);
@@ -736,13 +779,15 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     up_int(S.v_chunk_tc2, chunks_tc2, s);
     S.nchunks_oz = (int)chunks_oz.size() / 3;
     up_int(S.v_chunk_oz, chunks_oz, s);
-    up_int(S.v_src, vs, s);
-    up_int(S.v_tgt, vt, s);
+    S.v_src.alloc(std::max<long>(1, npair), s);
+    S.v_src.upload(gs.data(), npair);
+    S.v_tgt.alloc(std::max<long>(1, npair), s);
+    S.v_tgt.upload(gt.data(), npair);
     up_int(S.v_chunk, chunks, s);
     S.nxpairs = (long)xs.size();
     up_int(S.x_src, xs, s);
     up_int(S.x_tgt, xt, s);
-    trace_mark("lists: V and X pairs by operator");
+    trace_mark("lists: chunks, uploads");
     // target leaves and the near-field pair count (U and W lists); the FP64 kernel's merged
     // source ranges are built on first use (near64_lists)
     std::vector<int> tl;

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -72,6 +73,19 @@ struct DevBuf {
     void download(T *h, size_t count) const {
         if (count) IBIM_CUDA(cudaMemcpyAsync(h, ptr, sizeof(T) * count, cudaMemcpyDeviceToHost, stream));
     }
+};
+
+// Host scratch array without value-initialisation, for large arrays that are written in full
+// (by several threads) before they are read: a std::vector's zero fill is one serial pass.
+template <class T> struct HostArr {
+    std::unique_ptr<T[]> p;
+    size_t n = 0;
+    explicit HostArr(size_t k = 0) : p(k ? new T[k] : nullptr), n(k) {}
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
+    T *data() { return p.get(); }
+    const T *data() const { return p.get(); }
+    size_t size() const { return n; }
 };
 
 // Kernel categories timed with CUDA events when profiling is enabled on a context.
@@ -169,6 +183,9 @@ struct TreeHost {
 };
 
 TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int maxpoint, int maxlevel);
+// Frees per-node lists with all threads (lists filled in parallel are slow to free from one).
+void release_lists(std::vector<std::vector<int>> &U, std::vector<std::vector<int>> &V,
+                   std::vector<std::vector<int>> &W, std::vector<std::vector<int>> &X);
 
 struct ChebTables;
 
@@ -288,7 +305,10 @@ struct Plan {
     DevBuf<double> oz_sig, oz_tau;
     double kp64[5] = {-1, -1, -1, -1, -1}, kp32[5] = {-1, -1, -1, -1, -1};  // kernel parameters of the cached operators
     bool ops64_ready = false, ops32_ready = false;
-    ~Plan() { for (auto *t : targets) delete t; }
+    ~Plan() {
+        for (auto *t : targets) delete t;
+        release_lists(tree.U, tree.V, tree.W, tree.X);
+    }
 };
 
 // FMM engine.  dens: 4 x ns (tree order), out: 4 x nt of target set `ts` (tree order).

@@ -15,8 +15,11 @@
 // vectors hold), so every node owns one contiguous range of the tree-ordered points.
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <unordered_map>
+
+#include <omp.h>
 
 #include "internal.cuh"
 
@@ -91,25 +94,56 @@ struct Builder {
         for (int i = 0; i < 8; ++i) split(first + i);
     }
 
-    // stable 8-way partition of a node's range by octant
+    // stable 8-way partition of a node's range by octant; ranges of 16k points and more (the
+    // top levels, built outside any parallel region) by all threads: per-thread octant counts
+    // over contiguous slices, then each thread scatters its slice in order
     void partition(const BNode &p, int first, std::vector<int> &perm, const double *pts, bool is_src) {
         const int b = is_src ? p.sb : p.tb, e = is_src ? p.se : p.te;
-        int cnt[8] = {0};
         auto oct = [&](int idx) {
             const double *x = pts + 3 * (long)idx;
             return 4 * (x[2] < p.c[2] ? 0 : 1) + 2 * (x[1] < p.c[1] ? 0 : 1) + (x[0] < p.c[0] ? 0 : 1);
         };
         tmp.resize(std::max<size_t>(tmp.size(), (size_t)(e - b)));
-        for (int i = b; i < e; ++i) cnt[oct(perm[i])]++;
-        int off[8], o = b;
-        for (int i = 0; i < 8; ++i) {
-            off[i] = o;
-            BNode &q = nodes[first + i];
-            if (is_src) { q.sb = o; q.se = o + cnt[i]; } else { q.tb = o; q.te = o + cnt[i]; }
-            o += cnt[i];
+        const int nthr = (e - b >= (1 << 14) && !omp_in_parallel()) ? std::min(64, omp_get_max_threads()) : 1;
+        std::vector<std::array<int, 8>> cnt(nthr);
+        std::vector<unsigned char> o8(nthr > 1 ? e - b : 0);
+        auto slice = [&](int t, int &s0, int &s1) {
+            s0 = b + (int)((long)(e - b) * t / nthr);
+            s1 = b + (int)((long)(e - b) * (t + 1) / nthr);
+        };
+#pragma omp parallel for schedule(static) num_threads(nthr) if (nthr > 1)
+        for (int t = 0; t < nthr; ++t) {
+            int s0, s1;
+            slice(t, s0, s1);
+            std::array<int, 8> c{};
+            for (int i = s0; i < s1; ++i) {
+                const int o = oct(perm[i]);
+                if (nthr > 1) o8[i - b] = (unsigned char)o;
+                c[o]++;
+            }
+            cnt[t] = c;
         }
-        for (int i = b; i < e; ++i) tmp[off[oct(perm[i])]++ - b] = perm[i];
-        std::copy(tmp.begin(), tmp.begin() + (e - b), perm.begin() + b);
+        // cnt[t][o] becomes thread t's first slot for octant o
+        int o = b;
+        for (int i = 0; i < 8; ++i) {
+            BNode &q = nodes[first + i];
+            const int start = o;
+            for (int t = 0; t < nthr; ++t) {
+                const int c = cnt[t][i];
+                cnt[t][i] = o;
+                o += c;
+            }
+            if (is_src) { q.sb = start; q.se = o; } else { q.tb = start; q.te = o; }
+        }
+#pragma omp parallel for schedule(static) num_threads(nthr) if (nthr > 1)
+        for (int t = 0; t < nthr; ++t) {
+            int s0, s1;
+            slice(t, s0, s1);
+            std::array<int, 8> &off = cnt[t];
+            for (int i = s0; i < s1; ++i) tmp[off[nthr > 1 ? o8[i - b] : oct(perm[i])]++ - b] = perm[i];
+        }
+#pragma omp parallel for schedule(static) if (nthr > 1)
+        for (int i = b; i < e; ++i) perm[i] = tmp[i - b];
     }
 };
 
@@ -152,12 +186,20 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     B.maxlevel = maxlevel;
     // getCenterRadius (bbfmm.cpp:43-65)
     double mx[3], mn[3];
-    for (int a = 0; a < 3; ++a) mx[a] = mn[a] = src[a];
-    for (long i = 0; i < ns; ++i)
-        for (int a = 0; a < 3; ++a) {
-            mx[a] = std::max(mx[a], src[3 * i + a]);
-            mn[a] = std::min(mn[a], src[3 * i + a]);
+    {
+        double x0 = src[0], x1 = src[0], y0 = src[1], y1 = src[1], z0 = src[2], z1 = src[2];
+#pragma omp parallel for schedule(static) reduction(min : x0, y0, z0) reduction(max : x1, y1, z1) if (ns >= (1 << 16))
+        for (long i = 0; i < ns; ++i) {
+            x0 = std::min(x0, src[3 * i]);
+            x1 = std::max(x1, src[3 * i]);
+            y0 = std::min(y0, src[3 * i + 1]);
+            y1 = std::max(y1, src[3 * i + 1]);
+            z0 = std::min(z0, src[3 * i + 2]);
+            z1 = std::max(z1, src[3 * i + 2]);
         }
+        mn[0] = x0, mn[1] = y0, mn[2] = z0;
+        mx[0] = x1, mx[1] = y1, mx[2] = z1;
+    }
     BNode root;
     root.level = 0;
     root.parent = -1;
@@ -385,7 +427,21 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     for (int l = 0; l < T.nlevels; ++l) T.level_begin[l + 1] += T.level_begin[l];
     T.tgt_perm = B.same ? sp : std::move(tp);
     T.src_perm = std::move(sp);
+    // the working lists were filled by many threads: freeing them from one costs milliseconds
+    release_lists(U, V, W, X);
     return T;
+}
+
+void release_lists(std::vector<std::vector<int>> &U, std::vector<std::vector<int>> &V,
+                   std::vector<std::vector<int>> &W, std::vector<std::vector<int>> &X) {
+    const long n = (long)std::max(std::max(U.size(), V.size()), std::max(W.size(), X.size()));
+#pragma omp parallel for schedule(static) if (n >= 4096)
+    for (long i = 0; i < n; ++i) {
+        if (i < (long)U.size()) std::vector<int>().swap(U[i]);
+        if (i < (long)V.size()) std::vector<int>().swap(V[i]);
+        if (i < (long)W.size()) std::vector<int>().swap(W[i]);
+        if (i < (long)X.size()) std::vector<int>().swap(X[i]);
+    }
 }
 
 }  // namespace ibim

@@ -58,6 +58,27 @@ def test_host_tree_matches_reference(golden, case):
             assert np.array_equal(np.sort(G[f"tree_{c}_idx"][p[i]:p[i + 1]]), nd[c]), (i, c)
 
 
+@pytest.mark.parametrize("n,maxpoint", [(300_000, 80), (70_000, 40)])
+def test_host_tree_large_matches_oracle(n, maxpoint):
+    """Point sets large enough that the top levels are partitioned by all threads (ranges of 16k
+    points and more) give the oracle's tree and lists (the restated bbfmm::tree::populate)."""
+    import oracle as O
+
+    rng = np.random.default_rng(n)
+    v = rng.normal(size=(n, 3))
+    pts = 20.0 * v / np.linalg.norm(v, axis=1, keepdims=True) + rng.normal(scale=0.7, size=(n, 3))
+    pts[: n // 10] *= 0.4  # a denser inner shell: uneven octants
+    nodes = ibim.tree_lists_host(pts, maxpoint, 10)
+    T = O.Tree(pts, pts, maxpoint, 10)
+    assert len(nodes) == T.nnodes
+    for i, nd in enumerate(nodes):
+        ints, _ = T.node(i)
+        assert [nd["level"], nd["parent"], nd["leaf"], nd["empty"], nd["nsrc"]] == [int(x) for x in ints[:5]], i
+        L = T.lists(i)
+        for w, c in enumerate("UVWX"):
+            assert np.array_equal(L[w], nd[c]), (i, c)
+
+
 def test_tree_rejects_bad_arguments():
     with pytest.raises(ibim.IbimError) as e:
         ibim.tree_lists_host(np.zeros((4, 3)), 0)
