@@ -28,11 +28,14 @@ struct ChebTables32 {
 struct KParams32 {
     float kappa, eps, ieps, vr2, k2in, q4pi, k3f;
     float k2in_q, k3q;  // k2in / q4pi and k3f / q4pi: the near field's densities carry the 1 / (4 pi)
+    float kappa_l2;     // -kappa log2(e): e^(-kappa r) = 2^(kappa_l2 r)
 };
 
 static KParams32 to32(const KParams &k) {
-    return KParams32{(float)k.kappa, (float)k.eps, (float)k.ieps, (float)(k.vr * k.vr), (float)k.k2in,
-                     (float)k.q4pi, (float)k.k3f, (float)(k.k2in / k.q4pi), (float)(k.k3f / k.q4pi)};
+    return KParams32{(float)k.kappa,        (float)k.eps,  (float)k.ieps,
+                     (float)(k.vr * k.vr),  (float)k.k2in, (float)k.q4pi,
+                     (float)k.k3f,          (float)(k.k2in / k.q4pi), (float)(k.k3f / k.q4pi),
+                     (float)(-k.kappa * 1.4426950408889634)};
 }
 
 namespace {
@@ -424,6 +427,20 @@ __global__ void __launch_bounds__(128) k_m2l_x32(const ChebTables32 *__restrict_
     }
 }
 
+// Hardware approximations with subnormal inputs and results flushed to zero (PTX rsqrt.approx.ftz,
+// ex2.approx.ftz): one instruction each, where the non-flushing forms also handle subnormals.
+// The near field's distances and exponentials never come near the subnormal range.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float exp2_ftz(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Near field + L2P in FP32 for one target leaf per block: source leaves staged in shared memory
 // in the target leaf's frame (two 16-byte loads per source record); per-tile partial sums are
 // added with Kahan compensation.
@@ -509,8 +526,8 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                             a0 = fmaf(-kp.k2in_q, P1.z, a0);
                             continue;
                         }
-                        const float ir = rsqrtf(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
-                        const float t = kp.kappa * r, e = __expf(-t), et1 = fmaf(e, t, e);
+                        const float ir = rsqrt_ftz(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
+                        const float t = kp.kappa * r, e = exp2_ftz(kp.kappa_l2 * r), et1 = fmaf(e, t, e);
                         const float h3 = ir3 * kp.k3q;
                         const float c1 = fmaf(kp.eps, et1, -1.f) * ir3;
                         const float c4 = fmaf(-kp.ieps, et1, 1.f) * ir3;
