@@ -57,7 +57,8 @@ extern "C" {
 #define IBIM_PRECISION_FP64 0  /* reference-exact FP64 path */
 #define IBIM_PRECISION_MIXED 1 /* FP32-class far/near field inside FP64-class iterative refinement */
 /* FP64 operator whose V-list M2L runs on the tensor cores as exact products of BF16 integer
- * digits (Ozaki scheme, 7 digits of 6 bits under power-of-two row/column scales; ~1e-11 of the
+ * digits (Ozaki scheme, a 42-bit cut into 6 digits of 7 bits, or 7 of 6 bits from order 6 up,
+ * under power-of-two row/column scales; ~1e-11 of the
  * FP64 product): the operator of the mixed path's refinement residual.  Accepted by
  * ibim_fmm_plan (hence ibim_fmm_apply / ibim_bie_matvec), ibim_gmres_solve, and as a whole-solve
  * mode (ibim_config.precision: FP64 level set, plain FP64 GMRES on this operator). */
