@@ -336,6 +336,274 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC_RT * N));
 }
 
+// Persistent form of the scaled FP16 contraction: one CTA per SM walks work units u = blockIdx.x,
+// blockIdx.x + gridDim.x, ... (unit = chunk u / 2 against row tiles 2 (u % 2), + 1), so the
+// copies and gathers of the next unit stream while the current one's MMAs run, and its
+// accumulators (two slots of 2 x N TMEM columns) drain while the next unit's MMAs fill the other
+// slot.  Roles: warp 0 (one thread) bulk-copies the operator tiles, warp 1 (one thread) issues
+// the MMAs, the next TCP_BPROD / 32 warps gather the multipole rows, the last four drain the
+// accumulators (warp w reads TMEM lanes 32 (w % 4) .. + 31).  The stage ring (NST buffers of 2 row tiles) runs across
+// unit boundaries; every wait is bounded and an expired wait aborts the CTA through a shared
+// flag and the error word, after the copies and MMAs already issued have completed.
+constexpr int TCP_BPROD = 256, TCP_EPI = 128, TCP_THREADS = 64 + TCP_BPROD + TCP_EPI, TCP_RT = 2;
+constexpr int TCP_EPI_WARP0 = (64 + TCP_BPROD) / 32;  // first epilogue warp
+constexpr int TCP_STAGE = 2 * TCP_RT * TC_TILE_BYTES + 2 * 128 * TC_KS * 4;  // 24 KB
+constexpr int TCP_NST = 8, TCP_LAG = 4;
+constexpr int TCP_SMEM = TCP_NST * TCP_STAGE;                               // 192 KB
+
+__global__ void __launch_bounds__(TCP_THREADS, 1)
+    k_m2l_tc_persist(int n4, int kpad, int mtiles, int nunits, const int *__restrict__ chunks,
+                     const int *__restrict__ vsrc, const int *__restrict__ vtgt, const void *__restrict__ a_hi_,
+                     const void *__restrict__ a_lo_, const void *__restrict__ b_hi_, const void *__restrict__ b_lo_,
+                     const float *__restrict__ rscale, const float *__restrict__ cscale, float *local, int *err) {
+    constexpr int N = 128, KS = TC_KS16, ES = 2, BT = N * TC_KS * 4;
+    const char *a_hi = static_cast<const char *>(a_hi_), *a_lo = static_cast<const char *>(a_lo_);
+    const char *b_hi = static_cast<const char *>(b_hi_), *b_lo = static_cast<const char *>(b_lo_);
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full_a[TCP_NST], full_b[TCP_NST], empty_bar[TCP_NST];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int abort_s;
+    __shared__ int tgt_e[2][128];    // per accumulator slot: target node of each pair column
+    __shared__ float csc_e[2][128];  // and the column scale of its source
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nstage = kpad / KS;
+    const int npair = (mtiles + TCP_RT - 1) / TCP_RT;  // row-tile pairs per chunk
+    // units of this CTA: u = blockIdx.x + i gridDim.x, i < nmine
+    const int nmine = blockIdx.x < nunits ? (nunits - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        abort_s = 0;
+        for (int i = 0; i < TCP_NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(TCP_BPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
+        }
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[i])), "r"(TCP_EPI / 32));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem_d = tmem_base;
+    auto unit_of = [&](int i, int &op, int &b, int &cnt, int &tile0, int &rt) {
+        const int u = blockIdx.x + i * gridDim.x, c = u / npair;
+        op = chunks[3 * c];
+        b = chunks[3 * c + 1];
+        cnt = chunks[3 * c + 2];
+        tile0 = (u % npair) * TCP_RT;
+        rt = min(TCP_RT, mtiles - tile0);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {  // operator tiles: bulk copies, stage g = i nstage + st
+            long issued = -1;
+            for (int i = 0; i < nmine && !abort_s; ++i) {
+                int op, b, cnt, tile0, rt;
+                unit_of(i, op, b, cnt, tile0, rt);
+                const long atile0 = ((long)op * mtiles + tile0) * nstage;
+                for (int st = 0; st < nstage; ++st) {
+                    const long g = (long)i * nstage + st;
+                    const int buf = (int)(g % TCP_NST);
+                    if (g >= TCP_NST &&
+                        !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((g / TCP_NST) - 1) & 1))) {
+                        abort_s = 1;
+                        break;
+                    }
+                    if (abort_s) break;
+                    unsigned char *base = tc_smem + buf * TCP_STAGE;
+                    const uint32_t fb = smem_u32(&full_a[buf]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb),
+                                 "r"(2 * rt * TC_TILE_BYTES)
+                                 : "memory");
+                    for (int t = 0; t < rt; ++t) {
+                        const long ga = (atile0 + (long)t * nstage + st) * TC_TILE_BYTES;
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+                            "[%3];" ::"r"(smem_u32(base + t * TC_TILE_BYTES)),
+                            "l"(a_hi + ga), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+                            "[%3];" ::"r"(smem_u32(base + (TCP_RT + t) * TC_TILE_BYTES)),
+                            "l"(a_lo + ga), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                    }
+                    issued = g;
+                }
+            }
+            // every issued copy lands before the CTA may exit
+            for (long g2 = issued - TCP_NST + 1 < 0 ? 0 : issued - TCP_NST + 1; g2 <= issued; ++g2)
+                if (!mbar_wait(smem_u32(&full_a[g2 % TCP_NST]), (uint32_t)((g2 / TCP_NST) & 1))) abort_s = 1;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issue
+            long last = -1;
+            for (int i = 0; i < nmine && !abort_s; ++i) {
+                int op, b, cnt, tile0, rt;
+                unit_of(i, op, b, cnt, tile0, rt);
+                const int neff = max(16, (cnt + 15) & ~15);
+                constexpr uint32_t NMASK = 0x3Fu << 17;
+                const uint32_t idesc = (TcShape<128>::IDESC16 & ~NMASK) | ((uint32_t)(neff >> 3) << 17);
+                const int slot = i & 1;
+                // the epilogue has drained this slot's previous unit (i - 2)
+                if (i >= 2 && !mbar_wait(smem_u32(&acc_empty[slot]), (uint32_t)(((i >> 1) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                bool ok = true;
+                for (int st = 0; st < nstage; ++st) {
+                    const long g = (long)i * nstage + st;
+                    const int buf = (int)(g % TCP_NST);
+                    const uint32_t par = (uint32_t)((g / TCP_NST) & 1);
+                    if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) ||
+                        abort_s) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t base = smem_u32(tc_smem + buf * TCP_STAGE);
+                    const uint64_t bh = make_desc(base + (2 * TCP_RT) * TC_TILE_BYTES, 128, 256);
+                    const uint64_t bl = make_desc(base + (2 * TCP_RT) * TC_TILE_BYTES + BT, 128, 256);
+                    for (int t = 0; t < rt; ++t) {
+                        const uint64_t ah = make_desc(base + t * TC_TILE_BYTES, 128, 256);
+                        const uint64_t al = make_desc(base + (TCP_RT + t) * TC_TILE_BYTES, 128, 256);
+                        const uint32_t d = tmem_d + (uint32_t)(slot * TCP_RT * N + t * N);
+                        mma_f16(d, ah, bh, idesc, st > 0 ? 1u : 0u);
+                        mma_f16(d, ah, bl, idesc, 1u);
+                        mma_f16(d, al, bh, idesc, 1u);
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(&empty_bar[buf]))
+                                 : "memory");
+                    last = g;
+                }
+                if (!ok) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&acc_full[slot]))
+                             : "memory");
+            }
+            // every MMA issued completes before TMEM is released (also after an abort)
+            if (last >= 0 && !mbar_wait(smem_u32(&empty_bar[last % TCP_NST]), (uint32_t)((last / TCP_NST) & 1)))
+                abort_s = 1;
+        }
+    } else if (warp < TCP_EPI_WARP0) {  // multipole rows: cp.async by TCP_BPROD threads
+        const int t = tid - 64;
+        long issued = -1;
+        for (int i = 0; i < nmine && !abort_s; ++i) {
+            int op, b, cnt, tile0, rt;
+            unit_of(i, op, b, cnt, tile0, rt);
+            const int neff = max(16, (cnt + 15) & ~15);
+            // this thread's pieces of a stage (2 tiles x neff rows x 2 halves of 16 B), fixed per unit
+            constexpr int MAXP = (4 * 128 + TCP_BPROD - 1) / TCP_BPROD;
+            const char *srcp[MAXP];
+            uint32_t dsto[MAXP];
+            int np = 0;
+            for (int q = t; q < 4 * neff && np < MAXP; q += TCP_BPROD, ++np) {
+                const int tile = q / (2 * neff), row = (q >> 1) % neff, c = q & 1;
+                dsto[np] = (uint32_t)(2 * TCP_RT * TC_TILE_BYTES + tile * BT) + tile_off(row, c);
+                const int sn = row < cnt ? vsrc[b + row] : -1;
+                const char *B = tile == 0 ? b_hi : b_lo;
+                srcp[np] = sn >= 0 ? B + (long)sn * kpad * ES + 16 * c : nullptr;
+            }
+            for (int st = 0; st < nstage; ++st) {
+                const long g = (long)i * nstage + st;
+                const int buf = (int)(g % TCP_NST);
+                if (g >= TCP_NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((g / TCP_NST) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                if (abort_s) break;
+                const uint32_t base = smem_u32(tc_smem + buf * TCP_STAGE);
+                for (int j = 0; j < np; ++j)
+                    cp_async16(base + dsto[j], srcp[j] ? (const void *)(srcp[j] + (long)st * KS * ES) : (const void *)b_hi,
+                               srcp[j] ? 16u : 0u);
+                asm volatile("cp.async.commit_group;");
+                issued = g;
+                if (g >= TCP_LAG) {
+                    asm volatile("cp.async.wait_group %0;" ::"n"(TCP_LAG) : "memory");
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                     smem_u32(&full_b[(g - TCP_LAG) % TCP_NST]))
+                                 : "memory");
+                }
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (long g2 = issued - TCP_LAG + 1 < 0 ? 0 : issued - TCP_LAG + 1; g2 <= issued; ++g2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[g2 % TCP_NST])) : "memory");
+    } else {  // epilogue: the last four warps, TMEM lanes 32 (warp % 4) .. + 31
+        // decisions stay warp-uniform (tcgen05.ld is a warp-collective instruction), and every
+        // epilogue warp passes the same number of named barriers: after an abort the remaining
+        // units are skipped, not left
+        const int lg = warp & 3;
+        for (int i = 0; i < nmine; ++i) {
+            int op, b, cnt, tile0, rt;
+            unit_of(i, op, b, cnt, tile0, rt);
+            const int neff = max(16, (cnt + 15) & ~15);
+            const int slot = i & 1;
+            {  // this unit's column table, then a barrier among the four epilogue warps (id 1)
+                const int e = tid - 32 * TCP_EPI_WARP0;
+                tgt_e[slot][e] = e < cnt ? __ldg(vtgt + b + e) : -1;
+                csc_e[slot][e] = e < cnt ? __ldg(cscale + __ldg(vsrc + b + e)) : 0.f;
+                asm volatile("bar.sync 1, %0;" ::"n"(TCP_EPI) : "memory");
+            }
+            bool go = __shfl_sync(0xffffffffu, (int)abort_s, 0) == 0;
+            if (go) go = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_full[slot]), (uint32_t)((i >> 1) & 1)));
+            if (!go) {
+                abort_s = 1;
+                continue;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int tt = 0; tt < rt; ++tt) {
+                const int row = (tile0 + tt) * TC_M + 32 * lg + lane;
+                const float rs = rscale[(long)op * mtiles * TC_M + row];  // row < mtiles * 128
+                const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(slot * TCP_RT * N + tt * N);
+#pragma unroll 1
+                for (int c0 = 0; c0 < neff; c0 += 16) {
+                    uint32_t v[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr + (uint32_t)c0));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (row < n4) {
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            const int tg = tgt_e[slot][c0 + q];
+                            if (tg >= 0)
+                                atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]) * rs * csc_e[slot][c0 + q]);
+                        }
+                    }
+                }
+            }
+            // this slot may be overwritten once every epilogue warp has read it
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[slot])) : "memory");
+        }
+    }
+    __syncthreads();
+    if (abort_s && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(512));
+}
+
 // ---------------------------------------------------------------------------------------------
 // CTA-pair form (tcgen05 cta_group::2).  A cluster of two CTAs on two SMs takes one chunk of up to
 // 256 pairs of an operator against four operator row tiles.  Each MMA is M = 256 (128 operator
@@ -1274,16 +1542,19 @@ static bool tc_fp16() {
 
 bool m2l_tc_fp16_form() { return tc_fp16(); }
 
-// Two CTAs per SM of two row tiles each (default) or one CTA of four (IBIM_TC_RT=4): with two,
-// one CTA's prologue and epilogue overlap the other's MMAs, at twice the multipole gathers
-// (2,000-atom protein: 2.32 against 2.50 ms a launch).
-static bool tc_two_per_sm() {
-    static const bool on = [] {
+// Launch form of the contraction: two CTAs of two row tiles per SM (default: one CTA's prologue
+// and epilogue overlap the other's MMAs; 2.32 ms a launch on the 2,000-atom protein),
+// IBIM_TC_RT=4 (one CTA of four row tiles per SM; 2.50 ms) or, FP16 form only, IBIM_TC_RT=P
+// (persistent: one CTA per SM walking units of two row tiles with double-buffered accumulators;
+// 2.94 ms).
+static int tc_launch_form() {
+    static const int f = [] {
         const char *v = std::getenv("IBIM_TC_RT");
-        return !(v && v[0] == '4');
+        return v && v[0] == '4' ? 4 : (v && v[0] == 'P' ? 0 : 2);
     }();
-    return on;
+    return f;
 }
+static bool tc_two_per_sm() { return tc_launch_form() != 4; }
 
 void m2l_tc_pack(Plan &P, const float2 *ff) {
     P.tc_h16 = tc_fp16();
@@ -1335,6 +1606,7 @@ void m2l_tc_pack(Plan &P, const float2 *ff) {
                                    TcShape<M2L_CHTC>::SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TcShape<M2L_CHTC, 2, 2>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TCP_SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TcShape<M2L_CHTC, 2, 2>::SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
@@ -1364,6 +1636,17 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
                              n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        IBIM_CHECK_LAUNCH();
+        return;
+    }
+    if (P.tc_h16 && tc_launch_form() == 0) {
+        static_assert(N == 128, "persistent form: 128-pair chunks");
+        const int nunits = S.nchunks_tc * ((mt + TCP_RT - 1) / TCP_RT);
+        const int grid = std::min(nunits, P.ctx->num_sms);
+        (count_launch(), k_m2l_tc_persist<<<grid, TCP_THREADS, TCP_SMEM, s>>>(
+                             n4, P.tc_kpad, mt, nunits, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
+                             P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr,
+                             P.tc_err.ptr));
         IBIM_CHECK_LAUNCH();
         return;
     }

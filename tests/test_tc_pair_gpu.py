@@ -68,15 +68,18 @@ def test_pair_kernel_matches_one_cta_kernel(ctx, golden, case, order, tmp_path):
         assert np.abs(fp16[o] - tf32[o]).max() / np.abs(tf32[o]).max() < 4e-6, (o, case)
 
 
-@pytest.mark.parametrize("case,order", [("cavity", None), ("p1hje", None), ("synth30", 6)])
-@pytest.mark.parametrize("fp16", ["1", "0"])
-def test_two_ctas_per_sm_match_one(ctx, golden, case, order, fp16, tmp_path):
-    """Two CTAs of two row tiles per SM (the default) issue the same MMAs per row tile in the same
-    K order as one CTA of four (IBIM_TC_RT=4); only the order of the atomic adds into the locals
-    differs."""
+@pytest.mark.parametrize("case,order", [("cavity", None), ("p1hje", None), ("synth30", 6), ("synth30", 3)])
+@pytest.mark.parametrize("fp16,form", [("1", None), ("1", "P"), ("0", None)])
+def test_launch_forms_match_one_cta_of_four(ctx, golden, case, order, fp16, form, tmp_path):
+    """Two CTAs of two row tiles per SM (the default, IBIM_TC_RT unset) and the persistent form
+    (IBIM_TC_RT=P, FP16) issue the same MMAs per row tile in the same K order as one CTA of four
+    (IBIM_TC_RT=4); only the order of the atomic adds into the locals differs."""
     G = golden(case)
     p = order or G["params"]["np"]
-    two = run_child(tmp_path, case, p, {"IBIM_TC_FP16": fp16}, "two")
+    env = {"IBIM_TC_FP16": fp16}
+    if form is not None:
+        env["IBIM_TC_RT"] = form
+    got = run_child(tmp_path, case, p, env, "form")
     one = run_child(tmp_path, case, p, {"IBIM_TC_RT": "4", "IBIM_TC_FP16": fp16}, "one")
     for o in range(4):
-        assert np.abs(two[o] - one[o]).max() / np.abs(one[o]).max() < 1e-6, (o, case)
+        assert np.abs(got[o] - one[o]).max() / np.abs(one[o]).max() < 1e-6, (o, case)
