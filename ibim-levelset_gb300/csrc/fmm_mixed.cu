@@ -29,13 +29,16 @@ struct KParams32 {
     float kappa, eps, ieps, vr2, k2in, q4pi, k3f;
     float k2in_q, k3q;  // k2in / q4pi and k3f / q4pi: the near field's densities carry the 1 / (4 pi)
     float kappa_l2;     // -kappa log2(e): e^(-kappa r) = 2^(kappa_l2 r)
+    float vr2_band;     // |d2 - vr2| below this: the cutoff is decided in FP64
+    double vr2_64;      // the FP64 kernels' (tau h)^2
 };
 
 static KParams32 to32(const KParams &k) {
     return KParams32{(float)k.kappa,        (float)k.eps,  (float)k.ieps,
                      (float)(k.vr * k.vr),  (float)k.k2in, (float)k.q4pi,
                      (float)k.k3f,          (float)(k.k2in / k.q4pi), (float)(k.k3f / k.q4pi),
-                     (float)(-k.kappa * 1.4426950408889634)};
+                     (float)(-k.kappa * 1.4426950408889634),
+                     (float)(1e-4 * k.vr2), k.vr2};
 }
 
 namespace {
@@ -453,9 +456,13 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                                                  const float *__restrict__ tx, const float *__restrict__ ty,
                                                  const float *__restrict__ tz, long nt,
                                                  const float *__restrict__ local, double *out, int l2p_mask,
-                                                 int nseg, int *next) {
+                                                 int nseg, int *next, const double *__restrict__ sx64,
+                                                 const double *__restrict__ sy64, const double *__restrict__ sz64,
+                                                 const double *__restrict__ tx64, const double *__restrict__ ty64,
+                                                 const double *__restrict__ tz64) {
     __shared__ ChebTables32 T;
-    __shared__ float4 S4[TILE32][2];  // {x, y, z, q m_x}, {q m_y, q m_z, q psi, 0} in the target leaf's frame
+    // {x, y, z, q m_x}, {q m_y, q m_z, q psi, source index} in the target leaf's frame
+    __shared__ float4 S4[TILE32][2];
     __shared__ float red[NT32][4];
     __shared__ int cur;
     load_tables(T, tab);
@@ -484,6 +491,7 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
             const bool active = ph < nph;
             float X = 0.f, Y = 0.f, Z = 0.f;
             if (active) { X = tx[t0 + my_t]; Y = ty[t0 + my_t]; Z = tz[t0 + my_t]; }
+            const long tg64 = active ? t0 + my_t : t0;  // the target's FP64 coordinates, for the cutoff
             float sum[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
             // fill tiles across consecutive source leaves
             int rr = r0, pos = r1 > r0 ? nrange[2 * r0] : 0;
@@ -500,7 +508,7 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                         const int si = lpos + q;
                         const float4 A = __ldg(src8 + 2 * si), B = __ldg(src8 + 2 * si + 1);
                         S4[filled + q][0] = make_float4(A.x + ox, A.y + oy, A.z + oz, A.w);
-                        S4[filled + q][1] = B;
+                        S4[filled + q][1] = make_float4(B.x, B.y, B.z, __int_as_float(si));
                     }
                     filled += take;
                     lpos += take;
@@ -522,7 +530,16 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                         // the cutoff test is a discontinuity: d2 in the FP64 kernel's evaluation order
                         // (near_pair64), so points at exactly tau h decide alike in both precisions
                         const float d2 = dx * dx + dy * dy + dz * dz;
-                        if (d2 < kp.vr2) {
+                        bool inside = d2 < kp.vr2;
+                        if (fabsf(d2 - kp.vr2) < kp.vr2_band) {
+                            // within FP32 rounding of the cutoff: decide on the FP64 coordinates, as
+                            // the FP64 and float-float kernels do (rare)
+                            const int sj = __float_as_int(P1.w);
+                            const double ex = sx64[sj] - tx64[tg64], ey = sy64[sj] - ty64[tg64],
+                                         ez = sz64[sj] - tz64[tg64];
+                            inside = ex * ex + ey * ey + ez * ez < kp.vr2_64;
+                        }
+                        if (inside) {
                             a0 = fmaf(-kp.k2in_q, P1.z, a0);
                             continue;
                         }
@@ -883,6 +900,9 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     const float *tx = S.self ? P.sxf.ptr : S.txf.ptr;
     const float *ty = S.self ? P.syf.ptr : S.tyf.ptr;
     const float *tz = S.self ? P.szf.ptr : S.tzf.ptr;
+    const double *tx64 = S.self ? P.sx.ptr : S.tx.ptr;
+    const double *ty64 = S.self ? P.sy.ptr : S.ty.ptr;
+    const double *tz64 = S.self ? P.sz.ptr : S.tz.ptr;
     // near field (U and W lists): needs only the packed sources.  With the overlap on it starts on
     // the auxiliary stream at full occupancy, CTAs taking work segments from a counter, and fills
     // the SMs the latency-bound far-field launches (P2M, M2M levels) leave idle; the L2P follows
@@ -893,7 +913,8 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
         (count_launch(), k_near32<<<grid, NT32, 0, st>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr),
                                                       S.near32_range.ptr, S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr,
                                                       P.nrad32.ptr, P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out,
-                                                      l2p_mask, S.nnear32_seg, next));
+                                                      l2p_mask, S.nnear32_seg, next, P.sx.ptr, P.sy.ptr, P.sz.ptr,
+                                                      tx64, ty64, tz64));
     };
     const bool overlap = near_overlap() && S.ntleaves > 0;
     static const int occ = [] {

@@ -79,7 +79,9 @@ __global__ void k_encode(T *g, long n, int dir) {
 
 // levelset::expand: g = max(g, (R_a + probe) - |x - c_a|) over the cube of +-r cells around
 // each atom, r = (int)((R_a + probe)/dx) + band.  blockIdx.y = atom.  Cells outside the grid
-// are skipped (the reference's Grid::set does not clamp).
+// are skipped (the reference's Grid::set does not clamp).  The FP64 grid evaluates the distance
+// as written, in FP64; the FP32 grid in FP32 from the atom's sub-cell offset (computed in FP64)
+// plus whole cells, since FP64 square roots on GB300's narrow FP64 pipe dominated the kernel.
 template <class T>
 __global__ void k_expand(typename OrdT<T>::type *g, Dims d, double sx, double sy, double sz, double dx,
                          const double *__restrict__ centers, const double *__restrict__ radii, double probe,
@@ -91,14 +93,24 @@ __global__ void k_expand(typename OrdT<T>::type *g, Dims d, double sx, double sy
     const int icx = (int)((cx - sx) / dx), icy = (int)((cy - sy) / dx), icz = (int)((cz - sz) / dx);
     const int side = 2 * r + 1;
     const long total = (long)side * side * side;
+    // FP32 grid: the atom's offset from its own cell, then whole cells
+    const float fx = (float)((sx + icx * dx) - cx), fy = (float)((sy + icy * dx) - cy),
+                fz = (float)((sz + icz * dx) - cz), h = (float)dx;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
         const int c = icz - r + (int)(t % side);
         const int b = icy - r + (int)((t / side) % side);
         const int ia = icx - r + (int)(t / ((long)side * side));
         if (ia < 0 || b < 0 || c < 0 || ia >= d.nx || b >= d.ny || c >= d.nz) continue;
-        const double px = (sx + ia * dx) - cx, py = (sy + b * dx) - cy, pz = (sz + c * dx) - cz;
-        const double dist = R - sqrt(px * px + py * py + pz * pz);
-        atomicMax(g + d.idx(ia, b, c), ord((T)dist));
+        if constexpr (sizeof(T) == 4) {
+            const float px = fmaf((float)(ia - icx), h, fx), py = fmaf((float)(b - icy), h, fy),
+                        pz = fmaf((float)(c - icz), h, fz);
+            const float dist = (float)R - sqrtf(fmaf(px, px, fmaf(py, py, pz * pz)));
+            atomicMax(g + d.idx(ia, b, c), ord(dist));
+        } else {
+            const double px = (sx + ia * dx) - cx, py = (sy + b * dx) - cy, pz = (sz + c * dx) - cz;
+            const double dist = R - sqrt(px * px + py * py + pz * pz);
+            atomicMax(g + d.idx(ia, b, c), ord((T)dist));
+        }
     }
 }
 
