@@ -276,10 +276,10 @@ static void encode_lists(const TreeHost &T, int *buf, long cap, long *needed) {
         out.push_back(T.leaf[i]);
         out.push_back(T.empty[i]);
         out.push_back(T.src_end[i] - T.src_begin[i]);
-        const std::vector<int> *L[4] = {&T.U[i], &T.V[i], &T.W[i], &T.X[i]};
-        for (auto *l : L) {
+        const IdxSpan L[4] = {T.U[i], T.V[i], T.W[i], T.X[i]};
+        for (const IdxSpan &l : L) {
             std::vector<int> v;
-            for (int x : *l) v.push_back(T.ref_id[x]);
+            for (int x : l) v.push_back(T.ref_id[x]);
             std::sort(v.begin(), v.end());
             out.push_back((int)v.size());
             out.insert(out.end(), v.begin(), v.end());

@@ -169,6 +169,21 @@ struct Tube {
 };
 
 // Octree + interaction lists, host side (tree.cpp).  Node ids are level-ordered.
+// Per-node index lists in one array (compressed rows): lists[i] is node i's list.
+struct IdxSpan {
+    const int *b, *e;
+    const int *begin() const { return b; }
+    const int *end() const { return e; }
+    size_t size() const { return (size_t)(e - b); }
+    int operator[](size_t k) const { return b[k]; }
+};
+struct NodeLists {
+    std::vector<long> off;  // size nnodes + 1
+    std::vector<int> idx;
+    IdxSpan operator[](size_t i) const { return {idx.data() + off[i], idx.data() + off[i + 1]}; }
+    size_t size() const { return off.empty() ? 0 : off.size() - 1; }
+};
+
 struct TreeHost {
     int p = 0, R = 0;
     int nnodes = 0, nlevels = 0;
@@ -178,14 +193,12 @@ struct TreeHost {
     std::vector<int> src_begin, src_end, tgt_begin, tgt_end;
     std::vector<int> src_perm, tgt_perm;  // tree position -> caller index
     std::vector<int> ref_id;              // node id in the reference's numbering (bbfmm.cpp:88-91)
-    // lists (sorted node ids per node)
-    std::vector<std::vector<int>> U, V, W, X;
+    // interaction lists per node
+    NodeLists U, V, W, X;
 };
 
 TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int maxpoint, int maxlevel);
-// Frees per-node lists with all threads (lists filled in parallel are slow to free from one).
-void release_lists(std::vector<std::vector<int>> &U, std::vector<std::vector<int>> &V,
-                   std::vector<std::vector<int>> &W, std::vector<std::vector<int>> &X);
+
 
 struct ChebTables;
 
@@ -305,10 +318,7 @@ struct Plan {
     DevBuf<double> oz_sig, oz_tau;
     double kp64[5] = {-1, -1, -1, -1, -1}, kp32[5] = {-1, -1, -1, -1, -1};  // kernel parameters of the cached operators
     bool ops64_ready = false, ops32_ready = false;
-    ~Plan() {
-        for (auto *t : targets) delete t;
-        release_lists(tree.U, tree.V, tree.W, tree.X);
-    }
+    ~Plan() { for (auto *t : targets) delete t; }
 };
 
 // FMM engine.  dens: 4 x ns (tree order), out: 4 x nt of target set `ts` (tree order).

@@ -292,7 +292,16 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         }
         return (touch[0] && ot[1] && ot[2]) || (touch[1] && ot[0] && ot[2]) || (touch[2] && ot[0] && ot[1]);
     };
-    std::vector<std::vector<int>> U(nn), V(nn), W(nn), X(nn);
+    // Lists are appended to per-thread buffers (one per list kind): a node is handled by one
+    // thread, so its list is one contiguous segment [lbeg, lbeg + llen) of its thread's buffer
+    // (no per-node allocations)
+    const int nthr_l = omp_get_max_threads();
+    std::vector<std::array<std::vector<int>, 4>> lbuf(nthr_l);
+    std::vector<std::array<long, 4>> lbeg(nn);
+    std::vector<std::array<int, 4>> llen(nn);
+    std::vector<int> lown(nn, 0);
+    for (auto &b4 : lbuf)
+        for (auto &b : b4) b.reserve(1 << 16);
     // The candidates of a node are the 6 x 6 x 6 same-level cells around its parent, i.e. the
     // children of the parent's 3 x 3 x 3 neighbourhood: findNode is resolved once per parent
     // neighbour and shared by the 8 siblings.  A coarser leaf met by several candidates is
@@ -300,9 +309,7 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     std::vector<int> parents;
     for (int id = 0; id < nn; ++id)
         if (B.nodes[id].child[0] >= 0) parents.push_back(id);
-    auto push_once = [](std::vector<int> &v, int x) {
-        if (std::find(v.begin(), v.end(), x) == v.end()) v.push_back(x);
-    };
+    enum { LU = 0, LV = 1, LW = 2, LX = 3 };
 #pragma omp parallel for schedule(dynamic, 16)
     for (int k = 0; k < (int)parents.size(); ++k) {
         const int pid = parents[k];
@@ -316,10 +323,16 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
                         : find_node(pn.level, c);
         }
         std::vector<int> queue;
+        std::array<std::vector<int>, 4> &buf = lbuf[omp_get_thread_num()];
         for (int ci = 0; ci < 8; ++ci) {
             const int id = pn.child[ci];
             const BNode &n = B.nodes[id];
-            V[id].reserve(64);
+            lown[id] = omp_get_thread_num();
+            for (int w = 0; w < 4; ++w) lbeg[id][w] = (long)buf[w].size();
+            auto push = [&](int w, int x) { buf[w].push_back(x); };
+            auto push_once = [&](int w, int x) {
+                if (std::find(buf[w].begin() + lbeg[id][w], buf[w].end(), x) == buf[w].end()) buf[w].push_back(x);
+            };
             for (int xi = -2; xi < 4; ++xi)
                 for (int yi = -2; yi < 4; ++yi)
                     for (int zi = -2; zi < 4; ++zi) {
@@ -336,23 +349,23 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
                         const BNode &cn = B.nodes[cid];
                         if (cn.level < n.level) {
                             if (adj) {
-                                if (cn.leaf) push_once(U[id], cid);
+                                if (cn.leaf) push_once(LU, cid);
                             } else {
-                                push_once(X[id], cid);
+                                push_once(LX, cid);
                             }
                         }
                         if (cn.level == n.level) {
                             if (!adj) {
-                                V[id].push_back(cid);
+                                push(LV, cid);
                             } else if (n.leaf) {
                                 queue.clear();
                                 queue.push_back(cid);
                                 for (size_t q = 0; q < queue.size(); ++q) {
                                     const int f = queue[q];
                                     if (!adjacent(f, id)) {
-                                        W[id].push_back(f);
+                                        push(LW, f);
                                     } else if (B.nodes[f].leaf) {
-                                        U[id].push_back(f);
+                                        push(LU, f);
                                     } else {
                                         for (int ch = 0; ch < 8; ++ch) queue.push_back(B.nodes[f].child[ch]);
                                     }
@@ -360,10 +373,20 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
                             }
                         }
                     }
-            if (n.leaf) U[id].push_back(id);
+            if (n.leaf) push(LU, id);
+            for (int w = 0; w < 4; ++w) llen[id][w] = (int)((long)buf[w].size() - lbeg[id][w]);
         }
     }
-    if (B.nodes[0].leaf) U[0].push_back(0);
+    // the root (no parent): its own U entry when it is a leaf
+    for (int w = 0; w < 4; ++w) {
+        lbeg[0][w] = (long)lbuf[0][w].size();
+        llen[0][w] = 0;
+    }
+    lown[0] = 0;
+    if (B.nodes[0].leaf) {
+        lbuf[0][LU].push_back(0);
+        llen[0][LU] = 1;
+    }
     trace_mark("tree: U V W X lists");
     std::vector<int> ref_of;
     reference_ids(B.nodes, ref_of);
@@ -393,10 +416,14 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     T.tgt_begin.resize(nn);
     T.tgt_end.resize(nn);
     T.ref_id.resize(nn);
-    T.U.resize(nn);
-    T.V.resize(nn);
-    T.W.resize(nn);
-    T.X.resize(nn);
+    // compressed lists in the level-ordered numbering: sizes, offsets, then a parallel fill
+    NodeLists *dstl[4] = {&T.U, &T.V, &T.W, &T.X};
+    for (int w = 0; w < 4; ++w) {
+        NodeLists &L = *dstl[w];
+        L.off.assign(nn + 1, 0);
+        for (int i = 0; i < nn; ++i) L.off[i + 1] = L.off[i] + llen[order[i]][w];
+        L.idx.resize(L.off[nn]);
+    }
     for (int i = 0; i < nn; ++i) T.level_begin[B.nodes[order[i]].level + 1]++;
 #pragma omp parallel for schedule(dynamic, 64)
     for (int i = 0; i < nn; ++i) {
@@ -415,33 +442,17 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         T.tgt_begin[i] = n.tb;
         T.tgt_end[i] = n.te;
         T.ref_id[i] = ref_of[order[i]];
-        auto remap = [&](const std::vector<int> &in, std::vector<int> &out) {
-            out.resize(in.size());
-            for (size_t q = 0; q < in.size(); ++q) out[q] = newid[in[q]];
-        };
-        remap(U[order[i]], T.U[i]);
-        remap(V[order[i]], T.V[i]);
-        remap(W[order[i]], T.W[i]);
-        remap(X[order[i]], T.X[i]);
+        const int o = order[i];
+        for (int w = 0; w < 4; ++w) {
+            const int *in = lbuf[lown[o]][w].data() + lbeg[o][w];
+            int *out = dstl[w]->idx.data() + dstl[w]->off[i];
+            for (int q = 0; q < llen[o][w]; ++q) out[q] = newid[in[q]];
+        }
     }
     for (int l = 0; l < T.nlevels; ++l) T.level_begin[l + 1] += T.level_begin[l];
     T.tgt_perm = B.same ? sp : std::move(tp);
     T.src_perm = std::move(sp);
-    // the working lists were filled by many threads: freeing them from one costs milliseconds
-    release_lists(U, V, W, X);
     return T;
-}
-
-void release_lists(std::vector<std::vector<int>> &U, std::vector<std::vector<int>> &V,
-                   std::vector<std::vector<int>> &W, std::vector<std::vector<int>> &X) {
-    const long n = (long)std::max(std::max(U.size(), V.size()), std::max(W.size(), X.size()));
-#pragma omp parallel for schedule(static) if (n >= 4096)
-    for (long i = 0; i < n; ++i) {
-        if (i < (long)U.size()) std::vector<int>().swap(U[i]);
-        if (i < (long)V.size()) std::vector<int>().swap(V[i]);
-        if (i < (long)W.size()) std::vector<int>().swap(W[i]);
-        if (i < (long)X.size()) std::vector<int>().swap(X[i]);
-    }
 }
 
 }  // namespace ibim
