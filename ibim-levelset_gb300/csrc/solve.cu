@@ -483,13 +483,13 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
         for (outer = 0; outer < 8 && left > 0; ++outer) {
             d.zero();
             GmresStats si;
-            // inner tolerance relative to ||r||: half the outer target (the other half is left for the
-            // gap between the mixed and the FP64-class operator), above the FP32 noise floor.
-            // IBIM_IR_FACTOR in (0, 1) replaces the 0.5.
+            // inner tolerance relative to ||r||: 0.7 of the outer target (the rest is left for the gap
+            // between the mixed and the FP64-class operator, small once both decide the near-field
+            // cutoff alike), above the FP32 noise floor.  IBIM_IR_FACTOR in (0, 1) replaces the 0.7.
             static const double factor = [] {
                 const char *v = std::getenv("IBIM_IR_FACTOR");
-                const double f = v ? std::atof(v) : 0.5;
-                return f > 0.0 && f < 1.0 ? f : 0.5;
+                const double f = v ? std::atof(v) : 0.7;
+                return f > 0.0 && f < 1.0 ? f : 0.7;
             }();
             const double inner = std::min(0.5, std::max(factor * tol / rel, 3e-7));
             K.solve(A32, d.ptr, r.ptr, left, inner, true, si);
