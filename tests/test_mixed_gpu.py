@@ -139,3 +139,25 @@ def test_mixed_plan_follows_kernel_parameter_changes(ctx, golden):
         for o in range(4):
             assert np.abs(a[o] - b[o]).max() / np.abs(a[o]).max() < 2e-5, (kappa, o)
             assert np.abs(a[o] - c[o]).max() / np.abs(a[o]).max() < 1e-10, (kappa, o)
+
+
+@pytest.mark.parametrize("shift", [0.1, 0.37])
+def test_mixed_near_field_decides_the_cutoff_like_fp64(ctx, shift):
+    """Points on a lattice of spacing h (offset by a value FP64 cannot hold exactly) put thousands
+    of pairs within rounding of the cutoff r = tau h: the FP32 near field must decide each of them
+    as the FP64 kernel does (a pair decided the other way changes its target by O(1))."""
+    h = 0.5
+    g = np.arange(16) * h + shift
+    X, Y, Z = np.meshgrid(g, g, g[:6], indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    rng = np.random.default_rng(3)
+    nrm = rng.normal(size=pts.shape)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    w = 1.0 + 0.1 * rng.random(len(pts))
+    t = ctx.tube(pts, nrm, w, h)
+    kp = ibim.kernel_params(0.1, 80.0, 1.0, 1.0)  # tau = 1: cutoff at exactly the lattice spacing
+    dens = np.stack([np.sin(0.3 * np.arange(len(pts)) + k) for k in range(4)])
+    a = t.plan(4, 64, 1).apply(ibim.KERNEL_BIE_FUSED, kp, dens)  # level 1: near field only
+    b = t.plan(4, 64, 1, precision=ibim.PRECISION_MIXED).apply(ibim.KERNEL_BIE_FUSED, kp, dens)
+    for o in range(4):
+        assert np.abs(a[o] - b[o]).max() / np.abs(a[o]).max() < 2e-5, o
