@@ -307,6 +307,7 @@ const char *ibim_status_string(int st) {
         case IBIM_ERR_UNSUPPORTED_KERNEL: return "unsupported kernel";
         case IBIM_ERR_LIMIT: return "iteration limit reached";
         case IBIM_ERR_IO: return "I/O error";
+        case IBIM_ERR_CALLBACK: return "operator callback failed";
         default: return "unknown status";
     }
 }
@@ -518,6 +519,18 @@ int ibim_grid_download(ibim_grid g, double *host) {
             IBIM_CUDA(cudaStreamSynchronize(G.ctx->stream));
             std::copy(f.begin(), f.end(), host);
         }
+    });
+}
+
+int ibim_grid_set_geometry(ibim_grid g, double sx, double sy, double sz, double dx) {
+    return guard([&] {
+        IBIM_REQUIRE(g, "null handle");
+        IBIM_REQUIRE(dx > 0, "dx must be positive");
+        Grid &G = *g->g;
+        G.sx = sx;
+        G.sy = sy;
+        G.sz = sz;
+        G.dx = dx;
     });
 }
 
@@ -859,6 +872,49 @@ int ibim_gmres_solve(ibim_plan p, const ibim_kernel_params *kp, const double *b,
         hx.download(x, 2 * n);
         IBIM_CUDA(cudaStreamSynchronize(s));
         if (iters) *iters = st.iters;
+        if (gmres_status) *gmres_status = rc;
+        if (residual) *residual = st.residual;
+    });
+}
+
+int ibim_gmres_host(ibim_ctx ctx, long n, ibim_apply_fn apply, void *user, const double *b, double *x, int restart,
+                    int maxiter, double tol, int *iters, int *matvecs, int *gmres_status, double *residual) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && apply && b && x, "null argument");
+        IBIM_REQUIRE(n > 0, "vector length must be positive");
+        IBIM_REQUIRE(restart > 0 && maxiter > 0, "restart and maxiter must be positive");
+        Ctx *c = &ctx->c;
+        bind(c);
+        cudaStream_t s = c->stream;
+        DevBuf<double> db, dx;
+        db.alloc(n, s);
+        dx.alloc(n, s);
+        db.upload(b, n);
+        dx.upload(x, n);
+        // the operator's input and output pass through pinned host buffers
+        double *hin = nullptr, *hout = nullptr;
+        IBIM_CUDA(cudaMallocHost((void **)&hin, sizeof(double) * n));
+        struct Pinned {
+            double *&a, *&b;
+            ~Pinned() { if (a) cudaFreeHost(a); if (b) cudaFreeHost(b); }
+        } pinned{hin, hout};
+        IBIM_CUDA(cudaMallocHost((void **)&hout, sizeof(double) * n));
+        auto A = [&](const double *in, double *o) {
+            IBIM_CUDA(cudaMemcpyAsync(hin, in, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+            IBIM_CUDA(cudaStreamSynchronize(s));
+            if (apply(user, hin, hout, n) != 0)
+                throw Error(IBIM_ERR_CALLBACK, "the operator callback stopped the GMRES solve");
+            IBIM_CUDA(cudaMemcpyAsync(o, hout, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            IBIM_CUDA(cudaStreamSynchronize(s));
+        };
+        Krylov K(c, n, std::min(restart, 250));
+        GmresStats st;
+        // x is arbitrary here: the first product A x is applied, as gmres.cpp:72 does
+        const int rc = K.solve(A, dx.ptr, db.ptr, maxiter, tol, false, st);
+        dx.download(x, n);
+        IBIM_CUDA(cudaStreamSynchronize(s));
+        if (iters) *iters = st.iters;
+        if (matvecs) *matvecs = st.matvecs;
         if (gmres_status) *gmres_status = rc;
         if (residual) *residual = st.residual;
     });

@@ -28,6 +28,7 @@ ERR_OUT_OF_MEMORY = 3
 ERR_UNSUPPORTED_KERNEL = 4
 ERR_LIMIT = 5
 ERR_IO = 6
+ERR_CALLBACK = 7
 
 KERNELS = ["K1x", "K1y", "K1z", "K2", "K3xx", "K3yy", "K3zz", "K3xy", "K3yz", "K3zx", "K3yx", "K3zy", "K3xz",
            "K4x", "K4y", "K4z"]
@@ -49,7 +50,8 @@ EXPORTS = [
     "ibim_ctx_trim",
     "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
     "ibim_levelset_evolve_static", "ibim_server_create", "ibim_server_destroy", "ibim_server_submit",
-    "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate",
+    "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate", "ibim_gmres_host",
+    "ibim_grid_set_geometry",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
@@ -96,6 +98,8 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_long)
 _vp = C.c_void_p
+# int (*ibim_apply_fn)(void *user, const double *x, double *y, long n)
+APPLY_FN = C.CFUNCTYPE(C.c_int, _vp, _dp, _dp, C.c_long)
 
 
 def lib():
@@ -118,6 +122,7 @@ def lib():
         "ibim_grid_upload": ([_vp, _dp], C.c_int),
         "ibim_grid_download": ([_vp, _dp], C.c_int),
         "ibim_grid_scale": ([_vp, C.c_double], C.c_int),
+        "ibim_grid_set_geometry": ([_vp, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
         "ibim_grid_copy": ([_vp, _vp], C.c_int),
         "ibim_levelset_expand": ([_vp, _dp, _dp, C.c_int, C.c_double, C.c_int], C.c_int),
         "ibim_levelset_evolve": ([_vp, C.c_double, C.c_double, C.c_double], C.c_int),
@@ -161,6 +166,8 @@ def lib():
         "ibim_server_wait": ([_vp, C.c_long, _ip, C.POINTER(Result), _dp, _dp], C.c_int),
         "ibim_server_stats": ([_vp, _dp], C.c_int),
         "ibim_request_bytes_estimate": ([C.POINTER(Config)], C.c_double),
+        "ibim_gmres_host": ([_vp, C.c_long, APPLY_FN, _vp, _dp, _dp, C.c_int, C.c_int, C.c_double, _ip, _ip, _ip,
+                             _dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -256,6 +263,33 @@ class Context:
         v = C.c_double(0)
         _check(lib().ibim_measure_peak(self.h, {"fp64": 0, "fp32": 1}[kind], C.byref(v)))
         return v.value
+
+    def gmres(self, apply, b, x0=None, restart=30, maxiter=100, tol=1e-6):
+        """GMRES (gmres.h:20-21) on any operator `apply(x) -> y` evaluated on the host (numpy in,
+        numpy out); the Krylov basis and the orthogonalisation run on the device."""
+        b = _c(b)
+        n = len(b)
+        x = np.zeros_like(b) if x0 is None else _c(x0).copy()
+        err = []
+
+        def tramp(_user, xp, yp, nn):
+            try:
+                xin = np.ctypeslib.as_array(xp, shape=(nn,))
+                y = np.asarray(apply(xin.copy()), dtype=np.float64).reshape(nn)
+                np.ctypeslib.as_array(yp, shape=(nn,))[:] = y
+                return 0
+            except Exception as e:  # the callback must not raise through C
+                err.append(e)
+                return 1
+
+        fn = APPLY_FN(tramp)
+        it, mv, st, res = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
+        rc = lib().ibim_gmres_host(self.h, n, fn, None, _p(b), _p(x), restart, maxiter, tol, C.byref(it), C.byref(mv),
+                                   C.byref(st), C.byref(res))
+        if err:
+            raise err[0]
+        _check(rc)
+        return x, dict(iters=it.value, matvecs=mv.value, status=st.value, residual=res.value)
 
     def grid(self, n, lo, h, value=0.0) -> "Grid":
         g = _vp()

@@ -30,6 +30,7 @@ extern "C" {
 #define IBIM_ERR_UNSUPPORTED_KERNEL 4 /* kernel id outside the reference's kernel set */
 #define IBIM_ERR_LIMIT 5            /* a bounded device loop (flood fill) hit its iteration cap */
 #define IBIM_ERR_IO 6               /* unreadable or malformed input file */
+#define IBIM_ERR_CALLBACK 7         /* a caller-supplied operator callback returned non-zero */
 
 /* ---- kernel ids: the 16 kernels of electric.cpp:67-291, plus the fused forms ---- */
 #define IBIM_K1X 0
@@ -162,6 +163,9 @@ int ibim_grid_create(ibim_ctx ctx, int nx, int ny, int nz, double sx, double sy,
 int ibim_grid_destroy(ibim_grid g);
 int ibim_grid_upload(ibim_grid g, const double *host);                       /* row-major, k fastest */
 int ibim_grid_download(ibim_grid g, double *host);
+/* The grid's origin and spacing.  The reference keeps them on the levelset object
+ * (levelset.h:35-38), not on Grid; the C++ drop-in sets them from its levelset before each call. */
+int ibim_grid_set_geometry(ibim_grid g, double sx, double sy, double sz, double dx);
 int ibim_grid_scale(ibim_grid g, double s);                                  /* Grid::operator*= */
 int ibim_grid_copy(ibim_grid dst, ibim_grid src);                            /* Grid::operator= */
 int ibim_levelset_expand(ibim_grid g, const double *centers, const double *radii, int natoms,
@@ -231,6 +235,19 @@ int ibim_bie_rhs(ibim_plan p, const ibim_kernel_params *kp, const double *center
 /* GMRES(m, max_iter, tol) on the BIE operator from x (in/out, 2N) (gmres.cpp:50-164). */
 int ibim_gmres_solve(ibim_plan p, const ibim_kernel_params *kp, const double *b, double *x, int restart,
                      int maxiter, double tol, int precision, int *iters, int *gmres_status, double *residual);
+/* A linear operator applied by the caller on host vectors: y = A x, both of length n.  Return 0
+ * to continue; any other value stops the solve that called it. */
+typedef int (*ibim_apply_fn)(void *user, const double *x, double *y, long n);
+/* GMRES(m, max_iter, tol) on an arbitrary operator: the reference's
+ * int GMRES(std::function<Vector(Vector&)> A, Vector& x, Vector& b, int m, int max_iter, scalar_t tol)
+ * (gmres.h:20-21, gmres.cpp:50-164).  The Krylov basis, modified Gram-Schmidt and the updates run
+ * on the context's GPU in FP64 with the reference's Givens rotations and restarts; each product
+ * goes to the host, through `apply`, and back.  b and x (in/out, the initial guess) are host
+ * vectors of length n; the first product is A x, as in the reference, so *matvecs counts the
+ * same operator applications as the reference's GMRES makes.  A callback returning non-zero
+ * ends the solve with IBIM_ERR_CALLBACK and x unchanged. */
+int ibim_gmres_host(ibim_ctx ctx, long n, ibim_apply_fn apply, void *user, const double *b, double *x, int restart,
+                    int maxiter, double tol, int *iters, int *matvecs, int *gmres_status, double *residual);
 /* electric() after Surface: RHS, GMRES, polarizeMap, energy (electric.cpp:9-505).
  * x (2N) and atom_potential (natoms) may be NULL. */
 int ibim_electric(ibim_tube tube, const double *centers, const double *charges, int natoms,

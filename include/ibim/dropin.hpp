@@ -9,14 +9,19 @@
 //   levelset          levelset.h:33-60      (expand, evolve, reinitialize, countGradient)
 //   Surface           levelset.h:62-72      (nodes, normals, weight; device tube kept)
 //   bbfmm::kernel     bbfmm.h:200-270       (eval = one of the reference's kernel ids)
-//   GMRES             gmres.h:20-21         (on the BIE operator of a Surface)
+//   GMRES             gmres.h:20-21         (any std::function<Vector(Vector&)> operator; Krylov
+//                                           basis on the GPU, products through the callback)
+//   BIEOperator       electric.cpp:294-412  (dmapping and load on the GPU, for GMRES's closure)
 //   electric          electric.h:13         (prints the polarized energy, writes potent/energy files)
 // Errors: a failing library call throws ibim::dropin::Error (status + message), where the
 // reference would assert, exit or throw from std::stod.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
+#include <exception>
+#include <functional>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
@@ -130,10 +135,15 @@ class Molecule {
 
 class levelset;
 
+// Device grid.  Its origin and spacing come from the levelset that works on it (the reference
+// keeps them there, levelset.h:35-38); the optional geometry arguments preset them.
 class Grid {
   public:
     int Nx, Ny, Nz;
     ibim_grid h = nullptr;
+    // Grid(Nx, Ny, Nz) (levelset.h:18): the reference leaves the values unset; zero here
+    Grid(int nx, int ny, int nz) : Grid(0.0, nx, ny, nz) {}
+    // Grid(val, Nx, Ny, Nz) (levelset.h:19)
     Grid(double val, int nx, int ny, int nz, double sx = 0, double sy = 0, double sz = 0, double dx = 1)
         : Nx(nx), Ny(ny), Nz(nz) {
         check(ibim_grid_create(context(), nx, ny, nz, sx, sy, sz, dx, val, &h));
@@ -153,6 +163,12 @@ class Grid {
         j = std::min(std::max(j, 0), Ny - 1);
         k = std::min(std::max(k, 0), Nz - 1);
         return data()[((size_t)i * Ny + j) * Nz + k];
+    }
+    // Grid::set (levelset.cpp:35-37); writes go through a host copy
+    void set(double val, int i, int j, int k) {
+        std::vector<double> v = data();
+        v[((size_t)i * Ny + j) * Nz + k] = val;
+        check(ibim_grid_upload(h, v.data()));
     }
     void output(const std::string &file) const {
         std::ofstream f(file);
@@ -174,21 +190,30 @@ class levelset {
     }
     Grid *make_grid(double val) const { return new Grid(val, Nx, Ny, Nz, sx, sy, sz, dx); }
     void expand(Molecule &mol, Grid &g, double probe) {
+        place(g);
         const std::vector<double> c = mol.flat_centers();
         check(ibim_levelset_expand(g.h, c.data(), mol.radii.data(), mol.N, probe, bandwidth));
     }
-    void evolve(Grid &g, double final_t, double vel, double cfl) { check(ibim_levelset_evolve(g.h, final_t, vel, cfl)); }
+    void evolve(Grid &g, double final_t, double vel, double cfl) {
+        place(g);
+        check(ibim_levelset_evolve(g.h, final_t, vel, cfl));
+    }
     int reinitialize(Grid &g, Grid &phi0, double final_t, double vel, double cfl) {
+        place(g);
+        place(phi0);
         int steps = 0;
         check(ibim_levelset_reinitialize(g.h, phi0.h, final_t, vel, cfl, thickness, thres, &steps));
         return steps;
     }
     long countGradient(Grid &g, double thick, double thr) {
+        place(g);
         long bad = 0, total = 0;
         double acc = 0;
         check(ibim_levelset_count_gradient(g.h, thick, thr, &bad, &total, &acc));
         return bad;
     }
+    // the grid takes this levelset's origin and spacing
+    void place(Grid &g) const { check(ibim_grid_set_geometry(g.h, sx, sy, sz, dx)); }
 };
 
 class Surface {
@@ -199,6 +224,7 @@ class Surface {
     long inclusion = 0;
     double dx;
     Surface(Grid &g, levelset &ls, double /*s*/) : dx(ls.dx) {
+        ls.place(g);
         long n = 0;
         check(ibim_surface_extract_jacobian(g.h, ls.thickness, ls.jacobian, &tube, &n, &inclusion));
         std::vector<double> p(3 * (size_t)n), q(3 * (size_t)n);
@@ -287,6 +313,94 @@ inline ibim_config config_from(const Config &cfg, const levelset &ls) {
     c.tol = cfg.num("gmres_tol");
     return c;
 }
+
+typedef std::vector<double> Vector;
+
+// int GMRES(std::function<Vector(Vector&)> A, Vector& x, Vector& b, int m, int max_iter, scalar_t tol)
+// (gmres.h:20-21, gmres.cpp:50-164): restarted GMRES(m) on any operator A.  The Krylov basis,
+// modified Gram-Schmidt and the updates run on the GPU in FP64 (ibim_gmres_host); every product
+// A v is one call of A on a host Vector, as in the reference, starting with A x.  x holds the
+// initial guess and receives the solution.  Returns 0 when converged, 1 when not (gmres.cpp:186);
+// an exception thrown by A propagates to the caller with x unchanged.
+inline int GMRES(const std::function<Vector(Vector &)> A, Vector &x, Vector &b, int m, int max_iter, double tol) {
+    if (x.size() != b.size()) throw Error(IBIM_ERR_INVALID_ARGUMENT, "GMRES: x and b differ in length");
+    struct Call {
+        const std::function<Vector(Vector &)> *A;
+        Vector in;
+        std::exception_ptr err;
+    } call{&A, Vector(), nullptr};
+    auto tramp = +[](void *user, const double *xin, double *yout, long n) -> int {
+        Call &c = *static_cast<Call *>(user);
+        try {
+            c.in.assign(xin, xin + n);
+            const Vector y = (*c.A)(c.in);
+            if ((long)y.size() != n) throw Error(IBIM_ERR_INVALID_ARGUMENT, "GMRES: the operator changed the length");
+            std::copy(y.begin(), y.end(), yout);
+            return 0;
+        } catch (...) {
+            c.err = std::current_exception();
+            return 1;
+        }
+    };
+    int iters = 0, matvecs = 0, status = 1;
+    double resid = 0;
+    const int st = ibim_gmres_host(context(), (long)b.size(), tramp, &call, b.data(), x.data(), m, max_iter, tol,
+                                   &iters, &matvecs, &status, &resid);
+    if (call.err) std::rethrow_exception(call.err);
+    check(st);
+    std::cout << (status == 0 ? "=============== CONVERGED =============" : "============= NOT CONVERGED ===========")
+              << std::endl;
+    return status;
+}
+
+// The BIE operator of electric() over a Surface, evaluated on the GPU: dmapping
+// (electric.cpp:294-388) as the closure GMRES takes, and the right-hand side load
+// (electric.cpp:395-412).  Vectors are (phi, dphi) of length 2N in the Surface's point order.
+class BIEOperator {
+  public:
+    long N = 0;
+    BIEOperator(levelset &ls, Surface &surf, Config &cfg, double rescale = 1.0) {
+        N = (long)surf.nodes.size();
+        std::vector<double> p(3 * (size_t)N), q(3 * (size_t)N);
+        for (long i = 0; i < N; ++i)
+            for (int a = 0; a < 3; ++a) {
+                p[3 * i + a] = surf.nodes[i][a] / rescale;
+                q[3 * i + a] = surf.normals[i][a];
+            }
+        check(ibim_tube_create(context(), p.data(), q.data(), surf.weight.data(), N, ls.dx / rescale, &tube_));
+        kp_.kappa = cfg.num("solvent_kappa");
+        kp_.dE = cfg.num("solvent_dE");
+        kp_.dI = cfg.num("solvent_dI");
+        kp_.tau = cfg.num("tau");
+        kp_.k3_scaled = cfg.options.count("k3_scaled") ? (int)cfg.num("k3_scaled") : 0;
+        check(ibim_fmm_plan(tube_, nullptr, 0, (int)cfg.num("fmm_np"), (int)cfg.num("fmm_maxpoint"),
+                            (int)cfg.num("fmm_maxlevel"), IBIM_PRECISION_FP64, &plan_));
+        rescale_ = rescale;
+    }
+    BIEOperator(const BIEOperator &) = delete;
+    ~BIEOperator() {
+        ibim_plan_destroy(plan_);
+        ibim_tube_destroy(tube_);
+    }
+    Vector operator()(Vector &phi) const {
+        if ((long)phi.size() != 2 * N) throw Error(IBIM_ERR_INVALID_ARGUMENT, "dmapping: length is not 2N");
+        Vector y(2 * (size_t)N);
+        check(ibim_bie_matvec(plan_, &kp_, phi.data(), y.data()));
+        return y;
+    }
+    Vector load(Molecule &mol) const {
+        const std::vector<double> c = mol.flat_centers(1.0 / rescale_);
+        Vector b(2 * (size_t)N);
+        check(ibim_bie_rhs(plan_, &kp_, c.data(), mol.charges.data(), mol.N, b.data()));
+        return b;
+    }
+
+  private:
+    ibim_tube tube_ = nullptr;
+    ibim_plan plan_ = nullptr;
+    ibim_kernel_params kp_{0.0, 80.0, 1.0, 1.0, 0};
+    double rescale_ = 1.0;
+};
 
 // electric(Grid&, levelset&, Surface&, Molecule&, rescale, Config&) (electric.cpp:9-507): the
 // solve in Angstrom (lengths divided by rescale), energy printed as the reference prints it,

@@ -78,8 +78,14 @@ def lib():
         L.orc_solve.argtypes = [_dp, C.c_long, C.c_double, _dp, _dp, C.c_int, C.POINTER(BieParams), _dp, _dp, _dp,
                                 _ip, _ip]
         L.orc_solve.restype = C.c_int
+        L.orc_gmres.argtypes = [ORC_OP, C.c_void_p, C.c_long, _dp, _dp, C.c_int, C.c_int, C.c_double, _ip, _ip]
+        L.orc_gmres.restype = C.c_int
         _lib = L
     return _lib
+
+
+# void (*orc_op)(void *ctx, const double *x, double *y)
+ORC_OP = C.CFUNCTYPE(None, C.c_void_p, _dp, _dp)
 
 
 def _p(a):
@@ -222,3 +228,20 @@ def solve(surf7, h, centers, charges, bp: BieParams):
     rc = lib().orc_solve(_p(s), N, h, _p(c), _p(q), len(q), C.byref(bp), _p(x), _p(pot), C.byref(E), C.byref(it),
                          C.byref(mv))
     return dict(x=x, atom_pot=pot, energy=E.value, rc=rc, iters=it.value, matvecs=mv.value)
+
+
+def gmres(apply, b, x0=None, m=30, max_iter=100, tol=1e-6):
+    """Restarted GMRES of gmres.cpp:50-164 (orc_gmres) on an operator apply(x) -> y given in numpy.
+    Returns (x, status, iters, matvecs); matvecs counts the first product A x0 as the reference does."""
+    b = _c(b)
+    n = len(b)
+    x = np.zeros(n) if x0 is None else _c(x0).copy()
+
+    def op(_ctx, xp, yp):
+        y = np.asarray(apply(np.ctypeslib.as_array(xp, shape=(n,)).copy()), dtype=np.float64)
+        np.ctypeslib.as_array(yp, shape=(n,))[:] = y
+
+    fn = ORC_OP(op)
+    it, mv = C.c_int(0), C.c_int(0)
+    rc = lib().orc_gmres(fn, None, n, _p(x), _p(b), m, max_iter, tol, C.byref(it), C.byref(mv))
+    return x, rc, it.value, mv.value

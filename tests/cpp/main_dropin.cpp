@@ -1,6 +1,6 @@
 // main.cpp:14-79 of the reference written against the drop-in classes (include/ibim/dropin.hpp),
 // with an explicit box instead of the hard-wired [-300, 300]^3 rescaling: the same sequence of
-// calls, executed on the GPU.  Usage: main_dropin <input.cfg>
+// calls (grids sized by the levelset and placed by it, main.cpp:47-48), executed on the GPU.  Usage: main_dropin <input.cfg>
 // (keys: pqr_file, lo, h, n, reinit_step, plus the reference's lvlset_*, fmm_*, solvent_*, tau,
 // gmres_*, potent_file, energy_file keys; optional grid_file / node_file).
 #include <cstdio>
@@ -23,8 +23,8 @@ int main(int argc, char *argv[]) {
         const double lo = cfg.num("lo"), h = cfg.num("h");
         const int size = (int)cfg.num("n");
         levelset ls(size, size, size, 8, lo, lo, lo, h, cfg);
-        Grid g(-2.0 * size, size, size, size, lo, lo, lo, h);
-        Grid phi0(0., size, size, size, lo, lo, lo, h);
+        Grid g(-2.0 * size, ls.Nx, ls.Ny, ls.Nz);
+        Grid phi0(0., ls.Nx, ls.Ny, ls.Nz);
         ls.expand(mol, g, 1.4);
         ls.evolve(g, 1.4, 1.0, 0.2);
         g *= -1.0;

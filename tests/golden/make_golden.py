@@ -9,8 +9,11 @@ small cases and packs what it dumps into one .npz per case:
   synth30  30-atom synthetic protein (seed 7), h=0.5 A, p=5, kappa=0.125, eps 2/80
   cavity   closed shell of 110 atoms around an empty core (exercises the cavity fill)
   p1hje    the reference's data/1hje.pqr (174 atoms) at h=0.75 A, p=4, kappa=0.1257
+  synth300 300-atom synthetic protein (seed 300,000), h=0.5 A, p=5, kappa=0.125, eps 2/80, leaf<=128:
+           the benchmark protein's settings at a size with a deep tree and a real X list
 
-Run here (where the reference sources are): python tests/golden/make_golden.py [case ...]
+Run where the reference sources are, naming their directory:
+  IBIM_REFERENCE=<reference source dir> python tests/golden/make_golden.py [case ...]
 """
 
 from __future__ import annotations
@@ -30,7 +33,8 @@ sys.path.insert(0, os.path.join(ROOT, "ibim-levelset_gb300"))
 import synth  # noqa: E402
 
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "ibim_ref")
-REF_DATA = "/root/reference/data"
+REF_DIR = os.environ.get("IBIM_REFERENCE", "")
+REF_DATA = os.path.join(REF_DIR, "data") if REF_DIR else ""
 NSAMPLE = 768
 
 
@@ -57,7 +61,10 @@ def cases():
     m = cavity_shell()
     out["cavity"] = dict(mol=m, geo=synth.padded_geometry(m, 0.5), thickness=2, np_=4, maxpoint=64,
                          kappa=0.1, dI=2.0, dE=80.0, solve=False, fmm=True, reinit_steps=20)
-    if os.path.exists(os.path.join(REF_DATA, "1hje.pqr")):
+    m = synth.synthetic_protein(300, 300_000)
+    out["synth300"] = dict(mol=m, geo=synth.padded_geometry(m, 0.5), thickness=2, np_=5, maxpoint=128,
+                           kappa=0.125, dI=2.0, dE=80.0, solve=True, fmm=True, reinit_steps=20)
+    if REF_DATA and os.path.exists(os.path.join(REF_DATA, "1hje.pqr")):
         m = synth.Molecule.from_pqr(os.path.join(REF_DATA, "1hje.pqr"))
         out["p1hje"] = dict(mol=m, geo=synth.padded_geometry(m, 0.75), thickness=2, np_=4, maxpoint=80,
                             kappa=0.1257, dI=1.0, dE=80.0, solve=True, fmm=True, reinit_steps=20)
@@ -159,7 +166,9 @@ def run_case(name, c):
 
 def main():
     if not os.path.exists(REF_BIN):
-        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+        if not REF_DIR:
+            sys.exit("set IBIM_REFERENCE to the reference's source directory")
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF_DIR}"], check=True)
     want = sys.argv[1:]
     for name, c in cases().items():
         if want and name not in want:

@@ -16,13 +16,14 @@ from conftest import ROOT
 
 LIB_DIR = os.path.join(ROOT, "ibim-levelset_gb300", "_build")
 SRC = os.path.join(ROOT, "tests", "cpp", "main_dropin.cpp")
+SRC_GMRES = os.path.join(ROOT, "tests", "cpp", "main_gmres.cpp")
 
 
-def compile_dropin(out_dir):
+def compile_dropin(out_dir, src=SRC):
     if not shutil.which("g++"):
         pytest.skip("no g++")
-    exe = os.path.join(out_dir, "main_dropin")
-    cmd = ["g++", "-std=c++14", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"), SRC, "-L", LIB_DIR,
+    exe = os.path.join(out_dir, os.path.splitext(os.path.basename(src))[0])
+    cmd = ["g++", "-std=c++14", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"), src, "-L", LIB_DIR,
            "-libim_gb300", f"-Wl,-rpath,{LIB_DIR}", "-o", exe]
     cuda_lib = "/usr/local/cuda/lib64"
     if os.path.isdir(cuda_lib):
@@ -35,6 +36,52 @@ def compile_dropin(out_dir):
 def test_dropin_compiles_and_links():
     with tempfile.TemporaryDirectory() as td:
         assert os.path.exists(compile_dropin(td))
+        assert os.path.exists(compile_dropin(td, SRC_GMRES))
+
+
+def write_cfg(td, G, extra=""):
+    import synth
+
+    P = G["params"]
+    pqr = os.path.join(td, "m.pqr")
+    synth.Molecule(G["centers"], G["charges"], G["radii"]).to_pqr(pqr)
+    n = max(P["n"])
+    lo = min(P["lo"])
+    cfg = os.path.join(td, "input.cfg")
+    with open(cfg, "w") as f:
+        f.write(f"pqr_file = {pqr}\nlo = {lo!r}\nh = {P['h']!r}\nn = {n}\nreinit_step = {P['reinit_t']!r}\n"
+                f"lvlset_thickness = {P['thickness']}\nlvlset_thres = {P['thres']}\nfmm_np = {P['np']}\n"
+                f"fmm_maxpoint = {P['maxpoint']}\nfmm_maxlevel = {P['maxlevel']}\ntau = {P['tau']}\n"
+                f"solvent_kappa = {P['kappa']!r}\nsolvent_dE = {P['dE']!r}\nsolvent_dI = {P['dI']!r}\n"
+                f"gmres_restart = {P['restart']}\ngmres_maxiter = {P['maxiter']}\ngmres_tol = {P['tol']}\n" + extra)
+    return cfg, n, lo
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["synth30", "p1hje"])
+def test_dropin_gmres_closure_reproduces_reference(golden, case):
+    """GMRES(FullMap, start, load, m, max_iter, tol) called as electric.cpp:415 calls it, with the
+    closure on the drop-in BIE operator and the fixture's own box: the reference's number of
+    operator applications (its GMRES applies the operator to x0 = 0 too) and its solution."""
+    G = golden(case)
+    P = G["params"]
+    with tempfile.TemporaryDirectory() as td:
+        exe = compile_dropin(td, SRC_GMRES)
+        out = os.path.join(td, "solution.bin")
+        box = "".join(f"n{a} = {P['n'][i]}\nlo{a} = {P['lo'][i]!r}\n" for i, a in enumerate("xyz"))
+        cfg, _, _ = write_cfg(td, G, f"out_file = {out}\n" + box)
+        r = subprocess.run([exe, cfg], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        vals = dict(ln.split()[:2] for ln in r.stdout.splitlines() if ln.startswith("DROPIN_"))
+        assert int(vals["DROPIN_GMRES_RC"]) == 0
+        N = len(G["surface"])
+        assert int(vals["DROPIN_POINTS"]) == N
+        assert int(vals["DROPIN_MATVECS"]) == int(P["scalars"]["REF_MATVECS"])
+        x = np.fromfile(out, dtype=np.float64)
+        assert x.shape == (2 * N,)
+        idx = G["sample_idx"]
+        xs = np.concatenate([x[idx], x[N + idx]])
+        assert np.abs(xs - G["solution_sample"]).max() / np.abs(G["solution_sample"]).max() < 1e-8
 
 
 @pytest.mark.gpu

@@ -115,3 +115,46 @@ def test_gmres_nonconvergence_reported(ctx, golden):
     cfg.maxiter = 2
     r = ctx.solve(G["centers"], G["charges"], G["radii"], cfg)
     assert r["gmres_status"] == 1 and r["gmres_iters"] == 2
+
+
+def test_born_gap_comes_from_points_on_split_planes(ctx, golden):
+    """The Born ion's whole-path energy differs from the reference's by ~3e-5 while its tube agrees
+    to 1e-9.  The octree splits at geometric centres of the points' bounding box (bbfmm.cpp:44-
+    108, `x < centre ? 0 : 1`), and the symmetric ion puts tube points on those planes, where a
+    1e-9 difference picks the other side.  Snapping only those points (and the six points that
+    fix the bounding box) to the reference's coordinates gives the reference's tree, and the
+    energy then agrees to 1e-6: the gap is confined to the split-plane points."""
+    G = golden("born")
+    P = G["params"]
+    cfg = config_for(P)
+    g, _ = ctx.levelset(G["centers"], G["radii"], cfg)
+    ours = g.surface(P["thickness"]).surface7()
+    g.close()
+    ref = G["surface"]
+    assert ours.shape == ref.shape
+    assert np.abs(ours - ref).max() < 1e-9
+    # split planes of the reference's tree: the centres of its internal nodes, per axis
+    internal = G["tree_leaf"] == 0
+    near = np.zeros(len(ref), bool)
+    for a in range(3):
+        planes = np.unique(G["tree_center"][internal, a])
+        k = np.clip(np.searchsorted(planes, ref[:, a]), 1, len(planes) - 1)
+        d = np.minimum(np.abs(ref[:, a] - planes[k - 1]), np.abs(ref[:, a] - planes[k]))
+        near |= d < 1e-7
+    for a in range(3):  # the points that fix the bounding box (the root's centre and radius)
+        near |= (ref[:, a] - ref[:, a].min() < 1e-7) | (ref[:, a].max() - ref[:, a] < 1e-7)
+    snapped = ours.copy()
+    snapped[near] = ref[near]
+    E = P["scalars"]["REF_ENERGY_RESTATED"]
+
+    def energy(s7):
+        t = ctx.tube(s7[:, :3], s7[:, 3:6], s7[:, 6], P["h"])
+        r = t.electric(G["centers"], G["charges"], cfg)
+        t.close()
+        return r["energy"]
+
+    e_ours, e_snap = energy(ours), energy(snapped)
+    # a few percent of the points carry the whole difference
+    assert near.sum() < 0.1 * len(ref), near.sum()
+    assert abs(e_snap - E) / abs(E) < 1e-6, (e_ours, e_snap, E)
+    assert abs(e_ours - E) / abs(E) < FULL_TOL["born"]
