@@ -97,7 +97,7 @@ static const KernelMap kKernelMap[16] = {
     {3, 1, -1.}, {3, 2, -1.}, {3, 3, -1.},                         // K4x K4y K4z: G = -K4 psi
 };
 
-static void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4) {
+void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4) {
     std::vector<double> h(4 * (size_t)std::max(1, natoms));
     for (int a = 0; a < natoms; ++a) {
         h[4 * a] = centers[3 * a];
@@ -110,7 +110,7 @@ static void atoms_to_device(Ctx *c, const double *centers, const double *charges
     IBIM_CUDA(cudaStreamSynchronize(c->stream));
 }
 
-static void check_config(const ibim_config &cfg) {
+void check_config(const ibim_config &cfg) {
     IBIM_REQUIRE(cfg.h > 0, "h must be positive");
     IBIM_REQUIRE(cfg.n[0] > 0 && cfg.n[1] > 0 && cfg.n[2] > 0, "grid size must be positive");
     IBIM_REQUIRE(cfg.thickness > 0, "lvlset_thickness must be positive");
@@ -126,7 +126,7 @@ static void check_config(const ibim_config &cfg) {
     IBIM_REQUIRE(cfg.kp.k3_scaled == 0 || cfg.kp.k3_scaled == 1, "k3_scaled must be 0 or 1");
 }
 
-static void fill_plan_stats(const Plan &P, ibim_result &res) {
+void fill_plan_stats(const Plan &P, ibim_result &res) {
     const TargetSet &S = *P.targets[0];
     res.fmm_nodes = P.tree.nnodes;
     res.fmm_v_pairs = S.nv_list;
@@ -160,9 +160,11 @@ static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *
     return g;
 }
 
-static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
-                       const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
-                       const double *atoms4_dev) {
+// main.cpp:45-64 and electric.cpp:9-60 up to the solve: level set, surface, right-hand side (in
+// tube order), plan, operators and their images, and the area.
+void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
+                   const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
+                   const double *atoms4_dev, SolvePrep &out) {
     check_config(cfg);
     IBIM_REQUIRE(natoms > 0, "need at least one atom");
     std::memset(&res, 0, sizeof(res));
@@ -174,36 +176,35 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
     res.grid_cells = (long)cfg.n[0] * cfg.n[1] * cfg.n[2];
     res.levelset_stages = 3 * ((int)(cfg.probe / (0.2 * cfg.h)) + 1 + res.reinit_steps[0] + res.reinit_steps[1]);
     Timer t1(s);
-    Tube *tube = nullptr;
     try {
-        tube = surface_extract(*g, cfg.thickness, &res.inclusion, cfg.jacobian != 0);
+        out.tube = surface_extract(*g, cfg.thickness, &res.inclusion, cfg.jacobian != 0);
     } catch (...) {
         delete g;
         throw;
     }
     delete g;
+    Tube *tube = out.tube;
     res.n_points = tube->n;
     res.t_surface_ms = t1.ms();
     trace_mark("solve: level set + surface");
     IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
-    Plan *P = nullptr;
-    DevBuf<double> a4, b_tube;
     try {
-        const double *atoms4 = atoms4_dev;
-        if (!atoms4) {
-            atoms_to_device(c, centers_host, charges_host, natoms, a4);
-            atoms4 = a4.ptr;
+        out.atoms4 = atoms4_dev;
+        if (!out.atoms4) {
+            atoms_to_device(c, centers_host, charges_host, natoms, out.a4);
+            out.atoms4 = out.a4.ptr;
         }
         // the right-hand side needs only the tube and the atoms: it runs on the second stream
         // while the host builds the octree and its lists
-        b_tube.alloc(2 * (size_t)tube->n, s);
+        out.b_tube.alloc(2 * (size_t)tube->n, s);
         IBIM_CUDA(cudaEventRecord(c->ev_fork, s));
         IBIM_CUDA(cudaStreamWaitEvent(c->aux, c->ev_fork, 0));
-        bie_rhs_tube(*tube, cfg.kp, atoms4, natoms, b_tube.ptr, c->aux, cfg.precision);
+        bie_rhs_tube(*tube, cfg.kp, out.atoms4, natoms, out.b_tube.ptr, c->aux, cfg.precision);
         IBIM_CUDA(cudaEventRecord(c->ev_join, c->aux));
         trace_mark("solve: atoms, rhs enqueued");
         auto w0 = std::chrono::steady_clock::now();
-        P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
+        out.P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
+        Plan *P = out.P;
         IBIM_CUDA(cudaStreamSynchronize(s));
         const auto w1 = std::chrono::steady_clock::now();
         res.t_tree_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
@@ -246,18 +247,22 @@ static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_de
         double area = 0.;
         for (long i = 0; i < tube->n; ++i) area += w[i];
         res.area = area;
-        electric_solve(*P, cfg.kp, atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol, cfg.precision,
-                       nullptr, nullptr, res, b_tube.ptr);
         fill_plan_stats(*P, res);
-        trace_mark("solve: electric done");
     } catch (...) {
         cudaStreamSynchronize(c->aux);  // the right-hand side may still read the tube and atoms
-        delete P;
-        delete tube;
         throw;
     }
-    delete P;
-    delete tube;
+}
+
+static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
+                       const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
+                       const double *atoms4_dev) {
+    SolvePrep prep;
+    solve_prepare(c, centers_dev, radii_dev, centers_host, charges_host, natoms, cfg, res, atoms4_dev, prep);
+    electric_solve(*prep.P, cfg.kp, prep.atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol,
+                   cfg.precision, nullptr, nullptr, res, prep.b_tube.ptr);
+    fill_plan_stats(*prep.P, res);
+    trace_mark("solve: electric done");
 }
 
 // Serialise a tree in the reference's node numbering (see ibim_plan_lists).
@@ -991,6 +996,20 @@ int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charge
         IBIM_CUDA(cudaMemcpyAsync(hq.data(), charges_dev, sizeof(double) * natoms, cudaMemcpyDeviceToHost, c->stream));
         IBIM_CUDA(cudaStreamSynchronize(c->stream));
         solve_impl(c, centers_dev, radii_dev, hc.data(), hq.data(), natoms, *cfg, *res, nullptr);
+    });
+}
+
+int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
+                     const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
+                     ibim_result *results, int *statuses, double *info) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx, "null context");
+        Ctx *c = &ctx->c;
+        bind(c);
+        batch_solve(c, nmol, natoms, centers, charges, radii, cfgs, max_wave, hbm_budget_bytes, workers, results,
+                    statuses, info);
+        for (int i = 0; i < nmol; ++i)
+            if (statuses[i] != IBIM_OK) throw Error(statuses[i], ibim_last_error());
     });
 }
 

@@ -448,6 +448,9 @@ __device__ __forceinline__ float exp2_ftz(float x) {
 // in the target leaf's frame (two 16-byte loads per source record); per-tile partial sums are
 // added with Kahan compensation.
 constexpr int NT32 = 128, TILE32 = 256;
+// BATCH: a plan merged over several molecules (batch.cu); the kappa-dependent constants come from
+// the target leaf's molecule (kmol: kappa, -kappa log2 e, k2in / q4pi per molecule).
+template <bool BATCH>
 __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict__ tab, KParams32 kp,
                                                  const int4 *__restrict__ segs,
                                                  const int *__restrict__ nrange, const float *__restrict__ noff,
@@ -459,7 +462,8 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                                                  int nseg, int *next, const double *__restrict__ sx64,
                                                  const double *__restrict__ sy64, const double *__restrict__ sz64,
                                                  const double *__restrict__ tx64, const double *__restrict__ ty64,
-                                                 const double *__restrict__ tz64) {
+                                                 const double *__restrict__ tz64, const float4 *__restrict__ kmol,
+                                                 const int *__restrict__ node_mol) {
     __shared__ ChebTables32 T;
     // {x, y, z, q m_x}, {q m_y, q m_z, q psi, source index} in the target leaf's frame
     __shared__ float4 S4[TILE32][2];
@@ -483,6 +487,13 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
         const int4 sg = segs[si];
         const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
         const int tb = tb_[leaf], te = te_[leaf];
+        float kap = kp.kappa, kl2 = kp.kappa_l2, k2q = kp.k2in_q;
+        if (BATCH) {
+            const float4 km = kmol[node_mol[leaf]];
+            kap = km.x;
+            kl2 = km.y;
+            k2q = km.z;
+        }
         __syncthreads();
         for (int t0 = tb; t0 < te; t0 += NT32) {
             const int nT = min(NT32, te - t0);
@@ -540,11 +551,11 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                             inside = ex * ex + ey * ey + ez * ez < kp.vr2_64;
                         }
                         if (inside) {
-                            a0 = fmaf(-kp.k2in_q, P1.z, a0);
+                            a0 = fmaf(-k2q, P1.z, a0);
                             continue;
                         }
                         const float ir = rsqrt_ftz(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
-                        const float t = kp.kappa * r, e = exp2_ftz(kp.kappa_l2 * r), et1 = fmaf(e, t, e);
+                        const float t = kap * r, e = exp2_ftz(kl2 * r), et1 = fmaf(e, t, e);
                         const float h3 = ir3 * kp.k3q;
                         const float c1 = fmaf(kp.eps, et1, -1.f) * ir3;
                         const float c4 = fmaf(-kp.ieps, et1, 1.f) * ir3;
@@ -910,16 +921,17 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
     // launch after the far field
     auto near = [&](cudaStream_t st, int l2p_mask, int grid, int *next, double flops) {
         ProfScope ps_(PROF_NEAR, flops, flops > 0 ? 28.0 * P.ns + 40.0 * S.nt : 0., st);
-        (count_launch(), k_near32<<<grid, NT32, 0, st>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr),
-                                                      S.near32_range.ptr, S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr,
-                                                      P.nrad32.ptr, P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out,
-                                                      l2p_mask, S.nnear32_seg, next, P.sx.ptr, P.sy.ptr, P.sz.ptr,
-                                                      tx64, ty64, tz64));
+        auto kern = P.batched ? k_near32<true> : k_near32<false>;
+        (count_launch(), kern<<<grid, NT32, 0, st>>>(tab, k32, reinterpret_cast<const int4 *>(S.near32_seg.ptr),
+                                                  S.near32_range.ptr, S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr,
+                                                  P.nrad32.ptr, P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out,
+                                                  l2p_mask, S.nnear32_seg, next, P.sx.ptr, P.sy.ptr, P.sz.ptr,
+                                                  tx64, ty64, tz64, P.kmol32.ptr, P.node_mol.ptr));
     };
     const bool overlap = near_overlap() && S.ntleaves > 0;
     static const int occ = [] {
         int b = 0;
-        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near32, NT32, 0));
+        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near32<false>, NT32, 0));
         return std::max(1, b);
     }();
     const int full = occ * c->num_sms, side = near_side_ctas() > 0 ? near_side_ctas() * c->num_sms : full;

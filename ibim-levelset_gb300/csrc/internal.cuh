@@ -318,6 +318,12 @@ struct Plan {
     DevBuf<double> oz_sig, oz_tau;
     double kp64[5] = {-1, -1, -1, -1, -1}, kp32[5] = {-1, -1, -1, -1, -1};  // kernel parameters of the cached operators
     bool ops64_ready = false, ops32_ready = false;
+    // a plan merged over several molecules (batch.cu): the molecule of every node and each
+    // molecule's kappa-dependent near-field constants (FP32: kappa, -kappa log2 e, k2in / q4pi;
+    // float-float: kappa hi, lo, k2in hi, lo)
+    bool batched = false;
+    DevBuf<int> node_mol;
+    DevBuf<float4> kmol32, kmolff;
     ~Plan() { for (auto *t : targets) delete t; }
 };
 

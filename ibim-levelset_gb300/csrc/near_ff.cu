@@ -78,8 +78,16 @@ __device__ __forceinline__ f2 exp_neg(f2 t, const float2 *E0, const float2 *E1) 
 
 // Radial factors of the 16 kernels at squared distance d2 (radial64 in float-float): c1 (K1),
 // c4 (K4), k2 (K2), hd and ho (K3: hd delta_ab + ho d_a d_b); false inside the cutoff r < tau h.
-__device__ __forceinline__ bool radial_ff(const KParamsFF &k, const float2 *E0, const float2 *E1, f2 d2, f2 &c1,
-                                          f2 &c4, f2 &k2, f2 &hd, f2 &ho) {
+// kap: kappa in float-float and whether it is non-zero (the plan's, or the molecule's in a batch)
+struct KapFF {
+    f2 kappa, k2in;
+    bool yukawa;
+};
+
+__device__ __forceinline__ KapFF kap_of(const KParamsFF &k) { return {ld(k.kappa), ld(k.k2in), k.yukawa != 0}; }
+
+__device__ __forceinline__ bool radial_ff(const KParamsFF &k, const KapFF &kap, const float2 *E0, const float2 *E1,
+                                          f2 d2, f2 &c1, f2 &c4, f2 &k2, f2 &hd, f2 &ho) {
     if (d2.h < k.vr2.x || (d2.h == k.vr2.x && d2.l < k.vr2.y)) return false;
     // 1/sqrt(d2): FP32 estimate y, then y (1 + e/2 + 3e^2/8) with e = 1 - d2 y^2 from exact products
     const float y = rsqrtf(d2.h);
@@ -90,8 +98,8 @@ __device__ __forceinline__ bool radial_ff(const KParamsFF &k, const float2 *E0, 
     const f2 ir = quick_two_sum(y, __fmul_rn(y, __fmaf_rn(__fmul_rn(0.375f, e), e, __fmul_rn(0.5f, e))));
     const f2 r = mul(d2, ir), ir2 = sqr(ir), ir3 = mul(ir2, ir);
     f2 E = {1.f, 0.f}, t = {0.f, 0.f};
-    if (k.yukawa) {
-        t = mul(ld(k.kappa), r);
+    if (kap.yukawa) {
+        t = mul(kap.kappa, r);
         E = exp_neg(t, E0, E1);
     }
     const f2 et1 = mul(E, addf(t, 1.f));
@@ -106,12 +114,12 @@ __device__ __forceinline__ bool radial_ff(const KParamsFF &k, const float2 *E0, 
 
 // One source -> target update of the fused 4x4 block, the formulas of near_pair64
 // (electric.cpp:67-291) in float-float; d = source - target.
-__device__ __forceinline__ void pair_ff(const KParamsFF &k, const float2 *E0, const float2 *E1, f2 dx, f2 dy, f2 dz,
-                                        f2 m0, f2 m1, f2 m2, f2 psi, f2 acc[4]) {
+__device__ __forceinline__ void pair_ff(const KParamsFF &k, const KapFF &kap, const float2 *E0, const float2 *E1, f2 dx,
+                                        f2 dy, f2 dz, f2 m0, f2 m1, f2 m2, f2 psi, f2 acc[4]) {
     const f2 d2 = add(add(sqr(dx), sqr(dy)), sqr(dz));
     f2 c1, c4, k2, hd, ho;
-    if (!radial_ff(k, E0, E1, d2, c1, c4, k2, hd, ho)) {
-        acc[0] = sub(acc[0], mul(ld(k.k2in), psi));
+    if (!radial_ff(k, kap, E0, E1, d2, c1, c4, k2, hd, ho)) {
+        acc[0] = sub(acc[0], mul(kap.k2in, psi));
         return;
     }
     const f2 dm = add(add(mul(dx, m0), mul(dy, m1)), mul(dz, m2));
@@ -148,6 +156,9 @@ __global__ void k_pack_src_ff(long ns, const double *__restrict__ dens, const fl
 // ranges of the FP32 near lists; with a work counter the CTA takes segments until none is left, else it does segment
 // blockIdx.x.  Threads = targets x source phases as in the FP32 kernel.
 constexpr int NTF = 128, TILEF = 128;
+// BATCH: a plan merged over several molecules (batch.cu); kappa and the inner K2 constant come from
+// the target leaf's molecule (kmol: kappa hi, lo, k2in hi, lo per molecule).
+template <bool BATCH>
 __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__restrict__ segs, int nseg, int *next,
                                                  const int *__restrict__ nrange, const float *__restrict__ noff,
                                                  const float *__restrict__ noffl, const int *__restrict__ tb_,
@@ -155,7 +166,8 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
                                                  const float *__restrict__ txh, const float *__restrict__ tyh,
                                                  const float *__restrict__ tzh, const float *__restrict__ txl,
                                                  const float *__restrict__ tyl, const float *__restrict__ tzl, long nt,
-                                                 double *out) {
+                                                 double *out, const float4 *__restrict__ kmol,
+                                                 const int *__restrict__ node_mol) {
     __shared__ float S[14][TILEF];
     __shared__ double red[NTF][4];
     __shared__ float2 E0[64], E1[64];
@@ -179,6 +191,11 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
         const int4 sg = segs[si];
         const int leaf = sg.x, r0 = sg.y, r1 = sg.z, mode = sg.w;
         const int tb = tb_[leaf], te = te_[leaf];
+        KapFF kap = kap_of(kp);
+        if (BATCH) {
+            const float4 km = kmol[node_mol[leaf]];
+            kap = {{km.x, km.y}, {km.z, km.w}, km.x != 0.f};
+        }
         __syncthreads();
         for (int t0 = tb; t0 < te; t0 += NTF) {
             const int nT = min(NTF, te - t0);
@@ -235,7 +252,7 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
                 __syncthreads();
                 if (active)
                     for (int q = ph; q < filled; q += nph)
-                        pair_ff(kp, E0, E1, sub({S[0][q], S[1][q]}, X), sub({S[2][q], S[3][q]}, Y),
+                        pair_ff(kp, kap, E0, E1, sub({S[0][q], S[1][q]}, X), sub({S[2][q], S[3][q]}, Y),
                                 sub({S[4][q], S[5][q]}, Z), {S[6][q], S[7][q]}, {S[8][q], S[9][q]},
                                 {S[10][q], S[11][q]}, {S[12][q], S[13][q]}, acc);
             }
@@ -295,7 +312,7 @@ __global__ void __launch_bounds__(256) k_make_ops_ff(KParamsFF kp, const ChebTab
     for (int q = 0; q < 16; ++q) b[q] = {0.f, 0.f};
     const f2 d2 = add(add(sqr(d[0]), sqr(d[1])), sqr(d[2]));
     f2 c1, c4, k2, hd, ho;
-    if (radial_ff(kp, E0, E1, d2, c1, c4, k2, hd, ho)) {
+    if (radial_ff(kp, kap_of(kp), E0, E1, d2, c1, c4, k2, hd, ho)) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             b[a] = mul(d[a], c1);
@@ -354,7 +371,7 @@ bool near_ff_enabled() {
 int near_ff_occupancy() {
     static const int occ = [] {
         int b = 0;
-        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near_ff, NTF, 0));
+        IBIM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_near_ff<false>, NTF, 0));
         return std::max(1, b);
     }();
     return occ;
@@ -401,10 +418,11 @@ void near_ff_run(Plan &P, const TargetSet &S, const KParamsFF &kp, double *out, 
                 *zh = S.self ? P.szf.ptr : S.tzf.ptr;
     const float *xl = S.self ? P.sxl.ptr : S.txl.ptr, *yl = S.self ? P.syl.ptr : S.tyl.ptr,
                 *zl = S.self ? P.szl.ptr : S.tzl.ptr;
-    (count_launch(), k_near_ff<<<grid, NTF, 0, st>>>(kp, reinterpret_cast<const int4 *>(S.nearff_seg.ptr),
-                                                     S.nnearff_seg, next, S.near32_range.ptr, S.near32_off.ptr,
-                                                     S.near32_offl.ptr, S.tbeg.ptr, S.tend.ptr, P.src16.ptr, xh, yh, zh,
-                                                     xl, yl, zl, S.nt, out));
+    auto kern = P.batched ? k_near_ff<true> : k_near_ff<false>;
+    (count_launch(), kern<<<grid, NTF, 0, st>>>(kp, reinterpret_cast<const int4 *>(S.nearff_seg.ptr), S.nnearff_seg,
+                                                next, S.near32_range.ptr, S.near32_off.ptr, S.near32_offl.ptr,
+                                                S.tbeg.ptr, S.tend.ptr, P.src16.ptr, xh, yh, zh, xl, yl, zl, S.nt, out,
+                                                P.kmolff.ptr, P.node_mol.ptr));
     IBIM_CHECK_LAUNCH();
 }
 

@@ -261,6 +261,13 @@ void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *
     IBIM_CHECK_LAUNCH();
 }
 
+void bie_densities(Plan &P, const double *x, double *dens4) {
+    const long n = P.ns;
+    (count_launch(), k_densities<<<ew_grid(P.ctx, n), 256, 0, P.ctx->stream>>>(n, x, P.snx.ptr, P.sny.ptr, P.snz.ptr,
+                                                                               P.sw.ptr, dens4));
+    IBIM_CHECK_LAUNCH();
+}
+
 static void rhs_launch(Ctx *c, long n, const double *x, const double *y, const double *z, const double *nx,
                        const double *ny, const double *nz, const ibim_kernel_params &kp, const double *atoms4_dev,
                        int natoms, double *b, cudaStream_t st, bool fp32) {

@@ -30,6 +30,8 @@ struct Krylov {
 
 void permute(Ctx *c, long n, const int *perm, const double *in, double *out, bool scatter);
 void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision);
+// The four densities of dmapping (electric.cpp:324-329) from x (2 ns, tree order) into dens4.
+void bie_densities(Plan &P, const double *x, double *dens4);
 // load (electric.cpp:395-412) in tree order; FP32 with compensated sums on a mixed plan.
 void bie_rhs(Plan &P, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b);
 // b_tube: the right-hand side already computed in tube order (bie_rhs_tube), or null to compute
@@ -41,5 +43,31 @@ void electric_solve(Plan &P, const ibim_kernel_params &kp, const double *atoms4_
 // compensated sums when precision is IBIM_PRECISION_MIXED.
 void bie_rhs_tube(const Tube &t, const ibim_kernel_params &kp, const double *atoms4_dev, int natoms, double *b,
                   cudaStream_t st, int precision);
+
+// The part of a whole solve before GMRES (capi.cu): the tube, its plan with operators and
+// images, and the right-hand side in tube order (b_tube) from the atoms (atoms4: x, y, z, q).
+struct SolvePrep {
+    Tube *tube = nullptr;
+    Plan *P = nullptr;
+    DevBuf<double> a4, b_tube;
+    const double *atoms4 = nullptr;
+    SolvePrep() = default;
+    SolvePrep(const SolvePrep &) = delete;
+    ~SolvePrep() {
+        if (P) cudaStreamSynchronize(P->ctx->aux);  // a failed solve may leave near-field work there
+        delete P;
+        delete tube;
+    }
+};
+void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
+                   const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
+                   const double *atoms4_dev, SolvePrep &out);
+void check_config(const ibim_config &cfg);
+void fill_plan_stats(const Plan &P, ibim_result &res);
+void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4);
+// Many molecules in lock-step waves (batch.cu; the C ABI's ibim_batch_solve).
+void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
+                 const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
+                 ibim_result *results, int *statuses, double *info);
 
 }  // namespace ibim

@@ -51,7 +51,7 @@ EXPORTS = [
     "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
     "ibim_levelset_evolve_static", "ibim_server_create", "ibim_server_destroy", "ibim_server_submit",
     "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate", "ibim_gmres_host",
-    "ibim_grid_set_geometry",
+    "ibim_grid_set_geometry", "ibim_batch_solve",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
@@ -123,6 +123,8 @@ def lib():
         "ibim_grid_download": ([_vp, _dp], C.c_int),
         "ibim_grid_scale": ([_vp, C.c_double], C.c_int),
         "ibim_grid_set_geometry": ([_vp, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
+        "ibim_batch_solve": ([_vp, C.c_int, _ip, _dp, _dp, _dp, C.POINTER(Config), C.c_int, C.c_double, C.c_int,
+                              C.POINTER(Result), _ip, _dp], C.c_int),
         "ibim_grid_copy": ([_vp, _vp], C.c_int),
         "ibim_levelset_expand": ([_vp, _dp, _dp, C.c_int, C.c_double, C.c_int], C.c_int),
         "ibim_levelset_evolve": ([_vp, C.c_double, C.c_double, C.c_double], C.c_int),
@@ -290,6 +292,26 @@ class Context:
             raise err[0]
         _check(rc)
         return x, dict(iters=it.value, matvecs=mv.value, status=st.value, residual=res.value)
+
+    def batch_solve(self, molecules, cfgs, max_wave=32, hbm_budget_bytes=150e9, workers=4, check=True):
+        """Many molecules in lock-step waves (ibim_batch_solve).  molecules: list of (centers, charges,
+        radii); cfgs: one Config per molecule.  Returns (results, statuses, info)."""
+        n = len(molecules)
+        na = np.array([len(np.asarray(q)) for _, q, _ in molecules], dtype=np.int32)
+        cen = _c(np.concatenate([np.asarray(c, dtype=np.float64).reshape(-1, 3) for c, _, _ in molecules]))
+        chg = _c(np.concatenate([np.asarray(q, dtype=np.float64).ravel() for _, q, _ in molecules]))
+        rad = _c(np.concatenate([np.asarray(r, dtype=np.float64).ravel() for _, _, r in molecules]))
+        carr = (Config * n)(*cfgs)
+        res = (Result * n)()
+        st = np.zeros(n, dtype=np.int32)
+        info = np.zeros(6)
+        rc = lib().ibim_batch_solve(self.h, n, na.ctypes.data_as(_ip), _p(cen), _p(chg), _p(rad), carr, max_wave,
+                                    hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(info))
+        if check:
+            _check(rc)
+        keys = ["waves", "largest_wave", "peak_bytes", "merged_mixed_matvecs", "merged_fp64_matvecs",
+                "active_fraction"]
+        return [r.as_dict() for r in res], st.tolist(), dict(zip(keys, info.tolist()))
 
     def grid(self, n, lo, h, value=0.0) -> "Grid":
         g = _vp()

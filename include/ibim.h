@@ -263,6 +263,27 @@ int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charge
 /* PQR file (molecule.h:21-50: ATOM lines, tokens 5..9 = x y z q r). */
 int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, ibim_result *res);
 
+/* ---- many molecules in one launch per FMM stage (no counterpart in the reference: main.cpp solves
+ * one molecule per run; the operator batched is dmapping, electric.cpp:294-388) ----
+ * Solves nmol molecules on the mixed-precision path.  Worker threads (`workers`, each with its own
+ * context) prepare molecules in order (level set, tube, right-hand side, plan, operator images)
+ * while the device bytes of prepared molecules stay within hbm_budget_bytes (<= 0: 150e9).  Up to
+ * max_wave prepared molecules form a wave: their plans are merged into one (sources, nodes,
+ * operators, pairs and near-field work concatenated), so each FMM stage of a matvec is one launch
+ * over the wave, and GMRES advances every molecule of the wave in lock-step (one merged matvec per
+ * Arnoldi step, one host synchronisation per step for all molecules' Givens rotations), inside
+ * the FP64 iterative refinement of IBIM_PRECISION_MIXED with one merged FP64-class residual per
+ * pass.  Molecules must share h, fmm_np, eps_in/eps_out, tau, k3_scaled, restart and jacobian;
+ * kappa, geometry, atoms and tolerances may differ; precision must be IBIM_PRECISION_MIXED.
+ * Atoms of molecule i are rows aoff_i .. aoff_i + natoms[i] - 1 of centers (n, 3), charges and
+ * radii, aoff_i = natoms[0] + ... + natoms[i-1].  results[i] and statuses[i] per molecule; the
+ * call returns the first failing molecule's status (others still solved).  info (may be NULL,
+ * 6 doubles): waves, largest wave, peak budgeted bytes, merged mixed matvecs, merged FP64-class
+ * matvecs, mean fraction of a wave's molecules still iterating per merged matvec. */
+int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
+                     const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
+                     ibim_result *results, int *statuses, double *info);
+
 /* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
  * Solve requests queue in arrival order; `slots` worker threads, each with its own context and
  * stream, take the head of the queue while the estimated device footprints of the requests in

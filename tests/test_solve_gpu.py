@@ -123,7 +123,7 @@ def test_born_gap_comes_from_points_on_split_planes(ctx, golden):
     108, `x < centre ? 0 : 1`), and the symmetric ion puts tube points on those planes, where a
     1e-9 difference picks the other side.  Snapping only those points (and the six points that
     fix the bounding box) to the reference's coordinates gives the reference's tree, and the
-    energy then agrees to 1e-6: the gap is confined to the split-plane points."""
+    energy then agrees to 1e-6: the gap comes only from the split-plane points."""
     G = golden("born")
     P = G["params"]
     cfg = config_for(P)
@@ -154,7 +154,8 @@ def test_born_gap_comes_from_points_on_split_planes(ctx, golden):
         return r["energy"]
 
     e_ours, e_snap = energy(ours), energy(snapped)
-    # a few percent of the points carry the whole difference
-    assert near.sum() < 0.1 * len(ref), near.sum()
-    assert abs(e_snap - E) / abs(E) < 1e-6, (e_ours, e_snap, E)
+    assert abs(e_snap - E) / abs(E) < 1e-6, (e_ours, e_snap, E, int(near.sum()))
     assert abs(e_ours - E) / abs(E) < FULL_TOL["born"]
+    # the ion's tube points come from lattice points, so whole grid lines lie on the planes: about
+    # an eighth of the points are within 1e-7 of one, the rest land where the reference puts them
+    assert near.sum() < 0.2 * len(ref), near.sum()
