@@ -958,7 +958,11 @@ double estimate_request_bytes(const ibim_config &cfg);
 
 void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
                  const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
-                 ibim_result *results, int *statuses, double *info) {
+                 ibim_result *results, int *statuses, double *done_ms, double *info) {
+    const auto t_call = std::chrono::steady_clock::now();
+    auto since_call = [&] {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
+    };
     IBIM_REQUIRE(nmol > 0 && natoms && centers && charges && radii && cfgs && results && statuses, "null argument");
     const ibim_config &C0 = cfgs[0];
     for (int i = 0; i < nmol; ++i) {
@@ -982,6 +986,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     for (int i = 0; i < nmol; ++i) {
         statuses[i] = IBIM_OK;
         std::memset(&results[i], 0, sizeof(ibim_result));
+        if (done_ms) done_ms[i] = 0.;
     }
     struct Job {
         std::unique_ptr<SolvePrep> prep;
@@ -1073,6 +1078,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 std::lock_guard<std::mutex> lk(mu);
                 statuses[i] = st;
                 J.err = err;
+                if (st != IBIM_OK && done_ms) done_ms[i] = since_call();
                 held_bytes += J.bytes - J.est;
                 if (st != IBIM_OK) held--;
                 peak_bytes = std::max(peak_bytes, held_bytes);
@@ -1138,6 +1144,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 wst = IBIM_ERR_INVALID_ARGUMENT;
                 werr = e.what();
             }
+            const double t_wave_done = since_call();
             for (auto &b : bm) {
                 delete b.prep;
                 delete b.b_tree;
@@ -1145,6 +1152,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                     statuses[b.index] = wst;
                     jobs[b.index].err = werr;
                 }
+                if (done_ms) done_ms[b.index] = t_wave_done;
             }
             waves++;
             largest = std::max(largest, (int)wave.size());

@@ -68,6 +68,6 @@ void atoms_to_device(Ctx *c, const double *centers, const double *charges, int n
 // Many molecules in lock-step waves (batch.cu; the C ABI's ibim_batch_solve).
 void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
                  const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
-                 ibim_result *results, int *statuses, double *info);
+                 ibim_result *results, int *statuses, double *done_ms, double *info);
 
 }  // namespace ibim

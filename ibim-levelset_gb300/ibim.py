@@ -124,7 +124,7 @@ def lib():
         "ibim_grid_scale": ([_vp, C.c_double], C.c_int),
         "ibim_grid_set_geometry": ([_vp, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
         "ibim_batch_solve": ([_vp, C.c_int, _ip, _dp, _dp, _dp, C.POINTER(Config), C.c_int, C.c_double, C.c_int,
-                              C.POINTER(Result), _ip, _dp], C.c_int),
+                              C.POINTER(Result), _ip, _dp, _dp], C.c_int),
         "ibim_grid_copy": ([_vp, _vp], C.c_int),
         "ibim_levelset_expand": ([_vp, _dp, _dp, C.c_int, C.c_double, C.c_int], C.c_int),
         "ibim_levelset_evolve": ([_vp, C.c_double, C.c_double, C.c_double], C.c_int),
@@ -304,14 +304,18 @@ class Context:
         carr = (Config * n)(*cfgs)
         res = (Result * n)()
         st = np.zeros(n, dtype=np.int32)
+        done = np.zeros(n)
         info = np.zeros(6)
         rc = lib().ibim_batch_solve(self.h, n, na.ctypes.data_as(_ip), _p(cen), _p(chg), _p(rad), carr, max_wave,
-                                    hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(info))
+                                    hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(done), _p(info))
         if check:
             _check(rc)
         keys = ["waves", "largest_wave", "peak_bytes", "merged_mixed_matvecs", "merged_fp64_matvecs",
                 "active_fraction"]
-        return [r.as_dict() for r in res], st.tolist(), dict(zip(keys, info.tolist()))
+        out = [r.as_dict() for r in res]
+        for r, t in zip(out, done.tolist()):
+            r["done_ms"] = t
+        return out, st.tolist(), dict(zip(keys, info.tolist()))
 
     def grid(self, n, lo, h, value=0.0) -> "Grid":
         g = _vp()

@@ -277,12 +277,14 @@ int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, i
  * kappa, geometry, atoms and tolerances may differ; precision must be IBIM_PRECISION_MIXED.
  * Atoms of molecule i are rows aoff_i .. aoff_i + natoms[i] - 1 of centers (n, 3), charges and
  * radii, aoff_i = natoms[0] + ... + natoms[i-1].  results[i] and statuses[i] per molecule; the
- * call returns the first failing molecule's status (others still solved).  info (may be NULL,
- * 6 doubles): waves, largest wave, peak budgeted bytes, merged mixed matvecs, merged FP64-class
- * matvecs, mean fraction of a wave's molecules still iterating per merged matvec. */
+ * call returns the first failing molecule's status (others still solved).  done_ms (may be NULL)
+ * receives when each molecule's result was final, in ms since the call began (its latency when
+ * all are submitted at once).  info (may be NULL, 6 doubles): waves, largest wave, peak budgeted
+ * bytes, merged mixed matvecs, merged FP64-class matvecs, mean fraction of a wave's molecules
+ * still iterating per merged matvec. */
 int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
                      const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
-                     ibim_result *results, int *statuses, double *info);
+                     ibim_result *results, int *statuses, double *done_ms, double *info);
 
 /* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
  * Solve requests queue in arrival order; `slots` worker threads, each with its own context and

@@ -9,7 +9,7 @@ import oracle as O
 from test_oracle_golden import KD, bie_densities, fused_to_reference, probe_vector
 
 pytestmark = pytest.mark.gpu
-CASES = ["born", "synth30", "p1hje"]
+CASES = ["born", "synth30", "p1hje", "synth300"]
 
 
 def tube_of(ctx, G):

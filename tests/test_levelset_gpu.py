@@ -7,7 +7,7 @@ import oracle as O
 from conftest import config_for, grid_stats
 
 pytestmark = pytest.mark.gpu
-CASES = ["born", "synth30", "cavity", "p1hje"]
+CASES = ["born", "synth30", "cavity", "p1hje", "synth300"]
 
 
 @pytest.mark.parametrize("case", CASES)

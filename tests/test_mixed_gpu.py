@@ -49,7 +49,7 @@ def test_mixed_atom_targets(ctx, golden):
     assert np.abs(a - b).max() / np.abs(a).max() < 2e-5
 
 
-@pytest.mark.parametrize("case", ["born", "synth30", "p1hje"])
+@pytest.mark.parametrize("case", ["born", "synth30", "p1hje", "synth300"])
 def test_mixed_energy_within_1e4_of_fp64(ctx, golden, case):
     G = golden(case)
     P = G["params"]

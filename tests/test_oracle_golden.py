@@ -7,7 +7,7 @@ import pytest
 import oracle as O
 from conftest import grid_stats
 
-LS_CASES = ["born", "synth30", "cavity", "p1hje"]
+LS_CASES = ["born", "synth30", "cavity", "p1hje", "synth300"]
 KD = [0, 1, 2, 3, 0, 1, 2, 0, 1, 2, 1, 2, 0, 3, 3, 3]
 K3F1 = [0, 1, 2, 0, 1, 2, 0, 1, 2]
 K3F2 = [0, 1, 2, 1, 2, 0, 1, 2, 0]
@@ -92,6 +92,43 @@ def test_fmm_16_kernels(golden, case):
         err = np.abs(v[idx] - G["fmm16_sample"][k]).max() / G["fmm16_absmax"][k]
         assert err < 1e-12, (k, err)
     assert np.all(np.isfinite(full))
+
+
+def fused_field_of_reference(G, f):
+    """Field f of the fused FMM with all four densities set, as the signed sum of the reference's
+    16 single-kernel FMM samples (F = K1 m - K2 psi, G_a = sum_b K3ab m_b - K4a psi)."""
+    total = np.zeros(G["fmm16_sample"].shape[1])
+    for k in range(16):
+        if k <= 2:
+            fk, sg = 0, 1.0
+        elif k == 3:
+            fk, sg = 0, -1.0
+        elif k >= 13:
+            fk, sg = 1 + k - 13, -1.0
+        else:
+            b = KD[k]
+            a = K3F1[k - 4] if K3F2[k - 4] == b else K3F2[k - 4]
+            fk, sg = 1 + a, 1.0
+        if fk == f:
+            total += sg * G["fmm16_sample"][k]
+    return total
+
+
+def test_fused_fmm_on_benchmark_shaped_protein(golden):
+    """One fused FMM of the oracle on the 300-atom protein (p = 5, leaf 128, kappa 0.125, six tree
+    levels, an X list) against the sums of the reference's 16 single-kernel FMMs."""
+    G = golden("synth300")
+    P = G["params"]
+    s = G["surface"]
+    pts = s[:, :3]
+    T = O.Tree(pts, pts, P["maxpoint"], P["maxlevel"])
+    dens = bie_densities(s, P["h"], probe_vector(len(s)))
+    kp = O.KParams(P["kappa"], P["dE"], P["dI"], P["tau"] * P["h"])
+    out = T.fmm(P["np"], kp, 16, dens)
+    idx = G["sample_idx"]
+    for f in range(4):
+        ref = fused_field_of_reference(G, f)
+        assert np.abs(out[f][idx] - ref).max() / np.abs(ref).max() < 1e-12, f
 
 
 def test_fmm_scalar_kernel(golden):

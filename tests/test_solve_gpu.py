@@ -17,7 +17,7 @@ def tube_of(ctx, G):
     return ctx.tube(s[:, :3], s[:, 3:6], s[:, 6], G["params"]["h"])
 
 
-@pytest.mark.parametrize("case", ["born", "synth30", "p1hje"])
+@pytest.mark.parametrize("case", ["born", "synth30", "p1hje", "synth300"])
 def test_electric_matches_reference(ctx, golden, case):
     G = golden(case)
     P = G["params"]
@@ -40,10 +40,10 @@ def test_electric_matches_reference(ctx, golden, case):
 # the reference's x86 -Ofast build and the GPU pick either side, which changes the tree and so
 # the FMM approximation (not the tube: it agrees to 1e-9).  Asymmetric molecules have no such
 # points.  Against the oracle run on the GPU's own tube the trees are identical.
-FULL_TOL = {"born": 1e-4, "synth30": 1e-7, "p1hje": 1e-7}
+FULL_TOL = {"born": 1e-4, "synth30": 1e-7, "p1hje": 1e-7, "synth300": 1e-6}
 
 
-@pytest.mark.parametrize("case", ["born", "synth30", "p1hje"])
+@pytest.mark.parametrize("case", ["born", "synth30", "p1hje", "synth300"])
 def test_full_solve_matches_reference(ctx, golden, case):
     G = golden(case)
     P = G["params"]
