@@ -804,21 +804,41 @@ struct Lockstep {
 // one wave: merge, lock-step refinement, energy
 // ---------------------------------------------------------------------------------------------
 
-struct BatchMol {
-    int index = 0;
-    const double *charges = nullptr;  // host
-    int natoms = 0;
-    ibim_config cfg{};
-    ibim_result *res = nullptr;
-    SolvePrep *prep = nullptr;   // released once merged
-    DevBuf<double> *b_tree = nullptr;  // right-hand side in tree order (2N)
-};
+bool batch_compatible(const ibim_config &a, const ibim_config &b) {
+    return a.precision == IBIM_PRECISION_MIXED && b.precision == IBIM_PRECISION_MIXED && a.h == b.h &&
+           a.np == b.np && a.kp.dE == b.kp.dE && a.kp.dI == b.kp.dI && a.kp.tau == b.kp.tau &&
+           a.kp.k3_scaled == b.kp.k3_scaled && a.restart == b.restart && a.jacobian == b.jacobian;
+}
 
-struct WaveStats {
-    long merged_mixed = 0, merged_fp64 = 0;
-    double active_frac = 0;
-    double t_merge_ms = 0, t_solve_ms = 0, t_energy_ms = 0;
-};
+void batch_prepare(Ctx *c, const double *centers_host, const double *charges_host, const double *radii_host,
+                   int natoms, const ibim_config &cfg, ibim_result &res, BatchMol &out,
+                   const std::function<void(long)> *after_surface) {
+    cudaStream_t s = c->stream;
+    DevBuf<double> dc, dr;
+    dc.alloc(3 * (size_t)natoms, s);
+    dr.alloc(natoms, s);
+    dc.upload(centers_host, 3 * (size_t)natoms);
+    dr.upload(radii_host, natoms);
+    std::unique_ptr<SolvePrep> prep(new SolvePrep());
+    solve_prepare(c, dc.ptr, dr.ptr, centers_host, charges_host, natoms, cfg, res, nullptr, *prep, after_surface);
+    Plan &P = *prep->P;
+    for (TargetSet *ts : P.targets) prepare_mixed(P, *ts);
+    std::unique_ptr<DevBuf<double>> b(new DevBuf<double>());
+    b->alloc(2 * (size_t)P.ns, s);
+    permute(c, P.ns, P.src_perm.ptr, prep->b_tube.ptr, b->ptr, false);
+    permute(c, P.ns, P.src_perm.ptr, prep->b_tube.ptr + P.ns, b->ptr + P.ns, false);
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    prep->b_tube.release();
+    prep->a4.release();
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    out.natoms = natoms;
+    out.charges = charges_host;
+    out.cfg = cfg;
+    out.res = &res;
+    out.bytes = (double)plan_bytes(P) + 2.0 * sizeof(double) * P.ns + 7.0 * sizeof(double) * prep->tube->n;
+    out.prep = prep.release();
+    out.b_tree = b.release();
+}
 
 void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
     cudaStream_t s = c->stream;
@@ -954,8 +974,6 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
 // the whole batch: worker threads prepare molecules in order; waves merge and solve
 // ---------------------------------------------------------------------------------------------
 
-double estimate_request_bytes(const ibim_config &cfg);
-
 void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
                  const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
                  ibim_result *results, int *statuses, double *done_ms, double *info) {
@@ -964,15 +982,11 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
     };
     IBIM_REQUIRE(nmol > 0 && natoms && centers && charges && radii && cfgs && results && statuses, "null argument");
-    const ibim_config &C0 = cfgs[0];
     for (int i = 0; i < nmol; ++i) {
-        const ibim_config &C = cfgs[i];
-        check_config(C);
+        check_config(cfgs[i]);
         IBIM_REQUIRE(natoms[i] > 0, "batch: every molecule needs at least one atom");
-        IBIM_REQUIRE(C.precision == IBIM_PRECISION_MIXED, "batch: the lock-step path is the mixed-precision path");
-        IBIM_REQUIRE(C.h == C0.h && C.np == C0.np && C.kp.dE == C0.kp.dE && C.kp.dI == C0.kp.dI &&
-                         C.kp.tau == C0.kp.tau && C.kp.k3_scaled == C0.kp.k3_scaled && C.restart == C0.restart &&
-                         C.jacobian == C0.jacobian,
+        IBIM_REQUIRE(cfgs[i].precision == IBIM_PRECISION_MIXED, "batch: the lock-step path is the mixed-precision path");
+        IBIM_REQUIRE(batch_compatible(cfgs[i], cfgs[0]),
                      "batch: molecules must share h, fmm_np, eps, tau, k3_scaled, restart and jacobian "
                      "(kappa, geometry and tolerances may differ)");
     }
@@ -989,21 +1003,25 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
         if (done_ms) done_ms[i] = 0.;
     }
     struct Job {
-        std::unique_ptr<SolvePrep> prep;
-        std::unique_ptr<DevBuf<double>> b_tree;
-        double est = 0, bytes = 0;
-        bool ready = false;
+        BatchMol bm;
+        double held = 0;   // bytes this molecule holds in the budget
+        bool fmm = false;  // past its level set (holds FMM-phase memory)
+        bool ready = false, waiting = false;
         std::string err;
     };
     std::vector<Job> jobs(nmol);
-    for (int i = 0; i < nmol; ++i) jobs[i].est = estimate_request_bytes(cfgs[i]);
     std::mutex mu;
     std::condition_variable cv;
-    int next = 0, held = 0;  // next molecule to prepare; molecules holding device memory
+    // admission: a molecule's level set is admitted by its grids' bytes, its FMM phase (once its
+    // tube size is known) by an estimate from the point count, replaced by the prepared plan's
+    // bytes; a phase is always admitted when nothing else holds memory of that phase
+    int next = 0, held = 0, held_fmm = 0, nwaiting = 0;
     double held_bytes = 0, peak_bytes = 0;
     bool stop = false;
     const int device = c->device;
-    auto can_take = [&] { return next < nmol && (held == 0 || held_bytes + jobs[next].est <= budget); };
+    auto can_take = [&] {
+        return next < nmol && (held == 0 || held_bytes + estimate_levelset_bytes(cfgs[next]) <= budget);
+    };
     // worker contexts: prepared plans keep buffers on their streams, so the contexts outlive them
     std::vector<ibim_ctx> wctx(workers, nullptr);
     std::vector<int> wrc(workers, IBIM_OK);
@@ -1020,8 +1038,6 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     };
     auto worker = [&](int t) {
         ibim_ctx wc = wctx[t];
-        const int crc = wrc[t];
-        const std::string cerr = werr0[t];
         for (;;) {
             int i;
             {
@@ -1030,37 +1046,39 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 if (stop || next >= nmol) break;
                 i = next++;
                 held++;
-                held_bytes += jobs[i].est;
+                jobs[i].held = estimate_levelset_bytes(cfgs[i]);
+                held_bytes += jobs[i].held;
                 peak_bytes = std::max(peak_bytes, held_bytes);
             }
             Job &J = jobs[i];
-            int st = crc;
-            std::string err = cerr;
-            if (crc == IBIM_OK) {
-                Ctx *wctx = &wc->c;
+            int st = wrc[t];
+            std::string err = werr0[t];
+            const std::function<void(long)> admit = [&](long npoints) {
+                const double need = estimate_fmm_bytes(cfgs[i], npoints);
+                std::unique_lock<std::mutex> lk(mu);
+                held_bytes -= J.held;  // the grids are gone
+                J.held = 0;
+                J.waiting = true;
+                nwaiting++;
+                cv.notify_all();
+                cv.wait(lk, [&] { return stop || held_fmm == 0 || held_bytes + need <= budget; });
+                nwaiting--;
+                J.waiting = false;
+                if (stop) throw Error(IBIM_ERR_INVALID_ARGUMENT, "batch: stopped");
+                J.held = need;
+                J.fmm = true;
+                held_fmm++;
+                held_bytes += need;
+                peak_bytes = std::max(peak_bytes, held_bytes);
+            };
+            if (st == IBIM_OK) {
+                Ctx *wctx_ = &wc->c;
                 try {
                     IBIM_CUDA(cudaSetDevice(device));
-                    set_current_ctx(wctx);
-                    const double *ci = centers + 3 * aoff[i], *qi = charges + aoff[i], *ri = radii + aoff[i];
-                    DevBuf<double> dc, dr;
-                    dc.alloc(3 * (size_t)natoms[i], wctx->stream);
-                    dr.alloc(natoms[i], wctx->stream);
-                    dc.upload(ci, 3 * (size_t)natoms[i]);
-                    dr.upload(ri, natoms[i]);
-                    J.prep.reset(new SolvePrep());
-                    solve_prepare(wctx, dc.ptr, dr.ptr, ci, qi, natoms[i], cfgs[i], results[i], nullptr, *J.prep);
-                    Plan &P = *J.prep->P;
-                    for (TargetSet *ts : P.targets) prepare_mixed(P, *ts);
-                    J.b_tree.reset(new DevBuf<double>());
-                    J.b_tree->alloc(2 * (size_t)P.ns, wctx->stream);
-                    permute(wctx, P.ns, P.src_perm.ptr, J.prep->b_tube.ptr, J.b_tree->ptr, false);
-                    permute(wctx, P.ns, P.src_perm.ptr, J.prep->b_tube.ptr + P.ns, J.b_tree->ptr + P.ns, false);
-                    IBIM_CUDA(cudaStreamSynchronize(wctx->stream));
-                    J.prep->b_tube.release();
-                    J.prep->a4.release();
-                    IBIM_CUDA(cudaStreamSynchronize(wctx->stream));
-                    J.bytes = (double)plan_bytes(P) + 2.0 * sizeof(double) * P.ns + 7.0 * sizeof(double) * J.prep->tube->n;
-                    st = IBIM_OK;
+                    set_current_ctx(wctx_);
+                    batch_prepare(wctx_, centers + 3 * aoff[i], charges + aoff[i], radii + aoff[i], natoms[i],
+                                  cfgs[i], results[i], J.bm, &admit);
+                    J.bm.index = i;
                 } catch (const Error &e) {
                     st = e.status;
                     err = e.what();
@@ -1069,18 +1087,26 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                     err = e.what();
                 }
                 if (st != IBIM_OK) {
-                    J.prep.reset();
-                    J.b_tree.reset();
-                    J.bytes = 0;
+                    delete J.bm.prep;
+                    J.bm.prep = nullptr;
+                    delete J.bm.b_tree;
+                    J.bm.b_tree = nullptr;
                 }
             }
             {
                 std::lock_guard<std::mutex> lk(mu);
                 statuses[i] = st;
                 J.err = err;
-                if (st != IBIM_OK && done_ms) done_ms[i] = since_call();
-                held_bytes += J.bytes - J.est;
-                if (st != IBIM_OK) held--;
+                if (st == IBIM_OK) {
+                    held_bytes += J.bm.bytes - J.held;
+                    J.held = J.bm.bytes;
+                } else {
+                    held_bytes -= J.held;
+                    J.held = 0;
+                    held--;
+                    if (J.fmm) held_fmm--;
+                    if (done_ms) done_ms[i] = since_call();
+                }
                 peak_bytes = std::max(peak_bytes, held_bytes);
                 J.ready = true;
             }
@@ -1089,11 +1115,24 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     };
     std::vector<std::thread> pool;
     for (int t = 0; t < workers; ++t) pool.emplace_back(worker, t);
+    auto release_all = [&] {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        for (auto &t : pool) t.join();
+        for (Job &J : jobs) {
+            delete J.bm.prep;
+            J.bm.prep = nullptr;
+            delete J.bm.b_tree;
+            J.bm.b_tree = nullptr;
+        }
+        destroy_workers();
+    };
     int waves = 0, largest = 0;
     long merged_mixed = 0, merged_fp64 = 0;
-    double active_w = 0, peak_wave_bytes = 0;
-    std::string first_error;
-    int first_status = IBIM_OK;
+    double active_w = 0;
     int done = 0;
     try {
         while (done < nmol) {
@@ -1101,13 +1140,13 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
             {
                 std::unique_lock<std::mutex> lk(mu);
                 // a wave: the next prepared molecules in order, up to max_wave; it starts when full,
-                // when nothing is left to prepare, or when the budget keeps the workers from preparing more
+                // when nothing is left to prepare, or when a worker waits for memory the wave holds
                 cv.wait(lk, [&] {
                     int e = done;
                     while (e < nmol && jobs[e].ready && e - done < max_wave) ++e;
                     if (e == done) return false;
                     if (e - done >= max_wave || e == nmol) return true;
-                    return next == e && !can_take();
+                    return nwaiting > 0 || (next < nmol && !can_take());
                 });
                 int e = done;
                 while (e < nmol && jobs[e].ready && (int)wave.size() < max_wave) {
@@ -1122,15 +1161,11 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
             std::vector<BatchMol> bm(wave.size());
             double wave_bytes = 0;
             for (size_t k = 0; k < wave.size(); ++k) {
-                const int i = wave[k];
-                bm[k].index = i;
-                bm[k].charges = charges + aoff[i];
-                bm[k].natoms = natoms[i];
-                bm[k].cfg = cfgs[i];
-                bm[k].res = &results[i];
-                bm[k].prep = jobs[i].prep.release();
-                bm[k].b_tree = jobs[i].b_tree.release();
-                wave_bytes += jobs[i].bytes;
+                Job &J = jobs[wave[k]];
+                bm[k] = J.bm;
+                J.bm.prep = nullptr;
+                J.bm.b_tree = nullptr;
+                wave_bytes += J.held;
             }
             WaveStats ws;
             int wst = IBIM_OK;
@@ -1159,40 +1194,23 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
             merged_mixed += ws.merged_mixed;
             merged_fp64 += ws.merged_fp64;
             active_w += ws.active_frac * wave.size();
-            peak_wave_bytes = std::max(peak_wave_bytes, wave_bytes);
             {
                 std::lock_guard<std::mutex> lk(mu);
                 held -= (int)wave.size();
+                held_fmm -= (int)wave.size();
                 held_bytes -= wave_bytes;
                 if (held == 0) held_bytes = 0;
+                for (int i : wave) jobs[i].held = 0;
             }
             cv.notify_all();
         }
     } catch (...) {
-        {
-            std::lock_guard<std::mutex> lk(mu);
-            stop = true;
-        }
-        cv.notify_all();
-        for (auto &t : pool) t.join();
-        for (Job &J : jobs) {
-            J.prep.reset();
-            J.b_tree.reset();
-        }
-        destroy_workers();
+        release_all();
         throw;
     }
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        stop = true;
-    }
-    cv.notify_all();
-    for (auto &t : pool) t.join();
-    for (Job &J : jobs) {
-        J.prep.reset();
-        J.b_tree.reset();
-    }
-    destroy_workers();
+    release_all();
+    std::string first_error;
+    int first_status = IBIM_OK;
     for (int i = 0; i < nmol; ++i)
         if (statuses[i] != IBIM_OK && first_status == IBIM_OK) {
             first_status = statuses[i];

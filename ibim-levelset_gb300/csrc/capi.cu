@@ -164,7 +164,7 @@ static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *
 // tube order), plan, operators and their images, and the area.
 void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
                    const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
-                   const double *atoms4_dev, SolvePrep &out) {
+                   const double *atoms4_dev, SolvePrep &out, const std::function<void(long)> *after_surface) {
     check_config(cfg);
     IBIM_REQUIRE(natoms > 0, "need at least one atom");
     std::memset(&res, 0, sizeof(res));
@@ -188,6 +188,8 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
     res.t_surface_ms = t1.ms();
     trace_mark("solve: level set + surface");
     IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
+    // the caller may hold the FMM phase back until device memory for this many points is free
+    if (after_surface) (*after_surface)(tube->n);
     try {
         out.atoms4 = atoms4_dev;
         if (!out.atoms4) {
@@ -256,13 +258,27 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
 
 static void solve_impl(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
                        const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
-                       const double *atoms4_dev) {
+                       const double *atoms4_dev, const std::function<void(long)> *after_surface = nullptr) {
     SolvePrep prep;
-    solve_prepare(c, centers_dev, radii_dev, centers_host, charges_host, natoms, cfg, res, atoms4_dev, prep);
+    solve_prepare(c, centers_dev, radii_dev, centers_host, charges_host, natoms, cfg, res, atoms4_dev, prep,
+                  after_surface);
     electric_solve(*prep.P, cfg.kp, prep.atoms4, charges_host, natoms, cfg.restart, cfg.maxiter, cfg.tol,
                    cfg.precision, nullptr, nullptr, res, prep.b_tube.ptr);
     fill_plan_stats(*prep.P, res);
     trace_mark("solve: electric done");
+}
+
+void solve_host(Ctx *c, const double *centers, const double *charges, const double *radii, int natoms,
+                const ibim_config &cfg, ibim_result &res, const std::function<void(long)> *after_surface) {
+    IBIM_REQUIRE(centers && charges && radii && natoms > 0, "need at least one atom");
+    IBIM_CUDA(cudaSetDevice(c->device));
+    set_current_ctx(c);
+    DevBuf<double> dc, dr;
+    dc.alloc(3 * (size_t)natoms, c->stream);
+    dr.alloc(natoms, c->stream);
+    dc.upload(centers, 3 * (size_t)natoms);
+    dr.upload(radii, natoms);
+    solve_impl(c, dc.ptr, dr.ptr, centers, charges, natoms, cfg, res, nullptr, after_surface);
 }
 
 // Serialise a tree in the reference's node numbering (see ibim_plan_lists).

@@ -59,9 +59,49 @@ struct SolvePrep {
         delete tube;
     }
 };
+// after_surface (optional) runs once the tube is extracted, with its point count, before the
+// plan and operators are built (an admission point for the FMM phase's device memory).
 void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
                    const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
-                   const double *atoms4_dev, SolvePrep &out);
+                   const double *atoms4_dev, SolvePrep &out,
+                   const std::function<void(long)> *after_surface = nullptr);
+// A whole solve from host atom arrays (ibim_solve) with the FMM-phase admission hook.
+void solve_host(Ctx *c, const double *centers, const double *charges, const double *radii, int natoms,
+                const ibim_config &cfg, ibim_result &res, const std::function<void(long)> *after_surface);
+// Device bytes of a solve's phases, estimated from its configuration: the level set (grids), and
+// the FMM phase for npoints tube points (plan, operator images at their peak, Krylov basis).
+double estimate_levelset_bytes(const ibim_config &cfg);
+double estimate_fmm_bytes(const ibim_config &cfg, long npoints);
+// A request's footprint before its level set runs (the FMM phase for a tube point count guessed
+// from the grid).
+double estimate_request_bytes(const ibim_config &cfg);
+// For the lock-step paths (batch.cu): the preparation of one molecule -- solve_prepare, the
+// mixed near lists uploaded for both target sets, the right-hand side in tree order; bytes = the
+// device memory the prepared molecule holds.
+struct BatchMol {
+    int index = 0;
+    const double *charges = nullptr;  // host, natoms
+    int natoms = 0;
+    ibim_config cfg{};
+    ibim_result *res = nullptr;
+    SolvePrep *prep = nullptr;         // released once merged
+    DevBuf<double> *b_tree = nullptr;  // right-hand side in tree order (2N)
+    double bytes = 0;
+};
+void batch_prepare(Ctx *c, const double *centers_host, const double *charges_host, const double *radii_host,
+                   int natoms, const ibim_config &cfg, ibim_result &res, BatchMol &out,
+                   const std::function<void(long)> *after_surface = nullptr);
+struct WaveStats {
+    long merged_mixed = 0, merged_fp64 = 0;
+    double active_frac = 0;
+    double t_merge_ms = 0, t_solve_ms = 0, t_energy_ms = 0;
+};
+// One wave of prepared molecules (same h, order, eps, tau, restart): merged plan, lock-step
+// refinement and GMRES, energies into each molecule's result.  The molecules' preparations are
+// released once merged.
+void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws);
+// Whether two configurations can share a wave.
+bool batch_compatible(const ibim_config &a, const ibim_config &b);
 void check_config(const ibim_config &cfg);
 void fill_plan_stats(const Plan &P, ibim_result &res);
 void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4);

@@ -51,7 +51,7 @@ EXPORTS = [
     "ibim_launch_count", "ibim_profile_enable", "ibim_profile_read", "ibim_profile_work", "ibim_measure_peak",
     "ibim_levelset_evolve_static", "ibim_server_create", "ibim_server_destroy", "ibim_server_submit",
     "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate", "ibim_gmres_host",
-    "ibim_grid_set_geometry", "ibim_batch_solve",
+    "ibim_grid_set_geometry", "ibim_batch_solve", "ibim_server_create_lockstep", "ibim_fmm_bytes_estimate",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
@@ -168,6 +168,8 @@ def lib():
         "ibim_server_wait": ([_vp, C.c_long, _ip, C.POINTER(Result), _dp, _dp], C.c_int),
         "ibim_server_stats": ([_vp, _dp], C.c_int),
         "ibim_request_bytes_estimate": ([C.POINTER(Config)], C.c_double),
+        "ibim_fmm_bytes_estimate": ([C.POINTER(Config), C.c_long], C.c_double),
+        "ibim_server_create_lockstep": ([C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_vp)], C.c_int),
         "ibim_gmres_host": ([_vp, C.c_long, APPLY_FN, _vp, _dp, _dp, C.c_int, C.c_int, C.c_double, _ip, _ip, _ip,
                              _dp], C.c_int),
     }
@@ -579,13 +581,20 @@ class Workload:
 
 
 class Server:
-    """Request loop on one GPU (ibim_server): concurrent solves admitted by an HBM budget."""
+    """Request loop on one GPU (ibim_server): requests admitted by an HBM budget in two phases, run
+    as concurrent whole solves (`slots` threads), or with lockstep=True prepared by `slots` threads
+    and solved in waves of up to max_wave requests on merged plans (ibim_server_create_lockstep)."""
 
-    STAT_KEYS = ["submitted", "completed", "in_flight", "queued", "bytes_in_flight", "peak_bytes", "budget"]
+    STAT_KEYS = ["submitted", "completed", "in_flight", "queued", "bytes_in_flight", "peak_bytes", "budget",
+                 "waves"]
 
-    def __init__(self, device: int = 0, slots: int = 4, hbm_budget_bytes: float = 150e9):
+    def __init__(self, device: int = 0, slots: int = 4, hbm_budget_bytes: float = 150e9, lockstep: bool = False,
+                 max_wave: int = 32):
         h = _vp()
-        _check(lib().ibim_server_create(device, slots, float(hbm_budget_bytes), C.byref(h)))
+        if lockstep:
+            _check(lib().ibim_server_create_lockstep(device, slots, max_wave, float(hbm_budget_bytes), C.byref(h)))
+        else:
+            _check(lib().ibim_server_create(device, slots, float(hbm_budget_bytes), C.byref(h)))
         self.h = h
 
     def submit(self, centers, charges, radii, cfg: Config) -> int:
@@ -616,7 +625,7 @@ class Server:
         return self._out(st, res, lat, run)
 
     def stats(self) -> dict:
-        s = (C.c_double * 7)()
+        s = (C.c_double * 8)()
         _check(lib().ibim_server_stats(self.h, s))
         return dict(zip(self.STAT_KEYS, list(s)))
 
@@ -631,3 +640,7 @@ class Server:
 
 def request_bytes_estimate(cfg: Config) -> float:
     return float(lib().ibim_request_bytes_estimate(C.byref(cfg)))
+
+
+def fmm_bytes_estimate(cfg: Config, npoints: int) -> float:
+    return float(lib().ibim_fmm_bytes_estimate(C.byref(cfg), int(npoints)))

@@ -287,13 +287,24 @@ int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *ce
                      ibim_result *results, int *statuses, double *done_ms, double *info);
 
 /* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
- * Solve requests queue in arrival order; `slots` worker threads, each with its own context and
- * stream, take the head of the queue while the estimated device footprints of the requests in
- * flight plus the head's stay within hbm_budget_bytes (a request is always admitted when none
- * is in flight).  Requests run concurrently on the device and each keeps its level set, tree,
- * operators and Krylov basis resident until it finishes. */
+ * Solve requests queue in arrival order and are admitted by device memory in two phases: the
+ * head of the queue starts (its level set) when its grids fit in hbm_budget_bytes beside what the
+ * requests in flight hold; once its tube is extracted, its FMM phase (plan, operator images,
+ * Krylov basis) waits until the bytes estimated from the actual point count fit
+ * (ibim_fmm_bytes_estimate).  A phase is always admitted when no other request holds memory of
+ * that phase.  Each request keeps its level set, tree, operators and Krylov basis resident until
+ * it finishes.
+ * ibim_server_create: `slots` worker threads, each with its own context and stream, run whole
+ * solves concurrently on the device. */
 typedef struct ibim_server_s *ibim_server;
 int ibim_server_create(int device, int slots, double hbm_budget_bytes, ibim_server *out);
+/* Lock-step request loop (mixed-precision requests): `workers` threads prepare admitted requests
+ * (level set, tube, right-hand side, plan, operator images) while a solver thread takes the
+ * prepared ones in waves of up to max_wave requests of one shape (h, fmm_np, eps, tau, restart):
+ * a wave's plans are merged so that each FMM stage is one launch for all of them, and their GMRES
+ * iterations advance together (as ibim_batch_solve).  Requests arriving while a wave runs are
+ * prepared meanwhile and join the next wave.  Same submit / poll / wait / stats / destroy. */
+int ibim_server_create_lockstep(int device, int workers, int max_wave, double hbm_budget_bytes, ibim_server *out);
 /* Waits for every queued and running request, then stops the workers. */
 int ibim_server_destroy(ibim_server s);
 /* Queue one whole solve (as ibim_solve; inputs are copied); *id identifies it. */
@@ -304,10 +315,14 @@ int ibim_server_submit(ibim_server s, const double *centers, const double *charg
 int ibim_server_poll(ibim_server s, long id, int *done, int *status, ibim_result *res, double *latency_ms,
                      double *run_ms);
 int ibim_server_wait(ibim_server s, long id, int *status, ibim_result *res, double *latency_ms, double *run_ms);
-/* submitted, completed, in flight, queued, bytes admitted in flight, peak bytes admitted, budget */
-int ibim_server_stats(ibim_server s, double stats[7]);
-/* The device footprint the server budgets for one solve of this configuration. */
+/* submitted, completed, in flight, queued, bytes admitted in flight, peak bytes admitted, budget,
+ * waves run (lock-step loop; 0 for the pool) */
+int ibim_server_stats(ibim_server s, double stats[8]);
+/* A solve's device footprint estimated from its configuration alone (before its level set). */
 double ibim_request_bytes_estimate(const ibim_config *cfg);
+/* The FMM phase's device footprint for a tube of npoints points, which the request loops admit
+ * once the tube is extracted. */
+double ibim_fmm_bytes_estimate(const ibim_config *cfg, long npoints);
 
 #ifdef __cplusplus
 }
