@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--slots", type=int, default=4, help="serve/batch: solves in flight (request loop)")
     ap.add_argument("--batch-mode", choices=["lockstep", "pool"], default="lockstep",
                     help="batch: lock-step waves on merged plans (ibim_batch_solve) or the request loop's "
-                         "concurrent whole solves")
+                         "concurrent whole solves; serve: the request loop in lock-step or pool mode")
     ap.add_argument("--max-wave", type=int, default=32, help="batch lockstep: molecules per wave")
     ap.add_argument("--workers", type=int, default=4, help="batch lockstep: preparation threads")
     ap.add_argument("--atoms", type=str, default=None, help="serve/batch: log-uniform atom-count range")
@@ -550,7 +550,14 @@ def run_serve(args):
         W = workloads.protein(n, (3_000_000 if batch else 4_000_000) + k, h=h, order=5, kappa=kappa)
         reqs.append(W)
     arrivals = np.zeros(nreq) if batch else np.cumsum(rng.exponential(1.0 / args.rate, size=nreq))
-    srv = ibim.Server(0, slots=args.slots, hbm_budget_bytes=150e9)
+    # warm-up request (kernels loaded, memory pool grown), not counted
+    W0 = workloads.protein(100, 4_999_999, h=hs[0], order=5, kappa=0.1)
+    ctx0 = ibim.Context(0)
+    ctx0.solve(W0.mol.centers, W0.mol.charges, W0.mol.radii, W0.config(ibim.PRECISION_MIXED))
+    ctx0.close()
+    lock = args.batch_mode == "lockstep"
+    srv = ibim.Server(0, slots=args.workers if lock else args.slots, hbm_budget_bytes=150e9, lockstep=lock,
+                      max_wave=args.max_wave)
     ids, t0 = [], time.perf_counter()
     for W, ta in zip(reqs, arrivals):
         now = time.perf_counter() - t0
@@ -577,7 +584,9 @@ def run_serve(args):
            "dtype": "f32+f64", "data": "synthetic (seeded generator)",
            "config": {"workload": "batch" if batch else "serve_sample", "requests": nreq,
                       "offered_rate_per_s": None if batch else args.rate,
-                      "slots": args.slots, "atoms_range": [lo, hi], "h_choices": hs, "kappa_range": [0.0, 0.15],
+                      "mode": "lockstep" if lock else "pool",
+                      "threads": args.workers if lock else args.slots, "max_wave": args.max_wave if lock else None,
+                      "atoms_range": [lo, hi], "h_choices": hs, "kappa_range": [0.0, 0.15],
                       "eps_out": 80.0, "chebyshev_order": 5, "precision": "mixed", "hbm_budget_gb": 150},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "mean": float(lat.mean())},
