@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libibim_gb300.so")
 SOURCES = ["levelset.cu", "tree.cpp", "fmm.cu", "fmm_mixed.cu", "near_ff.cu", "m2l_tc.cu", "solve.cu", "capi.cu",
-           "server.cpp", "batch.cu"]
+           "server.cpp", "batch.cu", "tuning.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 OPENMP_CU = {"fmm.cu", "fmm_mixed.cu"}  # CUDA files whose host code (plan building) uses OpenMP
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",

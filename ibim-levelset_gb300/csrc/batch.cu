@@ -537,7 +537,23 @@ Plan *merge_wave(Ctx *c, Tube *mtube, const std::vector<Plan *> &mols, const std
         }
         T->out4.alloc((size_t)4 * std::max<long>(1, nt), s);
         T->mixed_ready = true;
+        // the molecule of each chunk (the heavy kernels skip molecules that stopped iterating)
+        std::vector<int> cm_tc, cm_oz;
+        for (int m = 0; m < M; ++m) {
+            cm_tc.insert(cm_tc.end(), S_(m).nchunks_tc, m);
+            cm_oz.insert(cm_oz.end(), S_(m).nchunks_oz, m);
+        }
+        if (cm_tc.empty()) cm_tc.push_back(0);
+        if (cm_oz.empty()) cm_oz.push_back(0);
+        T->chunk_mol_tc.alloc(cm_tc.size(), s);
+        T->chunk_mol_tc.upload(cm_tc.data(), cm_tc.size());
+        T->chunk_mol_oz.alloc(cm_oz.size(), s);
+        T->chunk_mol_oz.upload(cm_oz.data(), cm_oz.size());
     }
+    std::vector<int> ones(M, 1);
+    B->mol_active.alloc(M, s);
+    B->mol_active.upload(ones.data(), M);
+    B->tune = tuning_for(B->p, ns);
     IBIM_CUDA(cudaStreamSynchronize(s));
     return B.release();
 }
@@ -611,11 +627,15 @@ struct Lockstep {
         ydev.alloc((size_t)M * ldy, s);
         IBIM_CUDA(cudaMallocHost((void **)&hpin, sizeof(double) * M * (ldh + ldy)));
         IBIM_CUDA(cudaMallocHost((void **)&apin, sizeof(int) * 3 * M));
+        IBIM_CUDA(cudaMallocHost((void **)&mpin, sizeof(int) * M));
+        mask_of.resize(M);
+        for (int k = 0; k < M; ++k) mask_of[k] = k;  // the merged plan starts with every molecule on
         IBIM_CUDA(cudaStreamSynchronize(s));
     }
     ~Lockstep() {
         if (hpin) cudaFreeHost(hpin);
         if (apin) cudaFreeHost(apin);
+        if (mpin) cudaFreeHost(mpin);
     }
     Segs segs(int region) const { return {doff.ptr, dlen.ptr, dnblk.ptr, dact.ptr + (size_t)region * M, n}; }
     // a list of molecules into a region (after the stream's earlier copies from the pinned lists)
@@ -649,7 +669,20 @@ struct Lockstep {
             out[m] = hpin[(size_t)m * ldh];
         }
     }
+    // the merged plan's molecule mask follows the molecules whose products are used
+    Plan *plan = nullptr;
+    std::vector<int> mask_of;  // the list the device mask was last set from
+    int *mpin = nullptr;       // pinned mask (M)
+    void set_mask(const std::vector<int> &act) {
+        if (!plan || act == mask_of) return;
+        sync();  // the previous mask copy has been read
+        for (int k = 0; k < M; ++k) mpin[k] = 0;
+        for (int m : act) mpin[m] = 1;
+        IBIM_CUDA(cudaMemcpyAsync(plan->mol_active.ptr, mpin, sizeof(int) * M, cudaMemcpyHostToDevice, c->stream));
+        mask_of = act;
+    }
     void matvec(const Op &A, const double *in, double *o, const std::vector<int> &act) {
+        set_mask(act);
         A(in, o);
         merged_matvecs++;
         active_sum += (double)act.size();
@@ -889,6 +922,7 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
     Op A32 = [&](const double *in, double *o) { bie_matvec(*B, kp, in, o, IBIM_PRECISION_MIXED); };
     Op A64 = [&](const double *in, double *o) { bie_matvec(*B, kp, in, o, IBIM_PRECISION_FP64_TC); };
     Lockstep L(c, n, std::max(1, std::min(C0.restart, 250)), off, len);
+    L.plan = B.get();
     // FP64 iterative refinement of every molecule (electric_solve's mixed branch, in lock-step)
     std::vector<int> all(M);
     for (int m = 0; m < M; ++m) all[m] = m;
@@ -940,7 +974,8 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
     ws.active_frac = L.merged_matvecs ? L.active_sum / ((double)M * L.merged_matvecs) : 1.0;
     const double t_solve = tm.ms();
     if (m2l_tc_error(*B)) throw Error(IBIM_ERR_LIMIT, "tensor-core M2L: an MMA completion wait exceeded its bound");
-    // polarizeMap + energy (electric.cpp:442-505) on the merged atom targets
+    // polarizeMap + energy (electric.cpp:442-505) on the merged atom targets, every molecule on
+    L.set_mask(all);
     Timer te(s);
     TargetSet &TA = *B->targets[1];
     bie_densities(*B, x.ptr, B->dens4.ptr);
@@ -951,6 +986,7 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
     const double t_energy = te.ms();
     ws.t_solve_ms = t_solve;
     ws.t_energy_ms = t_energy;
+    L.sync();
     for (int m = 0; m < M; ++m) {
         ibim_result &R = *mols[m].res;
         const long o = W[m].tgt_off[1];
@@ -1005,6 +1041,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     struct Job {
         BatchMol bm;
         double held = 0;   // bytes this molecule holds in the budget
+        double est_fmm = 0;  // its FMM phase's admitted estimate
         bool fmm = false;  // past its level set (holds FMM-phase memory)
         bool ready = false, waiting = false;
         std::string err;
@@ -1066,6 +1103,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 J.waiting = false;
                 if (stop) throw Error(IBIM_ERR_INVALID_ARGUMENT, "batch: stopped");
                 J.held = need;
+                J.est_fmm = need;
                 J.fmm = true;
                 held_fmm++;
                 held_bytes += need;
@@ -1132,7 +1170,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     };
     int waves = 0, largest = 0;
     long merged_mixed = 0, merged_fp64 = 0;
-    double active_w = 0;
+    double active_w = 0, wave_ms = 0, bytes_actual = 0, bytes_est = 0;
     int done = 0;
     try {
         while (done < nmol) {
@@ -1166,6 +1204,8 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 J.bm.prep = nullptr;
                 J.bm.b_tree = nullptr;
                 wave_bytes += J.held;
+                bytes_actual += J.bm.bytes;
+                bytes_est += J.est_fmm;
             }
             WaveStats ws;
             int wst = IBIM_OK;
@@ -1190,6 +1230,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
                 if (done_ms) done_ms[b.index] = t_wave_done;
             }
             waves++;
+            wave_ms += ws.t_merge_ms + ws.t_solve_ms + ws.t_energy_ms;
             largest = std::max(largest, (int)wave.size());
             merged_mixed += ws.merged_mixed;
             merged_fp64 += ws.merged_fp64;
@@ -1226,6 +1267,9 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
         int ok = 0;
         for (int i = 0; i < nmol; ++i) ok += statuses[i] == IBIM_OK;
         info[5] = ok ? active_w / ok : 0.0;
+        info[6] = wave_ms;
+        info[7] = bytes_actual;
+        info[8] = bytes_est;
     }
 }
 

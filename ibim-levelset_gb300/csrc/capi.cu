@@ -10,6 +10,7 @@
 #include <sstream>
 #include <string>
 
+#include "fmm_common.cuh"
 #include "solve.cuh"
 
 namespace ibim {
@@ -1026,6 +1027,96 @@ int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *ce
                     statuses, done_ms, info);
         for (int i = 0; i < nmol; ++i)
             if (statuses[i] != IBIM_OK) throw Error(statuses[i], ibim_last_error());
+    });
+}
+
+int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, const double *radii, int natoms,
+                  const ibim_config *cfg, int reps, long install_min_points, double *report) {
+    return guard([&] {
+        IBIM_REQUIRE(ctx && centers && charges && radii && cfg && report && natoms > 0, "null argument");
+        IBIM_REQUIRE(cfg->precision == IBIM_PRECISION_MIXED, "autotune: tunes the mixed path's launches");
+        check_config(*cfg);
+        Ctx *c = &ctx->c;
+        bind(c);
+        cudaStream_t s = c->stream;
+        reps = std::max(1, std::min(reps, 50));
+        DevBuf<double> dc, dr;
+        dc.alloc(3 * (size_t)natoms, s);
+        dr.alloc(natoms, s);
+        dc.upload(centers, 3 * (size_t)natoms);
+        dr.upload(radii, natoms);
+        long npts = 0;
+        int timed = 0;
+        // a candidate's cost: one solve's mix of products (25 mixed, one FP64-class residual), timed
+        // with CUDA events on a plan prepared under the candidate's parameters
+        auto cost = [&](const Tuning &t) -> double {
+            tuning_override(&t);
+            SolvePrep prep;
+            ibim_result res;
+            try {
+                solve_prepare(c, dc.ptr, dr.ptr, centers, charges, natoms, *cfg, res, nullptr, prep);
+            } catch (...) {
+                tuning_override(nullptr);
+                throw;
+            }
+            tuning_override(nullptr);
+            Plan &P = *prep.P;
+            for (TargetSet *ts : P.targets) prepare_mixed(P, *ts);
+            npts = P.ns;
+            DevBuf<double> x, y;
+            x.alloc(2 * (size_t)P.ns, s);
+            y.alloc(2 * (size_t)P.ns, s);
+            permute(c, P.ns, P.src_perm.ptr, prep.b_tube.ptr, x.ptr, false);
+            permute(c, P.ns, P.src_perm.ptr, prep.b_tube.ptr + P.ns, x.ptr + P.ns, false);
+            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
+            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_FP64_TC);
+            Timer t1(s);
+            for (int r = 0; r < reps; ++r) bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
+            const double ms32 = t1.ms() / reps;
+            Timer t2(s);
+            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_FP64_TC);
+            const double ms64 = t2.ms();
+            IBIM_REQUIRE(!m2l_tc_error(P), "autotune: a tensor-core M2L wait exceeded its bound");
+            ++timed;
+            return 25.0 * ms32 + ms64;
+        };
+        Tuning best;
+        const double base = cost(best);
+        double best_cost = base;
+        auto consider = [&](Tuning t) {
+            const double v = cost(t);
+            if (v < best_cost) {
+                best_cost = v;
+                best = t;
+            }
+        };
+        {  // launch form of the tensor-core M2L, then the segment sizes, one coordinate at a time
+            Tuning t = best;
+            t.tc_form = 4;
+            consider(t);
+        }
+        for (long v : {1L << 15, 1L << 16, 1L << 18}) {
+            Tuning t = best;
+            t.near_seg_pairs = v;
+            consider(t);
+        }
+        for (long v : {1L << 13, 1L << 15, 1L << 16}) {
+            Tuning t = best;
+            t.nearff_seg_pairs = v;
+            consider(t);
+        }
+        report[0] = (double)npts;
+        report[1] = (double)best.near_seg_pairs;
+        report[2] = (double)best.nearff_seg_pairs;
+        report[3] = (double)best.tc_form;
+        report[4] = best_cost;
+        report[5] = base;
+        report[6] = timed;
+        if (install_min_points >= 0) {
+            const int st = ibim_tuning_set(cfg->np, install_min_points, best.near_seg_pairs, best.nearff_seg_pairs,
+                                           best.tc_form);
+            if (st != IBIM_OK) throw Error(st, ibim_last_error());
+        }
     });
 }
 

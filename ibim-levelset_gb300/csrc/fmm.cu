@@ -901,6 +901,7 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
     P->maxpoint = maxpoint;
     P->maxlevel = maxlevel;
     P->precision = precision;
+    P->tune = tuning_for(order, ns);
     try {
         trace_mark("plan: coordinates downloaded");
         P->tree = build_tree(pts.data(), ns, pts.data(), ns, maxpoint, maxlevel);

@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                                                  const double *__restrict__ sy64, const double *__restrict__ sz64,
                                                  const double *__restrict__ tx64, const double *__restrict__ ty64,
                                                  const double *__restrict__ tz64, const float4 *__restrict__ kmol,
-                                                 const int *__restrict__ node_mol) {
+                                                 const int *__restrict__ node_mol, const int *__restrict__ mol_active) {
     __shared__ ChebTables32 T;
     // {x, y, z, q m_x}, {q m_y, q m_z, q psi, source index} in the target leaf's frame
     __shared__ float4 S4[TILE32][2];
@@ -489,6 +489,7 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
         const int tb = tb_[leaf], te = te_[leaf];
         float kap = kp.kappa, kl2 = kp.kappa_l2, k2q = kp.k2in_q;
         if (BATCH) {
+            if (!mol_active[node_mol[leaf]]) continue;  // the molecule has stopped iterating
             const float4 km = kmol[node_mol[leaf]];
             kap = km.x;
             kl2 = km.y;
@@ -729,9 +730,9 @@ void mixed_lists_host(const Plan &P, TargetSet &S) {
         for (int u : T.U[i]) add_run(u);
         for (int w : T.W[i]) add_run(w);
     }
-    S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_seg32);
+    S.near32_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_seg32, P.tune.near_seg_pairs);
     S.nnear32_seg = tl32.empty() ? 0 : (int)S.h_seg32.size() / 4;
-    S.nearff_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_segff, NEAR_FF_SEG_PAIRS, 128);
+    S.nearff_atomic = near_segments(tl32, nt32, ptr, rng, false, S.h_segff, P.tune.nearff_seg_pairs, 128);
     S.nnearff_seg = tl32.empty() ? 0 : (int)S.h_segff.size() / 4;
     S.h_ptr32.swap(ptr);
     S.h_rng32.swap(rng);
@@ -926,7 +927,7 @@ void fmm_run_mixed(Plan &P, int ts, const ibim_kernel_params &kpp, const double 
                                                   S.near32_range.ptr, S.near32_off.ptr, S.tbeg.ptr, S.tend.ptr,
                                                   P.nrad32.ptr, P.src8.ptr, tx, ty, tz, S.nt, P.local32.ptr, out,
                                                   l2p_mask, S.nnear32_seg, next, P.sx.ptr, P.sy.ptr, P.sz.ptr,
-                                                  tx64, ty64, tz64, P.kmol32.ptr, P.node_mol.ptr));
+                                                  tx64, ty64, tz64, P.kmol32.ptr, P.node_mol.ptr, P.mol_active.ptr));
     };
     const bool overlap = near_overlap() && S.ntleaves > 0;
     static const int occ = [] {

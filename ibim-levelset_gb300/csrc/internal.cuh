@@ -222,6 +222,7 @@ struct TargetSet {
     int nchunks_tc2 = 0;
     DevBuf<int> v_chunk_oz;            // chunks of the sliced FP64-class contraction (<= 64 pairs)
     int nchunks_oz = 0;
+    DevBuf<int> chunk_mol_tc, chunk_mol_oz;  // merged plans: the molecule of each chunk
     long nvpairs = 0;                  // pairs of the operator contraction (V, plus X when x_as_ops)
     DevBuf<int> x_src, x_tgt;          // X pairs evaluated on the fly (when not x_as_ops)
     long nxpairs = 0;
@@ -259,12 +260,26 @@ struct TargetSet {
     DevBuf<float> x_off32;             // per X pair: source centre - target centre
 };
 
+// Launch parameters a plan takes from the tuning table (tuning.cpp) for its order and size.
+struct Tuning {
+    long near_seg_pairs = 1L << 17;    // FP32 near field: source-target pairs per work segment (CTA)
+    long nearff_seg_pairs = 1L << 14;  // float-float near field
+    int tc_form = 2;  // tensor-core M2L: 2 = two CTAs of two row tiles per SM, 4 = one CTA of four,
+                      // 0 = persistent (scaled FP16 form only)
+};
+// The table's parameters for Chebyshev order `order` and npoints sources (the entry of that order
+// with the largest min_points <= npoints; defaults without one).  IBIM_TC_RT overrides tc_form.
+Tuning tuning_for(int order, long npoints);
+// Plans made on this thread while t is set use it instead of the table; nullptr restores the table.
+void tuning_override(const Tuning *t);
+
 // Tree over the sources + operators + target sets.
 struct Plan {
     Ctx *ctx;
     Tube *tube;                 // sources
     long ns;
     int p, R, maxpoint, maxlevel, precision;
+    Tuning tune;  // launch parameters for this plan's order and size
     TreeHost tree;
     // sources in tree order
     DevBuf<double> sx, sy, sz, snx, sny, snz, sw;  // sw = w * h^3
@@ -324,6 +339,7 @@ struct Plan {
     bool batched = false;
     DevBuf<int> node_mol;
     DevBuf<float4> kmol32, kmolff;
+    DevBuf<int> mol_active;  // 1 while a molecule iterates: the heavy kernels skip the others' work
     ~Plan() { for (auto *t : targets) delete t; }
 };
 

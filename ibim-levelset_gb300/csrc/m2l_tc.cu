@@ -135,7 +135,10 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
     k_m2l_tc(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
                 const int *__restrict__ vtgt, const void *__restrict__ a_hi_, const void *__restrict__ a_lo_,
                 const void *__restrict__ b_hi_, const void *__restrict__ b_lo_, const float *__restrict__ rscale,
-                const float *__restrict__ cscale, float *local, int *err) {
+                const float *__restrict__ cscale, float *local, int *err, const int *__restrict__ chunk_mol,
+                const int *__restrict__ mol_active) {
+    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole
+    if (chunk_mol && !mol_active[chunk_mol[blockIdx.x]]) return;
     using SH = TcShape<N, RT, CPS>;
     constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
     constexpr int KS = H16 ? TC_KS16 : TC_KS, ES = H16 ? 2 : 4;  // K elements per stage, bytes per element
@@ -1321,7 +1324,10 @@ template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_m2l_oz(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
              const int *__restrict__ vtgt, const uint16_t *__restrict__ a, const double *__restrict__ sig,
-             const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err) {
+             const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err,
+             const int *__restrict__ chunk_mol, const int *__restrict__ mol_active) {
+    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole
+    if (chunk_mol && !mol_active[chunk_mol[blockIdx.x]]) return;
     using SH = OzShape<S>;
     constexpr int NST = SH::NST, LAG = SH::LAG, STAGE = SH::STAGE;
     extern __shared__ __align__(1024) unsigned char oz_smem[];
@@ -1542,19 +1548,10 @@ static bool tc_fp16() {
 
 bool m2l_tc_fp16_form() { return tc_fp16(); }
 
-// Launch form of the contraction: two CTAs of two row tiles per SM (default: one CTA's prologue
-// and epilogue overlap the other's MMAs; 2.32 ms a launch on the 2,000-atom protein),
-// IBIM_TC_RT=4 (one CTA of four row tiles per SM; 2.50 ms) or, FP16 form only, IBIM_TC_RT=P
-// (persistent: one CTA per SM walking units of two row tiles with double-buffered accumulators;
-// 2.94 ms).
-static int tc_launch_form() {
-    static const int f = [] {
-        const char *v = std::getenv("IBIM_TC_RT");
-        return v && v[0] == '4' ? 4 : (v && v[0] == 'P' ? 0 : 2);
-    }();
-    return f;
-}
-static bool tc_two_per_sm() { return tc_launch_form() != 4; }
+// Launch form of the contraction (the plan's tuning, tuning.cpp): two CTAs of two row tiles per SM
+// (2: one CTA's prologue and epilogue overlap the other's MMAs; 2.32 ms a launch on the 2,000-atom
+// protein), one CTA of four row tiles per SM (4; 2.50 ms) or, FP16 form only, persistent (0: one
+// CTA per SM walking units of two row tiles with double-buffered accumulators; 2.94 ms).
 
 void m2l_tc_pack(Plan &P, const float2 *ff) {
     P.tc_h16 = tc_fp16();
@@ -1639,7 +1636,7 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         IBIM_CHECK_LAUNCH();
         return;
     }
-    if (P.tc_h16 && tc_launch_form() == 0) {
+    if (P.tc_h16 && P.tune.tc_form == 0) {
         static_assert(N == 128, "persistent form: 128-pair chunks");
         const int nunits = S.nchunks_tc * ((mt + TCP_RT - 1) / TCP_RT);
         const int grid = std::min(nunits, P.ctx->num_sms);
@@ -1650,14 +1647,14 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         IBIM_CHECK_LAUNCH();
         return;
     }
-    if (tc_two_per_sm()) {
+    if (P.tune.tc_form != 4) {
         using SH2 = TcShape<N, 2, 2>;
         const dim3 grid(S.nchunks_tc, (mt + SH2::RT - 1) / SH2::RT);
         auto kern = P.tc_h16 ? k_m2l_tc<N, true, 2, 2> : k_m2l_tc<N, false, 2, 2>;
         (count_launch(), kern<<<grid, TC_THREADS, SH2::SMEM, s>>>(
                              n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr,
-                             P.tc_err.ptr));
+                             P.tc_err.ptr, S.chunk_mol_tc.ptr, P.mol_active.ptr));
         IBIM_CHECK_LAUNCH();
         return;
     }
@@ -1665,7 +1662,8 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     auto kern = P.tc_h16 ? k_m2l_tc<N, true> : k_m2l_tc<N, false>;
     (count_launch(), kern<<<grid, TC_THREADS, TcShape<N>::SMEM, s>>>(
                          n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr, P.tc_a_lo.ptr,
-                         P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr));
+                         P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr,
+                         S.chunk_mol_tc.ptr, P.mol_active.ptr));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -1738,7 +1736,8 @@ void m2l_oz_run(Plan &P, const TargetSet &S) {
         const int smem = ns == 6 ? OzShape<6>::SMEM : OzShape<7>::SMEM;
         (count_launch(), kern<<<grid, OZ_THREADS, smem, s>>>(n4, P.oz_kpad, P.oz_mtiles, S.v_chunk_oz.ptr, S.v_src.ptr,
                                                             S.v_tgt.ptr, P.oz_a.ptr, P.oz_sig.ptr, P.oz_b.ptr,
-                                                            P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr));
+                                                            P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr, S.chunk_mol_oz.ptr,
+                                                            P.mol_active.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
                                                  const float *__restrict__ tzh, const float *__restrict__ txl,
                                                  const float *__restrict__ tyl, const float *__restrict__ tzl, long nt,
                                                  double *out, const float4 *__restrict__ kmol,
-                                                 const int *__restrict__ node_mol) {
+                                                 const int *__restrict__ node_mol, const int *__restrict__ mol_active) {
     __shared__ float S[14][TILEF];
     __shared__ double red[NTF][4];
     __shared__ float2 E0[64], E1[64];
@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(NTF) k_near_ff(KParamsFF kp, const int4 *__res
         const int tb = tb_[leaf], te = te_[leaf];
         KapFF kap = kap_of(kp);
         if (BATCH) {
+            if (!mol_active[node_mol[leaf]]) continue;  // the molecule has stopped iterating
             const float4 km = kmol[node_mol[leaf]];
             kap = {{km.x, km.y}, {km.z, km.w}, km.x != 0.f};
         }
@@ -422,7 +423,7 @@ void near_ff_run(Plan &P, const TargetSet &S, const KParamsFF &kp, double *out, 
     (count_launch(), kern<<<grid, NTF, 0, st>>>(kp, reinterpret_cast<const int4 *>(S.nearff_seg.ptr), S.nnearff_seg,
                                                 next, S.near32_range.ptr, S.near32_off.ptr, S.near32_offl.ptr,
                                                 S.tbeg.ptr, S.tend.ptr, P.src16.ptr, xh, yh, zh, xl, yl, zl, S.nt, out,
-                                                P.kmolff.ptr, P.node_mol.ptr));
+                                                P.kmolff.ptr, P.node_mol.ptr, P.mol_active.ptr));
     IBIM_CHECK_LAUNCH();
 }
 

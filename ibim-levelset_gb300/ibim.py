@@ -20,6 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libibim_gb300.so")
+TUNING_TABLE = os.path.join(HERE, "tuning_gb300.txt")
 
 OK = 0
 ERR_INVALID_ARGUMENT = 1
@@ -52,6 +53,7 @@ EXPORTS = [
     "ibim_levelset_evolve_static", "ibim_server_create", "ibim_server_destroy", "ibim_server_submit",
     "ibim_server_poll", "ibim_server_wait", "ibim_server_stats", "ibim_request_bytes_estimate", "ibim_gmres_host",
     "ibim_grid_set_geometry", "ibim_batch_solve", "ibim_server_create_lockstep", "ibim_fmm_bytes_estimate",
+    "ibim_tuning_set", "ibim_tuning_clear", "ibim_tuning_get", "ibim_tuning_load", "ibim_autotune",
 ]
 PROFILE_CATEGORIES = ["expand", "weno_stage", "count_gradient", "flood_fill", "tube_extract", "m2l_operators", "p2m",
                       "m2m", "m2l_v", "m2l_x", "l2l", "near_l2p", "rhs", "gmres_vectors", "m2l_v_fp64", "m2l_x_fp64",
@@ -169,6 +171,11 @@ def lib():
         "ibim_server_stats": ([_vp, _dp], C.c_int),
         "ibim_request_bytes_estimate": ([C.POINTER(Config)], C.c_double),
         "ibim_fmm_bytes_estimate": ([C.POINTER(Config), C.c_long], C.c_double),
+        "ibim_tuning_set": ([C.c_int, C.c_long, C.c_long, C.c_long, C.c_int], C.c_int),
+        "ibim_tuning_clear": ([], C.c_int),
+        "ibim_tuning_get": ([C.c_int, C.c_long, _lp], C.c_int),
+        "ibim_tuning_load": ([C.c_char_p], C.c_int),
+        "ibim_autotune": ([_vp, _dp, _dp, _dp, C.c_int, C.POINTER(Config), C.c_int, C.c_long, _dp], C.c_int),
         "ibim_server_create_lockstep": ([C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_vp)], C.c_int),
         "ibim_gmres_host": ([_vp, C.c_long, APPLY_FN, _vp, _dp, _dp, C.c_int, C.c_int, C.c_double, _ip, _ip, _ip,
                              _dp], C.c_int),
@@ -178,6 +185,9 @@ def lib():
         fn.argtypes = args
         fn.restype = res
     _lib = L
+    # the launch-parameter table measured on GB300 by autotune.py
+    if os.path.exists(TUNING_TABLE):
+        _check(L.ibim_tuning_load(TUNING_TABLE.encode()))
     return L
 
 
@@ -307,17 +317,29 @@ class Context:
         res = (Result * n)()
         st = np.zeros(n, dtype=np.int32)
         done = np.zeros(n)
-        info = np.zeros(6)
+        info = np.zeros(9)
         rc = lib().ibim_batch_solve(self.h, n, na.ctypes.data_as(_ip), _p(cen), _p(chg), _p(rad), carr, max_wave,
                                     hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(done), _p(info))
         if check:
             _check(rc)
         keys = ["waves", "largest_wave", "peak_bytes", "merged_mixed_matvecs", "merged_fp64_matvecs",
-                "active_fraction"]
+                "active_fraction", "wave_ms", "prepared_bytes", "admitted_estimate_bytes"]
         out = [r.as_dict() for r in res]
         for r, t in zip(out, done.tolist()):
             r["done_ms"] = t
         return out, st.tolist(), dict(zip(keys, info.tolist()))
+
+    def autotune(self, centers, charges, radii, cfg: Config, reps=5, install_min_points=-1) -> dict:
+        """Time candidate launch parameters on this molecule (ibim_autotune); the best, with the
+        default's cost.  install_min_points >= 0 adds it to the table as (cfg.np, install_min_points)."""
+        c = _c(centers).reshape(-1, 3)
+        q = _c(charges)
+        r = _c(radii)
+        rep = np.zeros(7)
+        _check(lib().ibim_autotune(self.h, _p(c), _p(q), _p(r), len(q), C.byref(cfg), reps, install_min_points,
+                                   _p(rep)))
+        return dict(points=int(rep[0]), near_seg_pairs=int(rep[1]), nearff_seg_pairs=int(rep[2]),
+                    tc_form=int(rep[3]), best_ms=rep[4], default_ms=rep[5], candidates=int(rep[6]))
 
     def grid(self, n, lo, h, value=0.0) -> "Grid":
         g = _vp()
@@ -640,6 +662,12 @@ class Server:
 
 def request_bytes_estimate(cfg: Config) -> float:
     return float(lib().ibim_request_bytes_estimate(C.byref(cfg)))
+
+
+def tuning_get(order: int, npoints: int) -> dict:
+    out = (C.c_long * 3)()
+    _check(lib().ibim_tuning_get(order, npoints, out))
+    return dict(near_seg_pairs=out[0], nearff_seg_pairs=out[1], tc_form=out[2])
 
 
 def fmm_bytes_estimate(cfg: Config, npoints: int) -> float:

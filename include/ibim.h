@@ -279,12 +279,33 @@ int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, i
  * radii, aoff_i = natoms[0] + ... + natoms[i-1].  results[i] and statuses[i] per molecule; the
  * call returns the first failing molecule's status (others still solved).  done_ms (may be NULL)
  * receives when each molecule's result was final, in ms since the call began (its latency when
- * all are submitted at once).  info (may be NULL, 6 doubles): waves, largest wave, peak budgeted
+ * all are submitted at once).  info (may be NULL, 9 doubles): waves, largest wave, peak budgeted
  * bytes, merged mixed matvecs, merged FP64-class matvecs, mean fraction of a wave's molecules
- * still iterating per merged matvec. */
+ * still iterating per merged matvec, ms spent in waves (merge, solve, energy), device bytes the
+ * prepared molecules held, and the FMM-phase estimates they were admitted with. */
 int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
                      const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
                      ibim_result *results, int *statuses, double *done_ms, double *info);
+
+/* ---- launch-parameter table and autotuner (no counterpart in the reference) ----
+ * A plan of Chebyshev order p with N sources takes its launch parameters from the row of order p
+ * with the largest min_points <= N: pairs per work segment of the FP32 and the float-float near
+ * fields, and the tensor-core M2L's launch form (2 = two CTAs of two row tiles per SM, 4 = one CTA
+ * of four, 0 = persistent).  They change the partition of the same work only.  Without a row the
+ * defaults hold (2^17, 2^14, 2). */
+int ibim_tuning_set(int order, long min_points, long near_seg_pairs, long nearff_seg_pairs, int tc_form);
+int ibim_tuning_clear(void);
+/* out: near_seg_pairs, nearff_seg_pairs, tc_form for order and npoints */
+int ibim_tuning_get(int order, long npoints, long out[3]);
+/* Rows "order min_points near_seg_pairs nearff_seg_pairs tc_form" ('#' starts a comment). */
+int ibim_tuning_load(const char *path);
+/* Times candidate launch parameters on this molecule (mixed path): for each, a plan prepared under
+ * it and the CUDA-event time of a solve's mix of products (25 mixed, one FP64-class residual),
+ * one coordinate at a time (launch form, FP32 segments, float-float segments).  report (7
+ * doubles): tube points, best near_seg_pairs, nearff_seg_pairs, tc_form, best cost ms, default
+ * cost ms, candidates timed.  install_min_points >= 0 adds the best as the row (order, it). */
+int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, const double *radii, int natoms,
+                  const ibim_config *cfg, int reps, long install_min_points, double *report);
 
 /* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
  * Solve requests queue in arrival order and are admitted by device memory in two phases: the
