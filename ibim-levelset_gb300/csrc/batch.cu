@@ -1090,8 +1090,8 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
             Job &J = jobs[i];
             int st = wrc[t];
             std::string err = werr0[t];
-            const std::function<void(long)> admit = [&](long npoints) {
-                const double need = estimate_fmm_bytes(cfgs[i], npoints);
+            const std::function<void(long)> admit = [&](long bytes) {
+                const double need = (double)bytes;
                 std::unique_lock<std::mutex> lk(mu);
                 held_bytes -= J.held;  // the grids are gone
                 J.held = 0;

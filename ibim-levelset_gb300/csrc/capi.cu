@@ -125,6 +125,8 @@ void check_config(const ibim_config &cfg) {
                  "unknown precision");
     IBIM_REQUIRE(cfg.jacobian == 0 || cfg.jacobian == 1, "jacobian must be 0 or 1");
     IBIM_REQUIRE(cfg.kp.k3_scaled == 0 || cfg.kp.k3_scaled == 1, "k3_scaled must be 0 or 1");
+    IBIM_REQUIRE(cfg.narrow_band == 0 || cfg.narrow_band >= 2 * cfg.thickness + 6,
+                 "narrow_band must be 0 (whole grid) or at least 2 thickness + 6 cells");
 }
 
 void fill_plan_stats(const Plan &P, ibim_result &res) {
@@ -145,13 +147,13 @@ static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *
     Grid *phi0 = nullptr;
     try {
         levelset_expand(*g, centers_dev, radii_dev, natoms, cfg.probe, cfg.band);
-        levelset_evolve(*g, cfg.probe, 1.0, 0.2);
+        levelset_evolve(*g, cfg.probe, 1.0, 0.2, cfg.narrow_band);
         grid_scale(*g, -1.0);
         phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0., gprec);
         grid_copy(*phi0, *g);
-        steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
+        steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres, cfg.narrow_band);
         grid_copy(*phi0, *g);
-        steps[1] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
+        steps[1] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres, cfg.narrow_band);
     } catch (...) {
         delete phi0;
         delete g;
@@ -189,8 +191,6 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
     res.t_surface_ms = t1.ms();
     trace_mark("solve: level set + surface");
     IBIM_REQUIRE(tube->n > 0, "the level set has no tube points");
-    // the caller may hold the FMM phase back until device memory for this many points is free
-    if (after_surface) (*after_surface)(tube->n);
     try {
         out.atoms4 = atoms4_dev;
         if (!out.atoms4) {
@@ -209,6 +209,9 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
         out.P = make_plan(tube, true, centers_host, natoms, cfg.np, cfg.maxpoint, cfg.maxlevel, cfg.precision);
         Plan *P = out.P;
         IBIM_CUDA(cudaStreamSynchronize(s));
+        // the caller may hold the operators back until their device memory (the plan's exact
+        // operator and node counts) is free
+        if (after_surface) (*after_surface)((long)std::llround(plan_fmm_bytes(*P, cfg)));
         const auto w1 = std::chrono::steady_clock::now();
         res.t_tree_ms = std::chrono::duration<double, std::milli>(w1 - w0).count();
         trace_mark("solve: plan synced");

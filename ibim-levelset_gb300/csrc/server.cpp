@@ -1,9 +1,10 @@
 // Request loop on one GPU (no counterpart in the reference: main.cpp solves one molecule per
 // process).  Solve requests queue in arrival order and are admitted by device memory in two
 // phases: a request starts (its level set) when its grids fit in the HBM budget beside what the
-// requests in flight hold, and once its tube is extracted its FMM phase (plan, operator images,
-// Krylov basis) is admitted by an estimate from the actual tube point count; a phase is always
-// admitted when no other request holds memory of that phase, so the loop cannot stall.
+// requests in flight hold, and once its tree and lists are built its FMM phase (operator images,
+// expansions, Krylov basis) is admitted by the bytes its exact operator, node and point counts
+// need; a phase is always admitted when no other request holds memory of that phase, so the loop
+// cannot stall.
 //
 // Two ways to run the admitted requests:
 //   pool      (ibim_server_create) `slots` worker threads, each with its own context, run whole
@@ -82,12 +83,7 @@ double estimate_levelset_bytes(const ibim_config &cfg) {
 // (mixed: FP16 hi / lo tiles, BF16 digit tiles and the float-float operators they are cut from;
 // FP64: the FP64 operator), per node the expansions and multipole images, per point ~1.1 KB plus
 // the Krylov basis.
-double estimate_fmm_bytes(const ibim_config &cfg, long npoints) {
-    const double N = (double)std::max(1L, npoints);
-    const double mp = std::max(1, cfg.maxpoint);
-    const double nodes = 4.8 * N / mp + 1.0;
-    const double levels = std::ceil(std::log(std::max(1.0, N / mp)) / std::log(8.0)) + 1.0;
-    const double ops = 600.0 * std::max(1.0, levels);
+static double fmm_bytes(const ibim_config &cfg, double N, double nodes, double ops) {
     const double n4 = 4.0 * cfg.np * cfg.np * cfg.np;
     const double kpad = std::ceil(n4 / 16.0) * 16.0, mpad = std::ceil(n4 / 128.0) * 128.0;
     const double digits = kpad <= 800 ? 6.0 : 7.0;
@@ -101,6 +97,17 @@ double estimate_fmm_bytes(const ibim_config &cfg, long npoints) {
     }
     const double per_point = 1100.0 + 16.0 * (std::min(cfg.restart, 250) + 1);
     return ops * per_op + nodes * per_node + N * per_point;
+}
+
+double estimate_fmm_bytes(const ibim_config &cfg, long npoints) {
+    const double N = (double)std::max(1L, npoints);
+    const double mp = std::max(1, cfg.maxpoint);
+    const double levels = std::ceil(std::log(std::max(1.0, N / mp)) / std::log(8.0)) + 1.0;
+    return fmm_bytes(cfg, N, 4.8 * N / mp + 1.0, 600.0 * std::max(1.0, levels));
+}
+
+double plan_fmm_bytes(const Plan &P, const ibim_config &cfg) {
+    return fmm_bytes(cfg, (double)P.ns, (double)P.tree.nnodes, (double)P.nops);
 }
 
 // Before the level set runs the tube size is unknown: guessed as a fifth of the grid's cells in
@@ -138,10 +145,10 @@ Request *take_head(ibim_server_s *S) {
     return r;
 }
 
-// The FMM-phase admission of request r with npoints tube points (its grids are released first).
+// The FMM-phase admission of request r needing `bytes` (its grids are released first).
 std::function<void(long)> fmm_admission(ibim_server_s *S, Request *r) {
-    return [S, r](long npoints) {
-        const double need = ibim::estimate_fmm_bytes(r->cfg, npoints);
+    return [S, r](long bytes) {
+        const double need = (double)bytes;
         std::unique_lock<std::mutex> lk(S->mu);
         S->in_flight_bytes -= r->held;
         r->held = 0;

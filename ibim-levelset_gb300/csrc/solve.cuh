@@ -59,8 +59,8 @@ struct SolvePrep {
         delete tube;
     }
 };
-// after_surface (optional) runs once the tube is extracted, with its point count, before the
-// plan and operators are built (an admission point for the FMM phase's device memory).
+// after_surface (optional) runs once the plan's tree and lists exist, before its operators and
+// images are built, with the FMM phase's device bytes (plan_fmm_bytes): an admission point.
 void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, const double *centers_host,
                    const double *charges_host, int natoms, const ibim_config &cfg, ibim_result &res,
                    const double *atoms4_dev, SolvePrep &out,
@@ -72,6 +72,8 @@ void solve_host(Ctx *c, const double *centers, const double *charges, const doub
 // the FMM phase for npoints tube points (plan, operator images at their peak, Krylov basis).
 double estimate_levelset_bytes(const ibim_config &cfg);
 double estimate_fmm_bytes(const ibim_config &cfg, long npoints);
+// The FMM phase's bytes for a built plan (its operator and node counts are exact).
+double plan_fmm_bytes(const Plan &P, const ibim_config &cfg);
 // A request's footprint before its level set runs (the FMM phase for a tube point count guessed
 // from the grid).
 double estimate_request_bytes(const ibim_config &cfg);

@@ -100,6 +100,10 @@ typedef struct {
     int jacobian;      /* opt-in, 0 = the reference: 1 multiplies each tube weight by the surface
                           Jacobian 1 - phi (k1 + k2) + phi^2 k1 k2 of the level set through the
                           grid point (levelset.cpp:576 has no Jacobian) */
+    int narrow_band;   /* opt-in, 0 = the reference (every stage sweeps the whole grid,
+                          levelset.cpp:131-183, 216-281): > 0 advances only the cells within that
+                          many cells of the zero level set (rebuilt every 4 steps; the others keep
+                          their value); at least 2 thickness + 6 */
 } ibim_config;
 
 typedef struct {
@@ -310,10 +314,9 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
 /* ---- request loop (no counterpart in the reference: main.cpp solves one molecule per run) ----
  * Solve requests queue in arrival order and are admitted by device memory in two phases: the
  * head of the queue starts (its level set) when its grids fit in hbm_budget_bytes beside what the
- * requests in flight hold; once its tube is extracted, its FMM phase (plan, operator images,
- * Krylov basis) waits until the bytes estimated from the actual point count fit
- * (ibim_fmm_bytes_estimate).  A phase is always admitted when no other request holds memory of
- * that phase.  Each request keeps its level set, tree, operators and Krylov basis resident until
+ * requests in flight hold; once its octree and lists are built, its FMM phase (operator images,
+ * expansions, Krylov basis) waits until the bytes its exact operator, node and point counts need
+ * fit.  A phase is always admitted when no other request holds memory of that phase.  Each request keeps its level set, tree, operators and Krylov basis resident until
  * it finishes.
  * ibim_server_create: `slots` worker threads, each with its own context and stream, run whole
  * solves concurrently on the device. */
@@ -341,8 +344,8 @@ int ibim_server_wait(ibim_server s, long id, int *status, ibim_result *res, doub
 int ibim_server_stats(ibim_server s, double stats[8]);
 /* A solve's device footprint estimated from its configuration alone (before its level set). */
 double ibim_request_bytes_estimate(const ibim_config *cfg);
-/* The FMM phase's device footprint for a tube of npoints points, which the request loops admit
- * once the tube is extracted. */
+/* The FMM phase's device footprint for a tube of npoints points, estimated before the tree is
+ * built (the request loops admit that phase with the built tree's exact counts). */
 double ibim_fmm_bytes_estimate(const ibim_config *cfg, long npoints);
 
 #ifdef __cplusplus
