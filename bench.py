@@ -75,6 +75,7 @@ def parse():
                          "concurrent whole solves; serve: the request loop in lock-step or pool mode")
     ap.add_argument("--max-wave", type=int, default=32, help="batch lockstep: molecules per wave")
     ap.add_argument("--workers", type=int, default=4, help="batch lockstep: preparation threads")
+    ap.add_argument("--wave-slots", type=int, default=2, help="batch lockstep: waves solved at once")
     ap.add_argument("--atoms", type=str, default=None, help="serve/batch: log-uniform atom-count range")
     ap.add_argument("--accuracy-sample", type=int, default=2,
                     help="serve/batch: requests (smallest first) re-solved alone in FP64 to state the error")
@@ -629,7 +630,7 @@ def run_batch_lockstep(args):
     sampler.start()
     t0 = time.perf_counter()
     res, st, info = ctx.batch_solve(mols, cfgs, max_wave=args.max_wave, hbm_budget_bytes=150e9,
-                                    workers=args.workers)
+                                    workers=args.workers, wave_slots=args.wave_slots)
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     lat = np.array([r["done_ms"] for r in res])
@@ -644,7 +645,7 @@ def run_batch_lockstep(args):
            "value": len(res) / wall, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
            "dtype": "f32+f64", "data": "synthetic (seeded generator)",
            "config": {"workload": "batch", "mode": "lockstep", "molecules": len(reqs), "max_wave": args.max_wave,
-                      "workers": args.workers, "atoms_range": [lo, hi], "h": 0.5, "kappa_range": [0.0, 0.15],
+                      "workers": args.workers, "wave_slots": args.wave_slots, "atoms_range": [lo, hi], "h": 0.5, "kappa_range": [0.0, 0.15],
                       "eps_out": 80.0, "chebyshev_order": 5, "precision": "mixed", "hbm_budget_gb": 150},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "mean": float(lat.mean())},

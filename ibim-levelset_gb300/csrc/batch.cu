@@ -1011,8 +1011,8 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
 // ---------------------------------------------------------------------------------------------
 
 void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
-                 const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
-                 ibim_result *results, int *statuses, double *done_ms, double *info) {
+                 const double *radii, const ibim_config *cfgs, int max_wave, int wave_slots, double budget,
+                 int workers, ibim_result *results, int *statuses, double *done_ms, double *info) {
     const auto t_call = std::chrono::steady_clock::now();
     auto since_call = [&] {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
@@ -1029,6 +1029,7 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     IBIM_REQUIRE(m2l_tc_supported() && mixed_uses_tc() && m2l_tc_fp16_form() && near_ff_enabled() && ops_ff_enabled(),
                  "batch: needs the tensor-core mixed path (sm_103a, default switches)");
     max_wave = std::max(1, max_wave);
+    wave_slots = std::max(1, std::min(wave_slots, 4));
     workers = std::max(1, std::min(workers, 16));
     if (budget <= 0) budget = 150e9;
     std::vector<long> aoff(nmol + 1, 0);
@@ -1171,83 +1172,111 @@ void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, con
     int waves = 0, largest = 0;
     long merged_mixed = 0, merged_fp64 = 0;
     double active_w = 0, wave_ms = 0, bytes_actual = 0, bytes_est = 0;
-    int done = 0;
-    try {
-        while (done < nmol) {
-            std::vector<int> wave;
-            {
-                std::unique_lock<std::mutex> lk(mu);
-                // a wave: the next prepared molecules in order, up to max_wave; it starts when full,
-                // when nothing is left to prepare, or when a worker waits for memory the wave holds
-                cv.wait(lk, [&] {
+    int done = 0;  // the next molecule not yet given to a wave
+    // wave solvers: the caller's context and wave_slots - 1 more, each taking the next wave when
+    // it is free, so that one wave's host synchronisations and launch gaps overlap another's work
+    std::vector<ibim_ctx> sctx(std::max(0, wave_slots - 1), nullptr);
+    for (auto &x : sctx)
+        if (ibim_ctx_create(device, &x) != IBIM_OK) x = nullptr;
+    std::exception_ptr solver_error;
+    auto solver = [&](Ctx *sc) {
+        try {
+            for (;;) {
+                std::vector<int> wave;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    // a wave: the next prepared molecules in order, up to max_wave; it starts when
+                    // full, when nothing is left to prepare, or when a worker waits for memory
+                    cv.wait(lk, [&] {
+                        if (done >= nmol || solver_error) return true;
+                        int e = done;
+                        while (e < nmol && jobs[e].ready && e - done < max_wave) ++e;
+                        if (e == done) return false;
+                        if (e - done >= max_wave || e == nmol) return true;
+                        return nwaiting > 0 || (next < nmol && !can_take());
+                    });
+                    if (done >= nmol || solver_error) break;
                     int e = done;
-                    while (e < nmol && jobs[e].ready && e - done < max_wave) ++e;
-                    if (e == done) return false;
-                    if (e - done >= max_wave || e == nmol) return true;
-                    return nwaiting > 0 || (next < nmol && !can_take());
-                });
-                int e = done;
-                while (e < nmol && jobs[e].ready && (int)wave.size() < max_wave) {
-                    if (statuses[e] == IBIM_OK) wave.push_back(e);
-                    ++e;
+                    while (e < nmol && jobs[e].ready && (int)wave.size() < max_wave) {
+                        if (statuses[e] == IBIM_OK) wave.push_back(e);
+                        ++e;
+                    }
+                    done = e;
                 }
-                done = e;
-            }
-            if (wave.empty()) continue;
-            set_current_ctx(c);
-            IBIM_CUDA(cudaSetDevice(device));
-            std::vector<BatchMol> bm(wave.size());
-            double wave_bytes = 0;
-            for (size_t k = 0; k < wave.size(); ++k) {
-                Job &J = jobs[wave[k]];
-                bm[k] = J.bm;
-                J.bm.prep = nullptr;
-                J.bm.b_tree = nullptr;
-                wave_bytes += J.held;
-                bytes_actual += J.bm.bytes;
-                bytes_est += J.est_fmm;
-            }
-            WaveStats ws;
-            int wst = IBIM_OK;
-            std::string werr;
-            try {
-                batch_wave(c, bm, ws);
-            } catch (const Error &e) {
-                wst = e.status;
-                werr = e.what();
-            } catch (const std::exception &e) {
-                wst = IBIM_ERR_INVALID_ARGUMENT;
-                werr = e.what();
-            }
-            const double t_wave_done = since_call();
-            for (auto &b : bm) {
-                delete b.prep;
-                delete b.b_tree;
-                if (wst != IBIM_OK) {
-                    statuses[b.index] = wst;
-                    jobs[b.index].err = werr;
+                cv.notify_all();
+                if (wave.empty()) continue;
+                set_current_ctx(sc);
+                IBIM_CUDA(cudaSetDevice(device));
+                std::vector<BatchMol> bm(wave.size());
+                double wave_bytes = 0, wb_act = 0, wb_est = 0;
+                for (size_t k = 0; k < wave.size(); ++k) {
+                    Job &J = jobs[wave[k]];
+                    bm[k] = J.bm;
+                    J.bm.prep = nullptr;
+                    J.bm.b_tree = nullptr;
+                    wave_bytes += J.held;
+                    wb_act += J.bm.bytes;
+                    wb_est += J.est_fmm;
                 }
-                if (done_ms) done_ms[b.index] = t_wave_done;
+                WaveStats ws;
+                int wst = IBIM_OK;
+                std::string werr;
+                try {
+                    batch_wave(sc, bm, ws);
+                } catch (const Error &e) {
+                    wst = e.status;
+                    werr = e.what();
+                } catch (const std::exception &e) {
+                    wst = IBIM_ERR_INVALID_ARGUMENT;
+                    werr = e.what();
+                }
+                const double t_wave_done = since_call();
+                for (auto &b : bm) {
+                    delete b.prep;
+                    delete b.b_tree;
+                }
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    for (auto &b : bm) {
+                        if (wst != IBIM_OK) {
+                            statuses[b.index] = wst;
+                            jobs[b.index].err = werr;
+                        }
+                        if (done_ms) done_ms[b.index] = t_wave_done;
+                    }
+                    waves++;
+                    wave_ms += ws.t_merge_ms + ws.t_solve_ms + ws.t_energy_ms;
+                    largest = std::max(largest, (int)wave.size());
+                    merged_mixed += ws.merged_mixed;
+                    merged_fp64 += ws.merged_fp64;
+                    active_w += ws.active_frac * wave.size();
+                    bytes_actual += wb_act;
+                    bytes_est += wb_est;
+                    held -= (int)wave.size();
+                    held_fmm -= (int)wave.size();
+                    held_bytes -= wave_bytes;
+                    if (held == 0) held_bytes = 0;
+                    for (int i : wave) jobs[i].held = 0;
+                }
+                cv.notify_all();
             }
-            waves++;
-            wave_ms += ws.t_merge_ms + ws.t_solve_ms + ws.t_energy_ms;
-            largest = std::max(largest, (int)wave.size());
-            merged_mixed += ws.merged_mixed;
-            merged_fp64 += ws.merged_fp64;
-            active_w += ws.active_frac * wave.size();
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                held -= (int)wave.size();
-                held_fmm -= (int)wave.size();
-                held_bytes -= wave_bytes;
-                if (held == 0) held_bytes = 0;
-                for (int i : wave) jobs[i].held = 0;
-            }
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(mu);
+            if (!solver_error) solver_error = std::current_exception();
             cv.notify_all();
         }
-    } catch (...) {
+    };
+    std::vector<std::thread> solvers;
+    for (ibim_ctx x : sctx)
+        if (x) solvers.emplace_back(solver, &x->c);
+    solver(c);
+    for (auto &t : solvers) t.join();
+    for (ibim_ctx x : sctx)
+        if (x) ibim_ctx_destroy(x);
+    set_current_ctx(c);
+    if (solver_error) {
         release_all();
-        throw;
+        std::rethrow_exception(solver_error);
     }
     release_all();
     std::string first_error;

@@ -1020,14 +1020,15 @@ int ibim_solve_dev(ibim_ctx ctx, const double *centers_dev, const double *charge
 }
 
 int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
-                     const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
-                     ibim_result *results, int *statuses, double *done_ms, double *info) {
+                     const double *radii, const ibim_config *cfgs, int max_wave, int wave_slots,
+                     double hbm_budget_bytes, int workers, ibim_result *results, int *statuses, double *done_ms,
+                     double *info) {
     return guard([&] {
         IBIM_REQUIRE(ctx, "null context");
         Ctx *c = &ctx->c;
         bind(c);
-        batch_solve(c, nmol, natoms, centers, charges, radii, cfgs, max_wave, hbm_budget_bytes, workers, results,
-                    statuses, done_ms, info);
+        batch_solve(c, nmol, natoms, centers, charges, radii, cfgs, max_wave, wave_slots, hbm_budget_bytes, workers,
+                    results, statuses, done_ms, info);
         for (int i = 0; i < nmol; ++i)
             if (statuses[i] != IBIM_OK) throw Error(statuses[i], ibim_last_error());
     });

@@ -10,7 +10,7 @@
 //   pool      (ibim_server_create) `slots` worker threads, each with its own context, run whole
 //             solves concurrently on the device
 //   lock-step (ibim_server_create_lockstep) worker threads prepare requests (level set, tube,
-//             right-hand side, plan, operator images; batch.cu) while a solver thread takes the
+//             right-hand side, plan, operator images; batch.cu) while two solver threads take the
 //             prepared requests in waves: a wave merges their plans so that every FMM stage is one
 //             launch for all of them, and their GMRES iterations advance together.  Requests that
 //             arrive while a wave runs are prepared meanwhile and join the next wave (continuous
@@ -63,7 +63,7 @@ struct ibim_server_s {
     long next_id = 1, submitted = 0, completed = 0, waves = 0;
     bool stop = false;
     std::vector<std::thread> workers;
-    std::thread solver;
+    std::vector<std::thread> solvers;  // lock-step: wave solvers (two waves at once)
     std::vector<ibim_ctx> wctx;  // the workers' contexts (prepared requests keep buffers on their streams)
 };
 
@@ -343,11 +343,15 @@ void stop_threads(ibim_server_s *S) {
     S->cv_work.notify_all();
     for (auto &t : S->workers)
         if (t.joinable()) t.join();
-    if (S->solver.joinable()) S->solver.join();
+    for (auto &t : S->solvers)
+        if (t.joinable()) t.join();
     for (ibim_ctx c : S->wctx)
         if (c) ibim_ctx_destroy(c);
     S->wctx.clear();
 }
+
+// waves solved at once by the lock-step loop, each on its own context and stream
+constexpr int kWaveSlots = 2;
 
 int create(int device, int slots, int max_wave, double budget, bool lockstep, ibim_server *out) {
     if (!out || slots < 1 || slots > 64 || !(budget > 0) || max_wave < 1) {
@@ -371,7 +375,7 @@ int create(int device, int slots, int max_wave, double budget, bool lockstep, ib
             for (int i = 0; i < slots; ++i)
                 if (ibim_ctx_create(device, &S->wctx[i]) != IBIM_OK) S->wctx[i] = nullptr;
             for (int i = 0; i < slots; ++i) S->workers.emplace_back(lockstep_worker, S, i);
-            S->solver = std::thread(lockstep_solver, S);
+            for (int i = 0; i < kWaveSlots; ++i) S->solvers.emplace_back(lockstep_solver, S);
         } else {
             for (int i = 0; i < slots; ++i) S->workers.emplace_back(pool_worker, S);
         }

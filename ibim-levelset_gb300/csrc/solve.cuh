@@ -109,7 +109,7 @@ void fill_plan_stats(const Plan &P, ibim_result &res);
 void atoms_to_device(Ctx *c, const double *centers, const double *charges, int natoms, DevBuf<double> &a4);
 // Many molecules in lock-step waves (batch.cu; the C ABI's ibim_batch_solve).
 void batch_solve(Ctx *c, int nmol, const int *natoms, const double *centers, const double *charges,
-                 const double *radii, const ibim_config *cfgs, int max_wave, double budget, int workers,
-                 ibim_result *results, int *statuses, double *done_ms, double *info);
+                 const double *radii, const ibim_config *cfgs, int max_wave, int wave_slots, double budget,
+                 int workers, ibim_result *results, int *statuses, double *done_ms, double *info);
 
 }  // namespace ibim

@@ -125,8 +125,8 @@ def lib():
         "ibim_grid_download": ([_vp, _dp], C.c_int),
         "ibim_grid_scale": ([_vp, C.c_double], C.c_int),
         "ibim_grid_set_geometry": ([_vp, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
-        "ibim_batch_solve": ([_vp, C.c_int, _ip, _dp, _dp, _dp, C.POINTER(Config), C.c_int, C.c_double, C.c_int,
-                              C.POINTER(Result), _ip, _dp, _dp], C.c_int),
+        "ibim_batch_solve": ([_vp, C.c_int, _ip, _dp, _dp, _dp, C.POINTER(Config), C.c_int, C.c_int, C.c_double,
+                              C.c_int, C.POINTER(Result), _ip, _dp, _dp], C.c_int),
         "ibim_grid_copy": ([_vp, _vp], C.c_int),
         "ibim_levelset_expand": ([_vp, _dp, _dp, C.c_int, C.c_double, C.c_int], C.c_int),
         "ibim_levelset_evolve": ([_vp, C.c_double, C.c_double, C.c_double], C.c_int),
@@ -305,7 +305,8 @@ class Context:
         _check(rc)
         return x, dict(iters=it.value, matvecs=mv.value, status=st.value, residual=res.value)
 
-    def batch_solve(self, molecules, cfgs, max_wave=32, hbm_budget_bytes=150e9, workers=4, check=True):
+    def batch_solve(self, molecules, cfgs, max_wave=32, hbm_budget_bytes=150e9, workers=4, wave_slots=2,
+                    check=True):
         """Many molecules in lock-step waves (ibim_batch_solve).  molecules: list of (centers, charges,
         radii); cfgs: one Config per molecule.  Returns (results, statuses, info)."""
         n = len(molecules)
@@ -319,7 +320,8 @@ class Context:
         done = np.zeros(n)
         info = np.zeros(9)
         rc = lib().ibim_batch_solve(self.h, n, na.ctypes.data_as(_ip), _p(cen), _p(chg), _p(rad), carr, max_wave,
-                                    hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(done), _p(info))
+                                    wave_slots, hbm_budget_bytes, workers, res, st.ctypes.data_as(_ip), _p(done),
+                                    _p(info))
         if check:
             _check(rc)
         keys = ["waves", "largest_wave", "peak_bytes", "merged_mixed_matvecs", "merged_fp64_matvecs",

@@ -277,7 +277,7 @@ int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, i
  * over the wave, and GMRES advances every molecule of the wave in lock-step (one merged matvec per
  * Arnoldi step, one host synchronisation per step for all molecules' Givens rotations), inside
  * the FP64 iterative refinement of IBIM_PRECISION_MIXED with one merged FP64-class residual per
- * pass.  Molecules must share h, fmm_np, eps_in/eps_out, tau, k3_scaled, restart and jacobian;
+ * pass.  wave_slots (1..4) waves run at once, each on its own stream.  Molecules must share h, fmm_np, eps_in/eps_out, tau, k3_scaled, restart and jacobian;
  * kappa, geometry, atoms and tolerances may differ; precision must be IBIM_PRECISION_MIXED.
  * Atoms of molecule i are rows aoff_i .. aoff_i + natoms[i] - 1 of centers (n, 3), charges and
  * radii, aoff_i = natoms[0] + ... + natoms[i-1].  results[i] and statuses[i] per molecule; the
@@ -288,8 +288,9 @@ int ibim_solve_pqr(ibim_ctx ctx, const char *pqr_path, const ibim_config *cfg, i
  * still iterating per merged matvec, ms spent in waves (merge, solve, energy), device bytes the
  * prepared molecules held, and the FMM-phase estimates they were admitted with. */
 int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *centers, const double *charges,
-                     const double *radii, const ibim_config *cfgs, int max_wave, double hbm_budget_bytes, int workers,
-                     ibim_result *results, int *statuses, double *done_ms, double *info);
+                     const double *radii, const ibim_config *cfgs, int max_wave, int wave_slots,
+                     double hbm_budget_bytes, int workers, ibim_result *results, int *statuses, double *done_ms,
+                     double *info);
 
 /* ---- launch-parameter table and autotuner (no counterpart in the reference) ----
  * A plan of Chebyshev order p with N sources takes its launch parameters from the row of order p
@@ -323,8 +324,9 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
 typedef struct ibim_server_s *ibim_server;
 int ibim_server_create(int device, int slots, double hbm_budget_bytes, ibim_server *out);
 /* Lock-step request loop (mixed-precision requests): `workers` threads prepare admitted requests
- * (level set, tube, right-hand side, plan, operator images) while a solver thread takes the
- * prepared ones in waves of up to max_wave requests of one shape (h, fmm_np, eps, tau, restart):
+ * (level set, tube, right-hand side, plan, operator images) while two solver threads, each on its
+ * own stream, take the prepared ones in waves of up to max_wave requests of one shape (h, fmm_np,
+ * eps, tau, restart):
  * a wave's plans are merged so that each FMM stage is one launch for all of them, and their GMRES
  * iterations advance together (as ibim_batch_solve).  Requests arriving while a wave runs are
  * prepared meanwhile and join the next wave.  Same submit / poll / wait / stats / destroy. */
