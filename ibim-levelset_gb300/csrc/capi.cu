@@ -125,8 +125,6 @@ void check_config(const ibim_config &cfg) {
                  "unknown precision");
     IBIM_REQUIRE(cfg.jacobian == 0 || cfg.jacobian == 1, "jacobian must be 0 or 1");
     IBIM_REQUIRE(cfg.kp.k3_scaled == 0 || cfg.kp.k3_scaled == 1, "k3_scaled must be 0 or 1");
-    IBIM_REQUIRE(cfg.narrow_band == 0 || cfg.narrow_band >= 2 * cfg.thickness + 6,
-                 "narrow_band must be 0 (whole grid) or at least 2 thickness + 6 cells");
 }
 
 void fill_plan_stats(const Plan &P, ibim_result &res) {
@@ -147,13 +145,13 @@ static Grid *levelset_pipeline(Ctx *c, const double *centers_dev, const double *
     Grid *phi0 = nullptr;
     try {
         levelset_expand(*g, centers_dev, radii_dev, natoms, cfg.probe, cfg.band);
-        levelset_evolve(*g, cfg.probe, 1.0, 0.2, cfg.narrow_band);
+        levelset_evolve(*g, cfg.probe, 1.0, 0.2);
         grid_scale(*g, -1.0);
         phi0 = grid_create(c, cfg.n[0], cfg.n[1], cfg.n[2], cfg.lo[0], cfg.lo[1], cfg.lo[2], cfg.h, 0., gprec);
         grid_copy(*phi0, *g);
-        steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres, cfg.narrow_band);
+        steps[0] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
         grid_copy(*phi0, *g);
-        steps[1] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres, cfg.narrow_band);
+        steps[1] = levelset_reinitialize(*g, *phi0, cfg.reinit_t, 1.0, 0.5, cfg.thickness, cfg.thres);
     } catch (...) {
         delete phi0;
         delete g;

@@ -411,11 +411,9 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
 Grid *grid_create(Ctx *c, int nx, int ny, int nz, double sx, double sy, double sz, double dx, double value,
                   int prec = IBIM_PRECISION_FP64);
 void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev, int natoms, double probe, int band);
-// band_cells > 0 (opt-in narrow band; the reference sweeps the whole grid): only cells within
-// band_cells cells of the zero level set advance.
-void levelset_evolve(Grid &g, double final_t, double vel, double cfl, int band_cells = 0);
+void levelset_evolve(Grid &g, double final_t, double vel, double cfl);
 int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,
-                          double thres, int band_cells = 0);
+                          double thres);
 void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc);
 void grid_scale(Grid &g, double s);
 void grid_copy(Grid &dst, const Grid &src);

@@ -193,26 +193,16 @@ __device__ __forceinline__ T godunov(const T n[3], const T p[3]) {
 // One TVD-RK3 stage over the whole grid.  MODE 0: evolve (phi_t + vel|grad phi| = 0);
 // MODE 1: reinitialize (phi_t + S(phi0)(|grad phi| - 1) = 0, S = phi0/sqrt(phi0^2 + dx^2)).
 // STAGE 0: u1 = g - L(g); 1: u2 = (3g + u1 - L(u1))/4; 2: g = (g + 2(u2 - L(u2)))/3.
-// BAND (the opt-in narrow band): only cells flagged in `band` advance; the others keep their
-// value, which the stage buffers carry for the stencils of their neighbours.
-template <int MODE, int STAGE, class T, bool BAND = false>
+template <int MODE, int STAGE, class T>
 __global__ void __launch_bounds__(256) k_weno_stage(Dims dm, T h, T dtv, T eps, const T *__restrict__ src, T *g, T *u1,
-                                                    T *u2, const T *__restrict__ phi0,
-                                                    const unsigned char *__restrict__ band = nullptr) {
+                                                    T *u2, const T *__restrict__ phi0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z * blockDim.z + threadIdx.z;
     if (i >= dm.nx || j >= dm.ny || k >= dm.nz) return;
-    const long I = dm.idx(i, j, k);
-    if (BAND && !band[I]) {
-        if (STAGE == 0)
-            u1[I] = g[I];
-        else if (STAGE == 1)
-            u2[I] = g[I];
-        return;
-    }
     T up[3], un[3];
     gradients(src, dm, i, j, k, h, up, un);
+    const long I = dm.idx(i, j, k);
     T L;
     if (MODE == 0) {
         L = dtv * godunov(un, up);
@@ -229,13 +219,6 @@ __global__ void __launch_bounds__(256) k_weno_stage(Dims dm, T h, T dtv, T eps, 
         u2[I] = (3 * g[I] + u1[I] - L) * (T)0.25;
     else
         g[I] = D::q(g[I] + 2 * (u2[I] - L), (T)3.0);
-}
-
-// Narrow band: cells with |g| < w.
-template <class T>
-__global__ void k_band(long n, const T *__restrict__ g, T w, unsigned char *band) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        band[i] = fabs(g[i]) < w ? 1 : 0;
 }
 
 // levelset::countGradient: among cells with |g| < thickness*dx, count | |grad g| - 1 | > thres.
@@ -499,45 +482,8 @@ void expand_t(Grid &g, const double *centers_dev, const double *radii_dev, int n
     IBIM_CHECK_LAUNCH();
 }
 
-// The narrow band (band_cells > 0): cells within band_cells cells of the zero level set, rebuilt
-// every NB_REBUILD steps (the front moves at most cfl cells a step: 0.2 evolving, 0.5 in the
-// reinitialisation).
-constexpr int NB_REBUILD = 4;
-
 template <class T>
-struct Band {
-    DevBuf<unsigned char> mask;
-    int cells = 0;
-    void rebuild(Grid &g, T *G) {
-        if (cells <= 0) return;
-        const long n = g.cells();
-        if (!mask.ptr) mask.alloc(n, g.ctx->stream);
-        ProfScope ps_(PROF_WENO);
-        (count_launch(), k_band<T><<<4 * g.ctx->num_sms, 256, 0, g.ctx->stream>>>(n, G, (T)(cells * g.dx), mask.ptr));
-    }
-};
-
-// The three TVD-RK3 stages of one step, over the whole grid or the band.
-template <int MODE, class T>
-void rk3_step(Grid &g, const Band<T> &band, T h, T dtv, T eps, T *G, T *u1, T *u2, const T *P0, double fl,
-              double by) {
-    cudaStream_t s = g.ctx->stream;
-    const Dims dm = dims_of(g);
-    const dim3 gr = stencil_grid(g), bl = stencil_block();
-    if (band.cells > 0) {
-        const unsigned char *m = band.mask.ptr;
-        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 0, T, true><<<gr, bl, 0, s>>>(dm, h, dtv, eps, G, G, u1, u2, P0, m)); }
-        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 1, T, true><<<gr, bl, 0, s>>>(dm, h, dtv, eps, u1, G, u1, u2, P0, m)); }
-        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 2, T, true><<<gr, bl, 0, s>>>(dm, h, dtv, eps, u2, G, u1, u2, P0, m)); }
-        return;
-    }
-    { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, eps, G, G, u1, u2, P0)); }
-    { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, eps, u1, G, u1, u2, P0)); }
-    { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<MODE, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, eps, u2, G, u1, u2, P0)); }
-}
-
-template <class T>
-void evolve_t(Grid &g, double final_t, double vel, double cfl, int band_cells) {
+void evolve_t(Grid &g, double final_t, double vel, double cfl) {
     double dt = cfl * g.dx / vel;
     const int steps = (int)(final_t / dt) + 1;
     dt = final_t / (double)steps;
@@ -545,14 +491,15 @@ void evolve_t(Grid &g, double final_t, double vel, double cfl, int band_cells) {
     DevBuf<T> u1, u2;
     u1.alloc(g.cells(), s);
     u2.alloc(g.cells(), s);
+    const Dims dm = dims_of(g);
+    const dim3 gr = stencil_grid(g), bl = stencil_block();
     const T dtv = (T)(dt * vel), h = (T)g.dx;
     T *G = gdata<T>(g);
     const double fl = 350.0 * g.cells(), by = 3.0 * sizeof(T) * g.cells();
-    Band<T> band;
-    band.cells = band_cells;
     for (int st = 0; st < steps; ++st) {
-        if (st % NB_REBUILD == 0) band.rebuild(g, G);
-        rk3_step<0, T>(g, band, h, dtv, (T)0, G, u1.ptr, u2.ptr, nullptr, fl, by);
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, G, G, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, u1.ptr, G, u1.ptr, u2.ptr, nullptr)); }
+        { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<0, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)0, u2.ptr, G, u1.ptr, u2.ptr, nullptr)); }
     }
     IBIM_CHECK_LAUNCH();
 }
@@ -565,8 +512,7 @@ void count_t(const Grid &g, double thickness, double thres, unsigned long long *
 }
 
 template <class T>
-int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness, double thres,
-             int band_cells) {
+int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness, double thres) {
     double dt = cfl * g.dx / vel;
     const double eps = g.dx * g.dx;
     const int steps = (int)(final_t / dt) + 1;
@@ -596,14 +542,13 @@ int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, 
         return hcnt[0];
     };
     int step = 0;
-    Band<T> band;
-    band.cells = band_cells;
     try {
         unsigned long long bad = count();
         while (bad != 0 && step < steps) {
-            if (step % NB_REBUILD == 0) band.rebuild(g, G);
             step++;
-            rk3_step<1, T>(g, band, h, dtv, (T)eps, G, u1.ptr, u2.ptr, P0, fl, by);
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, G, G, u1.ptr, u2.ptr, P0)); }
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u1.ptr, G, u1.ptr, u2.ptr, P0)); }
+            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u2.ptr, G, u1.ptr, u2.ptr, P0)); }
             bad = count();
         }
     } catch (...) {
@@ -729,13 +674,12 @@ void levelset_expand(Grid &g, const double *centers_dev, const double *radii_dev
         expand_t<float>(g, centers_dev, radii_dev, natoms, probe, band);
 }
 
-void levelset_evolve(Grid &g, double final_t, double vel, double cfl, int band_cells) {
+void levelset_evolve(Grid &g, double final_t, double vel, double cfl) {
     IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "evolve: invalid time step parameters");
-    IBIM_REQUIRE(band_cells >= 0, "evolve: negative narrow band");
     if (g.prec == IBIM_PRECISION_FP64)
-        evolve_t<double>(g, final_t, vel, cfl, band_cells);
+        evolve_t<double>(g, final_t, vel, cfl);
     else
-        evolve_t<float>(g, final_t, vel, cfl, band_cells);
+        evolve_t<float>(g, final_t, vel, cfl);
 }
 
 void levelset_count_gradient(const Grid &g, double thickness, double thres, long *bad, long *total, double *acc) {
@@ -762,14 +706,12 @@ void levelset_count_gradient(const Grid &g, double thickness, double thres, long
 }
 
 int levelset_reinitialize(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, int thickness,
-                          double thres, int band_cells) {
+                          double thres) {
     IBIM_REQUIRE(phi0.nx == g.nx && phi0.ny == g.ny && phi0.nz == g.nz && phi0.prec == g.prec,
                  "reinitialize: phi0 size or precision mismatch");
     IBIM_REQUIRE(vel > 0 && cfl > 0 && final_t >= 0, "reinitialize: invalid time step parameters");
-    IBIM_REQUIRE(band_cells >= 0, "reinitialize: negative narrow band");
-    return g.prec == IBIM_PRECISION_FP64
-               ? reinit_t<double>(g, phi0, final_t, vel, cfl, thickness, thres, band_cells)
-               : reinit_t<float>(g, phi0, final_t, vel, cfl, thickness, thres, band_cells);
+    return g.prec == IBIM_PRECISION_FP64 ? reinit_t<double>(g, phi0, final_t, vel, cfl, thickness, thres)
+                                         : reinit_t<float>(g, phi0, final_t, vel, cfl, thickness, thres);
 }
 
 // Grid::operator*= (levelset.cpp:54-59)

@@ -76,7 +76,7 @@ class Config(C.Structure):
                 ("init", C.c_double), ("probe", C.c_double), ("reinit_t", C.c_double), ("thickness", C.c_int),
                 ("thres", C.c_double), ("np", C.c_int), ("maxpoint", C.c_int), ("maxlevel", C.c_int),
                 ("kp", KernelParams), ("restart", C.c_int), ("maxiter", C.c_int), ("tol", C.c_double),
-                ("precision", C.c_int), ("jacobian", C.c_int), ("narrow_band", C.c_int)]
+                ("precision", C.c_int), ("jacobian", C.c_int)]
 
 
 class Result(C.Structure):

@@ -100,10 +100,6 @@ typedef struct {
     int jacobian;      /* opt-in, 0 = the reference: 1 multiplies each tube weight by the surface
                           Jacobian 1 - phi (k1 + k2) + phi^2 k1 k2 of the level set through the
                           grid point (levelset.cpp:576 has no Jacobian) */
-    int narrow_band;   /* opt-in, 0 = the reference (every stage sweeps the whole grid,
-                          levelset.cpp:131-183, 216-281): > 0 advances only the cells within that
-                          many cells of the zero level set (rebuilt every 4 steps; the others keep
-                          their value); at least 2 thickness + 6 */
 } ibim_config;
 
 typedef struct {
@@ -317,8 +313,8 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
  * head of the queue starts (its level set) when its grids fit in hbm_budget_bytes beside what the
  * requests in flight hold; once its octree and lists are built, its FMM phase (operator images,
  * expansions, Krylov basis) waits until the bytes its exact operator, node and point counts need
- * fit.  A phase is always admitted when no other request holds memory of that phase.  Each request keeps its level set, tree, operators and Krylov basis resident until
- * it finishes.
+ * fit.  A phase is always admitted when no other request holds memory of that phase.  Each
+ * request keeps its level set, tree, operators and Krylov basis resident until it finishes.
  * ibim_server_create: `slots` worker threads, each with its own context and stream, run whole
  * solves concurrently on the device. */
 typedef struct ibim_server_s *ibim_server;

@@ -307,7 +307,6 @@ inline ibim_config config_from(const Config &cfg, const levelset &ls) {
     c.kp.tau = cfg.num("tau");
     // opt-in modes with no counterpart in the reference (absent keys keep its behaviour)
     if (cfg.options.count("k3_scaled")) c.kp.k3_scaled = (int)cfg.num("k3_scaled");
-    if (cfg.options.count("narrow_band")) c.narrow_band = (int)cfg.num("narrow_band");
     c.jacobian = ls.jacobian;
     c.restart = (int)cfg.num("gmres_restart");
     c.maxiter = (int)cfg.num("gmres_maxiter");

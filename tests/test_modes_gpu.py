@@ -113,38 +113,3 @@ def test_kirkwood_sphere(ctx, golden, kappa):
     print("kirkwood", kappa, E0, e, errs)
     assert errs[(1, 1)] < 0.02, errs
 
-
-@pytest.mark.parametrize("case,precision", [("synth30", ibim.PRECISION_FP64), ("synth300", ibim.PRECISION_FP64),
-                                            ("synth300", ibim.PRECISION_MIXED)])
-def test_narrow_band_matches_whole_grid(ctx, golden, case, precision):
-    """Opt-in narrow band (cells within 12 cells of the zero level set advance; the reference sweeps
-    the whole grid): the same tube (point count, points within 1e-6 A) and the same energy within
-    1e-6 as the whole-grid level set."""
-    from conftest import config_for
-
-    G = golden(case)
-    P = G["params"]
-    full = config_for(P, precision)
-    band = config_for(P, precision)
-    band.narrow_band = 12
-    tubes = []
-    for cfg in (full, band):
-        g, _ = ctx.levelset(G["centers"], G["radii"], cfg)
-        tubes.append(g.surface(P["thickness"]).surface7())
-        g.close()
-    assert len(tubes[0]) == len(tubes[1])
-    assert np.abs(tubes[0] - tubes[1]).max() < 1e-6
-    e_full = ctx.solve(G["centers"], G["charges"], G["radii"], full)["energy"]
-    e_band = ctx.solve(G["centers"], G["charges"], G["radii"], band)["energy"]
-    assert abs(e_band - e_full) <= 1e-6 * abs(e_full)
-
-
-def test_narrow_band_too_thin_is_rejected(ctx, golden):
-    from conftest import config_for
-
-    G = golden("synth30")
-    cfg = config_for(G["params"])
-    cfg.narrow_band = 5
-    with pytest.raises(ibim.IbimError) as e:
-        ctx.solve(G["centers"], G["charges"], G["radii"], cfg)
-    assert e.value.status == ibim.ERR_INVALID_ARGUMENT
