@@ -50,7 +50,7 @@ UNIT = "solves/s"
 # counts on every golden case, so the CPU baseline extrapolates with it when the run itself has no
 # FP64 solve to take the count from.
 REF_MATVECS = {"synthetic_protein_2000_atoms_h0.5": 26}
-FMM_STRIDE = 8
+FMM_STRIDE = 32
 # one kernel of each family timed by the CPU sample (ids of include/ibim.h), and how many of the
 # 16 FMMs of one matvec belong to each family
 FMM_FAMILIES = (("K1", 0), ("K2", 3), ("K3", 4), ("K4", 13))

@@ -278,7 +278,7 @@ std::vector<int> cat_levels(DevBuf<int> &dst, int M, int nlev, GetNodes nodes, G
 }
 
 struct WaveMol {
-    long src_off = 0, node_off = 0, op_off = 0;
+    long src_off = 0, node_off = 0;
     long tgt_off[2] = {0, 0};
     std::vector<int> perm_atoms;  // atom target set: tree position -> atom index
 };
@@ -354,7 +354,6 @@ Plan *merge_wave(Ctx *c, Tube *mtube, const std::vector<Plan *> &mols, const std
                      "batch: molecules with different plan shapes");
         W[m].src_off = ns;
         W[m].node_off = node_off[m] = nn;
-        W[m].op_off = nops;
         ns += P.ns;
         nn += P.tree.nnodes;
         nops += P.nops;
@@ -396,6 +395,22 @@ Plan *merge_wave(Ctx *c, Tube *mtube, const std::vector<Plan *> &mols, const std
     B->m2m_level_begin = cat_levels(
         B->m2m_nodes, M, nlev, [&](int m) { return P_(m).m2m_nodes.ptr; },
         [&](int m) { return P_(m).m2m_level_begin.data(); }, [&](int m) { return P_(m).tree.nlevels; }, node_off, sms, s);
+    // image shapes per operator and per node, from a molecule with operators
+    int ref = -1;
+    for (int m = 0; m < M && ref < 0; ++m)
+        if (P_(m).nops > 0) ref = m;
+    size_t oz_node = 0;
+    if (ref >= 0) oz_node = P_(ref).oz_b.n / P_(ref).tree.nnodes;
+    // the molecules' matvec workspaces are not used again: freed before the merged ones exist
+    for (int m = 0; m < M; ++m) {
+        Plan &P = *mols[m];
+        auto drop = [&](auto &buf) {
+            buf.stream = s;
+            buf.release();
+        };
+        drop(P.mult), drop(P.local), drop(P.dens4), drop(P.mult32), drop(P.local32), drop(P.dens32);
+        drop(P.src8), drop(P.tc_b_hi), drop(P.tc_b_lo), drop(P.tc_csc), drop(P.oz_b), drop(P.oz_tau);
+    }
     // tables (the same for every molecule of one order), workspaces
     B->tables.alloc(1, s);
     dcopy(B->tables.ptr, P0.tables.ptr, 1, s);
@@ -410,35 +425,39 @@ Plan *merge_wave(Ctx *c, Tube *mtube, const std::vector<Plan *> &mols, const std
     B->src8.alloc((size_t)2 * ns, s);
     B->near_next.alloc(1, s);
     B->mixed_ready = true;
-    // operator images: per operator blocks one after the other
-    int ref = -1;  // a molecule with operators (its image shapes per operator and per node)
-    for (int m = 0; m < M && ref < 0; ++m)
-        if (P_(m).nops > 0) ref = m;
+    // operator images
     B->tc_h16 = P0.tc_h16;
     B->tc_kpad = P0.tc_kpad;
     B->tc_mpad = P0.tc_mpad;
     B->oz_kpad = P0.oz_kpad;
     B->oz_mtiles = P0.oz_mtiles;
     B->oz_s = P0.oz_s;
-    const size_t tc_op = (size_t)B->tc_mpad * B->tc_kpad / (B->tc_h16 ? 2 : 1);
     const size_t tc_node = (size_t)B->tc_kpad / (B->tc_h16 ? 2 : 1);
-    cat_buf(B->tc_a_hi, M, [&](int m) { return P_(m).tc_a_hi.ptr; }, [&](int m) { return P_(m).nops * tc_op; }, s);
-    cat_buf(B->tc_a_lo, M, [&](int m) { return P_(m).tc_a_lo.ptr; }, [&](int m) { return P_(m).nops * tc_op; }, s);
-    if (B->tc_h16) {
-        cat_buf(B->tc_rsc, M, [&](int m) { return P_(m).tc_rsc.ptr; },
-                [&](int m) { return P_(m).nops * (size_t)B->tc_mpad; }, s);
-        B->tc_csc.alloc((size_t)nn, s);
+    // the images are the bulk of a plan (GB per molecule): they stay where each molecule's plan
+    // built them, owned by the merged plan from here on, and the kernels find them by molecule
+    std::vector<MolImg> imgs(M);
+    for (int m = 0; m < M; ++m) {
+        Plan &P = *mols[m];
+        imgs[m] = MolImg{P.tc_a_hi.ptr, P.tc_a_lo.ptr, P.tc_rsc.ptr, P.oz_a.ptr, P.oz_sig.ptr};
+        auto adopt = [&](auto &own, auto &buf) {
+            if (!buf.ptr) return;
+            buf.stream = s;
+            own.push_back(std::move(buf));
+        };
+        adopt(B->own_f, P.tc_a_hi);
+        adopt(B->own_f, P.tc_a_lo);
+        adopt(B->own_f, P.tc_rsc);
+        adopt(B->own_u16, P.oz_a);
+        adopt(B->own_d, P.oz_sig);
     }
+    B->mol_img.alloc(M, s);
+    B->mol_img.upload(imgs.data(), M);
+    if (B->tc_h16) B->tc_csc.alloc((size_t)nn, s);
     B->tc_b_hi.alloc((size_t)nn * tc_node, s);
     B->tc_b_lo.alloc((size_t)nn * tc_node, s);
     B->tc_err.alloc(1, s);
     B->tc_err.zero();
     if (ref >= 0) {
-        const Plan &Pr = P_(ref);
-        const size_t oz_op = Pr.oz_a.n / Pr.nops, sig_op = Pr.oz_sig.n / Pr.nops;
-        const size_t oz_node = Pr.oz_b.n / Pr.tree.nnodes;
-        cat_buf(B->oz_a, M, [&](int m) { return P_(m).oz_a.ptr; }, [&](int m) { return P_(m).nops * oz_op; }, s);
-        cat_buf(B->oz_sig, M, [&](int m) { return P_(m).oz_sig.ptr; }, [&](int m) { return P_(m).nops * sig_op; }, s);
         B->oz_b.alloc((size_t)nn * oz_node, s);
         B->oz_tau.alloc((size_t)nn, s);
     }
@@ -511,7 +530,7 @@ Plan *merge_wave(Ctx *c, Tube *mtube, const std::vector<Plan *> &mols, const std
         auto npair = [&](int m) { return (long)S_(m).nvpairs; };
         cat_shift(T->v_src, M, 1, 0, [&](int m) { return S_(m).v_src.ptr; }, npair, add_node, sms, s);
         cat_shift(T->v_tgt, M, 1, 0, [&](int m) { return S_(m).v_tgt.ptr; }, npair, add_node, sms, s);
-        auto add_chunk = [&](int m) { return make_int4((int)W[m].op_off, (int)pair_off[m], 0, 0); };
+        auto add_chunk = [&](int m) { return make_int4(0, (int)pair_off[m], 0, 0); };  // own operator ids
         cat_shift(T->v_chunk_tc, M, 3, 0, [&](int m) { return S_(m).v_chunk_tc.ptr; },
                   [&](int m) { return (long)S_(m).nchunks_tc; }, add_chunk, sms, s);
         cat_shift(T->v_chunk_oz, M, 3, 0, [&](int m) { return S_(m).v_chunk_oz.ptr; },

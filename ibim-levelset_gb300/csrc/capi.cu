@@ -15,6 +15,34 @@
 
 namespace ibim {
 
+void *device_alloc(size_t bytes, cudaStream_t s) {
+    void *p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, bytes, s);
+    if (e == cudaSuccess) return p;
+    if (e != cudaErrorMemoryAllocation) IBIM_CUDA(e);
+    (void)cudaGetLastError();
+    int dev = 0;
+    IBIM_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    IBIM_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    IBIM_CUDA(cudaDeviceSynchronize());  // every stream's pending frees have happened
+    IBIM_CUDA(cudaMemPoolTrimTo(pool, 0));
+    e = cudaMallocAsync(&p, bytes, s);
+    if (e == cudaSuccess) return p;
+    (void)cudaGetLastError();
+    size_t fr = 0, tot = 0;
+    uint64_t reserved = 0, used = 0;
+    cudaMemGetInfo(&fr, &tot);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    char msg[256];
+    std::snprintf(msg, sizeof msg,
+                  "device allocation of %.3f GB: out of memory (device free %.2f of %.2f GB; pool reserved %.2f GB, "
+                  "in use %.2f GB)",
+                  bytes / 1e9, fr / 1e9, tot / 1e9, reserved / 1e9, used / 1e9);
+    throw Error(IBIM_ERR_OUT_OF_MEMORY, msg);
+}
+
 static thread_local std::string g_last_error;
 static thread_local Ctx *g_current = nullptr;
 static std::atomic<long> g_launches{0};

@@ -38,6 +38,21 @@ void set_last_error(const std::string &msg);
         if (!(cond)) throw ::ibim::Error(IBIM_ERR_INVALID_ARGUMENT, (msg));       \
     } while (0)
 
+// cudaMallocAsync of `bytes` on `s`.  When the device is out of memory the stream-ordered pool
+// may still hold freed blocks that no allocation of this size fits into (the pool keeps what
+// solves free): wait for the device, hand the pool's unused memory back and try once more.  A
+// second failure throws IBIM_ERR_OUT_OF_MEMORY with the device's and the pool's figures.
+void *device_alloc(size_t bytes, cudaStream_t s);
+
+// One molecule's M2L operator images in a merged plan: tensor-core words (hi, lo; FP16 row
+// scales) and FP64-class digit tiles with their row scales.
+struct MolImg {
+    const void *tc_hi, *tc_lo;
+    const float *tc_rsc;
+    const uint16_t *oz_a;
+    const double *oz_sig;
+};
+
 // Stream-ordered device buffer owned by a context.
 template <typename T>
 struct DevBuf {
@@ -57,7 +72,7 @@ struct DevBuf {
         release();
         stream = s;
         n = count;
-        if (count) IBIM_CUDA(cudaMallocAsync((void **)&ptr, sizeof(T) * count, s));
+        if (count) ptr = static_cast<T *>(device_alloc(sizeof(T) * count, s));
     }
     void release() {
         if (ptr) cudaFreeAsync(ptr, stream);
@@ -340,6 +355,13 @@ struct Plan {
     DevBuf<int> node_mol;
     DevBuf<float4> kmol32, kmolff;
     DevBuf<int> mol_active;  // 1 while a molecule iterates: the heavy kernels skip the others' work
+    // each molecule's operator images stay where its own plan built them: the M2L kernels take
+    // the images of a chunk's molecule from mol_img (chunks carry the molecule's own operator
+    // ids), and the merged plan owns the buffers
+    DevBuf<MolImg> mol_img;
+    std::vector<DevBuf<float>> own_f;
+    std::vector<DevBuf<uint16_t>> own_u16;
+    std::vector<DevBuf<double>> own_d;
     ~Plan() { for (auto *t : targets) delete t; }
 };
 

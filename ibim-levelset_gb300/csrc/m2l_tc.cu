@@ -136,9 +136,16 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
                 const int *__restrict__ vtgt, const void *__restrict__ a_hi_, const void *__restrict__ a_lo_,
                 const void *__restrict__ b_hi_, const void *__restrict__ b_lo_, const float *__restrict__ rscale,
                 const float *__restrict__ cscale, float *local, int *err, const int *__restrict__ chunk_mol,
-                const int *__restrict__ mol_active) {
-    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole
-    if (chunk_mol && !mol_active[chunk_mol[blockIdx.x]]) return;
+                const int *__restrict__ mol_active, const MolImg *__restrict__ mol_img) {
+    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole,
+    // the others read their molecule's own operator images
+    if (chunk_mol) {
+        const int m = chunk_mol[blockIdx.x];
+        if (!mol_active[m]) return;
+        a_hi_ = mol_img[m].tc_hi;
+        a_lo_ = mol_img[m].tc_lo;
+        rscale = mol_img[m].tc_rsc;
+    }
     using SH = TcShape<N, RT, CPS>;
     constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
     constexpr int KS = H16 ? TC_KS16 : TC_KS, ES = H16 ? 2 : 4;  // K elements per stage, bytes per element
@@ -1325,9 +1332,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_m2l_oz(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
              const int *__restrict__ vtgt, const uint16_t *__restrict__ a, const double *__restrict__ sig,
              const uint16_t *__restrict__ bdig, const double *__restrict__ tau, double *local, int *err,
-             const int *__restrict__ chunk_mol, const int *__restrict__ mol_active) {
-    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole
-    if (chunk_mol && !mol_active[chunk_mol[blockIdx.x]]) return;
+             const int *__restrict__ chunk_mol, const int *__restrict__ mol_active,
+             const MolImg *__restrict__ mol_img) {
+    // a merged plan (batch.cu): chunks of molecules that have stopped iterating are skipped whole,
+    // the others read their molecule's own digit images
+    if (chunk_mol) {
+        const int m = chunk_mol[blockIdx.x];
+        if (!mol_active[m]) return;
+        a = mol_img[m].oz_a;
+        sig = mol_img[m].oz_sig;
+    }
     using SH = OzShape<S>;
     constexpr int NST = SH::NST, LAG = SH::LAG, STAGE = SH::STAGE;
     extern __shared__ __align__(1024) unsigned char oz_smem[];
@@ -1625,9 +1639,10 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         (count_launch(), k_split_mult_tc<<<4 * P.ctx->num_sms, 256, 0, s>>>(P.tree.nnodes, n4, P.tc_kpad, P.mult32.ptr,
                                                                             P.tc_b_hi.ptr, P.tc_b_lo.ptr));
     const int mt = P.tc_mpad / TC_M;
+    IBIM_REQUIRE(!S.chunk_mol_tc.ptr || (P.mol_img.ptr && P.mol_active.ptr), "merged plan without its image table");
     ProfScope ps_(PROF_M2L_V, 2.0 * n4 * (double)n4 * S.nvpairs,
                   4.0 * 2.0 * ((double)P.tc_mpad * P.tc_kpad * P.nops + (double)P.tc_kpad * S.nvpairs));
-    if (!P.tc_h16 && m2l_tc_pair()) {
+    if (!P.tc_h16 && m2l_tc_pair() && !P.batched) {
         if (S.nchunks_tc2 == 0) return;
         const dim3 grid2(2 * S.nchunks_tc2, (mt + 2 * TC2_PT - 1) / (2 * TC2_PT));
         (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
@@ -1636,7 +1651,7 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         IBIM_CHECK_LAUNCH();
         return;
     }
-    if (P.tc_h16 && P.tune.tc_form == 0) {
+    if (P.tc_h16 && P.tune.tc_form == 0 && !P.batched) {
         static_assert(N == 128, "persistent form: 128-pair chunks");
         const int nunits = S.nchunks_tc * ((mt + TCP_RT - 1) / TCP_RT);
         const int grid = std::min(nunits, P.ctx->num_sms);
@@ -1654,7 +1669,7 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         (count_launch(), kern<<<grid, TC_THREADS, SH2::SMEM, s>>>(
                              n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr,
-                             P.tc_err.ptr, S.chunk_mol_tc.ptr, P.mol_active.ptr));
+                             P.tc_err.ptr, S.chunk_mol_tc.ptr, P.mol_active.ptr, P.mol_img.ptr));
         IBIM_CHECK_LAUNCH();
         return;
     }
@@ -1663,7 +1678,7 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
     (count_launch(), kern<<<grid, TC_THREADS, TcShape<N>::SMEM, s>>>(
                          n4, P.tc_kpad, mt, S.v_chunk_tc.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr, P.tc_a_lo.ptr,
                          P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr,
-                         S.chunk_mol_tc.ptr, P.mol_active.ptr));
+                         S.chunk_mol_tc.ptr, P.mol_active.ptr, P.mol_img.ptr));
     IBIM_CHECK_LAUNCH();
 }
 
@@ -1728,6 +1743,7 @@ void m2l_oz_run(Plan &P, const TargetSet &S) {
         (count_launch(), k_split_mult_oz<7><<<gsplit, 256, 0, s>>>(P.tree.nnodes, n4, P.oz_kpad, P.mult.ptr,
                                                                    P.oz_b.ptr, P.oz_tau.ptr));
     const dim3 grid(S.nchunks_oz, P.oz_mtiles);
+    IBIM_REQUIRE(!S.chunk_mol_oz.ptr || (P.mol_img.ptr && P.mol_active.ptr), "merged plan without its image table");
     {
         const double nst = P.oz_kpad / OZ_KS;
         ProfScope ps_(PROF_M2L_VOZ, 2.0 * n4 * (double)n4 * S.nvpairs,
@@ -1737,7 +1753,7 @@ void m2l_oz_run(Plan &P, const TargetSet &S) {
         (count_launch(), kern<<<grid, OZ_THREADS, smem, s>>>(n4, P.oz_kpad, P.oz_mtiles, S.v_chunk_oz.ptr, S.v_src.ptr,
                                                             S.v_tgt.ptr, P.oz_a.ptr, P.oz_sig.ptr, P.oz_b.ptr,
                                                             P.oz_tau.ptr, P.local.ptr, P.tc_err.ptr, S.chunk_mol_oz.ptr,
-                                                            P.mol_active.ptr));
+                                                            P.mol_active.ptr, P.mol_img.ptr));
     }
     IBIM_CHECK_LAUNCH();
 }
