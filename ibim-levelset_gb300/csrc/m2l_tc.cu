@@ -48,6 +48,8 @@ template <int N, int RT_ = 512 / N, int CPS = 1> struct TcShape {
     static constexpr int STAGE = 2 * RT * TC_TILE_BYTES + 2 * BT;       // 40 KB (N 128, RT 4)
     static constexpr int NST = ((CPS == 1 ? 200 : 96) * 1024) / STAGE;  // 5 (RT 4) or 4 (RT 2, CPS 2)
     static constexpr int SMEM = NST * STAGE;
+    // stages of multipole copies a gathering thread keeps in flight before it signals the oldest
+    static constexpr int LAG = NST - 2;
     // D FP32, A and B TF32, both K-major, M = 128, N.
     static constexpr uint32_t IDESC =
         (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
@@ -122,9 +124,8 @@ __device__ __forceinline__ uint32_t tile_off(int row, int kchunk) {
 // as contiguous 4 KB blocks in the shared-memory layout) and of B_hi, B_lo in buffer st % TC_NST.
 // Warp-specialised: warp 0 (one thread) issues the operator bulk copies, warp 1 (one thread)
 // issues the MMAs, warps 2-7 gather the multipole rows with cp.async.
-// Per stage buffer: full_a (bulk copies, transaction count), full_b (the 192 gathering threads:
-// each thread's arrival is made by the hardware when its copies of the stage have landed, so all
-// stages of the ring can be in flight; the MMA thread fences them into the async proxy), empty
+// Per stage buffer: full_a (bulk copies, transaction count), full_b (the 192 gathering threads,
+// each after its own copies of the stage have landed and been fenced to the async proxy), empty
 // (tcgen05.commit of the stage's MMAs).  No CTA-wide barrier inside the K loop; every wait is
 // bounded and an expired wait aborts the CTA through a shared flag and the error word.
 constexpr int TC_BPROD = 192;
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
         rscale = mol_img[m].tc_rsc;
     }
     using SH = TcShape<N, RT, CPS>;
-    constexpr int TC_RT = SH::RT, TC_NST = SH::NST;
+    constexpr int TC_RT = SH::RT, TC_NST = SH::NST, TC_LAG = SH::LAG;
     constexpr int KS = H16 ? TC_KS16 : TC_KS, ES = H16 ? 2 : 4;  // K elements per stage, bytes per element
     const char *a_hi = static_cast<const char *>(a_hi_), *a_lo = static_cast<const char *>(a_lo_);
     const char *b_hi = static_cast<const char *>(b_hi_), *b_lo = static_cast<const char *>(b_lo_);
@@ -239,9 +240,6 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
                     abort_s = 1;
                     break;
                 }
-                // the gathered rows were written by cp.async (generic proxy); the MMAs read them
-                // through the async proxy
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t base = smem_u32(tc_smem + buf * kStageBytes);
                 const uint64_t bh = make_desc(base + (2 * rt) * TC_TILE_BYTES, 128, 256);
@@ -276,7 +274,9 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
         }
     } else {  // multipole rows: cp.async by 192 threads
         // each thread fills the same (tile, row, 16-byte piece) slots of every stage: up to
-        // ceil(4 N / 192) of them, addressed once here; a stage only adds its K offset
+        // ceil(4 N / 192) of them, addressed once here; a stage only adds its K offset.  (Arrivals
+        // made by the hardware on copy completion, cp.async.mbarrier.arrive.noinc with the proxy
+        // fence in the MMA thread, measured slower here: 2.38 -> 2.49 ms a launch.)
         const int t = tid - 64;
         constexpr int MAXS = (4 * N + TC_BPROD - 1) / TC_BPROD;
         uint32_t soff[MAXS], sbytes[MAXS];
@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
                 nsl = q + 1;
             }
         }
+        int issued = -1;
         for (int st = 0; st < nstage; ++st) {
             const int buf = st % TC_NST;
             if (st >= TC_NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / TC_NST) - 1) & 1))) {
@@ -309,12 +310,19 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
 #pragma unroll
             for (int q = 0; q < MAXS; ++q)
                 if (q < nsl) cp_async16(base + soff[q], sbytes[q] ? gsrc[q] + koff : gsrc[q], sbytes[q]);
-            // the stage's barrier receives this thread's arrival when its copies have landed; the
-            // MMA thread fences them into the async proxy after its wait
-            asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full_b[buf]))
-                         : "memory");
+            asm volatile("cp.async.commit_group;");
+            issued = st;
+            if (st >= TC_LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(TC_LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - TC_LAG) % TC_NST]))
+                             : "memory");
+            }
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s2 = max(0, issued - TC_LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % TC_NST])) : "memory");
     }
     __syncthreads();
     bool ok = !abort_s;
