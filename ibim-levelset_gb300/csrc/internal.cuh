@@ -280,7 +280,8 @@ struct Tuning {
     long near_seg_pairs = 1L << 17;    // FP32 near field: source-target pairs per work segment (CTA)
     long nearff_seg_pairs = 1L << 14;  // float-float near field
     int tc_form = 2;  // tensor-core M2L: 2 = two CTAs of two row tiles per SM, 4 = one CTA of four,
-                      // 0 = persistent (scaled FP16 form only)
+                      // 0 = persistent; 6, 7 = CTA pairs (2-SM MMAs of M = 256) with one or two
+                      // row-tile pairs per CTA (0, 6 and 7 in the scaled FP16 form only)
 };
 // The table's parameters for Chebyshev order `order` and npoints sources (the entry of that order
 // with the largest min_points <= npoints; defaults without one).  IBIM_TC_RT overrides tc_form.

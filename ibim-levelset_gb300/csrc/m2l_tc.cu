@@ -48,8 +48,11 @@ template <int N, int RT_ = 512 / N, int CPS = 1> struct TcShape {
     static constexpr int STAGE = 2 * RT * TC_TILE_BYTES + 2 * BT;       // 40 KB (N 128, RT 4)
     static constexpr int NST = ((CPS == 1 ? 200 : 96) * 1024) / STAGE;  // 5 (RT 4) or 4 (RT 2, CPS 2)
     static constexpr int SMEM = NST * STAGE;
-    // stages of multipole copies a gathering thread keeps in flight before it signals the oldest
-    static constexpr int LAG = NST - 2;
+    // stages of multipole copies a gathering thread keeps in flight before it signals the oldest:
+    // one (a deeper lag makes a stage's signal wait for a later stage's buffer, i.e. for an older
+    // stage's MMAs; lag 1 against NST - 2 measured 2.63 against 2.67 ms a launch in the one-CTA
+    // form of four row tiles, equal in the default form)
+    static constexpr int LAG = 1;
     // D FP32, A and B TF32, both K-major, M = 128, N.
     static constexpr uint32_t IDESC =
         (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
@@ -897,6 +900,283 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(TC2_PT * TC2_N));
 }
 
+// ---------------------------------------------------------------------------------------------
+// CTA-pair form of the scaled FP16 contraction.  One tcgen05.mma.cta_group::2 of M = 256 x N x
+// K = 16 reads, on each SM, only that CTA's 128 operator rows and its half of the N multipole
+// rows, where the one-CTA form reads 128 rows of both operands for half the work: per SM the
+// MMAs' shared-memory operand reads fall from 16 to 8 bytes per 1,024 flops, and the copies into
+// shared memory from 7.6 to 5.1.  The one-CTA form is bound by that bandwidth (its tensor pipe's
+// operand reads run at 1.27x the pipe's active fraction, the copies at 0.92x).  A cluster of two
+// CTAs takes one chunk of up to 256 pairs against PT row-tile pairs: pair T holds row tile
+// tile_base + 2T in the even CTA and tile_base + 2T + 1 in the odd one; the chunk's MMA width N
+// is its pair count rounded up to 16, each CTA gathering N / 2 multipole rows.  Barriers as in
+// the TF32 pair kernel (k_m2l_tc2): the odd CTA's relay thread passes its full stages to the
+// even CTA (a relaxed arrive: the release form's cluster-scope fence on every stage made the kernel
+// 3.62 instead of 2.62 ms a launch), whose MMA thread multicasts its commits to both CTAs; every
+// wait is bounded, and both CTAs meet at cluster barriers only on paths every thread takes.  The
+// epilogue applies the FP16 form's row and column scales.  Measured on the 2,000-atom protein:
+// 2.56 ms a launch (one row-tile pair per CTA, two CTAs per SM) against 2.34 ms for two CTAs of
+// two row tiles per SM, so it is a launch form the tuning table may pick (6, 7), not the default.
+// ---------------------------------------------------------------------------------------------
+template <int PT> struct Tc2hShape {
+    static constexpr int STAGE = (2 * PT + 2) * TC_TILE_BYTES;  // operator hi/lo per row tile + multipole hi/lo
+    static constexpr int NST = PT == 1 ? 6 : 8;                 // 96 KB (two CTAs per SM) or 192 KB
+    static constexpr int SMEM = NST * STAGE;
+    static constexpr int LAG = 1;  // copy lag (lags 2, 3, 4 and 5: 2.60, 2.61, 2.68 and 3.39 ms against 2.56)
+};
+
+__device__ __forceinline__ void mma_f16_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+template <int PT>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TC_THREADS, PT == 1 ? 2 : 1)
+    k_m2l_tc2h(int n4, int kpad, int mtiles, const int *__restrict__ chunks, const int *__restrict__ vsrc,
+               const int *__restrict__ vtgt, const char *__restrict__ a_hi, const char *__restrict__ a_lo,
+               const char *__restrict__ b_hi, const char *__restrict__ b_lo, const float *__restrict__ rscale,
+               const float *__restrict__ cscale, float *local, int *err) {
+    using SH = Tc2hShape<PT>;
+    constexpr int NST = SH::NST, LAG = SH::LAG, STAGE = SH::STAGE;
+    constexpr int KS = TC_KS16, ES = 2;
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full_a[NST], full_b[NST], empty_bar[NST], peer_full[NST], acc_bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int src_s[TC2_HALF], tgt_s[TC2_N];
+    __shared__ float csc_s[TC2_N];
+    __shared__ volatile int abort_s;
+    uint32_t rank;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int chunk = blockIdx.x >> 1;
+    const int op = chunks[3 * chunk], b = chunks[3 * chunk + 1], cnt = chunks[3 * chunk + 2];
+    const int neff = max(16, (cnt + 15) & ~15), half = neff >> 1;  // MMA width; rows per CTA
+    const int tile_base = blockIdx.y * 2 * PT;
+    const int pt = min(PT, (mtiles - tile_base + 1) / 2);
+    const int nstage = kpad / KS;
+    constexpr uint32_t IDESC0 = (1u << 4) | (0u << 7) | (0u << 10) | ((256u >> 4) << 24);
+    const uint32_t idesc = IDESC0 | ((uint32_t)(neff >> 3) << 17);
+    for (int i = tid; i < TC2_N; i += TC_THREADS) {
+        tgt_s[i] = i < cnt ? vtgt[b + i] : -1;
+        csc_s[i] = i < cnt ? cscale[vsrc[b + i]] : 0.f;
+    }
+    for (int i = tid; i < TC2_HALF; i += TC_THREADS) {
+        const int j = (int)rank * half + i;
+        src_s[i] = (i < half && j < cnt) ? vsrc[b + j] : -1;
+    }
+    if (tid == 0) {
+        abort_s = 0;
+        for (int i = 0; i < NST; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_a[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_b[i])), "r"(TC_BPROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty_bar[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&peer_full[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {  // collective over the pair: both CTAs allocate, and receive the same columns
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(PT * TC2_N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // both CTAs' barriers initialised and TMEM allocated
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem_d = tmem_base;
+    auto has_tile = [&](int T) { return tile_base + 2 * T + (int)rank < mtiles; };
+
+    if (warp == 0) {
+        if (lane == 0) {  // this CTA's operator tiles: bulk copies
+            int issued = -1;
+            int nbytes = 0;
+            for (int T = 0; T < pt; ++T)
+                if (has_tile(T)) nbytes += 2 * TC_TILE_BYTES;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % NST;
+                if (st >= NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / NST) - 1) & 1))) {
+                    abort_s = 1;
+                    break;
+                }
+                if (abort_s) break;
+                unsigned char *base = tc_smem + buf * STAGE;
+                const uint32_t fb = smem_u32(&full_a[buf]);
+                if (nbytes == 0) {
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(fb) : "memory");
+                } else {
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(nbytes)
+                                 : "memory");
+                    for (int T = 0; T < pt; ++T) {
+                        if (!has_tile(T)) continue;
+                        const int tile = tile_base + 2 * T + (int)rank;
+                        const long g = (((long)op * mtiles + tile) * nstage + st) * TC_TILE_BYTES;
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                smem_u32(base + T * TC_TILE_BYTES)),
+                            "l"(a_hi + g), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                smem_u32(base + (PT + T) * TC_TILE_BYTES)),
+                            "l"(a_lo + g), "r"(TC_TILE_BYTES), "r"(fb)
+                            : "memory");
+                    }
+                }
+                issued = st;
+            }
+            for (int s2 = max(0, issued - NST + 1); s2 <= issued; ++s2)
+                if (!mbar_wait(smem_u32(&full_a[s2 % NST]), (uint32_t)((s2 / NST) & 1))) abort_s = 1;
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && rank == 0) {  // MMA issue for the pair
+            int last = -1;
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % NST;
+                const uint32_t par = (uint32_t)((st / NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) ||
+                    !mbar_wait(smem_u32(&peer_full[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t base = smem_u32(tc_smem + buf * STAGE);
+                const uint64_t bh = make_desc(base + (2 * PT) * TC_TILE_BYTES, 128, 256);
+                const uint64_t bl = make_desc(base + (2 * PT + 1) * TC_TILE_BYTES, 128, 256);
+                for (int T = 0; T < pt; ++T) {
+                    const uint64_t ah = make_desc(base + T * TC_TILE_BYTES, 128, 256);
+                    const uint64_t al = make_desc(base + (PT + T) * TC_TILE_BYTES, 128, 256);
+                    const uint32_t d = tmem_d + (uint32_t)(T * TC2_N);
+                    mma_f16_pair(d, ah, bh, idesc, st > 0 ? 1u : 0u);
+                    mma_f16_pair(d, ah, bl, idesc, 1u);
+                    mma_f16_pair(d, al, bh, idesc, 1u);
+                }
+                commit_pair(smem_u32(&empty_bar[buf]));
+                last = st;
+            }
+            // the accumulator barriers of both CTAs always receive a commit: it tracks every MMA
+            // issued above, so after it neither CTA's shared memory is read any more
+            commit_pair(smem_u32(&acc_bar));
+            if (last != nstage - 1) abort_s = 1;
+        } else if (lane == 0) {  // odd CTA: relay its full stages to the even CTA
+            for (int st = 0; st < nstage; ++st) {
+                const int buf = st % NST;
+                const uint32_t par = (uint32_t)((st / NST) & 1);
+                if (!mbar_wait(smem_u32(&full_a[buf]), par) || !mbar_wait(smem_u32(&full_b[buf]), par) || abort_s) {
+                    abort_s = 1;
+                    break;
+                }
+                // relaxed: the data this stage holds is already in this CTA's shared memory (the
+                // waits above acquired its completion) and is read there by this SM's tensor core
+                asm volatile("mbarrier.arrive.relaxed.cluster.shared::cluster.b64 _, [%0];" ::"r"(
+                                 cluster_addr(smem_u32(&peer_full[buf]), 0))
+                             : "memory");
+            }
+        }
+    } else {  // this CTA's half of the multipole rows: cp.async by 192 threads, slots addressed once
+        const int t = tid - 64;
+        constexpr int MAXS = (4 * TC2_HALF + TC_BPROD - 1) / TC_BPROD;
+        uint32_t soff[MAXS], sbytes[MAXS];
+        const char *gsrc[MAXS];
+        int nsl = 0;
+#pragma unroll
+        for (int q = 0; q < MAXS; ++q) {
+            const int i = t + q * TC_BPROD;
+            soff[q] = 0;
+            sbytes[q] = 0;
+            gsrc[q] = b_hi;
+            if (i < 4 * half) {
+                const int tile = i / (2 * half), row = (i >> 1) % half, c = i & 1;
+                const int sn = src_s[row];
+                soff[q] = (2 * PT + tile) * TC_TILE_BYTES + tile_off(row, c);
+                sbytes[q] = sn >= 0 ? 16u : 0u;
+                gsrc[q] = (tile == 0 ? b_hi : b_lo) + (sn >= 0 ? (long)sn * kpad * ES + 16 * c : 0);
+                nsl = q + 1;
+            }
+        }
+        int issued = -1;
+        for (int st = 0; st < nstage; ++st) {
+            const int buf = st % NST;
+            if (st >= NST && !mbar_wait(smem_u32(&empty_bar[buf]), (uint32_t)(((st / NST) - 1) & 1))) {
+                abort_s = 1;
+                break;
+            }
+            if (abort_s) break;
+            const uint32_t base = smem_u32(tc_smem + buf * STAGE);
+            const long koff = (long)st * KS * ES;
+#pragma unroll
+            for (int q = 0; q < MAXS; ++q)
+                if (q < nsl) cp_async16(base + soff[q], sbytes[q] ? gsrc[q] + koff : gsrc[q], sbytes[q]);
+            asm volatile("cp.async.commit_group;");
+            issued = st;
+            if (st >= LAG) {
+                asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[(st - LAG) % NST]))
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s2 = max(0, issued - LAG + 1); s2 <= issued; ++s2)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_b[s2 % NST])) : "memory");
+    }
+    __syncthreads();
+    // every MMA of the pair is complete once the accumulator barrier flips (the even CTA commits
+    // to it on every path); an abort on either side is copied into the other CTA's flag
+    if (tid == 0) {
+        const bool acc = mbar_wait(smem_u32(&acc_bar), 0u);
+        if (!acc || abort_s) {
+            abort_s = 1;
+            asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr(smem_u32((const void *)&abort_s), rank ^ 1u)),
+                         "r"(1u)
+                         : "memory");
+        }
+    }
+    cluster_sync_all();
+    const bool ok = !abort_s;
+    if (!ok && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows); the two warp groups take
+        // alternate 16-column blocks of each accumulator
+        const int lg = warp & 3, grp = warp >> 2, nb = neff >> 4;
+        for (int u = grp; u < pt * nb; u += 2) {
+            const int T = u / nb, c0 = (u % nb) * 16;
+            if (!has_tile(T)) continue;  // uniform over the CTA
+            const int row = (tile_base + 2 * T + (int)rank) * TC_M + 32 * lg + lane;
+            const float rs = rscale[(long)op * mtiles * TC_M + row];  // row < mtiles * 128
+            const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(T * TC2_N + c0);
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                "%13, %14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < n4) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int tg = tgt_s[c0 + q];
+                    if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, __uint_as_float(v[q]) * rs * csc_s[c0 + q]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // neither CTA leaves while the other may still use the pair's TMEM
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(PT * TC2_N));
+}
+
 // hi = x rounded to TF32 (10 explicit mantissa bits, to nearest even), lo = x - hi.
 __device__ __forceinline__ float tf32_round(float x) {
     uint32_t u = __float_as_uint(x);
@@ -1101,7 +1381,7 @@ template <int S> struct OzShape {
     static_assert(S * D == 42, "42-bit cut");
     static constexpr int STAGE = S * (OZ_ATILE + OZ_BTILE);  // 48 KB (S 6), 56 KB (S 7)
     static constexpr int NST = (200 * 1024) / STAGE;        // 4 or 3 stage buffers
-    static constexpr int LAG = NST - 2;
+    static constexpr int LAG = 1;                           // copy lag (NST - 2: 14.49 against 14.24 ms)
     static constexpr int SMEM = NST * STAGE;
 };
 
@@ -1639,6 +1919,8 @@ void m2l_tc_pack(Plan &P, const float2 *ff) {
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TcShape<M2L_CHTC, 2, 2>::SMEM));
     IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<1>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<2>::SMEM));
 }
 
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating): chunks of 128 pairs against
@@ -1666,6 +1948,22 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
         (count_launch(), k_m2l_tc2<<<grid2, TC_THREADS, TC2_SMEM, s>>>(
                              n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, P.tc_a_hi.ptr,
                              P.tc_a_lo.ptr, P.tc_b_hi.ptr, P.tc_b_lo.ptr, P.local32.ptr, P.tc_err.ptr));
+        IBIM_CHECK_LAUNCH();
+        return;
+    }
+    if (P.tc_h16 && (P.tune.tc_form == 6 || P.tune.tc_form == 7) && !P.batched) {
+        // CTA pairs over chunks of up to 256 pairs: one (6) or two (7) row-tile pairs per CTA
+        if (S.nchunks_tc2 == 0) return;
+        const char *ah = reinterpret_cast<const char *>(P.tc_a_hi.ptr), *al = reinterpret_cast<const char *>(P.tc_a_lo.ptr);
+        const char *bh = reinterpret_cast<const char *>(P.tc_b_hi.ptr), *bl = reinterpret_cast<const char *>(P.tc_b_lo.ptr);
+        if (P.tune.tc_form == 6)
+            (count_launch(), k_m2l_tc2h<1><<<dim3(2 * S.nchunks_tc2, (mt + 1) / 2), TC_THREADS, Tc2hShape<1>::SMEM, s>>>(
+                                 n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, ah, al, bh, bl,
+                                 P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr));
+        else
+            (count_launch(), k_m2l_tc2h<2><<<dim3(2 * S.nchunks_tc2, (mt + 3) / 4), TC_THREADS, Tc2hShape<2>::SMEM, s>>>(
+                                 n4, P.tc_kpad, mt, S.v_chunk_tc2.ptr, S.v_src.ptr, S.v_tgt.ptr, ah, al, bh, bl,
+                                 P.tc_rsc.ptr, P.tc_csc.ptr, P.local32.ptr, P.tc_err.ptr));
         IBIM_CHECK_LAUNCH();
         return;
     }

@@ -34,7 +34,7 @@ thread_local const Tuning *g_override = nullptr;
 
 bool valid(long near, long nearff, int form) {
     return near >= 1024 && near <= (1L << 24) && nearff >= 256 && nearff <= (1L << 22) &&
-           (form == 0 || form == 2 || form == 4);
+           (form == 0 || form == 2 || form == 4 || form == 6 || form == 7);
 }
 
 }  // namespace
@@ -56,7 +56,8 @@ Tuning tuning_for(int order, long npoints) {
     }
     static const int env_form = [] {
         const char *v = std::getenv("IBIM_TC_RT");
-        return v ? (v[0] == '4' ? 4 : (v[0] == 'P' ? 0 : 2)) : -1;
+        if (!v) return -1;
+        return v[0] == '4' ? 4 : v[0] == '6' ? 6 : v[0] == '7' ? 7 : v[0] == 'P' ? 0 : 2;
     }();
     if (env_form >= 0) t.tc_form = env_form;
     return t;
@@ -76,7 +77,7 @@ extern "C" {
 
 int ibim_tuning_set(int order, long min_points, long near_seg_pairs, long nearff_seg_pairs, int tc_form) {
     if (order < 2 || order > 8 || min_points < 0 || !valid(near_seg_pairs, nearff_seg_pairs, tc_form)) {
-        set_last_error("tuning: order in [2, 8], min_points >= 0, segment pairs in range, launch form 0, 2 or 4");
+        set_last_error("tuning: order in [2, 8], min_points >= 0, segment pairs in range, launch form 0, 2, 4, 6 or 7");
         return IBIM_ERR_INVALID_ARGUMENT;
     }
     std::lock_guard<std::mutex> lk(g_mu);

@@ -69,11 +69,13 @@ def test_pair_kernel_matches_one_cta_kernel(ctx, golden, case, order, tmp_path):
 
 
 @pytest.mark.parametrize("case,order", [("cavity", None), ("p1hje", None), ("synth30", 6), ("synth30", 3)])
-@pytest.mark.parametrize("fp16,form", [("1", None), ("1", "P"), ("0", None)])
+@pytest.mark.parametrize("fp16,form", [("1", None), ("1", "P"), ("0", None), ("1", "6"), ("1", "7")])
 def test_launch_forms_match_one_cta_of_four(ctx, golden, case, order, fp16, form, tmp_path):
-    """Two CTAs of two row tiles per SM (the default, IBIM_TC_RT unset) and the persistent form
-    (IBIM_TC_RT=P, FP16) issue the same MMAs per row tile in the same K order as one CTA of four
-    (IBIM_TC_RT=4); only the order of the atomic adds into the locals differs."""
+    """Two CTAs of two row tiles per SM (IBIM_TC_RT=2), the persistent form (IBIM_TC_RT=P, FP16)
+    and the FP16 CTA-pair forms (IBIM_TC_RT=6 and 7: 2-SM MMAs of M = 256 over chunks of up to
+    256 pairs, odd row-tile counts included at orders 3 and 6) issue the same products per row
+    tile in the same K order as one CTA of four (IBIM_TC_RT=4); only the order of the atomic adds
+    into the locals differs."""
     G = golden(case)
     p = order or G["params"]["np"]
     env = {"IBIM_TC_FP16": fp16}
