@@ -1120,9 +1120,12 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
                 best = t;
             }
         };
-        {  // launch form of the tensor-core M2L, then the segment sizes, one coordinate at a time
+        // launch form of the tensor-core M2L (the CTA-pair forms in the scaled FP16 form only), then
+        // the segment sizes, one coordinate at a time
+        for (int f : {4, 6, 7}) {
+            if (f != 4 && !m2l_tc_fp16_form()) continue;
             Tuning t = best;
-            t.tc_form = 4;
+            t.tc_form = f;
             consider(t);
         }
         for (long v : {1L << 15, 1L << 16, 1L << 18}) {
