@@ -49,6 +49,7 @@ static std::atomic<long> g_launches{0};
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(); }
 Ctx *current_ctx() { return g_current; }
 

@@ -113,6 +113,7 @@ enum ProfCat {
 
 // Number of kernels this library launched (all contexts).
 void count_launch();
+void count_launches(long n);  // n kernels at once (a graph replay), or -n for captured ones
 long launch_count();
 
 struct Ctx {
@@ -363,7 +364,18 @@ struct Plan {
     std::vector<DevBuf<float>> own_f;
     std::vector<DevBuf<uint16_t>> own_u16;
     std::vector<DevBuf<double>> own_d;
-    ~Plan() { for (auto *t : targets) delete t; }
+    // the mixed-precision matvec as a CUDA graph (solve.cu bie_matvec): captured on its second call
+    // with the same kernel parameters and replayed with its input and output staged through gx / gy
+    struct MatvecGraph {
+        cudaGraphExec_t exec = nullptr;
+        double key[5] = {-1, -1, -1, -1, -1};
+        long kernels = 0;  // kernel nodes of the graph
+        int calls = 0;
+        bool failed = false;
+    } mvg;
+    DevBuf<double> gx, gy;
+    ~Plan() {
+        if (mvg.exec) cudaGraphExecDestroy(mvg.exec); for (auto *t : targets) delete t; }
 };
 
 // FMM engine.  dens: 4 x ns (tree order), out: 4 x nt of target set `ts` (tree order).

@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <string>
 
 #include "fmm_common.cuh"
@@ -248,10 +249,102 @@ void permute(Ctx *c, long n, const int *perm, const double *in, double *out, boo
 // BIE operator
 // ---------------------------------------------------------------------------------------
 
+namespace {
+
+bool matvec_graphs() {
+    static const bool on = [] {
+        const char *v = std::getenv("IBIM_GRAPHS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+void matvec_body(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision);
+
+// The mixed matvec (25 of a solve's 26 products) as one CUDA graph: the first call with given
+// kernel parameters runs the launches directly (it makes the plan's lazy set-up: operator images,
+// near lists, workspaces), the second captures them on the context stream (the near field's fork
+// to the second stream and its join are captured as dependencies) and every call from then on
+// stages its input into gx, replays the graph and copies gy out.  Not while per-kernel profiling
+// records events.  A capture that fails leaves the plan on direct launches.
+bool matvec_graph(Plan &P, const ibim_kernel_params &kp, const double *x, double *y) {
+    Ctx *c = P.ctx;
+    if (!matvec_graphs() || c->prof_mask != 0 || P.mvg.failed) return false;
+    Plan::MatvecGraph &G = P.mvg;
+    const double key[5] = {kp.kappa, kp.dE, kp.dI, kp.tau, (double)kp.k3_scaled};
+    if (std::memcmp(key, G.key, sizeof key) != 0) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+        G.calls = 0;
+        std::memcpy(G.key, key, sizeof key);
+    }
+    if (!G.exec && G.calls++ == 0) return false;
+    const long n2 = 2 * P.ns;
+    cudaStream_t s = c->stream;
+    if (!G.exec) {
+        if (!P.gx.ptr) {
+            P.gx.alloc(n2, s);
+            P.gy.alloc(n2, s);
+        }
+        IBIM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const long before = launch_count();
+        cudaGraph_t g = nullptr;
+        try {
+            matvec_body(P, kp, P.gx.ptr, P.gy.ptr, IBIM_PRECISION_MIXED);
+        } catch (...) {
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            G.failed = true;
+            return false;
+        }
+        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        count_launches(-(launch_count() - before));  // captured, not launched
+        if (e != cudaSuccess || !g) {
+            (void)cudaGetLastError();
+            G.failed = true;
+            return false;
+        }
+        size_t nn = 0;
+        IBIM_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        IBIM_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+        G.kernels = 0;
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            IBIM_CUDA(cudaGraphNodeGetType(nd, &t));
+            G.kernels += t == cudaGraphNodeTypeKernel;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&G.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            (void)cudaGetLastError();
+            G.exec = nullptr;
+            G.failed = true;
+            return false;
+        }
+        trace_mark("matvec graph captured");
+    }
+    IBIM_CUDA(cudaMemcpyAsync(P.gx.ptr, x, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
+    IBIM_CUDA(cudaGraphLaunch(G.exec, s));
+    IBIM_CUDA(cudaMemcpyAsync(y, P.gy.ptr, sizeof(double) * n2, cudaMemcpyDeviceToDevice, s));
+    count_launches(G.kernels);
+    return true;
+}
+
+}  // namespace
+
 void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision) {
+    IBIM_REQUIRE(!P.targets.empty() && P.targets[0]->self, "BIE operator needs a plan over the tube points");
+    if (precision == IBIM_PRECISION_MIXED && matvec_graph(P, kp, x, y)) return;
+    matvec_body(P, kp, x, y, precision);
+}
+
+namespace {
+
+void matvec_body(Plan &P, const ibim_kernel_params &kp, const double *x, double *y, int precision) {
     Ctx *c = P.ctx;
     const long n = P.ns;
-    IBIM_REQUIRE(!P.targets.empty() && P.targets[0]->self, "BIE operator needs a plan over the tube points");
     (count_launch(), k_densities<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, P.snx.ptr, P.sny.ptr, P.snz.ptr, P.sw.ptr, P.dens4.ptr));
     IBIM_CHECK_LAUNCH();
     TargetSet &S = *P.targets[0];
@@ -260,6 +353,8 @@ void bie_matvec(Plan &P, const ibim_kernel_params &kp, const double *x, double *
     (count_launch(), k_combine<<<ew_grid(c, n), 256, 0, c->stream>>>(n, x, S.out4.ptr, P.snx.ptr, P.sny.ptr, P.snz.ptr, e1, e2, y));
     IBIM_CHECK_LAUNCH();
 }
+
+}  // namespace
 
 void bie_densities(Plan &P, const double *x, double *dens4) {
     const long n = P.ns;
