@@ -292,8 +292,9 @@ int ibim_batch_solve(ibim_ctx ctx, int nmol, const int *natoms, const double *ce
  * A plan of Chebyshev order p with N sources takes its launch parameters from the row of order p
  * with the largest min_points <= N: pairs per work segment of the FP32 and the float-float near
  * fields, and the tensor-core M2L's launch form (2 = two CTAs of two row tiles per SM, 4 = one CTA
- * of four, 0 = persistent).  They change the partition of the same work only.  Without a row the
- * defaults hold (2^17, 2^14, 2). */
+ * of four, 0 = persistent, 6 / 7 = CTA pairs of 2-SM MMAs with one / two row-tile pairs per CTA;
+ * 0, 6 and 7 in the scaled FP16 operand form).  They change the partition of the same work only.
+ * Without a row the defaults hold (2^17, 2^14, 2). */
 int ibim_tuning_set(int order, long min_points, long near_seg_pairs, long nearff_seg_pairs, int tc_form);
 int ibim_tuning_clear(void);
 /* out: near_seg_pairs, nearff_seg_pairs, tc_form for order and npoints */
