@@ -73,9 +73,9 @@ def parse():
     ap.add_argument("--batch-mode", choices=["lockstep", "pool"], default="lockstep",
                     help="batch: lock-step waves on merged plans (ibim_batch_solve) or the request loop's "
                          "concurrent whole solves; serve: the request loop in lock-step or pool mode")
-    ap.add_argument("--max-wave", type=int, default=32, help="batch lockstep: molecules per wave")
+    ap.add_argument("--max-wave", type=int, default=6, help="batch lockstep: molecules per wave")
     ap.add_argument("--workers", type=int, default=4, help="batch lockstep: preparation threads")
-    ap.add_argument("--wave-slots", type=int, default=2, help="batch lockstep: waves solved at once")
+    ap.add_argument("--wave-slots", type=int, default=3, help="batch lockstep: waves solved at once")
     ap.add_argument("--atoms", type=str, default=None, help="serve/batch: log-uniform atom-count range")
     ap.add_argument("--accuracy-sample", type=int, default=2,
                     help="serve/batch: requests (smallest first) re-solved alone in FP64 to state the error")

@@ -351,7 +351,7 @@ void stop_threads(ibim_server_s *S) {
 }
 
 // waves solved at once by the lock-step loop, each on its own context and stream
-constexpr int kWaveSlots = 2;
+constexpr int kWaveSlots = 3;
 
 int create(int device, int slots, int max_wave, double budget, bool lockstep, ibim_server *out) {
     if (!out || slots < 1 || slots > 64 || !(budget > 0) || max_wave < 1) {

@@ -305,7 +305,7 @@ class Context:
         _check(rc)
         return x, dict(iters=it.value, matvecs=mv.value, status=st.value, residual=res.value)
 
-    def batch_solve(self, molecules, cfgs, max_wave=32, hbm_budget_bytes=150e9, workers=4, wave_slots=2,
+    def batch_solve(self, molecules, cfgs, max_wave=6, hbm_budget_bytes=150e9, workers=4, wave_slots=3,
                     check=True):
         """Many molecules in lock-step waves (ibim_batch_solve).  molecules: list of (centers, charges,
         radii); cfgs: one Config per molecule.  Returns (results, statuses, info)."""
