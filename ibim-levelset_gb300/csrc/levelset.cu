@@ -193,32 +193,79 @@ __device__ __forceinline__ T godunov(const T n[3], const T p[3]) {
 // One TVD-RK3 stage over the whole grid.  MODE 0: evolve (phi_t + vel|grad phi| = 0);
 // MODE 1: reinitialize (phi_t + S(phi0)(|grad phi| - 1) = 0, S = phi0/sqrt(phi0^2 + dx^2)).
 // STAGE 0: u1 = g - L(g); 1: u2 = (3g + u1 - L(u1))/4; 2: g = (g + 2(u2 - L(u2)))/3.
-template <int MODE, int STAGE, class T>
+// COUNT (stage 0 only): also countGradient of src = g (levelset.cpp:398-432) from the same WENO
+// gradients: among cells with |g| < band, |godunov(D-, D+) - 1| > thres into counts[0], the
+// cells into counts[1], the sum of the deviations into accum.
+template <int MODE, int STAGE, class T, bool COUNT = false>
 __global__ void __launch_bounds__(256) k_weno_stage(Dims dm, T h, T dtv, T eps, const T *__restrict__ src, T *g, T *u1,
-                                                    T *u2, const T *__restrict__ phi0) {
+                                                    T *u2, const T *__restrict__ phi0, T band = (T)0,
+                                                    T thres = (T)0, unsigned long long *counts = nullptr,
+                                                    double *accum = nullptr) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i >= dm.nx || j >= dm.ny || k >= dm.nz) return;
-    T up[3], un[3];
-    gradients(src, dm, i, j, k, h, up, un);
-    const long I = dm.idx(i, j, k);
-    T L;
-    if (MODE == 0) {
-        L = dtv * godunov(un, up);
-    } else {
-        const T p0 = phi0[I];
-        const T sign = DivOf<T>::type::over_sqrt(p0, p0 * p0 + eps);
-        const T nd = sign > (T)0 ? godunov(un, up) : godunov(up, un);
-        L = dtv * sign * (nd - (T)1.0);
+    const bool in = i < dm.nx && j < dm.ny && k < dm.nz;
+    if (!COUNT && !in) return;
+    unsigned bad = 0, tot = 0;
+    double acc = 0.;
+    if (in) {
+        T up[3], un[3];
+        gradients(src, dm, i, j, k, h, up, un);
+        const long I = dm.idx(i, j, k);
+        T L;
+        if (MODE == 0) {
+            L = dtv * godunov(un, up);
+        } else {
+            const T p0 = phi0[I];
+            const T sign = DivOf<T>::type::over_sqrt(p0, p0 * p0 + eps);
+            const T nd = sign > (T)0 ? godunov(un, up) : godunov(up, un);
+            L = dtv * sign * (nd - (T)1.0);
+        }
+        using D = typename DivOf<T>::type;
+        if (COUNT && fabs(src[I]) < band) {
+            const T nr = godunov(un, up);
+            tot = 1;
+            bad = fabs(nr - (T)1.0) > thres ? 1u : 0u;
+            acc = fabs((double)nr - 1.0);
+        }
+        if (STAGE == 0)
+            u1[I] = g[I] - L;
+        else if (STAGE == 1)
+            u2[I] = (3 * g[I] + u1[I] - L) * (T)0.25;
+        else
+            g[I] = D::q(g[I] + 2 * (u2[I] - L), (T)3.0);
     }
-    using D = typename DivOf<T>::type;
-    if (STAGE == 0)
-        u1[I] = g[I] - L;
-    else if (STAGE == 1)
-        u2[I] = (3 * g[I] + u1[I] - L) * (T)0.25;
-    else
-        g[I] = D::q(g[I] + 2 * (u2[I] - L), (T)3.0);
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            bad += __shfl_down_sync(0xffffffffu, bad, o);
+            tot += __shfl_down_sync(0xffffffffu, tot, o);
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+        }
+        __shared__ unsigned sb[8], st[8];
+        __shared__ double sa[8];
+        const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+        if ((tid & 31) == 0) {
+            sb[tid >> 5] = bad;
+            st[tid >> 5] = tot;
+            sa[tid >> 5] = acc;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            unsigned B = 0, Tt = 0;
+            double A = 0;
+            const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+            for (int w = 0; w < nw; ++w) {
+                B += sb[w];
+                Tt += st[w];
+                A += sa[w];
+            }
+            if (Tt) {
+                atomicAdd(counts, (unsigned long long)B);
+                atomicAdd(counts + 1, (unsigned long long)Tt);
+                atomicAdd(accum, A);
+            }
+        }
+    }
 }
 
 // levelset::countGradient: among cells with |g| < thickness*dx, count | |grad g| - 1 | > thres.
@@ -533,23 +580,27 @@ int reinit_t(Grid &g, const Grid &phi0, double final_t, double vel, double cfl, 
     T *G = gdata<T>(g);
     const T *P0 = gdata<T>(phi0);
     const double fl = 350.0 * g.cells(), by = 4.0 * sizeof(T) * g.cells();
-    auto count = [&]() -> unsigned long long {
-        cnt.zero();
-        count_t<T>(g, (double)thickness, thres, cnt.ptr, acc.ptr);
-        IBIM_CHECK_LAUNCH();
-        IBIM_CUDA(cudaMemcpyAsync(hcnt, cnt.ptr, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        IBIM_CUDA(cudaStreamSynchronize(s));
-        return hcnt[0];
-    };
     int step = 0;
+    // The count of the current grid comes from the first stage of the step that would follow: the
+    // stage evaluates the same gradients of g.  When no cell is left to fix, or the steps are
+    // spent, the stage's u1 is discarded and g is the grid the reference stops at.
+    const T band = (T)(thickness * g.dx), th = (T)thres;
     try {
-        unsigned long long bad = count();
-        while (bad != 0 && step < steps) {
+        for (;;) {
+            cnt.zero();
+            acc.zero();
+            {
+                ProfScope ps_(PROF_WENO, fl, by);
+                (count_launch(), k_weno_stage<1, 0, T, true><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, G, G, u1.ptr, u2.ptr,
+                                                                              P0, band, th, cnt.ptr, acc.ptr));
+            }
+            IBIM_CHECK_LAUNCH();
+            IBIM_CUDA(cudaMemcpyAsync(hcnt, cnt.ptr, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+            IBIM_CUDA(cudaStreamSynchronize(s));
+            if (hcnt[0] == 0 || step >= steps) break;
             step++;
-            { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 0, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, G, G, u1.ptr, u2.ptr, P0)); }
             { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 1, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u1.ptr, G, u1.ptr, u2.ptr, P0)); }
             { ProfScope ps_(PROF_WENO, fl, by); (count_launch(), k_weno_stage<1, 2, T><<<gr, bl, 0, s>>>(dm, h, dtv, (T)eps, u2.ptr, G, u1.ptr, u2.ptr, P0)); }
-            bad = count();
         }
     } catch (...) {
         cudaFreeHost(hcnt);
