@@ -5,12 +5,14 @@
 //   prepare     worker threads, each on its own context and streams, run the part of a solve before
 //               GMRES (level set, tube, right-hand side, plan, operator images) for the molecules
 //               in order, while the device bytes of the prepared molecules stay within the budget
-//   merge       a wave of prepared molecules becomes one plan: sources, nodes, operators, V/X pairs,
-//               near lists and both target sets concatenated with offsets (node lists kept level by
+//   merge       a wave of prepared molecules becomes one plan: sources, nodes, V/X pairs, near
+//               lists and both target sets concatenated with offsets (node lists kept level by
 //               level), so every FMM stage of a matvec (P2M, M2M per level, tensor-core M2L, L2L per
 //               level, near field, L2P) is one launch over all molecules of the wave -- a flattened
-//               multi-tree work list; the near-field kernels take each target leaf's molecule for
-//               its kappa, and near-field segments of all molecules are sorted by work
+//               multi-tree work list, replayed as one CUDA graph per matvec; the operator images
+//               stay in each molecule's buffers (the M2L kernels find a chunk's by its molecule),
+//               the near-field kernels take each target leaf's molecule for its kappa, and
+//               near-field segments of all molecules are sorted by work
 //   lock-step   GMRES advances every molecule of the wave together: one merged matvec per Arnoldi
 //               step, modified Gram-Schmidt per molecule by segmented reductions of fixed shape,
 //               one host synchronisation per step for all molecules' Givens rotations; molecules
@@ -927,7 +929,7 @@ void batch_wave(Ctx *c, std::vector<BatchMol> &mols, WaveStats &ws) {
         dcopy(b.ptr + n + off[m], mols[m].b_tree->ptr + N, N, s);
     }
     IBIM_CUDA(cudaStreamSynchronize(s));
-    // the per-molecule plans are no longer needed: their operator images live in the merged plan
+    // the per-molecule plans are no longer needed: the merged plan owns their operator images
     for (int m = 0; m < M; ++m) {
         delete mols[m].prep;
         mols[m].prep = nullptr;
