@@ -334,10 +334,15 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
     if (!ok && tid == 0) atomicExch(err, 1);
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (ok) {
+        // Each warp turns its 32 rows x 16 pairs through a 2 KB tile of the (now idle) stage
+        // buffers, so that a thread adds 4 consecutive rows of one target's local expansion with
+        // one vector atomic: a quarter of the atomic instructions.  4p^3 is a multiple of 4, so a
+        // group of 4 rows is all below n4 or all above, and every group is 16-byte aligned.
         const int lg = warp & 3;
+        float *tp = reinterpret_cast<float *>(tc_smem) + warp * 512;  // [16 pairs][32 rows]
         for (int tt = warp >> 2; tt < rt; tt += 2) {
-            const int row = (tile0 + tt) * TC_M + 32 * lg + lane;
-            const float rs = H16 ? rscale[(long)op * mtiles * TC_M + row] : 1.f;  // row < mtiles * 128
+            const int rowb = (tile0 + tt) * TC_M + 32 * lg;  // the warp's first row
+            const float rs = H16 ? rscale[(long)op * mtiles * TC_M + rowb + lane] : 1.f;  // < mtiles * 128
             const uint32_t taddr = tmem_d + ((uint32_t)(32 * lg) << 16) + (uint32_t)(tt * N);
 #pragma unroll 1
             for (int c0 = 0; c0 < neff; c0 += 16) {
@@ -350,14 +355,23 @@ __global__ void __launch_bounds__(TC_THREADS, CPS)
                       "=r"(v[15])
                     : "r"(taddr + (uint32_t)c0));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (row < n4) {
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int tg = tgt_s[c0 + q];
-                        const float x = H16 ? __uint_as_float(v[q]) * rs * csc_s[c0 + q] : __uint_as_float(v[q]);
-                        if (tg >= 0) atomicAdd(local + (long)tg * n4 + row, x);
+                for (int q = 0; q < 16; ++q)
+                    tp[q * 32 + lane] = H16 ? __uint_as_float(v[q]) * rs * csc_s[c0 + q] : __uint_as_float(v[q]);
+                __syncwarp();
+#pragma unroll
+                for (int hq = 0; hq < 4; ++hq) {
+                    const int j = lane + 32 * hq;            // float4 j: pair j / 8, rows 4 (j % 8) .. + 3
+                    const int q = j >> 3, r = rowb + 4 * (j & 7);
+                    const int tg = tgt_s[c0 + q];
+                    if (tg >= 0 && r < n4) {
+                        const float4 x = *reinterpret_cast<const float4 *>(tp + q * 32 + 4 * (j & 7));
+                        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(local + (long)tg * n4 + r),
+                                     "f"(x.x), "f"(x.y), "f"(x.z), "f"(x.w)
+                                     : "memory");
                     }
                 }
+                __syncwarp();
             }
         }
     }
