@@ -68,3 +68,11 @@ def test_batch_rejects_mixed_shapes(ctx):
     with pytest.raises(ibim.IbimError) as e:
         ctx.batch_solve(mols[:2], cfgs[:2])
     assert e.value.status == ibim.ERR_INVALID_ARGUMENT
+
+
+def test_single_molecule_batch(ctx, solo):
+    """A batch of one molecule is one wave of one: the molecule's own solve."""
+    ws, mols, cfgs = molecules()
+    res, st, info = ctx.batch_solve(mols[:1], cfgs[:1], max_wave=6, workers=1, wave_slots=1)
+    assert st == [0] and info["waves"] == 1 and info["largest_wave"] == 1
+    assert abs(res[0]["energy"] - solo[0]["energy"]) <= 1e-6 * abs(solo[0]["energy"])

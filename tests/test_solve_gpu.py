@@ -159,3 +159,17 @@ def test_born_gap_comes_from_points_on_split_planes(ctx, golden):
     # the ion's tube points come from lattice points, so whole grid lines lie on the planes: about
     # an eighth of the points are within 1e-7 of one, the rest land where the reference puts them
     assert near.sum() < 0.2 * len(ref), near.sum()
+
+
+def test_empty_tube_is_an_error_and_the_context_stays_usable(ctx, golden):
+    """An atom far outside the grid leaves the level set without tube points: the solve reports
+    an invalid argument before any launch over the (empty) tube, and the same context then solves
+    normally."""
+    G = golden("born")
+    cfg = config_for(G["params"])
+    with pytest.raises(ibim.IbimError) as e:
+        ctx.solve(np.array([[1000.0, 1000.0, 1000.0]]), np.ones(1), np.full(1, 2.0), cfg)
+    assert e.value.status == ibim.ERR_INVALID_ARGUMENT
+    r = ctx.solve(G["centers"], G["charges"], G["radii"], cfg)
+    E = G["params"]["scalars"]["REF_ENERGY_RESTATED"]
+    assert abs(r["energy"] - E) / abs(E) < FULL_TOL["born"]
