@@ -31,6 +31,7 @@ struct KParams32 {
     float kappa_l2;     // -kappa log2(e): e^(-kappa r) = 2^(kappa_l2 r)
     float vr2_band;     // |d2 - vr2| below this: the cutoff is decided in FP64
     double vr2_64;      // the FP64 kernels' (tau h)^2
+    float vr2_guard;    // vr2 + 2 vr2_band: every pair inside the cutoff or its band lies below
 };
 
 static KParams32 to32(const KParams &k) {
@@ -38,7 +39,7 @@ static KParams32 to32(const KParams &k) {
                      (float)(k.vr * k.vr),  (float)k.k2in, (float)k.q4pi,
                      (float)k.k3f,          (float)(k.k2in / k.q4pi), (float)(k.k3f / k.q4pi),
                      (float)(-k.kappa * 1.4426950408889634),
-                     (float)(1e-4 * k.vr2), k.vr2};
+                     (float)(1e-4 * k.vr2), k.vr2, (float)(k.vr2 * (1.0 + 2e-4))};
 }
 
 namespace {
@@ -542,18 +543,20 @@ __global__ void __launch_bounds__(NT32) k_near32(const ChebTables32 *__restrict_
                         // the cutoff test is a discontinuity: d2 in the FP64 kernel's evaluation order
                         // (near_pair64), so points at exactly tau h decide alike in both precisions
                         const float d2 = dx * dx + dy * dy + dz * dz;
-                        bool inside = d2 < kp.vr2;
-                        if (fabsf(d2 - kp.vr2) < kp.vr2_band) {
-                            // within FP32 rounding of the cutoff: decide on the FP64 coordinates, as
-                            // the FP64 and float-float kernels do (rare)
-                            const int sj = __float_as_int(P1.w);
-                            const double ex = sx64[sj] - tx64[tg64], ey = sy64[sj] - ty64[tg64],
-                                         ez = sz64[sj] - tz64[tg64];
-                            inside = ex * ex + ey * ey + ez * ez < kp.vr2_64;
-                        }
-                        if (inside) {
-                            a0 = fmaf(-k2q, P1.z, a0);
-                            continue;
+                        if (d2 < kp.vr2_guard) {  // rare: inside the cutoff or within rounding of it
+                            bool inside = d2 < kp.vr2;
+                            if (fabsf(d2 - kp.vr2) < kp.vr2_band) {
+                                // within FP32 rounding of the cutoff: decide on the FP64 coordinates,
+                                // as the FP64 and float-float kernels do
+                                const int sj = __float_as_int(P1.w);
+                                const double ex = sx64[sj] - tx64[tg64], ey = sy64[sj] - ty64[tg64],
+                                             ez = sz64[sj] - tz64[tg64];
+                                inside = ex * ex + ey * ey + ez * ez < kp.vr2_64;
+                            }
+                            if (inside) {
+                                a0 = fmaf(-k2q, P1.z, a0);
+                                continue;
+                            }
                         }
                         const float ir = rsqrt_ftz(d2), r = d2 * ir, ir2 = ir * ir, ir3 = ir2 * ir;
                         const float t = kap * r, e = exp2_ftz(kl2 * r), et1 = fmaf(e, t, e);
