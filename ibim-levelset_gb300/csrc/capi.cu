@@ -63,6 +63,22 @@ void trace_mark(const char *phase) {
 }
 void set_current_ctx(Ctx *c) { g_current = c; }
 
+void *Ctx::pinned_buffer(size_t bytes) {
+    if (bytes > pinned_bytes) {
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_bytes = 0;
+        const size_t grow = std::max(bytes, (size_t)1 << 20);
+        IBIM_CUDA(cudaMallocHost(&pinned, grow));
+        pinned_bytes = grow;
+    }
+    return pinned;
+}
+
+Ctx::~Ctx() {
+    if (pinned) cudaFreeHost(pinned);
+}
+
 cudaEvent_t Ctx::take_event() {
     if (ev_pool.empty()) {
         cudaEvent_t e;

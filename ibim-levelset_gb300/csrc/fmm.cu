@@ -878,15 +878,17 @@ Plan *make_plan(Tube *t, bool with_self, const double *extra, long n_extra, int 
     const long ns = t->n;
     std::vector<double> pts(3 * ns);
     {
-        std::vector<double> hx(ns), hy(ns), hz(ns);
-        t->x.download(hx.data(), ns);
-        t->y.download(hy.data(), ns);
-        t->z.download(hz.data(), ns);
+        // through the context's pinned staging buffer
+        double *h = static_cast<double *>(c->pinned_buffer(sizeof(double) * 3 * (size_t)ns));
+        t->x.download(h, ns);
+        t->y.download(h + ns, ns);
+        t->z.download(h + 2 * ns, ns);
         IBIM_CUDA(cudaStreamSynchronize(s));
+#pragma omp parallel for schedule(static) if (ns >= (1 << 16))
         for (long i = 0; i < ns; ++i) {
-            pts[3 * i] = hx[i];
-            pts[3 * i + 1] = hy[i];
-            pts[3 * i + 2] = hz[i];
+            pts[3 * i] = h[i];
+            pts[3 * i + 1] = h[ns + i];
+            pts[3 * i + 2] = h[2 * ns + i];
         }
     }
     Plan *P = new Plan();

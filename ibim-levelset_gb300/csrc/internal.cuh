@@ -131,6 +131,12 @@ struct Ctx {
     double prof_flops[PROF_NCAT] = {0}, prof_bytes[PROF_NCAT] = {0};  // algorithmic work of profiled launches
     std::vector<cudaEvent_t> ev_pool;
     cudaEvent_t take_event();
+    // pinned host staging for device-to-host copies on the solve's critical path (a pageable
+    // destination goes through the driver's bounce buffer); grown on demand, kept with the context
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    void *pinned_buffer(size_t bytes);
+    ~Ctx();
 };
 
 // Host phase trace for tuning: with IBIM_TRACE set, each mark prints to stderr the wall time
