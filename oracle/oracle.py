@@ -4,7 +4,10 @@ ctypes binding of the C restatement in oracle/ibim_oracle.c (the reference's CPU
 for the IBIM Poisson-Boltzmann path).  Only tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg use it, as the checker; the product never imports it.
 
-`build()` compiles oracle/_build/libibim_oracle.so with gcc (OpenMP).
+`build()` compiles oracle/_build/libibim_oracle.so with gcc (OpenMP), the checker's exact
+build, and oracle/_build/libibim_oracle_timing.so, the same source with -ffast-math: the
+reference is built -Ofast, and the CPU-baseline leg times this build (`use_timing_build()`),
+whose outputs are discarded.
 """
 
 from __future__ import annotations
@@ -17,6 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libibim_oracle.so")
+TIMING_LIB_PATH = os.path.join(HERE, "_build", "libibim_oracle_timing.so")
 
 _lib = None
 _dp = C.POINTER(C.c_double)
@@ -25,12 +29,25 @@ _ip = C.POINTER(C.c_int)
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "ibim_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "ibim_oracle.h"))):
-        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-        subprocess.run(["gcc", "-O3", "-fPIC", "-fopenmp", "-std=c11", "-ffp-contract=off", "-shared", "-o",
-                        LIB_PATH, src, "-lm"], check=True)
+    newest = max(os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "ibim_oracle.h")))
+    for path, flags in ((LIB_PATH, ["-ffp-contract=off"]), (TIMING_LIB_PATH, ["-ffast-math"])):
+        if force or not os.path.exists(path) or os.path.getmtime(path) < newest:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            subprocess.run(["gcc", "-O3", "-fPIC", "-fopenmp", "-std=c11", *flags, "-shared", "-o", path, src, "-lm"],
+                           check=True)
     return LIB_PATH
+
+
+_lib_path = LIB_PATH
+
+
+def use_timing_build() -> None:
+    """Bind the module to the -ffast-math build for the rest of the process (CPU-baseline timing
+    only: its results are not the checker's)."""
+    global _lib, _lib_path
+    build()
+    if _lib_path != TIMING_LIB_PATH:
+        _lib, _lib_path = None, TIMING_LIB_PATH
 
 
 class KParams(C.Structure):
@@ -47,7 +64,7 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(_lib_path)
         L.orc_expand.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, _dp, _dp, C.c_int, C.c_double]
         L.orc_evolve.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
