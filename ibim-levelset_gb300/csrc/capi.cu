@@ -1115,19 +1115,30 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
             y.alloc(2 * (size_t)P.ns, s);
             permute(c, P.ns, P.src_perm.ptr, prep.b_tube.ptr, x.ptr, false);
             permute(c, P.ns, P.src_perm.ptr, prep.b_tube.ptr + P.ns, x.ptr + P.ns, false);
+            // warm-up: the first mixed product sets the plan up, the second captures its graph
+            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
             bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
             bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_FP64_TC);
+            // at least reps mixed products and about 30 ms of them, and as many FP64-class ones as
+            // fit in the same time: short products are otherwise timed within launch jitter
+            Timer t0(s);
+            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
+            const double one32 = std::max(1e-3, t0.ms());
+            const int n32 = std::max(reps, std::min(1000, (int)std::ceil(30.0 / one32)));
             Timer t1(s);
-            for (int r = 0; r < reps; ++r) bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
-            const double ms32 = t1.ms() / reps;
+            for (int r = 0; r < n32; ++r) bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_MIXED);
+            const double ms32 = t1.ms() / n32;
+            const int n64 = std::max(1, std::min(50, (int)(30.0 / std::max(1e-3, 6.0 * ms32))));
             Timer t2(s);
-            bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_FP64_TC);
-            const double ms64 = t2.ms();
+            for (int r = 0; r < n64; ++r) bie_matvec(P, cfg->kp, x.ptr, y.ptr, IBIM_PRECISION_FP64_TC);
+            const double ms64 = t2.ms() / n64;
             IBIM_REQUIRE(!m2l_tc_error(P), "autotune: a tensor-core M2L wait exceeded its bound");
             ++timed;
             return 25.0 * ms32 + ms64;
         };
         Tuning best;
+        cost(best);  // untimed: the first candidate would otherwise also grow the memory pool
+        timed = 0;
         const double base = cost(best);
         double best_cost = base;
         auto consider = [&](Tuning t) {
@@ -1155,12 +1166,26 @@ int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, co
             t.nearff_seg_pairs = v;
             consider(t);
         }
+        // the minimum over the candidates is biased low: the best replaces the defaults only when a
+        // second measurement of both confirms it by 2 %
+        double best_ms = best_cost, default_ms = base;
+        if (best.near_seg_pairs != Tuning().near_seg_pairs || best.nearff_seg_pairs != Tuning().nearff_seg_pairs ||
+            best.tc_form != Tuning().tc_form) {
+            const double b2 = cost(best), d2 = cost(Tuning());
+            if (b2 < 0.98 * d2) {
+                best_ms = b2;
+                default_ms = d2;
+            } else {
+                best = Tuning();
+                best_ms = default_ms = d2;
+            }
+        }
         report[0] = (double)npts;
         report[1] = (double)best.near_seg_pairs;
         report[2] = (double)best.nearff_seg_pairs;
         report[3] = (double)best.tc_form;
-        report[4] = best_cost;
-        report[5] = base;
+        report[4] = best_ms;
+        report[5] = default_ms;
         report[6] = timed;
         if (install_min_points >= 0) {
             const int st = ibim_tuning_set(cfg->np, install_min_points, best.near_seg_pairs, best.nearff_seg_pairs,

@@ -303,9 +303,11 @@ int ibim_tuning_get(int order, long npoints, long out[3]);
 int ibim_tuning_load(const char *path);
 /* Times candidate launch parameters on this molecule (mixed path): for each, a plan prepared under
  * it and the CUDA-event time of a solve's mix of products (25 mixed, one FP64-class residual),
- * one coordinate at a time (launch form, FP32 segments, float-float segments).  report (7
- * doubles): tube points, best near_seg_pairs, nearff_seg_pairs, tc_form, best cost ms, default
- * cost ms, candidates timed.  install_min_points >= 0 adds the best as the row (order, it). */
+ * one coordinate at a time (launch form, FP32 segments, float-float segments), each over at least
+ * reps and about 30 ms of products; a best other than the defaults is kept only when a second
+ * measurement of both confirms it by 2 %.  report (7 doubles): tube points, best near_seg_pairs,
+ * nearff_seg_pairs, tc_form, best cost ms, default cost ms, candidates timed.
+ * install_min_points >= 0 adds the best as the row (order, it). */
 int ibim_autotune(ibim_ctx ctx, const double *centers, const double *charges, const double *radii, int natoms,
                   const ibim_config *cfg, int reps, long install_min_points, double *report);
 

@@ -40,8 +40,8 @@ def test_autotune_returns_a_row(ctx, restore_table):
     cfg = W.config(ibim.PRECISION_MIXED)
     r = ctx.autotune(W.mol.centers, W.mol.charges, W.mol.radii, cfg, reps=2, install_min_points=0)
     # the default, three other launch forms (4, and the CTA-pair forms 6 and 7), three sizes of
-    # each near-field segment
-    assert r["candidates"] == 10 and r["points"] > 0
+    # each near-field segment; two more when a winner other than the defaults is re-measured
+    assert r["candidates"] in (10, 12) and r["points"] > 0
     assert r["tc_form"] in (2, 4, 6, 7) and r["best_ms"] <= r["default_ms"]
     assert ibim.tuning_get(4, r["points"]) == dict(near_seg_pairs=r["near_seg_pairs"],
                                                    nearff_seg_pairs=r["nearff_seg_pairs"], tc_form=r["tc_form"])
