@@ -262,16 +262,18 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
             fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_FP64);
             if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
         } else {
-            // digit images for the FP64-class operator (the mixed path's residual), then the
-            // TF32 images from FP32 operators rounded from the FP64 ones; afterwards only the
-            // images are used, so the FP64 operators are released
-            // (order keeps the peak at 26 bytes per operator entry: FP64 8 + digits 14 + FP32 4,
-            // then digits + FP32 + TF32 images 8 once the FP64 operators are gone)
-            fmm_ensure_oz_images(*P, cfg.kp);
-            if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc() && m2l_tc_fp16_form() && P->opsff_ready) {
-                fmm_ensure_tc_images(*P, cfg.kp);  // FP16 images from the float-float operators
+            // Mixed path in the scaled FP16 form: the FP16 images of the mixed operator and the
+            // digit images of the FP64-class one (the refinement residual's) from one pass over
+            // float-float operators.  Otherwise the digit images, then the TF32 images from FP32
+            // operators rounded from the FP64 ones.  Afterwards only the images are used, so the
+            // FP64 / float-float operators are released (the order keeps the peak at 26 bytes per
+            // operator entry: FP64 8 + digits 14 + FP32 4, then digits + FP32 + TF32 images 8 once
+            // the FP64 operators are gone)
+            if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc() && fmm_ensure_images_ff(*P, cfg.kp)) {
+                // both images from one pass over the float-float operators
                 fmm_release_fp64_operators(*P);
             } else {
+                fmm_ensure_oz_images(*P, cfg.kp);
                 if (cfg.precision == IBIM_PRECISION_MIXED) fmm_prepare_operators(*P, cfg.kp, IBIM_PRECISION_MIXED);
                 fmm_release_fp64_operators(*P);
                 if (cfg.precision == IBIM_PRECISION_MIXED && mixed_uses_tc()) fmm_ensure_tc_images(*P, cfg.kp);

@@ -22,6 +22,7 @@
 #include <array>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <tuple>
 
@@ -478,49 +479,96 @@ void plan_gather(Ctx *c, long n, const int *perm, const double *a, double *b, do
 bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::vector<int> &ptr,
                    std::vector<int> &rng, bool split_long, std::vector<int> &seg, long max_pairs, long min_sources) {
     const int nl = (int)tl.size();
-    if (split_long) {
-        std::vector<int> p2{0}, r2;
+    auto cap_of = [&](int k) { return std::max<long>(min_sources, max_pairs / std::max(1, nt[k])); };
+    if (split_long && nl > 0) {  // leaves in parallel: piece counts, offsets, fill
+        std::vector<int> p2(nl + 1, 0);
+#pragma omp parallel for schedule(static) if (nl >= 4096)
         for (int k = 0; k < nl; ++k) {
-            const long cap = std::max<long>(min_sources, max_pairs / std::max(1, nt[k]));
+            const long cap = cap_of(k);
+            long c = 0;
+            for (int r = ptr[k]; r < ptr[k + 1]; ++r) c += (rng[2 * r + 1] - rng[2 * r] + cap - 1) / cap;
+            p2[k + 1] = (int)c;
+        }
+        for (int k = 0; k < nl; ++k) p2[k + 1] += p2[k];
+        std::vector<int> r2(2 * (size_t)p2[nl]);
+#pragma omp parallel for schedule(static) if (nl >= 4096)
+        for (int k = 0; k < nl; ++k) {
+            const long cap = cap_of(k);
+            long q = p2[k];
             for (int r = ptr[k]; r < ptr[k + 1]; ++r)
-                for (long b = rng[2 * r]; b < rng[2 * r + 1]; b += cap) {
-                    r2.push_back((int)b);
-                    r2.push_back((int)std::min<long>(b + cap, rng[2 * r + 1]));
+                for (long b = rng[2 * r]; b < rng[2 * r + 1]; b += cap, ++q) {
+                    r2[2 * q] = (int)b;
+                    r2[2 * q + 1] = (int)std::min<long>(b + cap, rng[2 * r + 1]);
                 }
-            p2.push_back((int)r2.size() / 2);
         }
         ptr.swap(p2);
         rng.swap(r2);
     }
-    struct Seg {
-        long work;
-        int leaf, r0, r1, mode;
-    };
-    std::vector<Seg> out;
-    bool atomic = false;
+    if (nl == 0) {
+        seg.assign(4, 0);
+        return false;
+    }
+    // leaves in parallel: segment counts, offsets, then each leaf fills its own slots
+    std::vector<long> soff(nl + 1, 0);
+#pragma omp parallel for schedule(static) if (nl >= 4096)
     for (int k = 0; k < nl; ++k) {
-        const long cap = std::max<long>(min_sources, max_pairs / std::max(1, nt[k]));
-        const size_t first = out.size();
-        int r0 = ptr[k];
-        long acc = 0;
+        const long cap = cap_of(k);
+        long acc = 0, c = 1;
         for (int r = ptr[k]; r < ptr[k + 1]; ++r) {
             const long len = rng[2 * r + 1] - rng[2 * r];
             if (acc > 0 && acc + len > cap) {
-                out.push_back({acc * nt[k], tl[k], r0, r, 0});
+                ++c;
+                acc = 0;
+            }
+            acc += len;
+        }
+        soff[k + 1] = c;
+    }
+    bool atomic = false;
+    for (int k = 0; k < nl; ++k) {
+        atomic = atomic || soff[k + 1] > 1;
+        soff[k + 1] += soff[k];
+    }
+    const long nseg = soff[nl];
+    std::vector<long> work(nseg);
+    std::vector<std::array<int, 4>> body(nseg);
+#pragma omp parallel for schedule(static) if (nl >= 4096)
+    for (int k = 0; k < nl; ++k) {
+        const long cap = cap_of(k), first = soff[k];
+        const int multi = soff[k + 1] - first > 1 ? 2 : 0;
+        long q = first, acc = 0;
+        int r0 = ptr[k];
+        auto emit = [&](int r1) {
+            work[q] = acc * nt[k];
+            body[q] = {tl[k], r0, r1, (q == first ? 1 : 0) | multi};
+            ++q;
+        };
+        for (int r = ptr[k]; r < ptr[k + 1]; ++r) {
+            const long len = rng[2 * r + 1] - rng[2 * r];
+            if (acc > 0 && acc + len > cap) {
+                emit(r);
                 r0 = r;
                 acc = 0;
             }
             acc += len;
         }
-        out.push_back({acc * nt[k], tl[k], r0, ptr[k + 1], 0});
-        const bool multi = out.size() - first > 1;
-        atomic = atomic || multi;
-        for (size_t q = first; q < out.size(); ++q) out[q].mode = (q == first ? 1 : 0) | (multi ? 2 : 0);
+        emit(ptr[k + 1]);
     }
-    std::stable_sort(out.begin(), out.end(), [](const Seg &a, const Seg &b) { return a.work > b.work; });
-    seg.clear();
-    for (auto &g : out) seg.insert(seg.end(), {g.leaf, g.r0, g.r1, g.mode});
-    if (seg.empty()) seg.assign(4, 0);
+    // descending work, ties in leaf order: a stable LSD radix sort of the segments by
+    // (max work - work), 11 bits a pass
+    long maxw = 0;
+    for (long q = 0; q < nseg; ++q) maxw = std::max(maxw, work[q]);
+    std::vector<long> order(nseg), tmp(nseg);
+    for (long q = 0; q < nseg; ++q) order[q] = q;
+    for (int sh = 0; sh < 63 && (maxw >> sh) > 0; sh += 11) {
+        std::array<long, 2049> c{};
+        for (long q = 0; q < nseg; ++q) c[1 + (((maxw - work[order[q]]) >> sh) & 2047)]++;
+        for (int d = 0; d < 2048; ++d) c[d + 1] += c[d];
+        for (long q = 0; q < nseg; ++q) tmp[c[((maxw - work[order[q]]) >> sh) & 2047]++] = order[q];
+        order.swap(tmp);
+    }
+    seg.resize(4 * nseg);
+    for (long q = 0; q < nseg; ++q) std::memcpy(&seg[4 * q], body[order[q]].data(), 4 * sizeof(int));
     return atomic;
 }
 
@@ -1082,6 +1130,23 @@ void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp) {
     }
     for (int i = 0; i < 5; ++i) P.oz_key[i] = key[i];
     P.oz_ready = true;
+}
+
+bool fmm_ensure_images_ff(Plan &P, const ibim_kernel_params &kp) {
+    if (P.precision == IBIM_PRECISION_FP64 || !ops_ff_enabled() || !m2l_tc_fp16_form()) return false;
+    double key[5];
+    kp_key(kp, key);
+    if (P.oz_ready && same_key(P.oz_key, key) && P.tc_ready && same_key(P.tc_key, key)) return true;
+    fmm_prepare_operators_ff(P, kp);
+    m2l_pack_images_ff(P, P.opsff.ptr);
+    const char *chk = std::getenv("IBIM_CHECK_IMAGES");  // read per call: a test switch
+    if (chk && chk[0] == '1') m2l_check_images_ff(P, P.opsff.ptr);
+    // the images replace the FP32 operators on this path
+    P.ops32.release();
+    P.ops32_ready = false;
+    for (int i = 0; i < 5; ++i) P.oz_key[i] = P.tc_key[i] = key[i];
+    P.oz_ready = P.tc_ready = true;
+    return true;
 }
 
 void fmm_release_fp64_operators(Plan &P) {

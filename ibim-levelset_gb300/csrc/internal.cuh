@@ -403,11 +403,18 @@ void m2l_tc_run(Plan &P, TargetSet &S);
 int m2l_tc_error(Plan &P);
 // BF16 digit images and row scales from P.ops64, or from float-float operators when ff is given.
 void m2l_oz_pack(Plan &P, const float2 *ff = nullptr);
+// Both images (digit tiles and scaled FP16 tiles) of the float-float operators in one pass.
+void m2l_pack_images_ff(Plan &P, const float2 *ff);
+// Test check: the one-pass images equal the separate passes' word for word (throws otherwise).
+void m2l_check_images_ff(Plan &P, const float2 *ff);
 void m2l_oz_run(Plan &P, const TargetSet &S);
 // Operator images for kernel parameters kp, built when missing or stale: the TF32 images (from
 // FP32 operators, which are then released) and the digit images (from the FP64 operators).
 void fmm_ensure_tc_images(Plan &P, const ibim_kernel_params &kp);
 void fmm_ensure_oz_images(Plan &P, const ibim_kernel_params &kp);
+// The mixed path's FP16 images and the FP64-class digit images together, from one set of
+// float-float operators (scaled FP16 form, float-float operators enabled); false otherwise.
+bool fmm_ensure_images_ff(Plan &P, const ibim_kernel_params &kp);
 // Release the FP64 operators (rebuilt on demand) once only their digit images are needed.
 void fmm_release_fp64_operators(Plan &P);
 // Whether the mixed path's V-list M2L runs on the tensor cores on this device.

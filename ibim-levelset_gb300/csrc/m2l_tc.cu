@@ -21,6 +21,7 @@
 
 #include <cstdint>
 #include <cstdlib>
+#include <type_traits>
 
 #include <cuda_fp16.h>
 
@@ -1535,9 +1536,15 @@ __global__ void k_scale_ops_oz(int n4, int mtiles, int nops, int scale_exp, cons
 // Operators (FP64 or float-float) -> digit tiles [op][row tile][stage][digit][4 KB] in the
 // shared-memory layout (tile_off with 16 K elements of 2 bytes per row).  One thread per (op, row,
 // group of 8 K elements): 8 reads, then one 16-byte store per digit.
-template <int S, class OW>
+// With H16 (float-float operators), the same pass also writes the scaled FP16 hi / lo tiles of
+// the mixed contraction (k_pack_ops_h16's values and layout) from the row scales rscale: the
+// operators are read once for both images.
+template <int S, class OW, bool H16 = false>
 __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *__restrict__ ops,
-                              const int *__restrict__ sexp, uint4 *a) {
+                              const int *__restrict__ sexp, uint4 *a, const float *__restrict__ rscale = nullptr,
+                              uint4 *a_hi = nullptr, uint4 *a_lo = nullptr) {
+    static_assert(!H16 || std::is_same<OW, float2>::value, "FP16 images from float-float operators");
+    static_assert(OZ_M == TC_M && OZ_KS == TC_KS16 && OZ_ATILE == TC_TILE_BYTES, "one tile layout");
     const int nstage = kpad / OZ_KS, mpad = mtiles * OZ_M, ngrp = kpad / 8;
     const long total = (long)nops * ngrp * mpad;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
@@ -1545,7 +1552,10 @@ __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *
         const long rest = i / mpad;
         const int grp = (int)(rest % ngrp), op = (int)(rest / ngrp);
         const int e = sexp[(long)op * mpad + r];
-        uint32_t w[S][4];
+        float inv = 1.f;
+        if constexpr (H16) inv = 1.f / rscale[(long)op * mpad + r];  // a power of two: exact
+        uint32_t w[S][4], wh[4], wl[4];
+#pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int k = grp * 8 + q;
             const OW v = (r < n4 && k < n4) ? ops[(long)op * n4 * n4 + (long)k * n4 + r] : OW{};
@@ -1556,13 +1566,57 @@ __global__ void k_pack_ops_oz(int n4, int mtiles, int kpad, int nops, const OW *
                 if (q & 1) w[d][q >> 1] |= (uint32_t)dig[d] << 16;
                 else w[d][q >> 1] = dig[d];
             }
+            if constexpr (H16) {
+                float2 x = op_word(&v, 0);
+                x.x *= inv;  // powers of two: exact
+                x.y *= inv;
+                uint16_t h, l;
+                split_h16(x, h, l);
+                if (q & 1) {
+                    wh[q >> 1] |= (uint32_t)h << 16;
+                    wl[q >> 1] |= (uint32_t)l << 16;
+                } else {
+                    wh[q >> 1] = h;
+                    wl[q >> 1] = l;
+                }
+            }
         }
         const int t = r / OZ_M, row = r % OZ_M, st = grp / 2, half = grp & 1;
-        const long tbase = (((long)op * mtiles + t) * nstage + st) * S;
+        const long tile = ((long)op * mtiles + t) * nstage + st, tbase = tile * S;
         const uint32_t off = tile_off(row, half);  // byte offset of the 16-byte piece
 #pragma unroll
         for (int d = 0; d < S; ++d)
             a[((tbase + d) * OZ_ATILE + off) / 16] = make_uint4(w[d][0], w[d][1], w[d][2], w[d][3]);
+        if constexpr (H16) {
+            const long idx = (tile * TC_TILE_BYTES + off) / 16;
+            a_hi[idx] = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+            a_lo[idx] = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+        }
+    }
+}
+
+// Row scales of both images from one read of the float-float operators: the FP16 form's s_r
+// (k_scale_ops_h16) and the digit form's exponent and s_r 2^(-2D) (k_scale_ops_oz), both from
+// max_k (|hi| + |lo|).
+__global__ void k_scale_ops_ff2(int n4, int mtiles, int nops, int scale_exp, const float2 *__restrict__ ops,
+                                float *rscale, double *sig, int *sexp) {
+    const int mpad = mtiles * OZ_M;
+    const long total = (long)nops * mpad;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int r = (int)(i % mpad), op = (int)(i / mpad);
+        float m = 0.f;
+        if (r < n4) {
+            const float2 *col0 = ops + (long)op * n4 * n4 + r;
+            for (int k = 0; k < n4; ++k) {
+                const float2 x = col0[(long)k * n4];
+                m = fmaxf(m, fabsf(x.x) + fabsf(x.y));
+            }
+        }
+        int e = 0;
+        if (m > 0.f) frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+        rscale[i] = h16_scale(m);
+        sig[i] = ldexp(1.0, e - scale_exp);
+        sexp[i] = e;
     }
 }
 
@@ -1879,16 +1933,14 @@ bool m2l_tc_fp16_form() { return tc_fp16(); }
 // protein), one CTA of four row tiles per SM (4; 2.50 ms) or, FP16 form only, persistent (0: one
 // CTA per SM walking units of two row tiles with double-buffered accumulators; 2.94 ms).
 
-void m2l_tc_pack(Plan &P, const float2 *ff) {
+// Shapes and device buffers of the contraction's images (operators, multipoles, scales).
+static void tc_alloc(Plan &P) {
     P.tc_h16 = tc_fp16();
-    if (!P.tc_h16) ff = nullptr;
-    IBIM_REQUIRE(P.ops32.ptr || ff || P.nops == 0, "tensor-core images need the operators");
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     const int ks = P.tc_h16 ? TC_KS16 : TC_KS;
     P.tc_kpad = (n4 + ks - 1) / ks * ks;
     P.tc_mpad = (n4 + TC_M - 1) / TC_M * TC_M;
-    const int mt = P.tc_mpad / TC_M;
     // image sizes in floats (an FP16 image takes half the words)
     const size_t na = (size_t)std::max(1, P.nops) * P.tc_mpad * P.tc_kpad / (P.tc_h16 ? 2 : 1);
     const size_t nb = (size_t)P.tree.nnodes * P.tc_kpad / (P.tc_h16 ? 2 : 1);
@@ -1897,6 +1949,36 @@ void m2l_tc_pack(Plan &P, const float2 *ff) {
     if (P.tc_h16) {
         P.tc_rsc.alloc((size_t)std::max(1, P.nops) * P.tc_mpad, s);
         P.tc_csc.alloc((size_t)P.tree.nnodes, s);
+    }
+    P.tc_b_hi.alloc(nb, s);
+    P.tc_b_lo.alloc(nb, s);
+    if (!P.tc_err.ptr) {
+        P.tc_err.alloc(1, s);
+        P.tc_err.zero();
+    }
+    // the contraction kernels' shared memory (above the 48 KB default)
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TCP_SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<1>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<2>::SMEM));
+}
+
+void m2l_tc_pack(Plan &P, const float2 *ff) {
+    tc_alloc(P);
+    if (!P.tc_h16) ff = nullptr;
+    IBIM_REQUIRE(P.ops32.ptr || ff || P.nops == 0, "tensor-core images need the operators");
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R;
+    const int mt = P.tc_mpad / TC_M;
+    if (P.tc_h16) {
         if (P.nops > 0) {
             const long rows = (long)P.nops * P.tc_mpad, pieces = rows * (P.tc_kpad / 8);
             const int gs = (int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms);
@@ -1916,25 +1998,7 @@ void m2l_tc_pack(Plan &P, const float2 *ff) {
         (count_launch(), k_pack_ops_tc<<<8 * P.ctx->num_sms, 256, 0, s>>>(n4, mt, P.tc_kpad, P.nops, P.ops32.ptr,
                                                                       P.tc_a_hi.ptr, P.tc_a_lo.ptr));
     }
-    P.tc_b_hi.alloc(nb, s);
-    P.tc_b_lo.alloc(nb, s);
-    if (!P.tc_err.ptr) {
-        P.tc_err.alloc(1, s);
-        P.tc_err.zero();
-    }
     IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TcShape<M2L_CHTC>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TcShape<M2L_CHTC>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, false, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, TCP_SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc<M2L_CHTC, true, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TcShape<M2L_CHTC, 2, 2>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<1>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_tc2h<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tc2hShape<2>::SMEM));
 }
 
 // V-list M2L on the tensor cores; mult32 -> local32 (accumulating): chunks of 128 pairs against
@@ -2014,9 +2078,8 @@ void m2l_tc_run(Plan &P, TargetSet &S) {
 
 // Digit tiles of the FP64 operators, or of the float-float ones when ff is given: 6 digits of 7
 // bits where K <= 800 (orders up to 5), else 7 of 6 bits.
-void m2l_oz_pack(Plan &P, const float2 *ff) {
-    if (P.nops == 0) return;
-    IBIM_REQUIRE(P.ops64.ptr || ff, "digit images need the FP64-class operators");
+// Shapes and device buffers of the digit images (nops > 0).
+static void oz_alloc(Plan &P) {
     cudaStream_t s = P.ctx->stream;
     const int n4 = 4 * P.R;
     P.oz_kpad = (n4 + OZ_KS - 1) / OZ_KS * OZ_KS;
@@ -2031,6 +2094,17 @@ void m2l_oz_pack(Plan &P, const float2 *ff) {
         P.tc_err.alloc(1, s);
         P.tc_err.zero();
     }
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<6>::SMEM));
+    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<7>::SMEM));
+}
+
+void m2l_oz_pack(Plan &P, const float2 *ff) {
+    if (P.nops == 0) return;
+    IBIM_REQUIRE(P.ops64.ptr || ff, "digit images need the FP64-class operators");
+    oz_alloc(P);
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R;
+    const int S = P.oz_s;
     const long rows = (long)P.nops * P.oz_mtiles * OZ_M;
     DevBuf<int> sexp;
     sexp.alloc((size_t)rows, s);
@@ -2047,17 +2121,93 @@ void m2l_oz_pack(Plan &P, const float2 *ff) {
                                                                    P.oz_sig.ptr, sexp.ptr));
     auto pack = [&](auto kf, auto kd) {
         if (ff)
-            (count_launch(), kf<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff, sexp.ptr, a));
+            (count_launch(), kf<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff, sexp.ptr, a, nullptr,
+                                                   nullptr, nullptr));
         else
-            (count_launch(), kd<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, sexp.ptr, a));
+            (count_launch(), kd<<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, P.ops64.ptr, sexp.ptr, a,
+                                                   nullptr, nullptr, nullptr));
     };
     if (S == 6)
         pack(k_pack_ops_oz<6, float2>, k_pack_ops_oz<6, double>);
     else
         pack(k_pack_ops_oz<7, float2>, k_pack_ops_oz<7, double>);
     IBIM_CHECK_LAUNCH();
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<6>::SMEM));
-    IBIM_CUDA(cudaFuncSetAttribute(k_m2l_oz<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, OzShape<7>::SMEM));
+}
+
+// Words of a and b (n 32-bit words each) that differ, added into *cnt.
+__global__ void k_count_diff(long n, const uint32_t *__restrict__ a, const uint32_t *__restrict__ b,
+                             unsigned long long *cnt) {
+    unsigned long long c = 0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        c += a[i] != b[i];
+    if (c) atomicAdd(cnt, c);
+}
+
+// Both images of the float-float operators in one pass over them: the digit tiles and scales of
+// the FP64-class contraction and the scaled FP16 tiles and row scales of the mixed one, equal word
+// for word to those m2l_oz_pack and m2l_tc_pack make from the same operators (two kernels instead
+// of four: the 8 bytes an entry are read twice instead of four times).
+void m2l_pack_images_ff(Plan &P, const float2 *ff) {
+    IBIM_REQUIRE(tc_fp16(), "one-pass images: the scaled FP16 form only");
+    IBIM_REQUIRE(ff || P.nops == 0, "one-pass images need the float-float operators");
+    tc_alloc(P);
+    if (P.nops == 0) return;
+    oz_alloc(P);
+    IBIM_REQUIRE(P.oz_kpad == P.tc_kpad && P.oz_mtiles * OZ_M == P.tc_mpad, "image shapes differ");
+    cudaStream_t s = P.ctx->stream;
+    const int n4 = 4 * P.R, S = P.oz_s;
+    const long rows = (long)P.nops * P.oz_mtiles * OZ_M, pieces = rows * (P.oz_kpad / 8);
+    DevBuf<int> sexp;
+    sexp.alloc((size_t)rows, s);
+    const int gs = (int)std::min<long>((rows + 255) / 256, 32L * P.ctx->num_sms);
+    const int gp = (int)std::min<long>((pieces + 255) / 256, 64L * P.ctx->num_sms);
+    (count_launch(), k_scale_ops_ff2<<<gs, 256, 0, s>>>(n4, P.oz_mtiles, P.nops, 2 * (42 / S), ff, P.tc_rsc.ptr,
+                                                        P.oz_sig.ptr, sexp.ptr));
+    uint4 *a = reinterpret_cast<uint4 *>(P.oz_a.ptr), *ah = reinterpret_cast<uint4 *>(P.tc_a_hi.ptr),
+          *al = reinterpret_cast<uint4 *>(P.tc_a_lo.ptr);
+    if (S == 6)
+        (count_launch(), k_pack_ops_oz<6, float2, true><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff,
+                                                                         sexp.ptr, a, P.tc_rsc.ptr, ah, al));
+    else
+        (count_launch(), k_pack_ops_oz<7, float2, true><<<gp, 256, 0, s>>>(n4, P.oz_mtiles, P.oz_kpad, P.nops, ff,
+                                                                         sexp.ptr, a, P.tc_rsc.ptr, ah, al));
+    IBIM_CHECK_LAUNCH();
+}
+
+// The one-pass images of m2l_pack_images_ff against those of m2l_oz_pack and m2l_tc_pack from the
+// same operators, word for word (a check for tests, IBIM_CHECK_IMAGES=1); the plan keeps the
+// four-kernel images.  Throws when a word differs.
+void m2l_check_images_ff(Plan &P, const float2 *ff) {
+    if (P.nops == 0) return;
+    cudaStream_t s = P.ctx->stream;
+    DevBuf<uint16_t> oz_a = std::move(P.oz_a);
+    DevBuf<double> oz_sig = std::move(P.oz_sig);
+    DevBuf<float> a_hi = std::move(P.tc_a_hi), a_lo = std::move(P.tc_a_lo), rsc = std::move(P.tc_rsc);
+    m2l_oz_pack(P, ff);
+    m2l_tc_pack(P, ff);
+    DevBuf<unsigned long long> cnt;
+    cnt.alloc(5, s);
+    cnt.zero();
+    auto diff = [&](const void *x, size_t xbytes, const void *y, size_t ybytes, int slot) {
+        IBIM_REQUIRE(xbytes == ybytes && xbytes % 4 == 0, "image sizes differ");
+        const long n = (long)(xbytes / 4);
+        if (n == 0) return;
+        (count_launch(), k_count_diff<<<(int)std::min<long>(div_up(n, 256), 8L * P.ctx->num_sms), 256, 0, s>>>(
+                             n, static_cast<const uint32_t *>(x), static_cast<const uint32_t *>(y), cnt.ptr + slot));
+        IBIM_CHECK_LAUNCH();
+    };
+    diff(oz_a.ptr, oz_a.n * 2, P.oz_a.ptr, P.oz_a.n * 2, 0);
+    diff(oz_sig.ptr, oz_sig.n * 8, P.oz_sig.ptr, P.oz_sig.n * 8, 1);
+    diff(a_hi.ptr, a_hi.n * 4, P.tc_a_hi.ptr, P.tc_a_hi.n * 4, 2);
+    diff(a_lo.ptr, a_lo.n * 4, P.tc_a_lo.ptr, P.tc_a_lo.n * 4, 3);
+    diff(rsc.ptr, rsc.n * 4, P.tc_rsc.ptr, P.tc_rsc.n * 4, 4);
+    unsigned long long h[5];
+    cnt.download(h, 5);
+    IBIM_CUDA(cudaStreamSynchronize(s));
+    static const char *what[5] = {"digit tiles", "digit row scales", "FP16 hi tiles", "FP16 lo tiles",
+                                  "FP16 row scales"};
+    for (int i = 0; i < 5; ++i)
+        if (h[i]) throw Error(IBIM_ERR_CUDA, std::string("one-pass operator images differ: ") + what[i]);
 }
 
 // V-list M2L of the FP64 operator by digit products on the tensor cores; mult -> local.

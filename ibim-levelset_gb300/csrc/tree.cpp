@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
+#include <cstdlib>
 #include <unordered_map>
 
 #include <omp.h>
@@ -330,9 +331,10 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
             lown[id] = omp_get_thread_num();
             for (int w = 0; w < 4; ++w) lbeg[id][w] = (long)buf[w].size();
             auto push = [&](int w, int x) { buf[w].push_back(x); };
-            auto push_once = [&](int w, int x) {
-                if (std::find(buf[w].begin() + lbeg[id][w], buf[w].end(), x) == buf[w].end()) buf[w].push_back(x);
-            };
+            // A candidate in a parent neighbour that is a leaf (at the parent's level or coarser)
+            // is that leaf, shared by the neighbour's 8 cells and possibly by other neighbours:
+            // it is classified once, at its first occurrence (the reference's lists are sets).
+            int seen[27], nseen = 0;
             for (int xi = -2; xi < 4; ++xi)
                 for (int yi = -2; yi < 4; ++yi)
                     for (int zi = -2; zi < 4; ++zi) {
@@ -342,19 +344,24 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
                         const int c[3] = {2 * pn.coord[0] + xi, 2 * pn.coord[1] + yi, 2 * pn.coord[2] + zi};
                         if (c[0] == n.coord[0] && c[1] == n.coord[1] && c[2] == n.coord[2]) continue;
                         const BNode &mn = B.nodes[m];
-                        const int cid = (mn.level == pn.level && mn.child[0] >= 0)
-                                            ? mn.child[((c[2] & 1) << 2) | ((c[1] & 1) << 1) | (c[0] & 1)]
-                                            : m;
-                        const bool adj = adjacent(id, cid);
-                        const BNode &cn = B.nodes[cid];
-                        if (cn.level < n.level) {
-                            if (adj) {
-                                if (cn.leaf) push_once(LU, cid);
+                        if (!(mn.level == pn.level && mn.child[0] >= 0)) {  // coarser than the child
+                            bool dup = false;
+                            for (int q = 0; q < nseen && !dup; ++q) dup = seen[q] == m;
+                            if (dup) continue;
+                            seen[nseen++] = m;
+                            if (adjacent(id, m)) {
+                                if (mn.leaf) push(LU, m);
                             } else {
-                                push_once(LX, cid);
+                                push(LX, m);
                             }
+                            continue;
                         }
-                        if (cn.level == n.level) {
+                        const int cid = mn.child[((c[2] & 1) << 2) | ((c[1] & 1) << 1) | (c[0] & 1)];
+                        // same level: adjacent when the lattice cells differ by at most one in
+                        // every axis (they are distinct)
+                        const bool adj = std::abs(c[0] - n.coord[0]) <= 1 && std::abs(c[1] - n.coord[1]) <= 1 &&
+                                         std::abs(c[2] - n.coord[2]) <= 1;
+                        {
                             if (!adj) {
                                 push(LV, cid);
                             } else if (n.leaf) {
@@ -390,13 +397,15 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
     trace_mark("tree: U V W X lists");
     std::vector<int> ref_of;
     reference_ids(B.nodes, ref_of);
-    // level-ordered renumbering
-    std::vector<int> order(nn);
-    for (int i = 0; i < nn; ++i) order[i] = i;
-    // by level, then by the reference's id (its creation order)
-    std::sort(order.begin(), order.end(), [&](int a, int b) {
-        return B.nodes[a].level != B.nodes[b].level ? B.nodes[a].level < B.nodes[b].level : ref_of[a] < ref_of[b];
-    });
+    // level-ordered renumbering: by level, then by the reference's id (its creation order, a
+    // permutation of 0 .. nn-1), as a counting sort by level over the nodes in reference order
+    std::vector<int> by_ref(nn), order(nn), lstart(depth + 2, 0);
+    for (int i = 0; i < nn; ++i) {
+        by_ref[ref_of[i]] = i;
+        lstart[B.nodes[i].level + 1]++;
+    }
+    for (int l = 0; l <= depth; ++l) lstart[l + 1] += lstart[l];
+    for (int r = 0; r < nn; ++r) order[lstart[B.nodes[by_ref[r]].level]++] = by_ref[r];
     std::vector<int> newid(nn);
     for (int i = 0; i < nn; ++i) newid[order[i]] = i;
 
