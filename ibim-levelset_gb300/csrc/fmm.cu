@@ -651,16 +651,21 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     std::vector<int> level_of(nn);
     for (int l = 0; l < T.nlevels; ++l)
         for (int i = T.level_begin[l]; i < T.level_begin[l + 1]; ++i) level_of[i] = l;
+    // which dense V keys occur: per-thread flags set while the pairs are generated, OR-ed afterwards
+    const size_t nd = opid.dense.size();
+    std::vector<std::vector<char>> vused(omp_get_max_threads(), std::vector<char>(nd, 0));
 #pragma omp parallel for schedule(dynamic, 64)
     for (int i = 0; i < nn; ++i) {
         if (!has_t(i)) continue;
         const int l = level_of[i];
+        char *used_t = vused[omp_get_thread_num()].data();
         long q = poff[i];
         for (int sidx : T.V[i]) {
             if (!has_s(sidx)) continue;
             const int ox = T.coord[3 * sidx] - T.coord[3 * i], oy = T.coord[3 * sidx + 1] - T.coord[3 * i + 1],
                       oz = T.coord[3 * sidx + 2] - T.coord[3 * i + 2];
             pkey[q] = l * 343 + (ox + 3) * 49 + (oy + 3) * 7 + (oz + 3);
+            used_t[pkey[q]] = 1;
             psrc[q] = sidx;
             ptgt[q] = i;
             ++q;
@@ -695,19 +700,9 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
     trace_mark("lists: pairs generated");
     // operator ids: V keys in dense-index order, then X keys in sorted order
     {
-        // which dense V keys occur: per-thread flags over pair ranges, OR-ed afterwards
-        const size_t nd = opid.dense.size();
-        const int nthr = std::max(1, std::min({32, omp_get_max_threads(), (int)(npair / 65536) + 1}));
-        std::vector<std::vector<char>> part(nthr, std::vector<char>(nd, 0));
-#pragma omp parallel for schedule(static) num_threads(nthr)
-        for (int t = 0; t < nthr; ++t) {
-            const long q0 = npair * t / nthr, q1 = npair * (t + 1) / nthr;
-            for (long q = q0; q < q1; ++q)
-                if (pkey[q] >= 0) part[t][pkey[q]] = 1;
-        }
         std::vector<char> used(nd, 0);
-        for (int t = 0; t < nthr; ++t)
-            for (size_t d = 0; d < nd; ++d) used[d] |= part[t][d];
+        for (const auto &part : vused)
+            for (size_t d = 0; d < nd; ++d) used[d] |= part[d];
         for (size_t d = 0; d < used.size(); ++d)
             if (used[d]) {
                 const int l = (int)(d / 343), c = (int)(d % 343);
@@ -800,22 +795,29 @@ static void build_target_lists(Plan &P, TargetSet &S, OpIndex &opid) {
             }
         }
     }
+    // chunks (operator, first pair, count) of each contraction's width, in operator order:
+    // counts per operator, offsets, then the operators in parallel
     std::vector<int> chunks, chunks32, chunks_tc, chunks_tc2, chunks_oz;
-    auto cut = [&](std::vector<int> &out, int op, long b, long n, int width) {
-        for (long q = 0; q < n; q += width) {
-            out.push_back(op);
-            out.push_back((int)(b + q));
-            out.push_back((int)std::min<long>(width, n - q));
+    auto cut = [&](std::vector<int> &out, int width) {
+        std::vector<long> coff(nop + 1, 0);
+        for (int op = 0; op < nop; ++op) coff[op + 1] = coff[op] + (opbeg[op + 1] - opbeg[op] + width - 1) / width;
+        out.resize(3 * coff[nop]);
+#pragma omp parallel for schedule(static) if (nop >= 256)
+        for (int op = 0; op < nop; ++op) {
+            const long b = opbeg[op], n = opbeg[op + 1] - opbeg[op];
+            long c = coff[op];
+            for (long q = 0; q < n; q += width, ++c) {
+                out[3 * c] = op;
+                out[3 * c + 1] = (int)(b + q);
+                out[3 * c + 2] = (int)std::min<long>(width, n - q);
+            }
         }
     };
-    for (int op = 0; op < nop; ++op) {
-        const long b = opbeg[op], n = opbeg[op + 1] - opbeg[op];
-        cut(chunks, op, b, n, M2L_CH);
-        cut(chunks32, op, b, n, M2L_CH32);
-        cut(chunks_tc, op, b, n, M2L_CHTC);
-        cut(chunks_tc2, op, b, n, 2 * M2L_CHTC);
-        cut(chunks_oz, op, b, n, M2L_CHOZ);
-    }
+    cut(chunks, M2L_CH);
+    cut(chunks32, M2L_CH32);
+    cut(chunks_tc, M2L_CHTC);
+    cut(chunks_tc2, 2 * M2L_CHTC);
+    cut(chunks_oz, M2L_CHOZ);
     trace_mark("lists: pairs grouped");
     S.nvpairs = npair;
     S.nchunks = (int)chunks.size() / 3;
