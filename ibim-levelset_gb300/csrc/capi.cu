@@ -285,6 +285,10 @@ void solve_prepare(Ctx *c, const double *centers_dev, const double *radii_dev, c
         if (cfg.precision == IBIM_PRECISION_MIXED ||
             (cfg.precision == IBIM_PRECISION_FP64_TC && m2l_tc_supported() && near_ff_enabled()))
             for (TargetSet *ts : P->targets) mixed_lists_host(*P, *ts);
+        // and the mixed plan's data (FP32 tables, leaf-relative coordinates, near lists on the
+        // device), queued behind the operators instead of after them
+        if (cfg.precision == IBIM_PRECISION_MIXED)
+            for (TargetSet *ts : P->targets) prepare_mixed(*P, *ts);
         IBIM_CUDA(cudaStreamSynchronize(s));
         const auto w2 = std::chrono::steady_clock::now();
         res.t_operators_ms = std::chrono::duration<double, std::milli>(w2 - w1).count();
