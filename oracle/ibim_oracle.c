@@ -703,21 +703,50 @@ static inline void kblock(const orc_kparams *kp, int kernel, const double dd[3],
 }
 
 static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
-                     int stride);
+                     const unsigned char *need);
 
 void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out) {
-    fmm_impl(t, p, kp, kernel, dens, out, 1);
+    fmm_impl(t, p, kp, kernel, dens, out, NULL);
 }
 
 /* Timing sample: the upward pass in full, the downward pass (M2L, L2L, near field, L2P) only
  * for nodes whose id is a multiple of `stride`; `out` is then incomplete. */
 void orc_fmm_sample(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
                     int stride) {
-    fmm_impl(t, p, kp, kernel, dens, out, stride < 1 ? 1 : stride);
+    if (stride < 1) stride = 1;
+    unsigned char *need = (unsigned char *)malloc((size_t)t->n);
+    for (int i = 0; i < t->n; ++i) need[i] = i % stride == 0;
+    fmm_impl(t, p, kp, kernel, dens, out, need);
+    free(need);
+}
+
+/* The FMM at chosen targets only (a checker for large trees): the upward pass in full, the
+ * downward pass for the leaves that hold the targets sel[0..nsel) and for their ancestors (whose
+ * locals the leaves' L2L chain needs), in the same arithmetic order as orc_fmm, so out equals
+ * orc_fmm's at those targets; elsewhere out is incomplete.  Returns the number of leaves. */
+int orc_fmm_targets(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                    const int *sel, int nsel) {
+    int *leaf_of = (int *)malloc(sizeof(int) * (size_t)(t->nt > 0 ? t->nt : 1));
+    for (int i = 0; i < t->nt; ++i) leaf_of[i] = -1;
+    for (int i = 0; i < t->n; ++i)
+        if (t->nd[i].leaf)
+            for (int q = 0; q < t->nd[i].ntgt; ++q) leaf_of[t->nd[i].tgt.v[q]] = i;
+    unsigned char *need = (unsigned char *)calloc((size_t)t->n, 1);
+    int nleaf = 0;
+    for (int q = 0; q < nsel; ++q) {
+        if (sel[q] < 0 || sel[q] >= t->nt || leaf_of[sel[q]] < 0) continue;
+        int i = leaf_of[sel[q]];
+        if (!need[i]) ++nleaf;
+        for (; i >= 0 && !need[i]; i = t->nd[i].parent) need[i] = 1;
+    }
+    fmm_impl(t, p, kp, kernel, dens, out, need);
+    free(need);
+    free(leaf_of);
+    return nleaf;
 }
 
 static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
-                     int stride) {
+                     const unsigned char *need) {
     const int nd = kernel == ORC_KERNEL_FUSED ? 4 : 1, no = nd, nb = nd * no;
     cheb_t ch;
     cheb_init(&ch, p);
@@ -777,7 +806,7 @@ static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel
 #pragma omp parallel for schedule(dynamic, 1)
         for (int i = 0; i < nn; ++i) {
             const onode *n = &t->nd[i];
-            if (n->level != lv || i % stride) continue;
+            if (n->level != lv || (need && !need[i])) continue;
             double *L = local + (size_t)i * no * R;
             double blk[16];
             for (int which = 1; which <= 3; which += 2) {
@@ -822,7 +851,7 @@ static void fmm_impl(const orc_tree *t, int p, const orc_kparams *kp, int kernel
 #pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < nn; ++i) {
         const onode *n = &t->nd[i];
-        if (!n->leaf || n->ntgt == 0 || i % stride) continue;
+        if (!n->leaf || n->ntgt == 0 || (need && !need[i])) continue;
         double *w = (double *)malloc(sizeof(double) * R);
         double blk[16];
         for (int tt = 0; tt < n->ntgt; ++tt) {

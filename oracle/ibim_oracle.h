@@ -66,6 +66,10 @@ void orc_fmm(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const 
 /* Timing sample of orc_fmm: full upward pass, downward pass only on nodes with id % stride == 0. */
 void orc_fmm_sample(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
                     int stride);
+/* orc_fmm at the targets sel[0..nsel) only (their leaves and those leaves' ancestors in the
+ * downward pass); equal to orc_fmm there.  Returns the number of leaves evaluated. */
+int orc_fmm_targets(const orc_tree *t, int p, const orc_kparams *kp, int kernel, const double *dens, double *out,
+                    const int *sel, int nsel);
 
 typedef struct {
     int np, maxpoint, maxlevel, restart, maxiter;

@@ -90,6 +90,8 @@ def lib():
         L.orc_tree_list.restype = C.c_int
         L.orc_fmm.argtypes = [C.c_void_p, C.c_int, C.POINTER(KParams), C.c_int, _dp, _dp]
         L.orc_fmm_sample.argtypes = [C.c_void_p, C.c_int, C.POINTER(KParams), C.c_int, _dp, _dp, C.c_int]
+        L.orc_fmm_targets.argtypes = [C.c_void_p, C.c_int, C.POINTER(KParams), C.c_int, _dp, _dp, _ip, C.c_int]
+        L.orc_fmm_targets.restype = C.c_int
         L.orc_rhs.argtypes = [_dp, C.c_long, _dp, _dp, C.c_int, C.POINTER(BieParams), _dp]
         L.orc_matvec.argtypes = [_dp, C.c_long, C.c_double, C.POINTER(BieParams), _dp, _dp]
         L.orc_solve.argtypes = [_dp, C.c_long, C.c_double, _dp, _dp, C.c_int, C.POINTER(BieParams), _dp, _dp, _dp,
@@ -207,6 +209,18 @@ class Tree:
         else:
             lib().orc_fmm(self.ptr, p, C.byref(kparams), kernel, _p(d), _p(out))
         return out
+
+    def fmm_at(self, p, kparams: KParams, kernel: int, dens, targets):
+        """orc_fmm at the given target indices only: the downward pass runs for the leaves that hold
+        them and those leaves' ancestors.  Returns (values at the targets, no x len(targets);
+        number of leaves evaluated)."""
+        nd = 4 if kernel == 16 else 1
+        d = _c(dens).reshape(nd, len(self.src))
+        sel = np.ascontiguousarray(targets, dtype=np.int32)
+        out = np.zeros((nd, len(self.tgt)))
+        nleaf = lib().orc_fmm_targets(self.ptr, p, C.byref(kparams), kernel, _p(d), _p(out), sel.ctypes.data_as(_ip),
+                                      len(sel))
+        return out[:, sel], nleaf
 
 
 def bie_params(np_=4, maxpoint=64, maxlevel=10, restart=30, maxiter=100, kappa=0.0, dE=80.0, dI=1.0, tau=1.0,
