@@ -649,10 +649,13 @@ Tube *surface_t(Grid &g, int thickness, long *inclusion, bool jacobian) {
     changed.alloc(1, s);
     const unsigned char one = 1;
     IBIM_CUDA(cudaMemcpyAsync(vis.ptr, &one, 1, cudaMemcpyHostToDevice, s));
-    // tiles of 16 x 8 x 8 cells, 4 rounds a launch: 28 launches instead of 64 for the 2,000-atom
-    // protein's 144 x 145 x 150 grid (2.85 -> 2.12 ms for the surface with 32 x 8 x 4 tiles and
-    // one round)
-    constexpr int FK = 16, FJ = 8, FI = 8, ROUNDS = 4;
+    // Up to 2^24 cells: tiles of 16 x 8 x 8 cells, 4 rounds a launch (the surface of the 2,000-atom
+    // protein's 144 x 145 x 150 grid in 2.2 ms and 32 launches, against 2.9 ms and 64 with one
+    // round of 32 x 8 x 4).  Larger grids: one round of 32 x 8 x 4, as the halo reloads of the
+    // many tiles away from the front cost more than the launches they save there (the 20,000-atom
+    // protein's 530 x 535 x 537 grid: 134 ms against 201 ms).
+    const bool small = n <= (1L << 24);
+    const int FK = small ? 16 : 32, FJ = 8, FI = small ? 8 : 4, rounds = small ? 4 : 1;
     const dim3 fb(FK, FJ, FI), fg(div_up(g.nz, FK), div_up(g.ny, FJ), div_up(g.nx, FI));
     // Each relaunch moves the front across at least one tile boundary along every open path,
     // so the count is bounded by the number of tiles; exceeding it is reported, not waited on.
@@ -665,8 +668,12 @@ Tube *surface_t(Grid &g, int thickness, long *inclusion, bool jacobian) {
             changed.zero();
             for (int r = 0; r < 4; ++r) {
                 ProfScope ps_(PROF_FLOOD);
-                (count_launch(), k_flood_tile<T, FK, FJ, FI><<<fg, fb, 0, s>>>(dm, (T)(-tw), G, vis.ptr, changed.ptr,
-                                                                             ROUNDS));
+                if (small)
+                    (count_launch(), k_flood_tile<T, 16, 8, 8><<<fg, fb, 0, s>>>(dm, (T)(-tw), G, vis.ptr, changed.ptr,
+                                                                             rounds));
+                else
+                    (count_launch(), k_flood_tile<T, 32, 8, 4><<<fg, fb, 0, s>>>(dm, (T)(-tw), G, vis.ptr, changed.ptr,
+                                                                             rounds));
             }
             IBIM_CHECK_LAUNCH();
             IBIM_CUDA(cudaMemcpyAsync(hflag, changed.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
