@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <tuple>
 
 #include <omp.h>
@@ -581,7 +582,14 @@ bool near_segments(const std::vector<int> &tl, const std::vector<int> &nt, std::
 struct OpIndex {
     std::vector<int> dense;  // level * 343 + offset -> operator id, -1 when absent
     std::vector<int> keys;   // 5 ints per operator
-    std::map<std::array<int, 5>, int> xmap;
+    struct KeyHash {
+        size_t operator()(const std::array<int, 5> &k) const {
+            uint64_t h = 1469598103934665603ULL;  // FNV-1a over the five ints
+            for (int v : k) h = (h ^ (uint32_t)v) * 1099511628211ULL;
+            return (size_t)h;
+        }
+    };
+    std::unordered_map<std::array<int, 5>, int, KeyHash> xmap;
     explicit OpIndex(int nlevels) : dense((size_t)std::max(1, nlevels) * 343, -1) {}
     int add(const std::array<int, 5> &k) {
         const int id = (int)keys.size() / 5;

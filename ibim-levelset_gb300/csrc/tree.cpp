@@ -251,19 +251,24 @@ TreeHost build_tree(const double *src, long ns, const double *tgt, long nt, int 
         S.nodes[0].parent = -1;
         S.split(0);
     }
-    for (size_t k = 0; k < frontier.size(); ++k) {
-        const int g = frontier[k];
-        const int base = (int)B.nodes.size() - 1;  // local j >= 1 -> base + j
-        auto map = [&](int j) { return j == 0 ? g : base + j; };
+    // subtree k's local node j >= 1 goes to base[k] + j (subtrees appended in order), in parallel
+    std::vector<int> base(frontier.size() + 1);
+    base[0] = (int)B.nodes.size() - 1;
+    for (size_t k = 0; k < frontier.size(); ++k) base[k + 1] = base[k] + (int)sub[k].nodes.size() - 1;
+    B.nodes.resize((size_t)base[frontier.size()] + 1);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)frontier.size(); ++k) {
+        const int g = frontier[k], b = base[k];
+        auto map = [&](int j) { return j == 0 ? g : b + j; };
         const std::vector<BNode> &L = sub[k].nodes;
         B.nodes[g].leaf = L[0].leaf;
         B.nodes[g].empty = L[0].empty;
         for (int i = 0; i < 8; ++i) B.nodes[g].child[i] = L[0].child[i] < 0 ? -1 : map(L[0].child[i]);
         for (size_t j = 1; j < L.size(); ++j) {
-            BNode q = L[j];
+            BNode &q = B.nodes[(size_t)b + j];
+            q = L[j];
             q.parent = map(q.parent);
             for (int i = 0; i < 8; ++i) q.child[i] = q.child[i] < 0 ? -1 : map(q.child[i]);
-            B.nodes.push_back(q);
         }
     }
 
